@@ -1,0 +1,168 @@
+"""ctypes binding of the oracle (test infrastructure only).
+
+Builds the oracle's field-pointer structs from host structs laid out as the
+reference's (game_archived_gb300.structs.Model), and exposes the oracle
+operators and step with the reference's argument meaning.
+"""
+import ctypes
+
+import numpy as np
+
+from . import build_oracle
+
+_lib = None
+P = ctypes.POINTER
+dp = P(ctypes.c_double)
+ip = P(ctypes.c_int)
+
+
+class OrcGrid(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("nc", "ne", "nt", "nl", "n_oro", "moisture_on", "n_const", "n_cond")] + [
+        ("radius", ctypes.c_double)] + [(n, dp) for n in (
+            "normal_distance", "volume", "area", "z_scalar", "z_vector", "gravity_m", "slope", "theta_v_bg",
+            "exner_bg", "exner_bg_grad", "ipw", "trsk_weights", "rhombi_weights")] + [(n, ip) for n in (
+                "trsk_indices", "trsk_mci", "from_", "to", "adj", "adj_sign", "rhombi_idx", "is_land")] + [
+        (n, dp) for n in ("dual_area", "dual_z_vector", "f_vec")] + [
+        (n, ip) for n in ("dual_from", "dual_to", "vort_idx", "vort_sign")] + [("gravity_potential", dp)]
+
+
+class OrcState(ctypes.Structure):
+    _fields_ = [(n, dp) for n in ("rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind")]
+
+
+class OrcDiag(ctypes.Structure):
+    _fields_ = [(n, dp) for n in ("flux_density", "flux_density_divv", "rel_vort_on_triangles", "rel_vort",
+                                  "pot_vort", "temperature", "v_squared", "scalar_field_placeholder")]
+
+
+class OrcForcings(ctypes.Structure):
+    _fields_ = [(n, dp) for n in ("pgrad_acc_old", "pgrad_nl", "pgrad_l", "pgrad_condensates_v",
+                                  "v_squared_grad", "pot_vort_tend", "radiation_tendency")]
+
+
+class OrcIrrev(ctypes.Structure):
+    _fields_ = [(n, dp) for n in ("temperature_diffusion_heating", "friction_acc", "heating_diss",
+                                  "pressure_gradient_decel_factor", "condensates_sediment_heat",
+                                  "mass_diff_tendency", "phase_trans_rates", "phase_trans_heating_rate")]
+
+
+class OrcConfig(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "totally_first_step_bool", "temperature_diff_h", "temperature_diff_v", "momentum_diff_h",
+        "momentum_diff_v", "mass_diff_h", "mass_diff_v", "rad_on", "prog_soil_temp", "sfc_phase_trans",
+        "sfc_sensible_heat_flux", "rad_update", "time_to_next_analysis", "pbl_scheme", "total_run_span")] + [
+        (n, ctypes.c_double) for n in ("damping_start_height_over_toa", "damping_coeff_max",
+                                       "impl_thermo_weight", "cloud_droplets_velocity", "rain_velocity",
+                                       "snow_velocity", "radiation_delta_t")]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build_oracle.build())
+        vp = ctypes.c_void_p
+        for name in ("orc_manage_rkhevi",):
+            getattr(_lib, name).argtypes = [vp] * 8 + [ctypes.c_double, ctypes.c_double]
+        _lib.orc_global_scalar_integrator.restype = ctypes.c_double
+        _lib.orc_global_scalar_integrator.argtypes = [vp, vp]
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(ip)
+
+
+class Oracle:
+    """The oracle bound to one Model (host structs in the reference layout)."""
+
+    def __init__(self, model):
+        self.m = model
+        lay = model.layout
+        g, dg = model.grid, model.dualgrid
+        self.g = OrcGrid(lay.nc, lay.ne, lay.nt, lay.nl, int(g["no_of_oro_layers"][0]), lay.moisture_on,
+                         lay.n_const, lay.n_cond, float(g["radius"][0]),
+                         _d(g["normal_distance"]), _d(g["volume"]), _d(g["area"]), _d(g["z_scalar"]),
+                         _d(g["z_vector"]), _d(g["gravity_m"]), _d(g["slope"]), _d(g["theta_v_bg"]),
+                         _d(g["exner_bg"]), _d(g["exner_bg_grad"]), _d(g["inner_product_weights"]),
+                         _d(g["trsk_weights"]), _d(g["density_to_rhombi_weights"]), _i(g["trsk_indices"]),
+                         _i(g["trsk_modified_curl_indices"]), _i(g["from_index"]), _i(g["to_index"]),
+                         _i(g["adjacent_vector_indices_h"]), _i(g["adjacent_signs_h"]),
+                         _i(g["density_to_rhombi_indices"]), _i(g["is_land"]), _d(dg["area"]), _d(dg["z_vector"]),
+                         _d(dg["f_vec"]), _i(dg["from_index"]), _i(dg["to_index"]),
+                         _i(dg["vorticity_indices_triangles"]), _i(dg["vorticity_signs_triangles"]),
+                         _d(g["gravity_potential"]))
+        self.lib = lib()
+
+    def state(self, s):
+        return OrcState(_d(s["rho"]), _d(s["rhotheta_v"]), _d(s["theta_v_pert"]), _d(s["exner_pert"]), _d(s["wind"]))
+
+    def diag(self):
+        d = self.m.diagnostics
+        return OrcDiag(*[_d(d[n]) for n in ("flux_density", "flux_density_divv", "rel_vort_on_triangles", "rel_vort",
+                                            "pot_vort", "temperature", "v_squared", "scalar_field_placeholder")])
+
+    def forcings(self):
+        f = self.m.forcings
+        return OrcForcings(*[_d(f[n]) for n in ("pgrad_acc_old", "pressure_gradient_acc_neg_nl",
+                                                "pressure_gradient_acc_neg_l", "pressure_grad_condensates_v",
+                                                "v_squared_grad", "pot_vort_tend", "radiation_tendency")])
+
+    def irrev(self):
+        r = self.m.irrev
+        return OrcIrrev(*[_d(r[n]) for n in ("temperature_diffusion_heating", "friction_acc", "heating_diss",
+                                             "pressure_gradient_decel_factor", "condensates_sediment_heat",
+                                             "mass_diff_tendency", "phase_trans_rates", "phase_trans_heating_rate")])
+
+    def config(self):
+        c = self.m.config
+        ints = [int(c[n][0]) for n, t in OrcConfig._fields_ if t is ctypes.c_int]
+        dbls = [float(c[n][0]) for n, t in OrcConfig._fields_ if t is ctypes.c_double]
+        return OrcConfig(*(ints + dbls))
+
+    # ---- operators on host arrays (reference argument meaning)
+    def scalar_times_vector(self, s, v, out):
+        self.lib.orc_scalar_times_vector(ctypes.byref(self.g), _d(s), _d(v), _d(out))
+
+    def calc_pot_vort(self, wind, rho):
+        d = self.diag()
+        self.lib.orc_calc_pot_vort(ctypes.byref(self.g), _d(wind), _d(rho), ctypes.byref(d))
+
+    def vorticity_flux(self, flux, pv, out):
+        self.lib.orc_vorticity_flux(ctypes.byref(self.g), _d(flux), _d(pv), _d(out))
+
+    def inner_product(self, a, b, out):
+        self.lib.orc_inner_product(ctypes.byref(self.g), _d(a), _d(b), _d(out))
+
+    def grad(self, s, out):
+        self.lib.orc_grad(ctypes.byref(self.g), _d(s), _d(out))
+
+    def divv_h(self, v, out):
+        self.lib.orc_divv_h(ctypes.byref(self.g), _d(v), _d(out))
+
+    def linear_combine_two_states(self, s0, s1, out, c0, c1):
+        a, b, o = self.state(s0), self.state(s1), self.state(out)
+        self.lib.orc_linear_combine_two_states(ctypes.byref(self.g), ctypes.byref(a), ctypes.byref(b),
+                                               ctypes.byref(o), ctypes.c_double(c0), ctypes.c_double(c1))
+
+    def manage_rkhevi(self, dt, t=0.0):
+        m = self.m
+        so, sn, st = self.state(m.state_old), self.state(m.state_new), self.state(m.state_tendency)
+        d, f, r, c = self.diag(), self.forcings(), self.irrev(), self.config()
+        rc = self.lib.orc_manage_rkhevi(ctypes.byref(self.g), ctypes.byref(so), ctypes.byref(sn), ctypes.byref(st),
+                                        ctypes.byref(d), ctypes.byref(f), ctypes.byref(r), ctypes.byref(c),
+                                        ctypes.c_double(dt), ctypes.c_double(t))
+        if rc != 0:
+            raise RuntimeError(f"oracle manage_rkhevi returned {rc}")
+
+    def surface_pressure(self, state, temperature):
+        out = np.zeros(self.m.layout.nc)
+        s = self.state(state)
+        self.lib.orc_surface_pressure(ctypes.byref(self.g), ctypes.byref(s), _d(temperature), _d(out))
+        return out
+
+    def integral(self, field):
+        return self.lib.orc_global_scalar_integrator(ctypes.byref(self.g), _d(field))

@@ -1,0 +1,1055 @@
+/*
+ * ORACLE -- test infrastructure only (see game_oracle.h).
+ *
+ * CPU restatement of the GAME RKHEVI step with run-time grid sizes.  Every
+ * function keeps the reference's order of floating-point operations; build
+ * with -ffp-contract=off.  Diffusion, PBL, surface fluxes, soil and radiation
+ * are not restated: the step returns -1 if their switches are on.
+ */
+#include "game_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* src/game_constants.h:10-27 */
+#define T_0 273.15
+#define N_A (6.02214076e23)
+#define P_0 100000.0
+#define C_D_V 717.942189
+#define C_V_V 1396.475121
+#define C_D_P 1005.0
+#define M_D (N_A * 0.004810e-23)
+#define M_V (N_A * 0.002991e-23)
+#define R_D 287.057811
+#define R_V 461.524879
+#define N_PENT 12
+
+#define NC (g->nc)
+#define NE (g->ne)
+#define NT (g->nt)
+#define NL (g->nl)
+#define VPL ((long)g->nc + g->ne)
+#define DPL ((long)g->ne + g->nt)
+#define NS ((long)g->nl * g->nc)
+#define NV ((long)g->nl * VPL + g->nc)
+#define NCURL ((long)g->nl * 2 * g->ne + g->ne)
+#define COND (g->n_cond)
+
+/* ------------------------------------------------------------ gradients
+ * src/spatial_operators/gradient_operators.c */
+int orc_grad_hor_cov(const orc_grid *g, const double *in, double *out)
+{
+    /* :14-33 */
+    for (long e = 0; e < NE; ++e)
+        for (long l = 0; l < NL; ++l) {
+            long vi = NC + l * VPL + e;
+            out[vi] = (in[g->to[e] + l * NC] - in[g->from[e] + l * NC]) / g->normal_distance[vi];
+        }
+    return 0;
+}
+
+int orc_grad_vert_cov(const orc_grid *g, const double *in, double *out)
+{
+    /* :35-54 (inner interfaces only; TOA and surface entries are left as they are) */
+    for (long i = NC; i < (long)(NL + 1) * NC - NC; ++i) {
+        long layer = i / NC, h = i - layer * NC;
+        long lower = h + layer * NC, upper = h + (layer - 1) * NC, vi = h + layer * VPL;
+        out[vi] = (in[upper] - in[lower]) / g->normal_distance[vi];
+    }
+    return 0;
+}
+
+int orc_grad_cov(const orc_grid *g, const double *in, double *out)
+{
+    /* :56-64 */
+    orc_grad_hor_cov(g, in, out);
+    orc_grad_vert_cov(g, in, out);
+    return 0;
+}
+
+int orc_grad(const orc_grid *g, const double *in, double *out)
+{
+    /* :66-74 */
+    orc_grad_cov(g, in, out);
+    orc_vector_field_hor_cov_to_con(g, out);
+    return 0;
+}
+
+int orc_grad_hor(const orc_grid *g, const double *in, double *out)
+{
+    /* :76-91 */
+    orc_grad(g, in, out);
+    for (long i = 0; i < (long)(NL + 1) * NC; ++i) {
+        long layer = i / NC, h = i - layer * NC;
+        out[h + layer * VPL] = 0;
+    }
+    return 0;
+}
+
+/* --------------------------------------------------------------- averaging
+ * src/spatial_operators/averaging.c */
+static double remap_verpri2horpri_vector(const orc_grid *g, const double *f, long layer, long e)
+{
+    /* :14-39 */
+    long fr = g->from[e], to = g->to[e];
+    double c = g->ipw[8 * (layer * NC + fr) + 6] * f[layer * VPL + fr];
+    c += g->ipw[8 * (layer * NC + to) + 6] * f[layer * VPL + to];
+    if (layer < NL - 1) {
+        c += g->ipw[8 * (layer * NC + fr) + 7] * f[(layer + 1) * VPL + fr];
+        c += g->ipw[8 * (layer * NC + to) + 7] * f[(layer + 1) * VPL + to];
+    }
+    c = 0.5 * c;
+    return c;
+}
+
+static double vertical_contravariant_corr(const orc_grid *g, const double *f, long layer, long h)
+{
+    /* :41-95 */
+    double r = 0;
+    int n_edges = h < N_PENT ? 5 : 6;
+    if (layer >= NL - g->n_oro) {
+        if (layer == NL - g->n_oro) {
+            for (int j = 0; j < n_edges; ++j) {
+                long si = layer * NC + h, vi = NC + layer * VPL + g->adj[6 * h + j];
+                r += -0.5 * g->ipw[8 * si + j] * g->slope[vi] * f[vi];
+            }
+        } else {
+            for (int j = 0; j < n_edges; ++j) {
+                long si = (layer - 1) * NC + h, vi = NC + (layer - 1) * VPL + g->adj[6 * h + j];
+                r += -0.5 * g->ipw[8 * si + j] * g->slope[vi] * f[vi];
+            }
+            for (int j = 0; j < n_edges; ++j) {
+                long si = layer * NC + h, vi = NC + layer * VPL + g->adj[6 * h + j];
+                r += -0.5 * g->ipw[8 * si + j] * g->slope[vi] * f[vi];
+            }
+        }
+    }
+    return r;
+}
+
+static double horizontal_covariant(const orc_grid *g, const double *f, long layer, long e)
+{
+    /* :97-111 */
+    long vi = NC + layer * VPL + e;
+    double r = f[vi];
+    if (layer >= NL - g->n_oro) {
+        double vc = remap_verpri2horpri_vector(g, f, layer, e);
+        r += g->slope[vi] * vc;
+    }
+    return r;
+}
+
+int orc_vector_field_hor_cov_to_con(const orc_grid *g, double *f)
+{
+    /* :113-133 */
+    for (long i = 0; i < (long)g->n_oro * NE; ++i) {
+        long li = i / NE, e = i - li * NE;
+        double vg = remap_verpri2horpri_vector(g, f, li + (NL - g->n_oro), e);
+        long vi = NC + (NL - g->n_oro + li) * VPL + e;
+        f[vi] += -g->slope[vi] * vg;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------- divergences
+ * src/spatial_operators/divergences.c */
+int orc_divv_h(const orc_grid *g, const double *in, double *out)
+{
+    /* :14-64 */
+    for (long h = 0; h < NC; ++h) {
+        int n_edges = h < N_PENT ? 5 : 6;
+        for (long l = 0; l < NL; ++l) {
+            long i = l * NC + h;
+            double comp_h = 0.0;
+            for (int j = 0; j < n_edges; ++j) {
+                long vi = NC + l * VPL + g->adj[6 * h + j];
+                comp_h += in[vi] * g->adj_sign[6 * h + j] * g->area[vi];
+            }
+            double comp_v = 0.0;
+            if (l == NL - g->n_oro - 1) {
+                double lo = vertical_contravariant_corr(g, in, l + 1, h);
+                comp_v = -lo * g->area[h + (l + 1) * VPL];
+            } else if (l == NL - 1) {
+                double up = vertical_contravariant_corr(g, in, l, h);
+                comp_v = up * g->area[h + l * VPL];
+            } else if (l > NL - g->n_oro - 1) {
+                double up = vertical_contravariant_corr(g, in, l, h);
+                double lo = vertical_contravariant_corr(g, in, l + 1, h);
+                comp_v = up * g->area[h + l * VPL] - lo * g->area[h + (l + 1) * VPL];
+            }
+            out[i] = 1.0 / g->volume[i] * (comp_h + comp_v);
+        }
+    }
+    return 0;
+}
+
+int orc_divv_h_tracer(const orc_grid *g, const double *in, const double *density, const double *wind, double *out)
+{
+    /* :66-148 */
+    for (long h = 0; h < NC; ++h) {
+        int n_edges = h < N_PENT ? 5 : 6;
+        for (long l = 0; l < NL; ++l) {
+            long i = l * NC + h;
+            double comp_h = 0.0;
+            for (int j = 0; j < n_edges; ++j) {
+                long vi = NC + l * VPL + g->adj[6 * h + j];
+                comp_h += in[vi] * g->adj_sign[6 * h + j] * g->area[vi];
+            }
+            double comp_v = 0.0, d_up, d_lo;
+            if (l == NL - g->n_oro - 1) {
+                double lo = vertical_contravariant_corr(g, wind, l + 1, h);
+                d_lo = lo <= 0.0 ? density[i] : density[i + NC];
+                comp_v = -d_lo * lo * g->area[h + (l + 1) * VPL];
+            } else if (l == NL - 1) {
+                double up = vertical_contravariant_corr(g, wind, l, h);
+                d_up = up <= 0.0 ? density[i - NC] : density[i];
+                comp_v = d_up * up * g->area[h + l * VPL];
+            } else if (l > NL - g->n_oro - 1) {
+                double up = vertical_contravariant_corr(g, wind, l, h);
+                d_up = up <= 0.0 ? density[i - NC] : density[i];
+                double lo = vertical_contravariant_corr(g, wind, l + 1, h);
+                d_lo = lo <= 0.0 ? density[i] : density[i + NC];
+                comp_v = d_up * up * g->area[h + l * VPL] - d_lo * lo * g->area[h + (l + 1) * VPL];
+            }
+            out[i] = 1.0 / g->volume[i] * (comp_h + comp_v);
+        }
+    }
+    return 0;
+}
+
+/* -------------------------------------------------------- multiplications
+ * src/spatial_operators/multiplications.c */
+int orc_scalar_times_vector_h(const orc_grid *g, const double *s, const double *v, double *out)
+{
+    /* :45-66 */
+    for (long e = 0; e < NE; ++e)
+        for (long l = 0; l < NL; ++l) {
+            long vi = NC + l * VPL + e;
+            double sv = 0.5 * (s[g->to[e] + l * NC] + s[g->from[e] + l * NC]);
+            out[vi] = sv * v[vi];
+        }
+    return 0;
+}
+
+int orc_scalar_times_vector_h_upstream(const orc_grid *g, const double *s, const double *v, double *out)
+{
+    /* :68-96 */
+    for (long e = 0; e < NE; ++e)
+        for (long l = 0; l < NL; ++l) {
+            long vi = NC + l * VPL + e;
+            double sv = v[vi] >= 0.0 ? s[g->from[e] + l * NC] : s[g->to[e] + l * NC];
+            out[vi] = sv * v[vi];
+        }
+    return 0;
+}
+
+int orc_scalar_times_vector_v(const orc_grid *g, const double *s, const double *v, double *out)
+{
+    /* :98-117 (inner interfaces only) */
+    for (long h = 0; h < NC; ++h)
+        for (long l = 1; l < NL; ++l) {
+            long i = l * VPL + h;
+            double sv = 0.5 * (s[h + (l - 1) * NC] + s[h + l * NC]);
+            out[i] = sv * v[i];
+        }
+    return 0;
+}
+
+int orc_scalar_times_vector(const orc_grid *g, const double *s, const double *v, double *out)
+{
+    /* :35-43 */
+    orc_scalar_times_vector_h(g, s, v, out);
+    orc_scalar_times_vector_v(g, s, v, out);
+    return 0;
+}
+
+/* ------------------------------------------------------------ inner product
+ * src/spatial_operators/inner_product.c:13-43 */
+int orc_inner_product(const orc_grid *g, const double *a, const double *b, double *out)
+{
+    for (long h = 0; h < NC; ++h) {
+        int n_edges = h < N_PENT ? 5 : 6;
+        for (long l = 0; l < NL; ++l) {
+            long i = l * NC + h, base = 8 * i;
+            out[i] = 0;
+            for (int j = 0; j < n_edges; ++j) {
+                long vi = NC + l * VPL + g->adj[6 * h + j];
+                out[i] += g->ipw[base + j] * a[vi] * b[vi];
+            }
+            out[i] += g->ipw[base + 6] * a[h + l * VPL] * b[h + l * VPL];
+            out[i] += g->ipw[base + 7] * a[h + (l + 1) * VPL] * b[h + (l + 1) * VPL];
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------- vorticities
+ * src/spatial_operators/vorticities.c */
+int orc_calc_rel_vort_on_triangles(const orc_grid *g, const double *w, double *out)
+{
+    /* :167-222 */
+    for (long i = 0; i < (long)NL * NT; ++i) {
+        long layer = i / NT, h = i - layer * NT;
+        out[i] = 0;
+        for (int j = 0; j < 3; ++j) {
+            long vi = NC + layer * VPL + g->vort_idx[3 * h + j];
+            double vel = w[vi];
+            double rescale = 1;
+            if (layer >= NL - g->n_oro) {
+                long dvi = NE + layer * DPL + h;
+                rescale = (g->radius + g->dual_z_vector[dvi]) / (g->radius + g->z_vector[vi]);
+                double dz = g->dual_z_vector[dvi] - g->z_vector[vi];
+                long vgi;
+                if (dz > 0) vgi = vi - VPL;
+                else if (layer == NL - 1) vgi = vi - VPL;
+                else vgi = vi + VPL;
+                double vgrad = (w[vi] - w[vgi]) / (g->z_vector[vi] - g->z_vector[vgi]);
+                vel += dz * vgrad;
+            }
+            out[i] += rescale * g->normal_distance[vi] * g->vort_sign[3 * h + j] * vel;
+        }
+        out[i] = out[i] / g->dual_area[NE + layer * DPL + h];
+    }
+    return 0;
+}
+
+int orc_calc_rel_vort(const orc_grid *g, const double *w, orc_diag *d)
+{
+    /* :104-165 */
+    orc_calc_rel_vort_on_triangles(g, w, d->rel_vort_on_triangles);
+    for (long i = NE; i < NCURL; ++i) {
+        long layer = i / (2 * NE), h = i - layer * 2 * NE;
+        if (h >= NE) {
+            long base = NE + layer * DPL, e = h - NE;
+            long tf = g->dual_from[e], tt = g->dual_to[e];
+            d->rel_vort[i] = (g->dual_area[base + tf] * d->rel_vort_on_triangles[layer * NT + tf]
+                              + g->dual_area[base + tt] * d->rel_vort_on_triangles[layer * NT + tt])
+                             / (g->dual_area[base + tf] + g->dual_area[base + tt]);
+        } else {
+            long base = layer * VPL;
+            if (layer == NL) {
+                long i2 = base - NE + h;
+                double c2 = horizontal_covariant(g, w, layer - 1, h);
+                d->rel_vort[i] = 1 / g->dual_area[h + layer * DPL] * g->normal_distance[i2] * c2;
+            } else {
+                long i0 = base + NC + h, i1 = base + g->from[h], i2 = base - NE + h, i3 = base + g->to[h];
+                double c0 = horizontal_covariant(g, w, layer, h);
+                double c2 = horizontal_covariant(g, w, layer - 1, h);
+                d->rel_vort[i] = 1 / g->dual_area[h + layer * DPL]
+                                 * (-g->normal_distance[i0] * c0 + g->normal_distance[i1] * w[i1]
+                                    + g->normal_distance[i2] * c2 - g->normal_distance[i3] * w[i3]);
+            }
+        }
+    }
+    for (long i = 0; i < NE; ++i) d->rel_vort[i] = d->rel_vort[i + 2 * NE];
+    return 0;
+}
+
+int orc_add_f_to_rel_vort(const orc_grid *g, const double *rel, double *out)
+{
+    /* :87-102 */
+    for (long i = 0; i < NCURL; ++i) {
+        long layer = i / (2 * NE), h = i - layer * 2 * NE;
+        out[i] = rel[i] + g->f_vec[h];
+    }
+    return 0;
+}
+
+/* Grid::z_vector read at index idx, as the reference's calc_pot_vort reads it.
+ * At the surface level it indexes z_vector[NO_OF_SCALARS + (layer - 2)*VPL + h]
+ * (vorticities.c:55-56), which lies past the end of z_vector for the standard
+ * sizes; the read then lands in the members that follow z_vector in the Grid
+ * struct (gravity_potential, then gravity_m), and results depend on them. */
+static double zv_ext(const orc_grid *g, long idx)
+{
+    if (idx < NV) return g->z_vector[idx];
+    idx -= NV;
+    if (idx < NS) return g->gravity_potential[idx];
+    return g->gravity_m[idx - NS];
+}
+
+int orc_calc_pot_vort(const orc_grid *g, const double *w, const double *rho, orc_diag *d)
+{
+    /* :18-85 */
+    orc_calc_rel_vort(g, w, d);
+    orc_add_f_to_rel_vort(g, d->rel_vort, d->pot_vort);
+    for (long i = 0; i < NCURL; ++i) {
+        long layer = i / (2 * NE), h = i - layer * 2 * NE;
+        double dens;
+        if (h >= NE) {
+            long e = h - NE;
+            dens = 0;
+            for (int j = 0; j < 4; ++j)
+                dens += g->rhombi_weights[4 * e + j] * rho[layer * NC + g->rhombi_idx[4 * e + j]];
+        } else {
+            long fr = g->from[h], to = g->to[h];
+            if (layer == 0) {
+                dens = 0.5 * (rho[fr] + rho[to])
+                       + (0.5 * (rho[fr] + rho[to]) - 0.5 * (rho[fr + NC] + rho[to + NC]))
+                             / (zv_ext(g, NS + h) - zv_ext(g, NS + VPL + h)) * (zv_ext(g, 0) - zv_ext(g, NS + h));
+            } else if (layer == NL) {
+                long a = (layer - 1) * NC, b = (layer - 2) * NC;
+                dens = 0.5 * (rho[a + fr] + rho[a + to])
+                       + (0.5 * (rho[b + fr] + rho[b + to]) - 0.5 * (rho[a + fr] + rho[a + to]))
+                             / (zv_ext(g, NS + (layer - 2) * VPL + h) - zv_ext(g, NS + (layer - 1) * VPL + h))
+                             * (0.5 * (zv_ext(g, layer * VPL + fr) + zv_ext(g, layer * VPL + to))
+                                - zv_ext(g, NS + (layer - 1) * VPL + h));
+            } else {
+                long uf = (layer - 1) * NC + fr, ut = (layer - 1) * NC + to;
+                dens = 0.25 * (rho[uf] + rho[ut] + rho[uf + NC] + rho[ut + NC]);
+            }
+        }
+        d->pot_vort[i] = d->pot_vort[i] / dens;
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------- vorticity flux
+ * src/spatial_operators/vorticity_flux.c:16-187 */
+int orc_vorticity_flux(const orc_grid *g, const double *mf, const double *pv, double *out)
+{
+    for (long h = 0; h < VPL; ++h) {
+        for (long l = 0; l < NL + 1; ++l) {
+            long i = l * VPL + h;
+            if (h >= NC && l < NL) {
+                out[i] = 0;
+                long e = h - NC, mb = NC + l * VPL, pb = NE + l * 2 * NE;
+                const double *tw = &g->trsk_weights[10 * e];
+                const int *ti = &g->trsk_indices[10 * e], *tm = &g->trsk_mci[10 * e];
+                if (g->from[e] < N_PENT) {
+                    for (int j = 0; j < 4; ++j) out[i] += tw[j] * mf[mb + ti[j]] * pv[pb + tm[j]];
+                } else {
+                    for (int j = 0; j < 5; ++j) {
+                        if (j == 2) out[i] += tw[j] * mf[mb + ti[j]] * 0.5 * (pv[pb + tm[j]] + pv[pb + e]);
+                        else out[i] += tw[j] * mf[mb + ti[j]] * pv[pb + tm[j]];
+                    }
+                }
+                if (g->to[e] < N_PENT) {
+                    for (int j = 5; j < 9; ++j) out[i] += tw[j] * mf[mb + ti[j]] * pv[pb + tm[j]];
+                } else {
+                    for (int j = 5; j < 10; ++j) {
+                        if (j == 7) out[i] += tw[j] * mf[mb + ti[j]] * 0.5 * (pv[pb + tm[j]] + pv[pb + e]);
+                        else out[i] += tw[j] * mf[mb + ti[j]] * pv[pb + tm[j]];
+                    }
+                }
+                long fr = g->from[e], to = g->to[e];
+                out[i] -= 0.5 * g->ipw[8 * (l * NC + fr) + 6] * mf[l * VPL + fr] * pv[e + l * 2 * NE];
+                out[i] -= 0.5 * g->ipw[8 * (l * NC + to) + 6] * mf[l * VPL + to] * pv[e + l * 2 * NE];
+                out[i] -= 0.5 * g->ipw[8 * (l * NC + fr) + 7] * mf[(l + 1) * VPL + fr] * pv[e + (l + 1) * 2 * NE];
+                out[i] -= 0.5 * g->ipw[8 * (l * NC + to) + 7] * mf[(l + 1) * VPL + to] * pv[e + (l + 1) * 2 * NE];
+            } else if (h < NC) {
+                out[i] = 0;
+                int n_edges = h < N_PENT ? 5 : 6;
+                double vw = (l == 0 || l == NL) ? 1 : 0.5;
+                if (l >= 1)
+                    for (int j = 0; j < n_edges; ++j) {
+                        long a = g->adj[6 * h + j];
+                        out[i] += vw * g->ipw[8 * ((l - 1) * NC + h) + j] * mf[NC + (l - 1) * VPL + a] * pv[l * 2 * NE + a];
+                    }
+                if (l <= NL - 1)
+                    for (int j = 0; j < n_edges; ++j) {
+                        long a = g->adj[6 * h + j];
+                        out[i] += vw * g->ipw[8 * (l * NC + h) + j] * mf[NC + l * VPL + a] * pv[l * 2 * NE + a];
+                    }
+            }
+        }
+    }
+    return 0;
+}
+
+/* -------------------------------------------------------- state blending
+ * src/spatial_operators/linear_combine_two_states.c:14-43 */
+int orc_linear_combine_two_states(const orc_grid *g, const orc_state *s0, const orc_state *s1, orc_state *o,
+                                  double c0, double c1)
+{
+    for (long i = 0; i < NS; ++i) {
+        for (int j = 0; j < g->n_const; ++j)
+            o->rho[j * NS + i] = c0 * s0->rho[j * NS + i] + c1 * s1->rho[j * NS + i];
+        o->rhotheta_v[i] = c0 * s0->rhotheta_v[i] + c1 * s1->rhotheta_v[i];
+        o->theta_v_pert[i] = o->rhotheta_v[i] / o->rho[COND * NS + i] - g->theta_v_bg[i];
+        o->exner_pert[i] = c0 * s0->exner_pert[i] + c1 * s1->exner_pert[i];
+    }
+    for (long i = 0; i < NV; ++i) o->wind[i] = c0 * s0->wind[i] + c1 * s1->wind[i];
+    return 0;
+}
+
+/* ------------------------------------------------------- thermodynamics
+ * src/constituents/derived_quantities.c, dictionary.c */
+int orc_temperature_diagnostics(const orc_grid *g, const orc_state *s, orc_diag *d)
+{
+    /* derived_quantities.c:15-40 */
+    if (!g->moisture_on) {
+        for (long i = 0; i < NS; ++i)
+            d->temperature[i] = (g->theta_v_bg[i] + s->theta_v_pert[i]) * (g->exner_bg[i] + s->exner_pert[i]);
+    } else {
+        for (long i = 0; i < NS; ++i)
+            d->temperature[i] = (g->theta_v_bg[i] + s->theta_v_pert[i]) * (g->exner_bg[i] + s->exner_pert[i])
+                                / (1.0 + s->rho[(COND + 1) * NS + i] / s->rho[COND * NS + i] * (M_D / M_V - 1.0));
+    }
+    return 0;
+}
+
+static double density_total(const orc_grid *g, const orc_state *s, long i)
+{
+    /* derived_quantities.c:83-95 */
+    double r = 0.0;
+    for (int k = 0; k < g->n_const; ++k) r += s->rho[k * NS + i];
+    return r;
+}
+
+static double c_p_ice(double t)
+{
+    /* dictionary.c:111-131 */
+    if (t > T_0) t = T_0;
+    if (t < 20.0) t = 20.0;
+    double r = -2.0572 + 0.14644 * t + 0.06163 * t * exp(-pow(t / 125.1, 2));
+    return r / M_V;
+}
+
+static double c_p_water(double t)
+{
+    /* dictionary.c:133-171 */
+    double tc = t - T_0, r;
+    if (tc >= 0.0) {
+        if (tc > 35.0) tc = 35.0;
+        r = 0.9979 + 3.1e-6 * pow(tc - 35.0, 2) + 3.8e-9 * pow(tc - 35.0, 4);
+    } else {
+        if (tc < -37.0) tc = -37.0;
+        r = 1.000938 - 2.7052e-3 * tc - 2.3235e-5 * pow(tc, 2) + 4.3778e-6 * pow(tc, 3) + 2.7136e-7 * pow(tc, 4);
+    }
+    return 4186.8 * r;
+}
+
+static double c_p_cond(int id, double t)
+{
+    /* dictionary.c:173-190 */
+    return fmod(id, 2) == 0 ? c_p_ice(t) : c_p_water(t);
+}
+
+static double enthalpy_evaporation(double t)
+{
+    /* dictionary.c:221-254 */
+    double r;
+    if (t < T_0) {
+        if (t < 30.0) t = 30.0;
+        r = 56579.0 - 42.212 * t + exp(0.1149 * (281.6 - t));
+        r = r / M_V;
+    } else {
+        if (t > T_0 + 100.0) t = T_0 + 100.0;
+        r = 3151378.0 - 2386.0 * t;
+    }
+    return r;
+}
+
+static double enthalpy_sublimation(double t)
+{
+    /* dictionary.c:256-279 */
+    if (t < 30.0) t = 30.0;
+    if (t > T_0) t = T_0;
+    double r = 46782.5 + 35.8925 * t - 0.07414 * pow(t, 2) + 541.5 * exp(-pow(t / 123.75, 2));
+    return r / M_V;
+}
+
+static double phase_trans_heat(int dir, double t)
+{
+    /* dictionary.c:192-219 */
+    double r = 0.0;
+    if (dir == 0) r = enthalpy_evaporation(t);
+    if (dir == 1) r = enthalpy_sublimation(t);
+    if (dir == 2) r = enthalpy_sublimation(t) - enthalpy_evaporation(t);
+    return r;
+}
+
+static double saturation_pressure_over_water(double t)
+{
+    /* dictionary.c:281-323 */
+    double tc = t - T_0, r;
+    if (tc > 100.0) tc = 100.0;
+    if (tc > 0.0) {
+        r = exp(34.494 - 4924.99 / (tc + 237.1)) / pow(tc + 105.0, 1.57);
+    } else {
+        if (tc < -50.0) tc = -50.0;
+        r = 6.107799961 + 4.436518521e-1 * tc + 1.428945805e-2 * pow(tc, 2) + 2.650648471e-4 * pow(tc, 3)
+            + 3.031240396e-6 * pow(tc, 4) + 2.034080948e-8 * pow(tc, 5) + 6.136820929e-11 * pow(tc, 6);
+        r = 100.0 * r;
+    }
+    return r;
+}
+
+static double dsaturation_pressure_over_water_dT(double t)
+{
+    /* dictionary.c:325-349 */
+    double tc = t - T_0;
+    if (tc > 100.0) tc = 100.0;
+    if (tc < 0.0) tc = 0.0;
+    return saturation_pressure_over_water(t) * (4924.99 / pow(tc + 237.1, 2.0) - 1.57 / (tc + 105.0));
+}
+
+static double saturation_pressure_over_ice(double t)
+{
+    /* dictionary.c:351-372 */
+    double tc = t - T_0;
+    if (tc < -80.0) tc = -80.0;
+    if (tc > 0.0) tc = 0.0;
+    return exp(43.494 - 6545.8 / (tc + 278.0)) / pow(tc + 868.0, 2);
+}
+
+static double dsaturation_pressure_over_ice_dT(double t)
+{
+    /* dictionary.c:374-398 */
+    double tc = t - T_0;
+    if (tc < -80.0) tc = -80.0;
+    if (tc > 0.0) tc = 0.0;
+    return saturation_pressure_over_ice(t) * (6545.8 / pow(tc + 278.0, 2.0) - 2.0 / (tc + 868.0));
+}
+
+static double enhancement_factor_over_water(double p) { return 1.00071 * exp(0.000000045 * p); } /* :400-410 */
+static double enhancement_factor_over_ice(double p) { return 0.99882 * exp(0.00000008 * p); }    /* :412-424 */
+
+static double c_v_mass_weighted_air(const orc_grid *g, const orc_state *s, const orc_diag *d, long i)
+{
+    /* derived_quantities.c:97-115 */
+    double r = 0.0;
+    for (int k = 0; k < COND; ++k) r += s->rho[k * NS + i] * c_p_cond(k, d->temperature[i]);
+    r += s->rho[COND * NS + i] * C_D_V;
+    if (g->moisture_on) r += s->rho[(COND + 1) * NS + i] * C_V_V;
+    return r;
+}
+
+/* src/constituents/phase_trans.c:16-311 (surface effects off) */
+int orc_calc_h2otracers_source_rates(const orc_grid *g, const orc_state *s, orc_diag *d, const orc_config *c,
+                                     orc_irrev *ir, double dt)
+{
+    const double max_cloud_water = 0.2e-3;
+    double *pr = ir->phase_trans_rates;
+    if (c->sfc_phase_trans) return -1;
+    for (long i = 0; i < NS; ++i) {
+        double T = d->temperature[i], sat, wvp, dry, air, a, b, cc, p, q, ef, diff, ptd;
+        sat = T >= T_0 ? saturation_pressure_over_water(T) : saturation_pressure_over_ice(T);
+        wvp = s->rho[(COND + 1) * NS + i] * R_V * T;
+        dry = (s->rho[COND * NS + i] - s->rho[(COND + 1) * NS + i]) * R_D * T;
+        air = dry + wvp;
+        ef = T >= T_0 ? enhancement_factor_over_water(air) : enhancement_factor_over_ice(air);
+        sat = ef * sat;
+        int dir = T >= T_0 ? 0 : 1;
+        a = -R_V * phase_trans_heat(dir, T) / c_v_mass_weighted_air(g, s, d, i);
+        b = R_V * T - R_V * s->rho[(COND + 1) * NS + i] * phase_trans_heat(dir, T) / c_v_mass_weighted_air(g, s, d, i)
+            + ef * (dir == 0 ? dsaturation_pressure_over_water_dT(T) : dsaturation_pressure_over_ice_dT(T))
+                  * phase_trans_heat(dir, T) / c_v_mass_weighted_air(g, s, d, i);
+        cc = wvp - sat;
+        p = b / a;
+        q = cc / a;
+        diff = -0.5 * p - pow(0.25 * pow(p, 2) - q, 0.5);
+        if (sat >= wvp) {
+            if (T >= T_0) {
+                pr[2 * NS + i] = -s->rho[2 * NS + i] / dt;
+                ptd = fmin(s->rho[3 * NS + i], diff);
+                pr[4 * NS + i] = ptd / dt;
+                pr[3 * NS + i] = s->rho[2 * NS + i] / dt - ptd / dt;
+                ir->phase_trans_heating_rate[i] = pr[2 * NS + i] * phase_trans_heat(2, T) - ptd * phase_trans_heat(0, T) / dt;
+            } else {
+                pr[3 * NS + i] = -s->rho[3 * NS + i] / dt;
+                ptd = fmin(s->rho[2 * NS + i], diff);
+                pr[4 * NS + i] = ptd / dt;
+                pr[2 * NS + i] = s->rho[3 * NS + i] / dt - ptd / dt;
+                ir->phase_trans_heating_rate[i] = -pr[3 * NS + i] * phase_trans_heat(2, T) - ptd * phase_trans_heat(1, T) / dt;
+            }
+        } else {
+            if (T >= T_0) {
+                pr[2 * NS + i] = -s->rho[2 * NS + i] / dt;
+                pr[4 * NS + i] = diff / dt;
+                pr[3 * NS + i] = s->rho[2 * NS + i] / dt - diff / dt;
+                ir->phase_trans_heating_rate[i] = pr[2 * NS + i] * phase_trans_heat(2, T) - diff * phase_trans_heat(0, T) / dt;
+            } else {
+                pr[3 * NS + i] = -s->rho[3 * NS + i] / dt;
+                pr[4 * NS + i] = diff / dt;
+                pr[2 * NS + i] = s->rho[3 * NS + i] / dt - diff / dt;
+                ir->phase_trans_heating_rate[i] = -pr[3 * NS + i] * phase_trans_heat(2, T) - diff * phase_trans_heat(1, T) / dt;
+            }
+        }
+        pr[i] = 0.0;
+        pr[NS + i] = 0.0;
+        if (T < T_0) {
+            pr[i] = fmax(s->rho[2 * NS + i] - max_cloud_water * s->rho[4 * NS + i], 0.0) / 1000.0;
+            pr[2 * NS + i] -= pr[i];
+        } else if (T >= T_0) {
+            pr[NS + i] = fmax(s->rho[3 * NS + i] - max_cloud_water * s->rho[4 * NS + i], 0.0) / 1000.0;
+            pr[3 * NS + i] -= pr[NS + i];
+        }
+        if (T >= T_0 && s->rho[i] > 0.0) {
+            pr[i] = -s->rho[i] / dt;
+            pr[NS + i] -= pr[i];
+            ir->phase_trans_heating_rate[i] += pr[i] * phase_trans_heat(2, T);
+        }
+        if (T < T_0 && s->rho[NS + i] > 0.0) {
+            pr[NS + i] = -s->rho[NS + i] / dt;
+            pr[i] -= pr[NS + i];
+            ir->phase_trans_heating_rate[i] += -pr[NS + i] * phase_trans_heat(2, T);
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------ pressure gradient
+ * src/time_stepping/manage_pressure_gradient.c */
+int orc_manage_pressure_gradient(const orc_grid *g, const orc_state *s, orc_diag *d, orc_forcings *f,
+                                 orc_irrev *ir, const orc_config *c)
+{
+    /* :17-72 */
+    if (c->totally_first_step_bool == 0)
+        for (long i = 0; i < NV; ++i) f->pgrad_acc_old[i] = -f->pgrad_nl[i] - f->pgrad_l[i];
+    for (long i = 0; i < NS; ++i) d->scalar_field_placeholder[i] = C_D_P * (g->theta_v_bg[i] + s->theta_v_pert[i]);
+    orc_grad(g, s->exner_pert, f->pgrad_nl);
+    orc_scalar_times_vector(g, d->scalar_field_placeholder, f->pgrad_nl, f->pgrad_nl);
+    for (long i = 0; i < NS; ++i) d->scalar_field_placeholder[i] = C_D_P * s->theta_v_pert[i];
+    orc_scalar_times_vector(g, d->scalar_field_placeholder, g->exner_bg_grad, f->pgrad_l);
+    for (long i = 0; i < NS; ++i)
+        ir->pressure_gradient_decel_factor[i] = s->rho[COND * NS + i] / density_total(g, s, i);
+    orc_scalar_times_vector(g, ir->pressure_gradient_decel_factor, f->pgrad_nl, f->pgrad_nl);
+    orc_scalar_times_vector(g, ir->pressure_gradient_decel_factor, f->pgrad_l, f->pgrad_l);
+    if (c->totally_first_step_bool == 1)
+        for (long i = 0; i < NV; ++i) f->pgrad_acc_old[i] = -f->pgrad_nl[i] - f->pgrad_l[i];
+    return 0;
+}
+
+int orc_calc_pressure_grad_condensates_v(const orc_grid *g, const orc_state *s, orc_forcings *f, orc_irrev *ir)
+{
+    /* :74-87 */
+    for (long i = 0; i < NS; ++i)
+        ir->pressure_gradient_decel_factor[i] = s->rho[COND * NS + i] / density_total(g, s, i) - 1.0;
+    orc_scalar_times_vector_v(g, ir->pressure_gradient_decel_factor, g->gravity_m, f->pgrad_condensates_v);
+    return 0;
+}
+
+/* ------------------------------------------------- explicit tendencies
+ * src/time_stepping/vector_tendencies_expl.c:18-133 */
+int orc_vector_tendencies_expl(const orc_grid *g, const orc_state *s, orc_state *tend, orc_diag *d,
+                               orc_forcings *f, orc_irrev *ir, const orc_config *c, int rk_step, double dt)
+{
+    (void)dt;
+    if (rk_step == 1 || c->totally_first_step_bool == 1) {
+        orc_scalar_times_vector(g, &s->rho[COND * NS], s->wind, d->flux_density);
+        orc_calc_pot_vort(g, s->wind, &s->rho[COND * NS], d);
+        orc_vorticity_flux(g, d->flux_density, d->pot_vort, f->pot_vort_tend);
+        orc_inner_product(g, s->wind, s->wind, d->v_squared);
+        orc_grad(g, d->v_squared, f->v_squared_grad);
+    }
+    double new_w = rk_step == 1 ? 0.5 : 1.0, old_w = 1.0 - new_w;
+    double cur_hor = 0.5 + c->impl_thermo_weight, old_hor = 1.0 - cur_hor, cur_ver = 1.0 - c->impl_thermo_weight;
+    for (long i = 0; i < NV; ++i) {
+        long layer = i / VPL, h = i - layer * VPL;
+        if (i < NC || i >= NV - NC) {
+            tend->wind[i] = 0.0;
+        } else if (h >= NC) {
+            tend->wind[i] = old_w * tend->wind[i]
+                            + new_w * (old_hor * f->pgrad_acc_old[i] - cur_hor * (f->pgrad_nl[i] + f->pgrad_l[i])
+                                       + f->pot_vort_tend[i] - 0.5 * f->v_squared_grad[i] + ir->friction_acc[i]);
+        } else {
+            tend->wind[i] = old_w * tend->wind[i]
+                            + new_w * (-cur_ver * (f->pgrad_nl[i] + f->pgrad_l[i]) + f->pot_vort_tend[i]
+                                       - 0.5 * f->v_squared_grad[i] + ir->friction_acc[i] + f->pgrad_condensates_v[i]);
+        }
+    }
+    return 0;
+}
+
+/* src/time_stepping/scalar_tendencies_expl.c:17-181 (diffusion off) */
+int orc_scalar_tendencies_expl(const orc_grid *g, const orc_state *s_old, const orc_state *s, orc_state *tend,
+                               double dt, orc_diag *d, orc_forcings *f, orc_irrev *ir, const orc_config *c,
+                               int rk_step)
+{
+    (void)s_old; (void)dt;
+    double old_w[8], new_w[8];
+    for (int k = 0; k < g->n_const; ++k) {
+        new_w[k] = 1.0;
+        if (rk_step == 1 && k != COND) new_w[k] = 0.5;
+        old_w[k] = 1.0 - new_w[k];
+    }
+    if (c->mass_diff_h || c->temperature_diff_h) return -1;
+    for (int k = 0; k < g->n_const; ++k) {
+        long shift = k * NS, shift_pt = shift;
+        if (g->moisture_on && k == COND + 1) shift_pt = shift - NS;
+        if (k == COND) {
+            orc_scalar_times_vector_h(g, &s->rho[shift], s->wind, d->flux_density);
+            orc_divv_h(g, d->flux_density, d->flux_density_divv);
+        } else {
+            orc_scalar_times_vector_h_upstream(g, &s->rho[shift], s->wind, d->flux_density);
+            orc_divv_h_tracer(g, d->flux_density, &s->rho[shift], s->wind, d->flux_density_divv);
+        }
+        for (long j = 0; j < NS; ++j) {
+            long si = shift + j;
+            tend->rho[si] = old_w[k] * tend->rho[si]
+                            + new_w[k] * (-d->flux_density_divv[j] + ir->mass_diff_tendency[shift + j]
+                                          + ir->phase_trans_rates[shift_pt + j]);
+        }
+        if (k == COND) {
+            for (long j = 0; j < NS; ++j) d->scalar_field_placeholder[j] = s->rhotheta_v[j] / s->rho[shift + j];
+            orc_scalar_times_vector_h(g, d->scalar_field_placeholder, d->flux_density, d->flux_density);
+            orc_divv_h(g, d->flux_density, d->flux_density_divv);
+            for (long j = 0; j < NS; ++j) {
+                tend->rhotheta_v[j] = old_w[k] * tend->rhotheta_v[j]
+                    + new_w[k] * (-d->flux_density_divv[j]
+                                  + C_D_V * s->rho[shift + j] / c_v_mass_weighted_air(g, s, d, j)
+                                        * (ir->heating_diss[j] + ir->temperature_diffusion_heating[j]
+                                           + f->radiation_tendency[j] + ir->phase_trans_heating_rate[j]
+                                           + ir->condensates_sediment_heat[j])
+                                        / (C_D_P * (g->exner_bg[j] + s->exner_pert[j]))
+                                  + (ir->phase_trans_rates[shift + j] + ir->mass_diff_tendency[shift + j])
+                                        * d->scalar_field_placeholder[j]);
+            }
+        }
+    }
+    return 0;
+}
+
+/* --------------------------------------------------------- column solvers
+ * src/time_stepping/column_solvers.c */
+static void thomas(const double *cv, const double *dv, const double *ev, const double *rv, double *x, int n)
+{
+    /* :641-669 */
+    double ep[64], rp[64];
+    ep[0] = ev[0] / dv[0];
+    for (int j = 1; j < n - 1; ++j) ep[j] = ev[j] / (dv[j] - ep[j - 1] * cv[j - 1]);
+    rp[0] = rv[0] / dv[0];
+    for (int j = 1; j < n; ++j) rp[j] = (rv[j] - rp[j - 1] * cv[j - 1]) / (dv[j] - ep[j - 1] * cv[j - 1]);
+    x[n - 1] = rp[n - 1];
+    for (int j = n - 2; j >= 0; --j) x[j] = rp[j] - ep[j] * x[j + 1];
+}
+
+int orc_three_band_solver_ver_waves(const orc_grid *g, const orc_state *so, orc_state *sn, const orc_state *st,
+                                    const orc_config *c, double dt, int rk_step)
+{
+    /* :19-383 (sensible heat flux and soil off) */
+    if (c->sfc_sensible_heat_flux || c->prog_soil_temp) return -1;
+    if (NL > 64) return -2;
+    const double iw = c->impl_thermo_weight;
+    const double damp_start = c->damping_start_height_over_toa * g->z_vector[0];
+    const double pdw = 0.5;
+    const long gp = COND * NS;
+    for (long i = 0; i < NC; ++i) {
+        double cvec[64], dvec[64], evec[64], rvec[64], rho_expl[64], rt_expl[64], tp_expl[64], ep_expl[64];
+        double th_int[64], sol[64], rho_io[64], rho_ie[64], alpha[64], beta[64], gam[64];
+        for (long j = 0; j < NL; ++j) {
+            long b = i + j * NC;
+            rho_expl[j] = so->rho[gp + b] + dt * st->rho[gp + b];
+            rt_expl[j] = so->rhotheta_v[b] + dt * st->rhotheta_v[b];
+            if (rk_step == 0) {
+                alpha[j] = -so->rhotheta_v[b] / pow(so->rho[gp + b], 2) / g->volume[b];
+                beta[j] = 1.0 / so->rho[gp + b] / g->volume[b];
+                gam[j] = R_D / (C_D_V * so->rhotheta_v[b]) * (g->exner_bg[b] + so->exner_pert[b]) / g->volume[b];
+            } else {
+                double ao = -so->rhotheta_v[b] / pow(so->rho[gp + b], 2);
+                double bo = 1.0 / so->rho[gp + b];
+                double go = R_D / (C_D_V * so->rhotheta_v[b]) * (g->exner_bg[b] + so->exner_pert[b]);
+                double an = -sn->rhotheta_v[b] / pow(sn->rho[gp + b], 2);
+                double bn = 1.0 / sn->rho[gp + b];
+                double gn = R_D / (C_D_V * sn->rhotheta_v[b]) * (g->exner_bg[b] + sn->exner_pert[b]);
+                alpha[j] = ((1.0 - pdw) * ao + pdw * an) / g->volume[b];
+                beta[j] = ((1.0 - pdw) * bo + pdw * bn) / g->volume[b];
+                gam[j] = ((1.0 - pdw) * go + pdw * gn) / g->volume[b];
+            }
+            tp_expl[j] = so->theta_v_pert[b] + dt * g->volume[b] * (alpha[j] * st->rho[gp + b] + beta[j] * st->rhotheta_v[b]);
+            ep_expl[j] = so->exner_pert[b] + dt * g->volume[b] * gam[j] * st->rhotheta_v[b];
+        }
+        for (long j = 0; j < NL - 1; ++j) {
+            long b = i + j * NC, lo = i + (j + 1) * NC;
+            rho_io[j] = 0.5 * (so->rho[gp + b] + so->rho[gp + lo]);
+            rho_ie[j] = 0.5 * (rho_expl[j] + rho_expl[j + 1]);
+            th_int[j] = 0.5 * (sn->rhotheta_v[b] / sn->rho[gp + b] + sn->rhotheta_v[lo] / sn->rho[gp + lo]);
+        }
+        for (long j = 0; j < NL - 1; ++j) {
+            long b = i + j * NC, lo = i + (j + 1) * NC, wi = i + (j + 1) * VPL;
+            dvec[j] = -pow(th_int[j], 2) * (gam[j] + gam[j + 1])
+                      + 0.5 * (g->exner_bg[b] - g->exner_bg[lo]) * (alpha[j + 1] - alpha[j] + th_int[j] * (beta[j + 1] - beta[j]))
+                      - (g->z_scalar[b] - g->z_scalar[lo]) / (iw * pow(dt, 2) * C_D_P * rho_io[j])
+                            * (2.0 / g->area[wi] + dt * so->wind[wi] * 0.5 * (-1.0 / g->volume[b] + 1.0 / g->volume[lo]));
+            rvec[j] = -(so->wind[wi] + dt * st->wind[wi]) * (g->z_scalar[b] - g->z_scalar[lo]) / (iw * pow(dt, 2) * C_D_P)
+                      + th_int[j] * (ep_expl[j] - ep_expl[j + 1]) / dt
+                      + 0.5 / dt * (tp_expl[j] + tp_expl[j + 1]) * (g->exner_bg[b] - g->exner_bg[lo])
+                      - (g->z_scalar[b] - g->z_scalar[lo]) / (iw * pow(dt, 2) * C_D_P) * so->wind[wi] * rho_ie[j] / rho_io[j];
+        }
+        for (long j = 0; j < NL - 2; ++j) {
+            long b = i + j * NC, lo = i + (j + 1) * NC, lo2 = (j + 2) * NC + i;
+            cvec[j] = th_int[j + 1] * gam[j + 1] * th_int[j]
+                      + 0.5 * (g->exner_bg[lo] - g->exner_bg[lo2]) * (alpha[j + 1] + beta[j + 1] * th_int[j])
+                      - (g->z_scalar[lo] - g->z_scalar[lo2]) / (iw * dt * C_D_P) * 0.5 * so->wind[i + (j + 2) * VPL]
+                            / (g->volume[lo] * rho_io[j + 1]);
+            evec[j] = th_int[j] * gam[j + 1] * th_int[j + 1]
+                      - 0.5 * (g->exner_bg[b] - g->exner_bg[lo]) * (alpha[j + 1] + beta[j + 1] * th_int[j + 1])
+                      + (g->z_scalar[b] - g->z_scalar[lo]) / (iw * dt * C_D_P) * 0.5 * so->wind[i + (j + 1) * VPL]
+                            / (g->volume[lo] * rho_io[j]);
+        }
+        thomas(cvec, dvec, evec, rvec, sol, (int)NL - 1);
+        for (long j = 0; j < NL - 1; ++j) {
+            double zad = g->z_vector[i + (j + 1) * VPL] - damp_start, dc;
+            if (zad < 0.0) dc = 0.0;
+            else dc = c->damping_coeff_max * pow(sin(0.5 * M_PI * zad / (g->z_vector[0] - damp_start)), 2);
+            sol[j] = sol[j] / (1.0 + dt * dc);
+        }
+        for (long j = 0; j < NL; ++j) {
+            long b = i + j * NC;
+            if (j == 0) sn->rho[gp + b] = rho_expl[j] + dt * (sol[j]) / g->volume[b];
+            else if (j == NL - 1) sn->rho[gp + b] = rho_expl[j] + dt * (-sol[j - 1]) / g->volume[b];
+            else sn->rho[gp + b] = rho_expl[j] + dt * (-sol[j - 1] + sol[j]) / g->volume[b];
+        }
+        for (long j = 0; j < NL; ++j) {
+            long b = i + j * NC;
+            if (j == 0) sn->rhotheta_v[b] = rt_expl[j] + dt * (th_int[j] * sol[j]) / g->volume[b];
+            else if (j == NL - 1) sn->rhotheta_v[b] = rt_expl[j] + dt * (-th_int[j - 1] * sol[j - 1]) / g->volume[b];
+            else sn->rhotheta_v[b] = rt_expl[j] + dt * (-th_int[j - 1] * sol[j - 1] + th_int[j] * sol[j]) / g->volume[b];
+        }
+        for (long j = 0; j < NL - 1; ++j) {
+            long b = i + j * NC, wi = i + (j + 1) * VPL;
+            double dint = 0.5 * (sn->rho[gp + b] + sn->rho[gp + i + (j + 1) * NC]);
+            sn->wind[wi] = (2.0 * sol[j] / g->area[wi] - dint * so->wind[wi]) / rho_io[j];
+        }
+        for (long j = 0; j < NL; ++j) {
+            long b = i + j * NC;
+            sn->theta_v_pert[b] = sn->rhotheta_v[b] / sn->rho[gp + b] - g->theta_v_bg[b];
+        }
+        for (long j = 0; j < NL; ++j) {
+            long b = i + j * NC;
+            sn->exner_pert[b] = so->exner_pert[b] + g->volume[b] * gam[j] * (sn->rhotheta_v[b] - so->rhotheta_v[b]);
+        }
+    }
+    return 0;
+}
+
+int orc_three_band_solver_gen_densities(const orc_grid *g, const orc_state *so, orc_state *sn, const orc_state *st,
+                                        const orc_diag *d, orc_irrev *ir, const orc_config *c, double dt, int rk_step)
+{
+    /* :385-639 */
+    const double iw = 0.5, ew = 1.0 - iw;
+    if (NL > 64) return -2;
+    double *sh = ir->condensates_sediment_heat;
+    for (int k = 0; k < g->n_const; ++k) {
+        if (k == COND) continue;
+        /* sink velocity of the constituent: snow, rain, cloud particles, none for vapour */
+        double vsink = 0.0;
+        int has_sink = 0;
+        if (k < COND / 4) { vsink = c->snow_velocity; has_sink = 1; }
+        else if (k < COND / 2) { vsink = c->rain_velocity; has_sink = 1; }
+        else if (k < COND) { vsink = c->cloud_droplets_velocity; has_sink = 1; }
+        for (long i = 0; i < NC; ++i) {
+            double cvec[64], dvec[64], evec[64], rvec[64], fi[64], fr[64], fe[64], sol[64];
+            for (long j = 0; j < NL - 1; ++j) {
+                if (rk_step == 0 && k == 0) sh[j * NC + i] = 0.0;
+                long b = i + j * NC, lo = i + (j + 1) * NC, up = b;
+                fi[j] = so->wind[i + (j + 1) * VPL];
+                fr[j] = sn->wind[i + (j + 1) * VPL];
+                if (has_sink) { fi[j] -= vsink; fr[j] -= vsink; }
+                double a = g->area[i + (j + 1) * VPL];
+                fi[j] = a * fi[j];
+                fr[j] = a * fr[j];
+                double dio, tio;
+                if (fr[j] >= 0.0) { dio = so->rho[k * NS + lo]; tio = d->temperature[lo]; }
+                else { dio = so->rho[k * NS + up]; tio = d->temperature[up]; }
+                fr[j] = dio * fr[j];
+                fe[j] = c_p_cond(k, tio) * tio * fr[j];
+            }
+            if (rk_step == 0 && k == 0) sh[(NL - 1) * NC + i] = 0.0;
+            for (long j = 0; j < NL - 1; ++j) {
+                long b = i + j * NC;
+                if (fi[j] >= 0.0) { cvec[j] = 0.0; evec[j] = -iw * dt / g->volume[b] * fi[j]; }
+                else { cvec[j] = iw * dt / g->volume[i + (j + 1) * NC] * fi[j]; evec[j] = 0.0; }
+            }
+            const long bot = i + NS - NC;
+            const double a_sfc = g->area[i + NV - NC];
+            for (long j = 0; j < NL; ++j) {
+                long b = i + j * NC;
+                if (j == 0) {
+                    if (fi[0] >= 0.0) dvec[j] = 1.0;
+                    else dvec[j] = 1.0 - iw * dt / g->volume[b] * fi[0];
+                } else if (j == NL - 1) {
+                    if (fi[j - 1] >= 0.0) dvec[j] = 1.0 + iw * dt / g->volume[b] * fi[j - 1];
+                    else dvec[j] = 1.0;
+                    if (has_sink) dvec[j] += iw * vsink * dt * a_sfc / g->volume[b];
+                } else {
+                    dvec[j] = 1.0;
+                    if (fi[j - 1] >= 0.0) dvec[j] += iw * dt / g->volume[b] * fi[j - 1];
+                    if (fi[j] < 0.0) dvec[j] -= iw * dt / g->volume[b] * fi[j];
+                }
+                rvec[j] = so->rho[k * NS + b] + dt * st->rho[k * NS + b];
+                if (j == 0) {
+                    rvec[j] += ew * dt * fr[j] / g->volume[b];
+                    if (rk_step == 0 && k < COND) sh[b] += fe[j] / g->volume[b];
+                } else if (j == NL - 1) {
+                    rvec[j] += -ew * dt * fr[j - 1] / g->volume[b];
+                    if (rk_step == 0 && k < COND) sh[b] += -fe[j - 1] / g->volume[b];
+                    if (has_sink) {
+                        rvec[j] += -ew * vsink * dt * so->rho[k * NS + bot] * a_sfc / g->volume[b];
+                        if (rk_step == 0)
+                            sh[b] += -vsink * d->temperature[bot] * c_p_cond(k, d->temperature[bot])
+                                     * so->rho[k * NS + bot] * a_sfc / g->volume[b];
+                    }
+                } else {
+                    rvec[j] += ew * dt * (-fr[j - 1] + fr[j]) / g->volume[b];
+                    if (rk_step == 0 && k < COND) sh[b] += (-fe[j - 1] + fe[j]) / g->volume[b];
+                }
+            }
+            thomas(cvec, dvec, evec, rvec, sol, (int)NL);
+            for (long j = 0; j < NL; ++j) if (sol[j] < 0.0) sol[j] = 0.0;
+            for (long j = 0; j < NL; ++j) sn->rho[k * NS + i + j * NC] = sol[j];
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ step
+ * src/time_stepping/manage_rkhevi.c:20-100 */
+int orc_manage_rkhevi(const orc_grid *g, const orc_state *so, orc_state *sn, orc_state *st, orc_diag *d,
+                      orc_forcings *f, orc_irrev *ir, const orc_config *c, double dt, double t)
+{
+    (void)t;
+    if (c->sfc_sensible_heat_flux || c->sfc_phase_trans || c->pbl_scheme || c->rad_on || c->momentum_diff_h
+        || c->momentum_diff_v || c->mass_diff_h || c->temperature_diff_h || c->prog_soil_temp)
+        return -1;
+    orc_temperature_diagnostics(g, so, d);
+    if (g->moisture_on) orc_calc_h2otracers_source_rates(g, so, d, c, ir, dt);
+    for (int rk = 0; rk < 2; ++rk) {
+        if (rk == 0) orc_manage_pressure_gradient(g, sn, d, f, ir, c);
+        orc_calc_pressure_grad_condensates_v(g, sn, f, ir);
+        orc_vector_tendencies_expl(g, sn, st, d, f, ir, c, rk, dt);
+        for (long e = 0; e < NE; ++e)
+            for (long l = 0; l < NL; ++l) {
+                long vi = NC + l * VPL + e;
+                sn->wind[vi] = so->wind[vi] + dt * st->wind[vi];
+            }
+        if (orc_scalar_tendencies_expl(g, so, sn, st, dt, d, f, ir, c, rk)) return -1;
+        if (orc_three_band_solver_ver_waves(g, so, sn, st, c, dt, rk)) return -1;
+        if (g->n_const > 1) orc_three_band_solver_gen_densities(g, so, sn, st, d, ir, c, dt, rk);
+    }
+    return 0;
+}
+
+/* --------------------------------------------------------------- metrics */
+double orc_global_scalar_integrator(const orc_grid *g, const double *field)
+{
+    /* src/io/write_output.c:1659-1668 (serial sum, kept in its order) */
+    double r = 0.0;
+    for (long i = 0; i < NS; ++i) r += field[i] * g->volume[i];
+    return r;
+}
+
+int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *temperature, double *p_sfc)
+{
+    /* src/io/write_output.c:105-121 with gas_constant_diagnostics
+     * (src/constituents/derived_quantities.c:42-61) */
+    const double lapse = 0.0065;
+    for (long i = 0; i < NC; ++i) {
+        long si = (NL - 1) * NC + i;
+        double rgas;
+        if (!g->moisture_on) rgas = R_D;
+        else {
+            rgas = (s->rho[COND * NS + si] - s->rho[(COND + 1) * NS + si]) * R_D + s->rho[(COND + 1) * NS + si] * R_V;
+            rgas = rgas / s->rho[COND * NS + si];
+        }
+        double t_low = temperature[si];
+        double p = s->rho[COND * NS + si] * rgas * t_low;
+        double t_sfc = t_low + lapse * (g->z_scalar[i + (NL - 1) * NC] - g->z_vector[NV - NC + i]);
+        double fac = pow(1.0 - (t_sfc - t_low) / t_sfc, g->gravity_m[(NL - 1) * VPL + i] / (rgas * lapse));
+        p_sfc[i] = p / fac;
+    }
+    return 0;
+}

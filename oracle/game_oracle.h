@@ -1,0 +1,104 @@
+/*
+ * ORACLE -- test infrastructure only.  Never linked into, loaded by or called
+ * from the product path (libgame_gb300.so); only tests/, the smoke check and
+ * the CPU-baseline arm of bench.py use it, as the checker.
+ *
+ * A CPU restatement, in plain C99 with run-time grid sizes, of GAME's RKHEVI
+ * step (MHBalsmeier/GAME_archived, src/time_stepping/manage_rkhevi.c:20-100)
+ * and of every operator it calls.  Each function cites the reference lines it
+ * follows and keeps the reference's order of floating-point operations, so
+ * that, compiled with -ffp-contract=off, it reproduces the reference's own
+ * results bit for bit (pinned by tests/test_oracle_vs_reference.py against the
+ * reference compiled from its sources, and by the fixtures in tests/golden/).
+ *
+ * Arrays use the reference layout: Scalar_field [layer][cell], Vector_field
+ * level blocks of (NO_OF_SCALARS_H vertical | NO_OF_VECTORS_H horizontal),
+ * Curl_field level blocks of (edges | rhombi), Dual_vector_field level blocks
+ * of (edges | triangles).
+ */
+#ifndef GAME_ORACLE_H
+#define GAME_ORACLE_H
+
+typedef struct orc_grid {
+    int nc, ne, nt, nl, n_oro, moisture_on, n_const, n_cond;
+    double radius;
+    const double *normal_distance, *volume, *area, *z_scalar, *z_vector, *gravity_m, *slope;
+    const double *theta_v_bg, *exner_bg, *exner_bg_grad, *ipw, *trsk_weights, *rhombi_weights;
+    const int *trsk_indices, *trsk_mci, *from, *to, *adj, *adj_sign, *rhombi_idx, *is_land;
+    const double *dual_area, *dual_z_vector, *f_vec;
+    const int *dual_from, *dual_to, *vort_idx, *vort_sign;
+    const double *gravity_potential; /* only the output metrics use it */
+} orc_grid;
+
+typedef struct orc_state {
+    double *rho, *rhotheta_v, *theta_v_pert, *exner_pert, *wind;
+} orc_state;
+
+typedef struct orc_diag {
+    double *flux_density, *flux_density_divv, *rel_vort_on_triangles, *rel_vort, *pot_vort;
+    double *temperature, *v_squared, *scalar_field_placeholder;
+} orc_diag;
+
+typedef struct orc_forcings {
+    double *pgrad_acc_old, *pgrad_nl, *pgrad_l, *pgrad_condensates_v, *v_squared_grad, *pot_vort_tend;
+    double *radiation_tendency;
+} orc_forcings;
+
+typedef struct orc_irrev {
+    double *temperature_diffusion_heating, *friction_acc, *heating_diss, *pressure_gradient_decel_factor;
+    double *condensates_sediment_heat, *mass_diff_tendency, *phase_trans_rates, *phase_trans_heating_rate;
+} orc_irrev;
+
+typedef struct orc_config {
+    int totally_first_step_bool, temperature_diff_h, temperature_diff_v, momentum_diff_h, momentum_diff_v;
+    int mass_diff_h, mass_diff_v, rad_on, prog_soil_temp, sfc_phase_trans, sfc_sensible_heat_flux;
+    int rad_update, time_to_next_analysis, pbl_scheme, total_run_span;
+    double damping_start_height_over_toa, damping_coeff_max, impl_thermo_weight;
+    double cloud_droplets_velocity, rain_velocity, snow_velocity, radiation_delta_t;
+} orc_config;
+
+/* operators (same argument meaning as the reference functions) */
+int orc_grad_hor_cov(const orc_grid *g, const double *in, double *out);
+int orc_grad_vert_cov(const orc_grid *g, const double *in, double *out);
+int orc_grad_cov(const orc_grid *g, const double *in, double *out);
+int orc_grad(const orc_grid *g, const double *in, double *out);
+int orc_grad_hor(const orc_grid *g, const double *in, double *out);
+int orc_vector_field_hor_cov_to_con(const orc_grid *g, double *f);
+int orc_divv_h(const orc_grid *g, const double *in, double *out);
+int orc_divv_h_tracer(const orc_grid *g, const double *in, const double *density, const double *wind, double *out);
+int orc_scalar_times_vector(const orc_grid *g, const double *s, const double *v, double *out);
+int orc_scalar_times_vector_h(const orc_grid *g, const double *s, const double *v, double *out);
+int orc_scalar_times_vector_h_upstream(const orc_grid *g, const double *s, const double *v, double *out);
+int orc_scalar_times_vector_v(const orc_grid *g, const double *s, const double *v, double *out);
+int orc_inner_product(const orc_grid *g, const double *a, const double *b, double *out);
+int orc_calc_rel_vort_on_triangles(const orc_grid *g, const double *wind, double *out);
+int orc_calc_rel_vort(const orc_grid *g, const double *wind, orc_diag *d);
+int orc_add_f_to_rel_vort(const orc_grid *g, const double *rel, double *out);
+int orc_calc_pot_vort(const orc_grid *g, const double *wind, const double *density, orc_diag *d);
+int orc_vorticity_flux(const orc_grid *g, const double *flux, const double *pot_vort, double *out);
+int orc_linear_combine_two_states(const orc_grid *g, const orc_state *s0, const orc_state *s1, orc_state *out,
+                                  double c0, double c1);
+int orc_temperature_diagnostics(const orc_grid *g, const orc_state *s, orc_diag *d);
+int orc_calc_h2otracers_source_rates(const orc_grid *g, const orc_state *s, orc_diag *d, const orc_config *c,
+                                     orc_irrev *ir, double dt);
+int orc_manage_pressure_gradient(const orc_grid *g, const orc_state *s, orc_diag *d, orc_forcings *f,
+                                 orc_irrev *ir, const orc_config *c);
+int orc_calc_pressure_grad_condensates_v(const orc_grid *g, const orc_state *s, orc_forcings *f, orc_irrev *ir);
+int orc_vector_tendencies_expl(const orc_grid *g, const orc_state *s, orc_state *tend, orc_diag *d,
+                               orc_forcings *f, orc_irrev *ir, const orc_config *c, int rk_step, double dt);
+int orc_scalar_tendencies_expl(const orc_grid *g, const orc_state *s_old, const orc_state *s, orc_state *tend,
+                               double dt, orc_diag *d, orc_forcings *f, orc_irrev *ir, const orc_config *c,
+                               int rk_step);
+int orc_three_band_solver_ver_waves(const orc_grid *g, const orc_state *s_old, orc_state *s_new,
+                                    const orc_state *tend, const orc_config *c, double dt, int rk_step);
+int orc_three_band_solver_gen_densities(const orc_grid *g, const orc_state *s_old, orc_state *s_new,
+                                        const orc_state *tend, const orc_diag *d, orc_irrev *ir,
+                                        const orc_config *c, double dt, int rk_step);
+int orc_manage_rkhevi(const orc_grid *g, const orc_state *s_old, orc_state *s_new, orc_state *tend,
+                      orc_diag *d, orc_forcings *f, orc_irrev *ir, const orc_config *c, double dt, double t);
+
+/* output metrics (src/io/write_output.c:105-121, 1515-1668) */
+double orc_global_scalar_integrator(const orc_grid *g, const double *field);
+int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *temperature, double *p_sfc);
+
+#endif
