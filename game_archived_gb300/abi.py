@@ -1,0 +1,161 @@
+"""ctypes declarations of include/game_gb300.h and a thin host-side wrapper.
+
+``GpuModel`` binds the C library to one ``structs.Model`` (host structs in the
+reference layout) and exposes the reference's calls with the reference's
+argument meaning, so tests and the benchmark drive the library exactly as the
+reference's own driver (src/coordinator.c) would.
+"""
+import ctypes
+
+from . import native
+
+vp, dbl, cint = ctypes.c_void_p, ctypes.c_double, ctypes.c_int
+
+SIGNATURES = {
+    "game_gpu_init": ([cint, cint, cint, vp, vp], cint),
+    "game_gpu_finalize": ([], cint),
+    "game_gpu_set_precision": ([cint], cint),
+    "game_gpu_set_resident": ([cint], cint),
+    "game_gpu_set_graphs": ([cint], cint),
+    "game_gpu_sync_to_device": ([vp], cint),
+    "game_gpu_sync_to_host": ([vp], cint),
+    "game_gpu_sync_aux_to_host": ([vp, vp, vp], cint),
+    "game_gpu_synchronize": ([], cint),
+    "game_gpu_last_error": ([], ctypes.c_char_p),
+    "game_gpu_host_alloc": ([ctypes.POINTER(vp), ctypes.c_size_t], cint),
+    "game_gpu_host_free": ([vp], cint),
+    "game_gpu_kernel_launches": ([cint], ctypes.c_longlong),
+    "manage_rkhevi": ([vp] * 9 + [dbl, dbl], cint),
+    "linear_combine_two_states": ([vp, vp, vp, dbl, dbl, vp], cint),
+    "grad_hor_cov": ([vp] * 3, cint),
+    "grad_vert_cov": ([vp] * 3, cint),
+    "vector_field_hor_cov_to_con": ([vp] * 2, cint),
+    "grad_cov": ([vp] * 3, cint),
+    "grad": ([vp] * 3, cint),
+    "grad_hor": ([vp] * 3, cint),
+    "calc_pot_vort": ([vp] * 5, cint),
+    "add_f_to_rel_vort": ([vp] * 3, cint),
+    "calc_rel_vort": ([vp] * 4, cint),
+    "vorticity_flux": ([vp] * 5, cint),
+    "divv_h": ([vp] * 3, cint),
+    "divv_h_tracer": ([vp] * 5, cint),
+    "scalar_times_vector": ([vp] * 4, cint),
+    "scalar_times_vector_h": ([vp] * 4, cint),
+    "scalar_times_vector_h_upstream": ([vp] * 4, cint),
+    "scalar_times_vector_v": ([vp] * 4, cint),
+    "inner_product": ([vp] * 4, cint),
+}
+
+FP64, MIXED = 0, 1
+
+
+def declare(lib):
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class GpuError(RuntimeError):
+    pass
+
+
+class GpuModel:
+    """The CUDA library bound to a Model."""
+
+    def __init__(self, model, precision=FP64, resident=False, graphs=True):
+        self.lib = native.gpu()
+        self.m = model
+        lay = model.layout
+        self._check(self.lib.game_gpu_init(lay.res_id, lay.n_layers, lay.moisture_on, model.grid.ptr,
+                                           model.dualgrid.ptr), "game_gpu_init")
+        self._check(self.lib.game_gpu_set_precision(precision), "set_precision")
+        self._check(self.lib.game_gpu_set_resident(1 if resident else 0), "set_resident")
+        self._check(self.lib.game_gpu_set_graphs(1 if graphs else 0), "set_graphs")
+        self.resident = resident
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise GpuError(f"{what}: {self.lib.game_gpu_last_error().decode()}")
+
+    def close(self):
+        self.lib.game_gpu_finalize()
+
+    # -- the reference's calls
+    def manage_rkhevi(self, dt, t=0.0):
+        m = self.m
+        self._check(self.lib.manage_rkhevi(m.state_old.ptr, m.state_new.ptr, m.grid.ptr, m.dualgrid.ptr,
+                                           m.state_tendency.ptr, m.diagnostics.ptr, m.forcings.ptr, m.irrev.ptr,
+                                           m.config.ptr, dt, t), "manage_rkhevi")
+
+    def linear_combine_two_states(self, s0, s1, out, c0, c1):
+        self._check(self.lib.linear_combine_two_states(s0.ptr, s1.ptr, out.ptr, c0, c1, self.m.grid.ptr),
+                    "linear_combine_two_states")
+
+    def sync_to_device(self, s):
+        self._check(self.lib.game_gpu_sync_to_device(s.ptr), "sync_to_device")
+
+    def sync_to_host(self, s):
+        self._check(self.lib.game_gpu_sync_to_host(s.ptr), "sync_to_host")
+
+    def sync_aux_to_host(self):
+        m = self.m
+        self._check(self.lib.game_gpu_sync_aux_to_host(m.diagnostics.ptr, m.forcings.ptr, m.irrev.ptr), "sync_aux")
+
+    def synchronize(self):
+        self._check(self.lib.game_gpu_synchronize(), "synchronize")
+
+    def kernel_launches(self, reset=False):
+        return int(self.lib.game_gpu_kernel_launches(1 if reset else 0))
+
+    # -- single operators on host arrays
+    def grad(self, s, out):
+        self._check(self.lib.grad(_p(s), _p(out), self.m.grid.ptr), "grad")
+
+    def divv_h(self, v, out):
+        self._check(self.lib.divv_h(_p(v), _p(out), self.m.grid.ptr), "divv_h")
+
+    def divv_h_tracer(self, v, dens, wind, out):
+        self._check(self.lib.divv_h_tracer(_p(v), _p(dens), _p(wind), _p(out), self.m.grid.ptr), "divv_h_tracer")
+
+    def scalar_times_vector(self, s, v, out, variant=""):
+        f = getattr(self.lib, "scalar_times_vector" + variant)
+        self._check(f(_p(s), _p(v), _p(out), self.m.grid.ptr), "scalar_times_vector" + variant)
+
+    def inner_product(self, a, b, out):
+        self._check(self.lib.inner_product(_p(a), _p(b), _p(out), self.m.grid.ptr), "inner_product")
+
+    def calc_pot_vort(self, wind, rho):
+        m = self.m
+        self._check(self.lib.calc_pot_vort(_p(wind), _p(rho), m.diagnostics.ptr, m.grid.ptr, m.dualgrid.ptr),
+                    "calc_pot_vort")
+
+    def vorticity_flux(self, flux, pv, out):
+        m = self.m
+        self._check(self.lib.vorticity_flux(_p(flux), _p(pv), _p(out), m.grid.ptr, m.dualgrid.ptr), "vorticity_flux")
+
+
+def pinned_model(layout):
+    """A Model whose structs live in pinned host memory (fast asynchronous
+    copies), allocated through the library."""
+    from .structs import Model
+    lib = native.gpu()
+    bufs = {}
+    keep = []
+    for k in Model.KINDS:
+        kind = "state" if k.startswith("state") else k
+        size = layout.sizes[kind]
+        p = ctypes.c_void_p()
+        if lib.game_gpu_host_alloc(ctypes.byref(p), size) != 0:
+            raise GpuError(lib.game_gpu_last_error().decode())
+        arr = (ctypes.c_uint8 * size).from_address(p.value)
+        keep.append(p)
+        import numpy as np
+        bufs[k] = np.frombuffer(arr, dtype=np.uint8)
+    m = Model(layout, bufs)
+    m._pinned = keep
+    return m

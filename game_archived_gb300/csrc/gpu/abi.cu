@@ -1,0 +1,514 @@
+/*
+ * extern "C" entry points of include/game_gb300.h.
+ */
+#include <cstring>
+#include <string>
+
+#include "context.h"
+#include "game_gb300.h"
+#include "ops.h"
+
+using namespace game;
+
+/* implemented in aux.cu */
+namespace game {
+void aux_sum_to_work(Context *c, const double *nl, const double *l, const double *pvt, const double *v2g,
+                     const double *flux, const double *, const double *);
+int aux_export(Context *c, double *P, double *pvt, double *v2g);
+}  // namespace game
+
+namespace {
+
+struct Bound {
+    const void *grid = nullptr, *dualgrid = nullptr;
+    const void *aux_diag = nullptr, *aux_forc = nullptr, *aux_irrev = nullptr;
+} g_bound;
+
+size_t off(int sid, const char *name) { return game_layout_offset(&ctx()->dims, sid, name); }
+template <typename T>
+T *member(const void *base, int sid, const char *name)
+{
+    return (T *)((char *)base + off(sid, name));
+}
+
+int check_ready(const void *grid)
+{
+    if (!ctx()) return fail("game_gpu_init has not been called");
+    if (grid && grid != g_bound.grid) return fail("grid pointer differs from the one given to game_gpu_init");
+    return 0;
+}
+
+int finish()
+{
+    Context *c = ctx();
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fail(std::string("CUDA error: ") + cudaGetErrorString(e));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(std::string("CUDA error: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+/* device-layout offsets inside a scratch vector / curl field */
+double *vec_w(double *v) { return v; }
+
+StepParams params_from_config(Context *c, const void *config, double dt)
+{
+    StepParams p{};
+    p.n_const = c->n_const;
+    p.n_cond = c->n_cond;
+    p.moist = c->moist;
+    p.dt = dt;
+    p.impl_thermo_weight = *member<double>(config, GAME_CONFIG, "impl_thermo_weight");
+    p.damping_start_height = *member<double>(config, GAME_CONFIG, "damping_start_height_over_toa") * c->toa;
+    p.damping_coeff_max = *member<double>(config, GAME_CONFIG, "damping_coeff_max");
+    p.toa = c->toa;
+    p.snow_velocity = *member<double>(config, GAME_CONFIG, "snow_velocity");
+    p.rain_velocity = *member<double>(config, GAME_CONFIG, "rain_velocity");
+    p.cloud_velocity = *member<double>(config, GAME_CONFIG, "cloud_droplets_velocity");
+    p.first_step = *member<int>(config, GAME_CONFIG, "totally_first_step_bool");
+    return p;
+}
+
+int check_config(const void *config)
+{
+    static const char *off_switches[] = {"temperature_diff_h", "temperature_diff_v", "momentum_diff_h", "momentum_diff_v",
+                                         "mass_diff_h", "mass_diff_v", "rad_on", "prog_soil_temp", "sfc_phase_trans",
+                                         "sfc_sensible_heat_flux", "pbl_scheme"};
+    for (const char *s : off_switches)
+        if (*member<int>(config, GAME_CONFIG, s) != 0)
+            return fail(std::string("config switch ") + s + " is on; diffusion, PBL, surface fluxes, soil and radiation are not part of this library's step");
+    return 0;
+}
+
+/* first use of a (diagnostics, forcings, irrev) triple: import the lagged
+ * step fields the reference carries between calls */
+int import_aux(const void *diag, const void *forc, const void *irrev)
+{
+    Context *c = ctx();
+    if (diag == g_bound.aux_diag && forc == g_bound.aux_forc && irrev == g_bound.aux_irrev) return 0;
+    const long long nv = c->nv, ns = c->ns;
+    const long long woff = (long long)(c->nl + 1) * c->nc;
+    double *t0 = c->dev_tmp[0], *t1 = c->dev_tmp[1];
+    /* P = nl + l */
+    if (upload_field(member<double>(forc, GAME_FORCINGS, "pressure_gradient_acc_neg_nl"), t0, c->map_vec, nv, nv)) return -1;
+    if (upload_field(member<double>(forc, GAME_FORCINGS, "pressure_gradient_acc_neg_l"), t1, c->map_vec, nv, nv)) return -1;
+    double *t2 = c->dev_tmp[2], *t3 = c->dev_tmp[3];
+    if (upload_field(member<double>(forc, GAME_FORCINGS, "pot_vort_tend"), t2, c->map_vec, nv, nv)) return -1;
+    if (upload_field(member<double>(forc, GAME_FORCINGS, "v_squared_grad"), t3, c->map_vec, nv, nv)) return -1;
+    /* flux_density: the TOA/surface vertical entries are never written by the step */
+    CK(cudaStreamSynchronize(c->stream));
+    double *fl = nullptr;
+    CK(cudaMalloc(&fl, (size_t)nv * sizeof(double)));
+    if (upload_field(member<double>(diag, GAME_DIAGNOSTICS, "flux_density"), fl, c->map_vec, nv, nv)) return -1;
+    aux_sum_to_work(c, t0, t1, t2, t3, fl, nullptr, nullptr);
+    if (upload_field(member<double>(irrev, GAME_IRREV, "condensates_sediment_heat"), c->sed_heat, c->map_s, ns, ns)) return -1;
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(fl);
+    (void)woff;
+    g_bound.aux_diag = diag;
+    g_bound.aux_forc = forc;
+    g_bound.aux_irrev = irrev;
+    return 0;
+}
+
+long long g_graph_kernels = 0;
+
+int run_device_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st)
+{
+    auto launch = [&]() {
+        return c->precision == PREC_FP64 ? launch_step_f64(c, p, so, sn, st) : launch_step_mixed(c, p, so, sn, st);
+    };
+    if (!c->use_graphs) return launch();
+    Context::GraphKey key{p.first_step, c->precision, p.dt, so, sn, st};
+    auto it = c->graphs.find(key);
+    if (it == c->graphs.end()) {
+        const int before = c->kernel_launches;
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = launch();
+        cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        if (rc) return rc;
+        if (e != cudaSuccess) return fail(std::string("graph capture: ") + cudaGetErrorString(e));
+        cudaGraphExec_t exec;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(std::string("graph instantiate: ") + cudaGetErrorString(e));
+        it = c->graphs.emplace(key, exec).first;
+        g_graph_kernels = c->kernel_launches - before;
+        c->kernel_launches = before;
+    }
+    CK(cudaGraphLaunch(it->second, c->stream));
+    c->kernel_launches += (int)g_graph_kernels;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int game_gpu_init(int res_id, int no_of_layers, int moisture_on, struct grid *grid, struct dualgrid *dualgrid)
+{
+    g_bound = Bound();
+    int rc = init_context(res_id, no_of_layers, moisture_on, grid, dualgrid);
+    if (rc) {
+        destroy_context();
+        return rc;
+    }
+    g_bound.grid = grid;
+    g_bound.dualgrid = dualgrid;
+    return 0;
+}
+
+int game_gpu_finalize(void)
+{
+    g_bound = Bound();
+    return destroy_context();
+}
+
+int game_gpu_set_precision(int precision)
+{
+    if (check_ready(nullptr)) return -1;
+    if (precision != GAME_GPU_FP64 && precision != GAME_GPU_MIXED) return fail("unknown precision");
+    ctx()->precision = precision;
+    return 0;
+}
+
+int game_gpu_set_resident(int resident)
+{
+    if (check_ready(nullptr)) return -1;
+    ctx()->resident = resident ? 1 : 0;
+    return 0;
+}
+
+int game_gpu_set_graphs(int on)
+{
+    if (check_ready(nullptr)) return -1;
+    ctx()->use_graphs = on ? 1 : 0;
+    return 0;
+}
+
+int game_gpu_sync_to_device(struct state *state)
+{
+    if (check_ready(nullptr)) return -1;
+    StateMirror *m = mirror(state, 1);
+    if (!m) return -1;
+    if (upload_state(state, m)) return -1;
+    return finish();
+}
+
+int game_gpu_sync_to_host(struct state *state)
+{
+    if (check_ready(nullptr)) return -1;
+    StateMirror *m = mirror(state, 0);
+    if (!m) return fail("state has no device mirror");
+    if (download_state(state, m, 63)) return -1;
+    return finish();
+}
+
+int game_gpu_sync_aux_to_host(struct diagnostics *diagnostics, struct forcings *forcings,
+                              struct irreversible_quantities *irrev)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    const long long nv = c->nv, ns = c->ns;
+    double *t0 = c->dev_tmp[0], *t1 = c->dev_tmp[1], *t2 = c->dev_tmp[2];
+    CK(cudaMemsetAsync(t0, 0, (size_t)nv * sizeof(double), c->stream));
+    CK(cudaMemsetAsync(t1, 0, (size_t)nv * sizeof(double), c->stream));
+    CK(cudaMemsetAsync(t2, 0, (size_t)nv * sizeof(double), c->stream));
+    if (aux_export(c, t0, t1, t2)) return -1;
+    if (forcings) {
+        double *nl = member<double>(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_nl");
+        double *l = member<double>(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_l");
+        if (download_field(nl, t0, c->map_vec, nv, nv, 0, nv)) return -1;
+        CK(cudaStreamSynchronize(c->stream));
+        memset(l, 0, (size_t)nv * sizeof(double));
+        if (download_field(member<double>(forcings, GAME_FORCINGS, "pot_vort_tend"), t1, c->map_vec, nv, nv, 0, nv)) return -1;
+        CK(cudaStreamSynchronize(c->stream));
+        if (download_field(member<double>(forcings, GAME_FORCINGS, "v_squared_grad"), t2, c->map_vec, nv, nv, 0, nv)) return -1;
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    if (diagnostics) {
+        if (download_field(member<double>(diagnostics, GAME_DIAGNOSTICS, "temperature"), c->temperature, c->map_s, ns, ns,
+                           0, ns)) return -1;
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    if (irrev) {
+        if (download_field(member<double>(irrev, GAME_IRREV, "condensates_sediment_heat"), c->sed_heat, c->map_s, ns,
+                           ns, 0, ns)) return -1;
+        CK(cudaStreamSynchronize(c->stream));
+        if (c->moist) {
+            double *pr = member<double>(irrev, GAME_IRREV, "phase_trans_rates");
+            for (int k = 0; k < 5; ++k) {
+                if (download_field(pr + k * ns, c->pt_rates + k * ns, c->map_s, ns, ns, 0, ns)) return -1;
+                CK(cudaStreamSynchronize(c->stream));
+            }
+            if (download_field(member<double>(irrev, GAME_IRREV, "phase_trans_heating_rate"), c->pt_heat, c->map_s, ns,
+                               ns, 0, ns)) return -1;
+        }
+    }
+    return finish();
+}
+
+int game_gpu_synchronize(void)
+{
+    if (check_ready(nullptr)) return -1;
+    return finish();
+}
+
+const char *game_gpu_last_error(void) { return last_error(); }
+
+int game_gpu_host_alloc(void **ptr, size_t bytes)
+{
+    cudaError_t e = cudaMallocHost(ptr, bytes);
+    if (e != cudaSuccess) return fail(std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    memset(*ptr, 0, bytes);
+    return 0;
+}
+
+int game_gpu_host_free(void *ptr)
+{
+    cudaError_t e = cudaFreeHost(ptr);
+    if (e != cudaSuccess) return fail(std::string("cudaFreeHost: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+long long game_gpu_kernel_launches(int reset)
+{
+    if (!ctx()) return 0;
+    long long n = ctx()->kernel_launches;
+    if (reset) ctx()->kernel_launches = 0;
+    return n;
+}
+
+/* ---------------------------------------------------------------- the step */
+int manage_rkhevi(struct state *state_old, struct state *state_new, struct grid *grid, struct dualgrid *dualgrid,
+                  struct state *state_tendency, struct diagnostics *diagnostics, struct forcings *forcings,
+                  struct irreversible_quantities *irrev, struct config *config, double delta_t,
+                  double time_coordinate)
+{
+    (void)time_coordinate;
+    (void)dualgrid;
+    if (check_ready(grid)) return -1;
+    if (check_config(config)) return -1;
+    Context *c = ctx();
+    StateMirror *so = mirror(state_old, 1), *sn = mirror(state_new, 1), *st = mirror(state_tendency, 1);
+    if (!so || !sn || !st) return -1;
+    if (so == sn || so == st || sn == st) return fail("state_old, state_new and state_tendency must be distinct");
+    if (import_aux(diagnostics, forcings, irrev)) return -1;
+    if (!c->resident) {
+        if (upload_state(state_old, so)) return -1;
+        if (upload_state(state_new, sn)) return -1;
+    }
+    StepParams p = params_from_config(c, config, delta_t);
+    if (run_device_step(c, p, so, sn, st)) return -1;
+    if (!c->resident) {
+        if (download_state(state_new, sn, 1 | 2 | 4 | 8 | 16)) return -1;
+        if (download_state(state_tendency, st, 1 | 2 | 16)) return -1;
+    }
+    return finish();
+}
+
+int linear_combine_two_states(struct state *state_0, struct state *state_1, struct state *state_out, double coeff_0,
+                              double coeff_1, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    StateMirror *a = mirror(state_0, 1), *b = mirror(state_1, 1), *o = mirror(state_out, 1);
+    if (!a || !b || !o) return -1;
+    if (!c->resident) {
+        if (upload_state(state_0, a)) return -1;
+        if (b != a && upload_state(state_1, b)) return -1;
+    }
+    op_linear_combine(c, a, b, o, coeff_0, coeff_1);
+    if (!c->resident && download_state(state_out, o, 63)) return -1;
+    return finish();
+}
+
+/* --------------------------------------------------------- single operators */
+static int vec_op_prologue(double *out_field, double *dev_out)
+{
+    /* the output keeps the entries the operator does not write */
+    Context *c = ctx();
+    return upload_field(out_field, dev_out, c->map_vec, c->nv, c->nv);
+}
+
+static int grad_parts(double *in_field, double *out_field, struct grid *grid, int parts)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *f = c->dev_tmp[0], *v = c->dev_tmp[1];
+    if (upload_field(in_field, f, c->map_s, c->ns, c->ns)) return -1;
+    if (vec_op_prologue(out_field, v)) return -1;
+    op_grad(c, f, v, parts);
+    if (download_field(out_field, v, c->map_vec, c->nv, c->nv, 0, c->nv)) return -1;
+    return finish();
+}
+
+int grad_hor_cov(double *in_field, double *out_field, struct grid *grid)
+{
+    return grad_parts(in_field, out_field, grid, OP_GRAD_H);
+}
+int grad_vert_cov(double *in_field, double *out_field, struct grid *grid)
+{
+    return grad_parts(in_field, out_field, grid, OP_GRAD_V);
+}
+int grad_cov(double *in_field, double *out_field, struct grid *grid)
+{
+    return grad_parts(in_field, out_field, grid, OP_GRAD_H | OP_GRAD_V);
+}
+int grad(double *in_field, double *out_field, struct grid *grid)
+{
+    return grad_parts(in_field, out_field, grid, OP_GRAD_H | OP_GRAD_V | OP_GRAD_CON);
+}
+int grad_hor(double *in_field, double *out_field, struct grid *grid)
+{
+    if (grad(in_field, out_field, grid)) return -1;
+    /* gradient_operators.c:76-91: vertical components set to zero */
+    Context *c = ctx();
+    const long long vpl = (long long)c->nc + c->ne;
+    for (int k = 0; k <= c->nl; ++k) memset(out_field + k * vpl, 0, (size_t)c->nc * sizeof(double));
+    return 0;
+}
+
+int vector_field_hor_cov_to_con(double *field, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *v = c->dev_tmp[1];
+    if (upload_field(field, v, c->map_vec, c->nv, c->nv)) return -1;
+    op_cov_to_con(c, v);
+    if (download_field(field, v, c->map_vec, c->nv, c->nv, 0, c->nv)) return -1;
+    return finish();
+}
+
+static int stv(double *s, double *vec, double *out, struct grid *grid, int parts)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *fs = c->dev_tmp[0], *fv = c->dev_tmp[1], *fo = c->dev_tmp[2];
+    if (upload_field(s, fs, c->map_s, c->ns, c->ns)) return -1;
+    if (upload_field(vec, fv, c->map_vec, c->nv, c->nv)) return -1;
+    if (vec_op_prologue(out, fo)) return -1;
+    op_scalar_times_vector(c, fs, fv, fo, parts);
+    if (download_field(out, fo, c->map_vec, c->nv, c->nv, 0, c->nv)) return -1;
+    return finish();
+}
+
+int scalar_times_vector(double *scalar_field, double *vector_field, double *out_field, struct grid *grid)
+{
+    return stv(scalar_field, vector_field, out_field, grid, OP_STV_H | OP_STV_V);
+}
+int scalar_times_vector_h(double *in_field_h, double *vector_field, double *out_field, struct grid *grid)
+{
+    return stv(in_field_h, vector_field, out_field, grid, OP_STV_H);
+}
+int scalar_times_vector_h_upstream(double *in_field_h, double *vector_field, double *out_field, struct grid *grid)
+{
+    return stv(in_field_h, vector_field, out_field, grid, OP_STV_H | OP_STV_UPSTREAM);
+}
+int scalar_times_vector_v(double *in_field_v, double *vector_field, double *out_field, struct grid *grid)
+{
+    return stv(in_field_v, vector_field, out_field, grid, OP_STV_V);
+}
+
+int divv_h(double *in_field, double *out_field, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *fv = c->dev_tmp[1], *fo = c->dev_tmp[0];
+    if (upload_field(in_field, fv, c->map_vec, c->nv, c->nv)) return -1;
+    op_divv(c, fv, nullptr, nullptr, fo, 0);
+    if (download_field(out_field, fo, c->map_s, c->ns, c->ns, 0, c->ns)) return -1;
+    return finish();
+}
+
+int divv_h_tracer(double *in_field, double *density_field, double *wind_field, double *out_field, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *fv = c->dev_tmp[1], *fd = c->dev_tmp[0], *fw = c->dev_tmp[2], *fo = c->dev_tmp[3];
+    if (upload_field(in_field, fv, c->map_vec, c->nv, c->nv)) return -1;
+    if (upload_field(density_field, fd, c->map_s, c->ns, c->ns)) return -1;
+    if (upload_field(wind_field, fw, c->map_vec, c->nv, c->nv)) return -1;
+    op_divv(c, fv, fd, fw, fo, 1);
+    if (download_field(out_field, fo, c->map_s, c->ns, c->ns, 0, c->ns)) return -1;
+    return finish();
+}
+
+int inner_product(double *in_field_0, double *in_field_1, double *out_field, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *a = c->dev_tmp[1], *b = c->dev_tmp[2], *o = c->dev_tmp[0];
+    if (upload_field(in_field_0, a, c->map_vec, c->nv, c->nv)) return -1;
+    if (upload_field(in_field_1, b, c->map_vec, c->nv, c->nv)) return -1;
+    op_inner_product(c, a, b, o);
+    if (download_field(out_field, o, c->map_s, c->ns, c->ns, 0, c->ns)) return -1;
+    return finish();
+}
+
+static int rel_vort_common(double *velocity_field, double *density_field, struct diagnostics *diagnostics,
+                           struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    const long long ntri = (long long)c->nl * c->nt;
+    double *wind = c->dev_tmp[0], *rel = c->dev_tmp[1], *tri = c->dev_tmp[2], *pv = c->dev_tmp[3];
+    if (upload_field(velocity_field, wind, c->map_vec, c->nv, c->nv)) return -1;
+    op_rel_vort(c, wind, tri, rel);
+    if (download_field(member<double>(diagnostics, GAME_DIAGNOSTICS, "rel_vort_on_triangles"), tri, c->map_tri, ntri,
+                       ntri, 0, ntri)) return -1;
+    CK(cudaStreamSynchronize(c->stream));
+    if (download_field(member<double>(diagnostics, GAME_DIAGNOSTICS, "rel_vort"), rel, c->map_curl, c->ncurl,
+                       c->ncurl, 0, c->ncurl)) return -1;
+    if (density_field) {
+        CK(cudaStreamSynchronize(c->stream));
+        double *rho = wind; /* wind no longer needed */
+        if (upload_field(density_field, rho, c->map_s, c->ns, c->ns)) return -1;
+        op_pot_vort(c, rel, rho, pv);
+        if (download_field(member<double>(diagnostics, GAME_DIAGNOSTICS, "pot_vort"), pv, c->map_curl, c->ncurl,
+                           c->ncurl, 0, c->ncurl)) return -1;
+    }
+    return finish();
+}
+
+int calc_rel_vort(double *velocity_field, struct diagnostics *diagnostics, struct grid *grid, struct dualgrid *dualgrid)
+{
+    (void)dualgrid;
+    return rel_vort_common(velocity_field, nullptr, diagnostics, grid);
+}
+
+int calc_pot_vort(double *velocity_field, double *density_field, struct diagnostics *diagnostics, struct grid *grid,
+                  struct dualgrid *dualgrid)
+{
+    (void)dualgrid;
+    return rel_vort_common(velocity_field, density_field, diagnostics, grid);
+}
+
+int add_f_to_rel_vort(double *rel_vort, double *out_field, struct dualgrid *dualgrid)
+{
+    if (check_ready(nullptr)) return -1;
+    if (dualgrid != g_bound.dualgrid) return fail("dualgrid pointer differs from the one given to game_gpu_init");
+    Context *c = ctx();
+    double *rel = c->dev_tmp[1], *pv = c->dev_tmp[3];
+    if (upload_field(rel_vort, rel, c->map_curl, c->ncurl, c->ncurl)) return -1;
+    op_pot_vort(c, rel, nullptr, pv);
+    if (download_field(out_field, pv, c->map_curl, c->ncurl, c->ncurl, 0, c->ncurl)) return -1;
+    return finish();
+}
+
+int vorticity_flux(double *mass_flux_density, double *pot_vorticity, double *out_field, struct grid *grid,
+                   struct dualgrid *dualgrid)
+{
+    (void)dualgrid;
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *fl = c->dev_tmp[0], *pv = c->dev_tmp[1], *o = c->dev_tmp[2];
+    if (upload_field(mass_flux_density, fl, c->map_vec, c->nv, c->nv)) return -1;
+    if (upload_field(pot_vorticity, pv, c->map_curl, c->ncurl, c->ncurl)) return -1;
+    op_vorticity_flux(c, fl, pv, o);
+    if (download_field(out_field, o, c->map_vec, c->nv, c->nv, 0, c->nv)) return -1;
+    return finish();
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+/*
+ * Library context: grid dimensions, struct layout, SFC permutation, device
+ * tables, device mirrors of the caller's State structs and the work arrays
+ * of the step.  One context per process (the reference runs one model per
+ * process, src/coordinator.c:27).
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "devgrid.cuh"
+#include "layout.h"
+
+namespace game {
+
+/* device buffer owned by the context */
+struct DBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+/* precision mode of the step */
+enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+/* work arrays of the step in the horizontal precision R */
+template <typename R>
+struct Work {
+    R *P_h, *P_v;           /* pressure-gradient sum nl + l   [L][Ne], [L+1][Nc] */
+    R *pg_old_h;            /* previous step's pressure gradient, horizontal part */
+    R *pvt_h, *pvt_v;       /* vorticity flux (pot_vort_tend) */
+    R *v2g_h, *v2g_v;       /* kinetic-energy gradient */
+    R *flux_h, *flux_v;     /* mass flux density */
+    R *zh, *zv;             /* potential vorticity: tangential [L+1][Ne], rhombus [L][Ne] */
+    R *tri_vort;            /* [L][Nt] */
+    R *v2;                  /* kinetic energy [L][Nc] */
+};
+
+struct StateMirror {
+    double *dev = nullptr;  /* device layout, (C+3)*S + Vt doubles */
+    DState ds{};
+};
+
+struct Context {
+    game_dims dims{};
+    int nc = 0, ne = 0, nt = 0, nl = 0, n_oro = 0, n_const = 0, n_cond = 0, moist = 0;
+    long long ns = 0, nv = 0, ndv = 0, ncurl = 0, state_len = 0;
+    double radius = 0.0, toa = 0.0;
+    int precision = PREC_FP64;
+    int resident = 0;
+    cudaStream_t stream = nullptr;
+
+    /* host struct offsets (bytes) */
+    size_t off_grid_z_vector = 0;
+    size_t off_state_rho = 0, off_state_wind = 0, off_state_rhotheta = 0, off_state_theta = 0, off_state_exner = 0;
+
+    /* permutations: new -> old and old -> new */
+    std::vector<int> c_n2o, c_o2n, e_n2o, e_o2n, t_n2o, t_o2n;
+
+    /* device tables */
+    HGrid<double> hg64{};
+    HGrid<float> hg32{};
+    VGrid vg{};
+    std::vector<DBuf> owned;
+
+    /* index maps device position -> reference position */
+    int *map_state = nullptr;   /* state block, length state_len */
+    int *map_s = nullptr;       /* scalar field, length S */
+    int *map_vec = nullptr;     /* vector field: [w (L+1)*Nc][u L*Ne], length Vt */
+    int *map_curl = nullptr;    /* curl field: [zh (L+1)*Ne][zv L*Ne], length NCURL */
+    int *map_tri = nullptr;     /* triangle field, length L*Nt */
+    double *staging = nullptr;  /* reference-layout staging, max field length */
+    size_t staging_len = 0;
+    double *dev_tmp[4] = {nullptr, nullptr, nullptr, nullptr}; /* device-layout scratch fields for operators */
+
+    /* persistent step fields (device layout) */
+    double *temperature = nullptr;    /* [L][Nc] */
+    double *theta = nullptr;          /* rho*theta_v / rho_gas, [L][Nc] */
+    double *pt_rates = nullptr;       /* [5][L][Nc] (moist) */
+    double *pt_heat = nullptr;        /* [L][Nc] */
+    double *sed_heat = nullptr;       /* [L][Nc] */
+    Work<double> w64{};
+    Work<float> w32{};
+
+    std::map<const void *, StateMirror> states;
+
+    /* CUDA graphs of the device-side step, keyed by (first_step, precision, dt) */
+    struct GraphKey {
+        int first, prec;
+        double dt;
+        const void *so, *sn, *st;
+        bool operator<(const GraphKey &o) const;
+    };
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    int use_graphs = 1;
+    int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */
+};
+
+Context *ctx();
+void set_error(const std::string &msg);
+int fail(const std::string &msg);
+#define CK(call)                                                                                \
+    do {                                                                                        \
+        cudaError_t _e = (call);                                                                \
+        if (_e != cudaSuccess) return ::game::fail(std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+int init_context(int res_id, int n_layers, int moisture_on, const void *grid, const void *dualgrid);
+int destroy_context();
+StateMirror *mirror(const void *host_state, int create);
+int upload_state(const void *host_state, StateMirror *m);
+int download_state(const void *host_state, StateMirror *m, int which_mask);
+int upload_field(const double *host, double *dev, const int *map, long long n, long long host_len);
+int download_field(double *host, const double *dev, const int *map, long long n, long long host_len,
+                   long long host_lo, long long host_hi);
+
+/* the step on device mirrors (step.cu templates) */
+int run_step(Context *c, StateMirror *so, StateMirror *sn, StateMirror *st, const void *config, double dt);
+
+/* gather / scatter kernels */
+void launch_gather(double *dst, const double *src, const int *map, long long n, cudaStream_t s);
+void launch_scatter(double *dst, const double *src, const int *map, long long n, cudaStream_t s);
+
+}  // namespace game

@@ -1,0 +1,103 @@
+/*
+ * Device-resident grid tables and fields of the RKHEVI step.
+ *
+ * Layout in HBM (all arrays structure-of-arrays, renumbered along a 3-D
+ * Hilbert curve so that neighbour gathers stay local; the 12 pentagons keep
+ * cell numbers 0..11):
+ *   cell fields       [layer][cell]          (Nc fastest)
+ *   interface fields  [level][cell]          (w, vertical metric, L+1 levels)
+ *   edge fields       [layer][edge]          (u, horizontal metric)
+ *   tangential curl   [level][edge]          (L+1 levels)
+ *   rhombus curl      [layer][edge]
+ *   triangle fields   [layer][triangle]
+ *   per-entity tables [slot][entity]         (slot-major, e.g. TRSK [10][Ne])
+ * so a warp's 32 consecutive threads read 32 consecutive entities of one
+ * layer: every streamed field access is coalesced.
+ */
+#pragma once
+
+#include <cstdint>
+
+namespace game {
+
+constexpr int N_PENT = 12;
+
+/* physical constants of GAME (src/game_constants.h:10-27) */
+constexpr double T_0 = 273.15;
+constexpr double N_A = 6.02214076e23;
+constexpr double P_0 = 100000.0;
+constexpr double C_D_V = 717.942189;
+constexpr double C_V_V = 1396.475121;
+constexpr double C_D_P = 1005.0;
+constexpr double M_D = N_A * 0.004810e-23;
+constexpr double M_V = N_A * 0.002991e-23;
+constexpr double R_D = 287.057811;
+constexpr double R_V = 461.524879;
+
+/* horizontal-operator tables, element type R (double on the FP64 path,
+ * float on the mixed path) */
+template <typename R>
+struct HGrid {
+    int nc, ne, nt, nl, n_oro;
+    R radius;
+    /* cells */
+    const R *volume;        /* [L][Nc] */
+    const R *ipw;           /* [8][L][Nc] inner-product weights */
+    const int *adj;         /* [6][Nc] edges of the cell, reference order */
+    const int *adj_sign;    /* [6][Nc] +1 cell is the edge's from cell, -1 to cell, 0 none */
+    const int *adj_nbr;     /* [6][Nc] cell on the other side of edge j */
+    /* interfaces */
+    const R *nd_v;          /* [L+1][Nc] vertical normal distance */
+    const R *area_v;        /* [L+1][Nc] */
+    const R *exner_bg_grad_v; /* [L+1][Nc] */
+    const R *gravity_m_v;   /* [L+1][Nc] */
+    /* edges */
+    const int *from, *to;   /* [Ne] */
+    const R *nd_h;          /* [L][Ne] */
+    const R *area_h;        /* [L][Ne] */
+    const R *z_h;           /* [L][Ne] */
+    const R *slope_h;       /* [L][Ne] */
+    const R *exner_bg_grad_h; /* [L][Ne] */
+    const R *trsk_w;        /* [10][Ne] */
+    const int *trsk_i;      /* [10][Ne] */
+    const int *trsk_m;      /* [10][Ne] modified curl indices */
+    const R *rhombi_w;      /* [4][Ne] */
+    const int *rhombi_i;    /* [4][Ne] */
+    const R *f_vec;         /* [2][Ne] */
+    const int *dual_from, *dual_to; /* [Ne] */
+    const R *dual_area_h;   /* [L+1][Ne] */
+    const R *pvz;           /* [4][Ne] height differences of the TOA/surface density extrapolation */
+    /* triangles */
+    const int *vort_i;      /* [3][Nt] */
+    const int *vort_s;      /* [3][Nt] */
+    const R *dual_area_t;   /* [L][Nt] */
+    const R *dual_z_t;      /* [L][Nt] */
+};
+
+/* vertical-solver tables (always double) */
+struct VGrid {
+    int nc, nl;
+    const double *volume, *z_scalar, *exner_bg, *theta_v_bg; /* [L][Nc] */
+    const double *area_v, *z_v;                             /* [L+1][Nc] */
+};
+
+/* one State in device layout (always double: the prognostic variables) */
+struct DState {
+    double *rho;          /* [C][L][Nc] */
+    double *rhotheta_v;   /* [L][Nc] */
+    double *theta_v_pert; /* [L][Nc] */
+    double *exner_pert;   /* [L][Nc] */
+    double *w;            /* [L+1][Nc] */
+    double *u;            /* [L][Ne] */
+};
+
+/* run configuration of one step */
+struct StepParams {
+    int n_const, n_cond, moist;
+    double dt;
+    double impl_thermo_weight, damping_start_height, damping_coeff_max, toa;
+    double snow_velocity, rain_velocity, cloud_velocity;
+    int first_step;
+};
+
+}  // namespace game

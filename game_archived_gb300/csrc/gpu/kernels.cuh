@@ -1,0 +1,995 @@
+/*
+ * RKHEVI step kernels.
+ *
+ * Every device function restates one reference operator at one point and
+ * keeps the reference's order of floating-point operations, so that the FP64
+ * instantiation (compiled with --fmad=false) rounds like the reference C.
+ * Horizontal operators are templated on R: double on the FP64 path, float on
+ * the mixed path, where the prognostic state, the vertical solves and the
+ * density/mass-flux divergence accumulation stay in double.
+ *
+ * Kernels of one RK substage (src/time_stepping/manage_rkhevi.c:48-97):
+ *   k_cell_prepare      T, theta_v, moist phase-transition rates (once per step)
+ *   k_tri_vort          vertical relative vorticity on triangles        (rk 1)
+ *   k_edge_vort         rhombus / tangential potential vorticity, mass flux (rk 1)
+ *   k_cell_kinetic      kinetic energy, vertical mass flux               (rk 1)
+ *   k_momentum_h        pressure gradient + vorticity flux + KE gradient
+ *                       -> horizontal tendency and wind update
+ *   k_momentum_v        the same for w at the interfaces
+ *   k_scalar_tend       mass / rho*theta_v flux divergences -> tendencies
+ *   k_vertical_waves    implicit vertical sound-wave column solve
+ *   k_vertical_tracers  implicit vertical tracer advection column solve
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "devgrid.cuh"
+
+namespace game {
+/* internal linkage: the FP64 and the mixed translation unit each compile
+ * their own copy with their own contraction flags */
+namespace {
+
+/* ------------------------------------------------------------ utilities */
+__device__ __forceinline__ long long gtid() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
+
+template <typename R>
+__device__ __forceinline__ R ipw_at(const HGrid<R> &g, int j, int l, int c)
+{
+    return g.ipw[((long long)j * g.nl + l) * g.nc + c];
+}
+
+/* vertical covariant gradient of a cell field at an inner interface k
+ * (src/spatial_operators/gradient_operators.c:35-54) */
+template <typename R, typename F>
+__device__ __forceinline__ R grad_v(const HGrid<R> &g, const F *f, int k, int c)
+{
+    return (R(f[(long long)(k - 1) * g.nc + c]) - R(f[(long long)k * g.nc + c])) / g.nd_v[(long long)k * g.nc + c];
+}
+
+/* horizontal gradient at edge e of layer l, with the terrain-following
+ * covariant -> contravariant correction in the orography layers
+ * (gradient_operators.c:14-33, averaging.c:14-39 and :113-133) */
+template <typename R, typename F>
+__device__ __forceinline__ R grad_h(const HGrid<R> &g, const F *f, int l, int e)
+{
+    const int fr = g.from[e], to = g.to[e];
+    const long long le = (long long)l * g.ne + e;
+    R out = (R(f[(long long)l * g.nc + to]) - R(f[(long long)l * g.nc + fr])) / g.nd_h[le];
+    if (l >= g.nl - g.n_oro) {
+        R c = ipw_at(g, 6, l, fr) * grad_v(g, f, l, fr);
+        c += ipw_at(g, 6, l, to) * grad_v(g, f, l, to);
+        if (l < g.nl - 1) {
+            c += ipw_at(g, 7, l, fr) * grad_v(g, f, l + 1, fr);
+            c += ipw_at(g, 7, l, to) * grad_v(g, f, l + 1, to);
+        }
+        c = R(0.5) * c;
+        out += -g.slope_h[le] * c;
+    }
+    return out;
+}
+
+/* horizontal covariant wind component (averaging.c:97-111) */
+template <typename R>
+__device__ __forceinline__ R hor_covariant(const HGrid<R> &g, const double *u, const double *w, int l, int e)
+{
+    const long long le = (long long)l * g.ne + e;
+    R r = R(u[le]);
+    if (l >= g.nl - g.n_oro) {
+        const int fr = g.from[e], to = g.to[e];
+        R c = ipw_at(g, 6, l, fr) * R(w[(long long)l * g.nc + fr]);
+        c += ipw_at(g, 6, l, to) * R(w[(long long)l * g.nc + to]);
+        if (l < g.nl - 1) {
+            c += ipw_at(g, 7, l, fr) * R(w[(long long)(l + 1) * g.nc + fr]);
+            c += ipw_at(g, 7, l, to) * R(w[(long long)(l + 1) * g.nc + to]);
+        }
+        c = R(0.5) * c;
+        r += g.slope_h[le] * c;
+    }
+    return r;
+}
+
+/* sum of all constituent densities (src/constituents/derived_quantities.c:83-95) */
+__device__ __forceinline__ double density_total(const double *rho, int n_const, long long ns, long long i)
+{
+    double r = 0.0;
+    for (int k = 0; k < n_const; ++k) r += rho[k * ns + i];
+    return r;
+}
+
+/* ------------------------------------------------------ thermodynamics
+ * src/constituents/dictionary.c (FP64 on both paths) */
+__device__ __forceinline__ double c_p_ice(double t)
+{
+    if (t > T_0) t = T_0;
+    if (t < 20.0) t = 20.0;
+    double q = t / 125.1;
+    double r = -2.0572 + 0.14644 * t + 0.06163 * t * exp(-(q * q));
+    return r / M_V;
+}
+
+__device__ __forceinline__ double c_p_water(double t)
+{
+    double tc = t - T_0, r;
+    if (tc >= 0.0) {
+        if (tc > 35.0) tc = 35.0;
+        double a = tc - 35.0;
+        r = 0.9979 + 3.1e-6 * (a * a) + 3.8e-9 * pow(a, 4.0);
+    } else {
+        if (tc < -37.0) tc = -37.0;
+        r = 1.000938 - 2.7052e-3 * tc - 2.3235e-5 * (tc * tc) + 4.3778e-6 * pow(tc, 3.0) + 2.7136e-7 * pow(tc, 4.0);
+    }
+    return 4186.8 * r;
+}
+
+__device__ __forceinline__ double c_p_cond(int id, double t) { return (id % 2 == 0) ? c_p_ice(t) : c_p_water(t); }
+
+__device__ __forceinline__ double enthalpy_evaporation(double t)
+{
+    double r;
+    if (t < T_0) {
+        if (t < 30.0) t = 30.0;
+        r = 56579.0 - 42.212 * t + exp(0.1149 * (281.6 - t));
+        r = r / M_V;
+    } else {
+        if (t > T_0 + 100.0) t = T_0 + 100.0;
+        r = 3151378.0 - 2386.0 * t;
+    }
+    return r;
+}
+
+__device__ __forceinline__ double enthalpy_sublimation(double t)
+{
+    if (t < 30.0) t = 30.0;
+    if (t > T_0) t = T_0;
+    double q = t / 123.75;
+    double r = 46782.5 + 35.8925 * t - 0.07414 * (t * t) + 541.5 * exp(-(q * q));
+    return r / M_V;
+}
+
+__device__ __forceinline__ double phase_trans_heat(int dir, double t)
+{
+    double r = 0.0;
+    if (dir == 0) r = enthalpy_evaporation(t);
+    if (dir == 1) r = enthalpy_sublimation(t);
+    if (dir == 2) r = enthalpy_sublimation(t) - enthalpy_evaporation(t);
+    return r;
+}
+
+__device__ __forceinline__ double sat_pressure_water(double t)
+{
+    double tc = t - T_0, r;
+    if (tc > 100.0) tc = 100.0;
+    if (tc > 0.0) {
+        r = exp(34.494 - 4924.99 / (tc + 237.1)) / pow(tc + 105.0, 1.57);
+    } else {
+        if (tc < -50.0) tc = -50.0;
+        r = 6.107799961 + 4.436518521e-1 * tc + 1.428945805e-2 * (tc * tc) + 2.650648471e-4 * pow(tc, 3.0)
+            + 3.031240396e-6 * pow(tc, 4.0) + 2.034080948e-8 * pow(tc, 5.0) + 6.136820929e-11 * pow(tc, 6.0);
+        r = 100.0 * r;
+    }
+    return r;
+}
+
+__device__ __forceinline__ double dsat_pressure_water_dT(double t)
+{
+    double tc = t - T_0;
+    if (tc > 100.0) tc = 100.0;
+    if (tc < 0.0) tc = 0.0;
+    double a = tc + 237.1;
+    return sat_pressure_water(t) * (4924.99 / (a * a) - 1.57 / (tc + 105.0));
+}
+
+__device__ __forceinline__ double sat_pressure_ice(double t)
+{
+    double tc = t - T_0;
+    if (tc < -80.0) tc = -80.0;
+    if (tc > 0.0) tc = 0.0;
+    double a = tc + 868.0;
+    return exp(43.494 - 6545.8 / (tc + 278.0)) / (a * a);
+}
+
+__device__ __forceinline__ double dsat_pressure_ice_dT(double t)
+{
+    double tc = t - T_0;
+    if (tc < -80.0) tc = -80.0;
+    if (tc > 0.0) tc = 0.0;
+    double a = tc + 278.0;
+    return sat_pressure_ice(t) * (6545.8 / (a * a) - 2.0 / (tc + 868.0));
+}
+
+/* mass-weighted c_v (derived_quantities.c:97-115) */
+__device__ __forceinline__ double c_v_mass_weighted(const double *rho, int n_cond, int moist, long long ns,
+                                                    long long i, double temperature)
+{
+    double r = 0.0;
+    for (int k = 0; k < n_cond; ++k) r += rho[k * ns + i] * c_p_cond(k, temperature);
+    r += rho[n_cond * ns + i] * C_D_V;
+    if (moist) r += rho[(n_cond + 1) * ns + i] * C_V_V;
+    return r;
+}
+
+/* --------------------------------------------------- k_cell_prepare
+ * temperature (derived_quantities.c:15-40) from state_old and, for the moist
+ * build, phase-transition rates and heating (phase_trans.c:16-311) */
+__global__ void k_cell_prepare(VGrid vg, StepParams p, DState so, double *temperature, double *pt_rates,
+                               double *pt_heat)
+{
+    const long long ns = (long long)vg.nl * vg.nc;
+    const long long i = gtid();
+    if (i >= ns) return;
+    const int cond = p.n_cond;
+    double T;
+    if (!p.moist) {
+        T = (vg.theta_v_bg[i] + so.theta_v_pert[i]) * (vg.exner_bg[i] + so.exner_pert[i]);
+        temperature[i] = T;
+        return;
+    }
+    const double *rho = so.rho;
+    T = (vg.theta_v_bg[i] + so.theta_v_pert[i]) * (vg.exner_bg[i] + so.exner_pert[i])
+        / (1.0 + rho[(cond + 1) * ns + i] / rho[cond * ns + i] * (M_D / M_V - 1.0));
+    temperature[i] = T;
+    const double dt = p.dt;
+    const double max_cloud_water = 0.2e-3;
+    double sat = T >= T_0 ? sat_pressure_water(T) : sat_pressure_ice(T);
+    double wvp = rho[(cond + 1) * ns + i] * R_V * T;
+    double dry = (rho[cond * ns + i] - rho[(cond + 1) * ns + i]) * R_D * T;
+    double air = dry + wvp;
+    double ef = T >= T_0 ? 1.00071 * exp(0.000000045 * air) : 0.99882 * exp(0.00000008 * air);
+    sat = ef * sat;
+    int dir = T >= T_0 ? 0 : 1;
+    double cv = c_v_mass_weighted(rho, cond, 1, ns, i, T);
+    double pth = phase_trans_heat(dir, T);
+    double a = -R_V * pth / cv;
+    double b = R_V * T - R_V * rho[(cond + 1) * ns + i] * pth / cv
+               + ef * (dir == 0 ? dsat_pressure_water_dT(T) : dsat_pressure_ice_dT(T)) * pth / cv;
+    double cc = wvp - sat;
+    double pp = b / a;
+    double q = cc / a;
+    double diff = -0.5 * pp - sqrt(0.25 * (pp * pp) - q);
+    double r0, r1, r2, r3, r4, heat;
+    if (sat >= wvp) {
+        if (T >= T_0) {
+            r2 = -rho[2 * ns + i] / dt;
+            double ptd = fmin(rho[3 * ns + i], diff);
+            r4 = ptd / dt;
+            r3 = rho[2 * ns + i] / dt - ptd / dt;
+            heat = r2 * phase_trans_heat(2, T) - ptd * phase_trans_heat(0, T) / dt;
+        } else {
+            r3 = -rho[3 * ns + i] / dt;
+            double ptd = fmin(rho[2 * ns + i], diff);
+            r4 = ptd / dt;
+            r2 = rho[3 * ns + i] / dt - ptd / dt;
+            heat = -r3 * phase_trans_heat(2, T) - ptd * phase_trans_heat(1, T) / dt;
+        }
+    } else {
+        if (T >= T_0) {
+            r2 = -rho[2 * ns + i] / dt;
+            r4 = diff / dt;
+            r3 = rho[2 * ns + i] / dt - diff / dt;
+            heat = r2 * phase_trans_heat(2, T) - diff * phase_trans_heat(0, T) / dt;
+        } else {
+            r3 = -rho[3 * ns + i] / dt;
+            r4 = diff / dt;
+            r2 = rho[3 * ns + i] / dt - diff / dt;
+            heat = -r3 * phase_trans_heat(2, T) - diff * phase_trans_heat(1, T) / dt;
+        }
+    }
+    r0 = 0.0;
+    r1 = 0.0;
+    if (T < T_0) {
+        r0 = fmax(rho[2 * ns + i] - max_cloud_water * rho[4 * ns + i], 0.0) / 1000.0;
+        r2 -= r0;
+    } else if (T >= T_0) {
+        r1 = fmax(rho[3 * ns + i] - max_cloud_water * rho[4 * ns + i], 0.0) / 1000.0;
+        r3 -= r1;
+    }
+    if (T >= T_0 && rho[i] > 0.0) {
+        r0 = -rho[i] / dt;
+        r1 -= r0;
+        heat += r0 * phase_trans_heat(2, T);
+    }
+    if (T < T_0 && rho[ns + i] > 0.0) {
+        r1 = -rho[ns + i] / dt;
+        r0 -= r1;
+        heat += -r1 * phase_trans_heat(2, T);
+    }
+    pt_rates[i] = r0;
+    pt_rates[ns + i] = r1;
+    pt_rates[2 * ns + i] = r2;
+    pt_rates[3 * ns + i] = r3;
+    pt_rates[4 * ns + i] = r4;
+    pt_heat[i] = heat;
+}
+
+/* ------------------------------------------------------- k_tri_vort
+ * vertical relative vorticity on triangles (vorticities.c:167-222) */
+template <typename R>
+__global__ void k_tri_vort(HGrid<R> g, const double *u, R *tri_vort)
+{
+    const long long n = (long long)g.nl * g.nt;
+    const long long i = gtid();
+    if (i >= n) return;
+    const int l = (int)(i / g.nt), t = (int)(i - (long long)l * g.nt);
+    R acc = R(0);
+    for (int j = 0; j < 3; ++j) {
+        const int e = g.vort_i[j * g.nt + t];
+        const long long le = (long long)l * g.ne + e;
+        R vel = R(u[le]);
+        R rescale = R(1);
+        if (l >= g.nl - g.n_oro) {
+            const R zt = g.dual_z_t[i];
+            rescale = (g.radius + zt) / (g.radius + g.z_h[le]);
+            R dz = zt - g.z_h[le];
+            int lo;
+            if (dz > R(0)) lo = l - 1;
+            else if (l == g.nl - 1) lo = l - 1;
+            else lo = l + 1;
+            const long long lo_e = (long long)lo * g.ne + e;
+            R vgrad = (R(u[le]) - R(u[lo_e])) / (g.z_h[le] - g.z_h[lo_e]);
+            vel += dz * vgrad;
+        }
+        acc += rescale * g.nd_h[le] * R(g.vort_s[j * g.nt + t]) * vel;
+    }
+    tri_vort[i] = acc / g.dual_area_t[i];
+}
+
+/* relative vorticity of level k (tangential) or layer k (rhombus) at edge e
+ * (vorticities.c:104-165) */
+template <typename R>
+__device__ __forceinline__ R rel_vort_tangential(const HGrid<R> &g, const double *u, const double *w, int k, int e)
+{
+    const int nl = g.nl;
+    if (k == 0) k = 1; /* no vertical shear of the tangential vorticity at the TOA */
+    const R inv_area = R(1) / g.dual_area_h[(long long)k * g.ne + e];
+    if (k == nl) {
+        R c2 = hor_covariant(g, u, w, k - 1, e);
+        return inv_area * g.nd_h[(long long)(k - 1) * g.ne + e] * c2;
+    }
+    const int fr = g.from[e], to = g.to[e];
+    R c0 = hor_covariant(g, u, w, k, e);
+    R c2 = hor_covariant(g, u, w, k - 1, e);
+    return inv_area * (-g.nd_h[(long long)k * g.ne + e] * c0
+                       + g.nd_v[(long long)k * g.nc + fr] * R(w[(long long)k * g.nc + fr])
+                       + g.nd_h[(long long)(k - 1) * g.ne + e] * c2
+                       - g.nd_v[(long long)k * g.nc + to] * R(w[(long long)k * g.nc + to]));
+}
+
+/* --------------------------------------------------------- k_edge_vort
+ * potential vorticity (vorticities.c:18-85) and the horizontal mass flux
+ * density (multiplications.c:45-66), one thread per (edge, level 0..L) */
+template <typename R>
+__global__ void k_edge_vort(HGrid<R> g, const double *u, const double *w, const double *rho_gas, const R *tri_vort,
+                            R *zh, R *zv, R *flux_h)
+{
+    const long long n = (long long)(g.nl + 1) * g.ne;
+    const long long i = gtid();
+    if (i >= n) return;
+    const int k = (int)(i / g.ne), e = (int)(i - (long long)k * g.ne);
+    const int nl = g.nl, nc = g.nc, ne = g.ne;
+    const int fr = g.from[e], to = g.to[e];
+    /* tangential component at level k */
+    {
+        R rel = rel_vort_tangential(g, u, w, k, e);
+        R pv = rel + g.f_vec[e];
+        R dens;
+        if (k == 0) {
+            R top = R(0.5) * (R(rho_gas[fr]) + R(rho_gas[to]));
+            R below = R(0.5) * (R(rho_gas[nc + fr]) + R(rho_gas[nc + to]));
+            dens = top + (top - below) / g.pvz[ne + e] * g.pvz[e];
+        } else if (k == nl) {
+            long long a = (long long)(nl - 1) * nc, b = (long long)(nl - 2) * nc;
+            R low = R(0.5) * (R(rho_gas[a + fr]) + R(rho_gas[a + to]));
+            R above = R(0.5) * (R(rho_gas[b + fr]) + R(rho_gas[b + to]));
+            dens = low + (above - low) / g.pvz[3 * (long long)ne + e] * g.pvz[2 * (long long)ne + e];
+        } else {
+            long long uf = (long long)(k - 1) * nc + fr, ut = (long long)(k - 1) * nc + to;
+            dens = R(0.25) * (R(rho_gas[uf]) + R(rho_gas[ut]) + R(rho_gas[uf + nc]) + R(rho_gas[ut + nc]));
+        }
+        zh[i] = pv / dens;
+    }
+    if (k < nl) {
+        const long long le = (long long)k * ne + e;
+        /* rhombus: area-weighted mean of the two triangles */
+        const int tf = g.dual_from[e], tt = g.dual_to[e];
+        const long long kt = (long long)k * g.nt;
+        R af = g.dual_area_t[kt + tf], at = g.dual_area_t[kt + tt];
+        R rel = (af * tri_vort[kt + tf] + at * tri_vort[kt + tt]) / (af + at);
+        R pv = rel + g.f_vec[ne + e];
+        R dens = R(0);
+        for (int j = 0; j < 4; ++j)
+            dens += g.rhombi_w[j * (long long)ne + e] * R(rho_gas[(long long)k * nc + g.rhombi_i[j * (long long)ne + e]]);
+        zv[le] = pv / dens;
+        /* mass flux density */
+        R sv = R(0.5) * (R(rho_gas[(long long)k * nc + to]) + R(rho_gas[(long long)k * nc + fr]));
+        flux_h[le] = sv * R(u[le]);
+    }
+}
+
+/* ------------------------------------------------------ k_cell_kinetic
+ * kinetic energy v^2 (inner_product.c:13-43) at (cell, layer) and the vertical
+ * mass flux density (multiplications.c:98-117) at the inner interfaces */
+template <typename R>
+__global__ void k_cell_kinetic(HGrid<R> g, const double *u, const double *w, const double *rho_gas, R *v2,
+                               R *flux_v)
+{
+    const long long ns = (long long)g.nl * g.nc;
+    const long long i = gtid();
+    if (i >= ns) return;
+    const int l = (int)(i / g.nc), c = (int)(i - (long long)l * g.nc);
+    const int n_edges = c < N_PENT ? 5 : 6;
+    R acc = R(0);
+    for (int j = 0; j < n_edges; ++j) {
+        R ue = R(u[(long long)l * g.ne + g.adj[j * g.nc + c]]);
+        acc += ipw_at(g, j, l, c) * ue * ue;
+    }
+    R wu = R(w[i]), wl = R(w[i + g.nc]);
+    acc += ipw_at(g, 6, l, c) * wu * wu;
+    acc += ipw_at(g, 7, l, c) * wl * wl;
+    v2[i] = acc;
+    if (l >= 1) {
+        R sv = R(0.5) * (R(rho_gas[i - g.nc]) + R(rho_gas[i]));
+        flux_v[i] = sv * wu;
+    }
+}
+
+/* modified TRSK vorticity flux at edge e of layer l (vorticity_flux.c:35-137) */
+template <typename R>
+__device__ __forceinline__ R vorticity_flux_h(const HGrid<R> &g, const R *flux_h, const R *flux_v, const R *zh,
+                                              const R *zv, int l, int e)
+{
+    const long long ne = g.ne;
+    const R *mf = flux_h + (long long)l * ne;
+    const R *pv = zv + (long long)l * ne;
+    const int fr = g.from[e], to = g.to[e];
+    R out = R(0);
+    if (fr < N_PENT) {
+        for (int j = 0; j < 4; ++j)
+            out += g.trsk_w[j * ne + e] * mf[g.trsk_i[j * ne + e]] * pv[g.trsk_m[j * ne + e]];
+    } else {
+        for (int j = 0; j < 5; ++j) {
+            if (j == 2)
+                out += g.trsk_w[j * ne + e] * mf[g.trsk_i[j * ne + e]] * R(0.5) * (pv[g.trsk_m[j * ne + e]] + pv[e]);
+            else
+                out += g.trsk_w[j * ne + e] * mf[g.trsk_i[j * ne + e]] * pv[g.trsk_m[j * ne + e]];
+        }
+    }
+    if (to < N_PENT) {
+        for (int j = 5; j < 9; ++j)
+            out += g.trsk_w[j * ne + e] * mf[g.trsk_i[j * ne + e]] * pv[g.trsk_m[j * ne + e]];
+    } else {
+        for (int j = 5; j < 10; ++j) {
+            if (j == 7)
+                out += g.trsk_w[j * ne + e] * mf[g.trsk_i[j * ne + e]] * R(0.5) * (pv[g.trsk_m[j * ne + e]] + pv[e]);
+            else
+                out += g.trsk_w[j * ne + e] * mf[g.trsk_i[j * ne + e]] * pv[g.trsk_m[j * ne + e]];
+        }
+    }
+    const R zt = zh[(long long)l * ne + e], zb = zh[(long long)(l + 1) * ne + e];
+    const long long nc = g.nc;
+    out -= R(0.5) * ipw_at(g, 6, l, fr) * flux_v[l * nc + fr] * zt;
+    out -= R(0.5) * ipw_at(g, 6, l, to) * flux_v[l * nc + to] * zt;
+    out -= R(0.5) * ipw_at(g, 7, l, fr) * flux_v[(l + 1) * nc + fr] * zb;
+    out -= R(0.5) * ipw_at(g, 7, l, to) * flux_v[(l + 1) * nc + to] * zb;
+    return out;
+}
+
+/* decelerated pressure-gradient sum nl + l at edge e, layer l
+ * (manage_pressure_gradient.c:17-72) */
+template <typename R>
+__device__ __forceinline__ R pgrad_h(const HGrid<R> &g, const StepParams &p, const DState &s, const double *theta_bg,
+                                     int l, int e)
+{
+    const long long ns = (long long)g.nl * g.nc;
+    const int fr = g.from[e], to = g.to[e];
+    const long long cf = (long long)l * g.nc + fr, ct = (long long)l * g.nc + to;
+    R nl = grad_h(g, s.exner_pert, l, e);
+    R s_to = R(C_D_P * (theta_bg[ct] + s.theta_v_pert[ct])), s_fr = R(C_D_P * (theta_bg[cf] + s.theta_v_pert[cf]));
+    nl = (R(0.5) * (s_to + s_fr)) * nl;
+    R l_term = (R(0.5) * (R(C_D_P * s.theta_v_pert[ct]) + R(C_D_P * s.theta_v_pert[cf])))
+               * g.exner_bg_grad_h[(long long)l * g.ne + e];
+    R d_to = R(s.rho[p.n_cond * ns + ct] / density_total(s.rho, p.n_const, ns, ct));
+    R d_fr = R(s.rho[p.n_cond * ns + cf] / density_total(s.rho, p.n_const, ns, cf));
+    R dec = R(0.5) * (d_to + d_fr);
+    nl = dec * nl;
+    l_term = dec * l_term;
+    return nl + l_term;
+}
+
+/* the same at the inner interface k of cell c */
+template <typename R>
+__device__ __forceinline__ R pgrad_v(const HGrid<R> &g, const StepParams &p, const DState &s, const double *theta_bg,
+                                     int k, int c)
+{
+    const long long ns = (long long)g.nl * g.nc;
+    const long long up = (long long)(k - 1) * g.nc + c, lo = (long long)k * g.nc + c;
+    R nl = grad_v(g, s.exner_pert, k, c);
+    R s_up = R(C_D_P * (theta_bg[up] + s.theta_v_pert[up])), s_lo = R(C_D_P * (theta_bg[lo] + s.theta_v_pert[lo]));
+    nl = (R(0.5) * (s_up + s_lo)) * nl;
+    R l_term = (R(0.5) * (R(C_D_P * s.theta_v_pert[up]) + R(C_D_P * s.theta_v_pert[lo])))
+               * g.exner_bg_grad_v[(long long)k * g.nc + c];
+    R d_up = R(s.rho[p.n_cond * ns + up] / density_total(s.rho, p.n_const, ns, up));
+    R d_lo = R(s.rho[p.n_cond * ns + lo] / density_total(s.rho, p.n_const, ns, lo));
+    R dec = R(0.5) * (d_up + d_lo);
+    nl = dec * nl;
+    l_term = dec * l_term;
+    return nl + l_term;
+}
+
+/* ------------------------------------------------------- k_momentum_h
+ * horizontal momentum: explicit tendency (vector_tendencies_expl.c:74-131) and
+ * the wind update (manage_rkhevi.c:67-75).  ADV: the advection terms are
+ * recomputed in this substage; PG: the pressure gradient is recomputed. */
+template <typename R, bool ADV, bool PG>
+__global__ void k_momentum_h(HGrid<R> g, StepParams p, DState sn, const double *u_old, const double *theta_bg,
+                             double *tend_u, R *P_h, R *pg_old_h, R *pvt_h, R *v2g_h, const R *flux_h,
+                             const R *flux_v, const R *zh, const R *zv, const R *v2, double new_w, double old_w)
+{
+    const long long n = (long long)g.nl * g.ne;
+    const long long i = gtid();
+    if (i >= n) return;
+    const int l = (int)(i / g.ne), e = (int)(i - (long long)l * g.ne);
+    R P, pgo;
+    if (PG) {
+        P = pgrad_h(g, p, sn, theta_bg, l, e);
+        pgo = p.first_step ? -P : -P_h[i];
+        P_h[i] = P;
+        pg_old_h[i] = pgo;
+    } else {
+        P = P_h[i];
+        pgo = pg_old_h[i];
+    }
+    R pvt, v2g;
+    if (ADV) {
+        pvt = vorticity_flux_h(g, flux_h, flux_v, zh, zv, l, e);
+        v2g = grad_h(g, v2, l, e);
+        pvt_h[i] = pvt;
+        v2g_h[i] = v2g;
+    } else {
+        pvt = pvt_h[i];
+        v2g = v2g_h[i];
+    }
+    const R cur_hor = R(0.5 + p.impl_thermo_weight), old_hor = R(1.0 - (0.5 + p.impl_thermo_weight));
+    R y = old_hor * pgo - cur_hor * P + pvt - R(0.5) * v2g;
+    double t = (new_w == 1.0) ? double(y) : old_w * tend_u[i] + new_w * double(y);
+    tend_u[i] = t;
+    sn.u[i] = u_old[i] + p.dt * t;
+}
+
+/* ------------------------------------------------------- k_momentum_v
+ * vertical momentum at interface k of cell c: tendency including the
+ * condensate term (manage_pressure_gradient.c:74-87) */
+template <typename R, bool ADV, bool PG>
+__global__ void k_momentum_v(HGrid<R> g, StepParams p, DState sn, const double *theta_bg, double *tend_w, R *P_v,
+                             R *pvt_v, R *v2g_v, const R *flux_h, const R *zh, const R *v2, double new_w, double old_w)
+{
+    const long long n = (long long)(g.nl + 1) * g.nc;
+    const long long i = gtid();
+    if (i >= n) return;
+    const int k = (int)(i / g.nc), c = (int)(i - (long long)k * g.nc);
+    const int nl = g.nl;
+    R pvt = R(0);
+    if (ADV) {
+        /* vertical part of the vorticity flux (vorticity_flux.c:143-183), all levels */
+        const int n_edges = c < N_PENT ? 5 : 6;
+        const R vw = (k == 0 || k == nl) ? R(1) : R(0.5);
+        const R *z = zh + (long long)k * g.ne;
+        if (k >= 1)
+            for (int j = 0; j < n_edges; ++j) {
+                const int a = g.adj[j * g.nc + c];
+                pvt += vw * ipw_at(g, j, k - 1, c) * flux_h[(long long)(k - 1) * g.ne + a] * z[a];
+            }
+        if (k <= nl - 1)
+            for (int j = 0; j < n_edges; ++j) {
+                const int a = g.adj[j * g.nc + c];
+                pvt += vw * ipw_at(g, j, k, c) * flux_h[(long long)k * g.ne + a] * z[a];
+            }
+        pvt_v[i] = pvt;
+    }
+    if (k == 0 || k == nl) {
+        tend_w[i] = 0.0;
+        return;
+    }
+    R P, v2g;
+    if (PG) {
+        P = pgrad_v(g, p, sn, theta_bg, k, c);
+        P_v[i] = P;
+    } else {
+        P = P_v[i];
+    }
+    if (ADV) {
+        v2g = grad_v(g, v2, k, c);
+        v2g_v[i] = v2g;
+    } else {
+        pvt = pvt_v[i];
+        v2g = v2g_v[i];
+    }
+    const long long ns = (long long)nl * g.nc;
+    const long long up = (long long)(k - 1) * g.nc + c, lo = (long long)k * g.nc + c;
+    R d_up = R(sn.rho[p.n_cond * ns + up] / density_total(sn.rho, p.n_const, ns, up) - 1.0);
+    R d_lo = R(sn.rho[p.n_cond * ns + lo] / density_total(sn.rho, p.n_const, ns, lo) - 1.0);
+    R pgc = (R(0.5) * (d_up + d_lo)) * g.gravity_m_v[i];
+    const R cur_ver = R(1.0 - p.impl_thermo_weight);
+    R y = -cur_ver * P + pvt - R(0.5) * v2g + pgc;
+    double t = (new_w == 1.0) ? double(y) : old_w * tend_w[i] + new_w * double(y);
+    tend_w[i] = t;
+}
+
+/* ------------------------------------------------------ k_scalar_tend
+ * explicit mass and rho*theta_v tendencies (scalar_tendencies_expl.c:90-178)
+ * at (cell, layer).  Edge fluxes are recomputed from the neighbouring cells
+ * instead of being stored; the divergence sums run in double. */
+template <typename R>
+__device__ __forceinline__ R flux_centred(const HGrid<R> &g, const double *f, const double *u, int l, int c, int j)
+{
+    const int nb = g.adj_nbr[j * g.nc + c], a = g.adj[j * g.nc + c];
+    const long long o = (long long)l * g.nc;
+    return (R(0.5) * (R(f[o + c]) + R(f[o + nb]))) * R(u[(long long)l * g.ne + a]);
+}
+
+template <typename R>
+__device__ __forceinline__ R flux_theta(const HGrid<R> &g, const double *rho, const double *theta, const double *u,
+                                        int l, int c, int j)
+{
+    const int nb = g.adj_nbr[j * g.nc + c];
+    const long long o = (long long)l * g.nc;
+    return (R(0.5) * (R(theta[o + c]) + R(theta[o + nb]))) * flux_centred(g, rho, u, l, c, j);
+}
+
+template <typename R>
+__device__ __forceinline__ R flux_upstream(const HGrid<R> &g, const double *f, const double *u, int l, int c, int j)
+{
+    const int nb = g.adj_nbr[j * g.nc + c], a = g.adj[j * g.nc + c], sg = g.adj_sign[j * g.nc + c];
+    const long long o = (long long)l * g.nc;
+    const R ue = R(u[(long long)l * g.ne + a]);
+    /* upstream: the edge's from cell where u >= 0 (multiplications.c:68-96) */
+    const bool self_is_from = sg > 0;
+    const double fs = (ue >= R(0)) == self_is_from ? f[o + c] : f[o + nb];
+    return R(fs) * ue;
+}
+
+enum FluxKind { FLUX_MAIN = 0, FLUX_THETA = 1, FLUX_TRACER = 2 };
+
+template <typename R, int KIND>
+__device__ __forceinline__ R edge_flux(const HGrid<R> &g, const double *f, const double *rho_gas, const double *theta,
+                                       const double *u, int l, int c, int j)
+{
+    if (KIND == FLUX_MAIN) return flux_centred(g, f, u, l, c, j);
+    if (KIND == FLUX_THETA) return flux_theta(g, rho_gas, theta, u, l, c, j);
+    return flux_upstream(g, f, u, l, c, j);
+}
+
+/* vertical_contravariant_corr (averaging.c:41-95) of an edge field given
+ * by the functor flux(l, j) at level k of cell c */
+template <typename R, typename FX>
+__device__ __forceinline__ R contra_corr(const HGrid<R> &g, int k, int c, int n_edges, FX flux)
+{
+    R r = R(0);
+    if (k >= g.nl - g.n_oro) {
+        if (k > g.nl - g.n_oro)
+            for (int j = 0; j < n_edges; ++j) {
+                const int a = g.adj[j * g.nc + c];
+                r += R(-0.5) * ipw_at(g, j, k - 1, c) * g.slope_h[(long long)(k - 1) * g.ne + a] * flux(k - 1, j);
+            }
+        for (int j = 0; j < n_edges; ++j) {
+            const int a = g.adj[j * g.nc + c];
+            r += R(-0.5) * ipw_at(g, j, k, c) * g.slope_h[(long long)k * g.ne + a] * flux(k, j);
+        }
+    }
+    return r;
+}
+
+/* divergence (divv_h / divv_h_tracer, divergences.c:14-148) of one edge flux
+ * at (cell c, layer l); horizontal sum accumulated in double */
+template <typename R, int KIND>
+__device__ __forceinline__ double divergence(const HGrid<R> &g, const double *f, const double *rho_gas,
+                                             const double *theta, const double *u, int l, int c)
+{
+    const int n_edges = c < N_PENT ? 5 : 6;
+    const int nl = g.nl, n_oro = g.n_oro;
+    const long long nc = g.nc;
+    double comp_h = 0.0;
+    for (int j = 0; j < n_edges; ++j) {
+        const int a = g.adj[j * nc + c];
+        const double fx = double(edge_flux<R, KIND>(g, f, rho_gas, theta, u, l, c, j));
+        const double ar = double(g.area_h[(long long)l * g.ne + a]);
+        comp_h += fx * double(g.adj_sign[j * nc + c]) * ar;
+    }
+    double comp_v = 0.0;
+    if (l >= nl - n_oro - 1) {
+        const int ne_ = n_edges;
+        if (KIND != FLUX_TRACER) {
+            auto fl = [&](int ll, int j) { return edge_flux<R, KIND>(g, f, rho_gas, theta, u, ll, c, j); };
+            if (l == nl - n_oro - 1) {
+                R lo = contra_corr(g, l + 1, c, ne_, fl);
+                comp_v = double(-lo * g.area_v[(long long)(l + 1) * nc + c]);
+            } else if (l == nl - 1) {
+                R up = contra_corr(g, l, c, ne_, fl);
+                comp_v = double(up * g.area_v[(long long)l * nc + c]);
+            } else {
+                R up = contra_corr(g, l, c, ne_, fl);
+                R lo = contra_corr(g, l + 1, c, ne_, fl);
+                comp_v = double(up * g.area_v[(long long)l * nc + c] - lo * g.area_v[(long long)(l + 1) * nc + c]);
+            }
+        } else {
+            auto fw = [&](int ll, int j) { return R(u[(long long)ll * g.ne + g.adj[j * nc + c]]); };
+            const long long i = (long long)l * nc + c;
+            if (l == nl - n_oro - 1) {
+                R lo = contra_corr(g, l + 1, c, ne_, fw);
+                R d_lo = lo <= R(0) ? R(f[i]) : R(f[i + nc]);
+                comp_v = double(-d_lo * lo * g.area_v[(long long)(l + 1) * nc + c]);
+            } else if (l == nl - 1) {
+                R up = contra_corr(g, l, c, ne_, fw);
+                R d_up = up <= R(0) ? R(f[i - nc]) : R(f[i]);
+                comp_v = double(d_up * up * g.area_v[(long long)l * nc + c]);
+            } else {
+                R up = contra_corr(g, l, c, ne_, fw);
+                R d_up = up <= R(0) ? R(f[i - nc]) : R(f[i]);
+                R lo = contra_corr(g, l + 1, c, ne_, fw);
+                R d_lo = lo <= R(0) ? R(f[i]) : R(f[i + nc]);
+                comp_v = double(d_up * up * g.area_v[(long long)l * nc + c]
+                                - d_lo * lo * g.area_v[(long long)(l + 1) * nc + c]);
+            }
+        }
+    }
+    return 1.0 / double(g.volume[(long long)l * nc + c]) * (comp_h + comp_v);
+}
+
+template <typename R>
+__global__ void k_theta(VGrid vg, StepParams p, DState sn, double *theta)
+{
+    const long long ns = (long long)vg.nl * vg.nc;
+    const long long i = gtid();
+    if (i >= ns) return;
+    theta[i] = sn.rhotheta_v[i] / sn.rho[p.n_cond * ns + i];
+}
+
+template <typename R>
+__global__ void k_scalar_tend(HGrid<R> g, VGrid vg, StepParams p, DState sn, DState st, const double *theta,
+                              const double *temperature, const double *pt_rates, const double *pt_heat,
+                              const double *sed_heat, int rk)
+{
+    const long long ns = (long long)g.nl * g.nc;
+    const long long i = gtid();
+    if (i >= ns) return;
+    const int l = (int)(i / g.nc), c = (int)(i - (long long)l * g.nc);
+    const int cond = p.n_cond;
+    const double *rho_gas = sn.rho + cond * ns;
+    for (int k = 0; k < p.n_const; ++k) {
+        const double new_w = (rk == 1 && k != cond) ? 0.5 : 1.0, old_w = 1.0 - new_w;
+        const double *f = sn.rho + k * ns;
+        double div = (k == cond) ? divergence<R, FLUX_MAIN>(g, f, rho_gas, theta, sn.u, l, c)
+                                 : divergence<R, FLUX_TRACER>(g, f, rho_gas, theta, sn.u, l, c);
+        double y = -div;
+        if (p.moist) {
+            long long pt = k * ns;
+            if (k == cond + 1) pt -= ns;
+            y = y + pt_rates[pt + i];
+        }
+        st.rho[k * ns + i] = (new_w == 1.0 && rk == 0) ? y : old_w * st.rho[k * ns + i] + new_w * y;
+        if (k == cond) {
+            double div_t = divergence<R, FLUX_THETA>(g, f, rho_gas, theta, sn.u, l, c);
+            double yt = -div_t;
+            if (p.moist) {
+                const double cv = c_v_mass_weighted(sn.rho, cond, 1, ns, i, temperature[i]);
+                yt = yt + C_D_V * sn.rho[cond * ns + i] / cv * (pt_heat[i] + sed_heat[i])
+                              / (C_D_P * (vg.exner_bg[i] + sn.exner_pert[i]))
+                     + pt_rates[cond * ns + i] * theta[i];
+            }
+            st.rhotheta_v[i] = (rk == 0) ? yt : old_w * st.rhotheta_v[i] + new_w * yt;
+        }
+    }
+}
+
+/* ------------------------------------------------------- column solvers
+ * src/time_stepping/column_solvers.c, one column per thread, FP64 */
+constexpr int MAX_L = 64;
+
+/* tridiagonal solve (column_solvers.c:641-669); c, e: sub/super diagonal,
+ * solution written over r */
+__device__ __forceinline__ void thomas(const double *cv, const double *dv, const double *ev, double *rv, int n)
+{
+    double ep[MAX_L];
+    ep[0] = ev[0] / dv[0];
+    for (int j = 1; j < n - 1; ++j) ep[j] = ev[j] / (dv[j] - ep[j - 1] * cv[j - 1]);
+    rv[0] = rv[0] / dv[0];
+    for (int j = 1; j < n; ++j) rv[j] = (rv[j] - rv[j - 1] * cv[j - 1]) / (dv[j] - ep[j - 1] * cv[j - 1]);
+    for (int j = n - 2; j >= 0; --j) rv[j] = rv[j] - ep[j] * rv[j + 1];
+}
+
+/* vertical sound-wave solver (column_solvers.c:19-383; soil and surface
+ * fluxes off) */
+__global__ void k_vertical_waves(VGrid vg, StepParams p, DState so, DState sn, DState st, int rk)
+{
+    const int i = (int)gtid();
+    if (i >= vg.nc) return;
+    const int nl = vg.nl, nc = vg.nc;
+    const long long ns = (long long)nl * nc;
+    const long long gp = p.n_cond * ns;
+    const double dt = p.dt, iw = p.impl_thermo_weight, pdw = 0.5;
+    double cvec[MAX_L], dvec[MAX_L], evec[MAX_L], rvec[MAX_L];
+    double rho_expl[MAX_L], rt_expl[MAX_L], tp_expl[MAX_L], ep_expl[MAX_L];
+    double th_int[MAX_L], rho_io[MAX_L], rho_ie[MAX_L], alpha[MAX_L], beta[MAX_L], gam[MAX_L];
+    for (int j = 0; j < nl; ++j) {
+        const long long b = i + (long long)j * nc;
+        const double vol = vg.volume[b];
+        rho_expl[j] = so.rho[gp + b] + dt * st.rho[gp + b];
+        rt_expl[j] = so.rhotheta_v[b] + dt * st.rhotheta_v[b];
+        if (rk == 0) {
+            const double ro = so.rho[gp + b];
+            alpha[j] = -so.rhotheta_v[b] / (ro * ro) / vol;
+            beta[j] = 1.0 / ro / vol;
+            gam[j] = R_D / (C_D_V * so.rhotheta_v[b]) * (vg.exner_bg[b] + so.exner_pert[b]) / vol;
+        } else {
+            const double ro = so.rho[gp + b], rn = sn.rho[gp + b];
+            const double ao = -so.rhotheta_v[b] / (ro * ro), bo = 1.0 / ro;
+            const double go = R_D / (C_D_V * so.rhotheta_v[b]) * (vg.exner_bg[b] + so.exner_pert[b]);
+            const double an = -sn.rhotheta_v[b] / (rn * rn), bn = 1.0 / rn;
+            const double gn = R_D / (C_D_V * sn.rhotheta_v[b]) * (vg.exner_bg[b] + sn.exner_pert[b]);
+            alpha[j] = ((1.0 - pdw) * ao + pdw * an) / vol;
+            beta[j] = ((1.0 - pdw) * bo + pdw * bn) / vol;
+            gam[j] = ((1.0 - pdw) * go + pdw * gn) / vol;
+        }
+        tp_expl[j] = so.theta_v_pert[b] + dt * vol * (alpha[j] * st.rho[gp + b] + beta[j] * st.rhotheta_v[b]);
+        ep_expl[j] = so.exner_pert[b] + dt * vol * gam[j] * st.rhotheta_v[b];
+    }
+    for (int j = 0; j < nl - 1; ++j) {
+        const long long b = i + (long long)j * nc, lo = b + nc;
+        rho_io[j] = 0.5 * (so.rho[gp + b] + so.rho[gp + lo]);
+        rho_ie[j] = 0.5 * (rho_expl[j] + rho_expl[j + 1]);
+        th_int[j] = 0.5 * (sn.rhotheta_v[b] / sn.rho[gp + b] + sn.rhotheta_v[lo] / sn.rho[gp + lo]);
+    }
+    const double dt2 = dt * dt;
+    for (int j = 0; j < nl - 1; ++j) {
+        const long long b = i + (long long)j * nc, lo = b + nc, wi = i + (long long)(j + 1) * nc;
+        const double dz = vg.z_scalar[b] - vg.z_scalar[lo], dpi = vg.exner_bg[b] - vg.exner_bg[lo];
+        const double wo = so.w[wi];
+        dvec[j] = -(th_int[j] * th_int[j]) * (gam[j] + gam[j + 1])
+                  + 0.5 * dpi * (alpha[j + 1] - alpha[j] + th_int[j] * (beta[j + 1] - beta[j]))
+                  - dz / (iw * dt2 * C_D_P * rho_io[j])
+                        * (2.0 / vg.area_v[wi] + dt * wo * 0.5 * (-1.0 / vg.volume[b] + 1.0 / vg.volume[lo]));
+        rvec[j] = -(wo + dt * st.w[wi]) * dz / (iw * dt2 * C_D_P) + th_int[j] * (ep_expl[j] - ep_expl[j + 1]) / dt
+                  + 0.5 / dt * (tp_expl[j] + tp_expl[j + 1]) * dpi
+                  - dz / (iw * dt2 * C_D_P) * wo * rho_ie[j] / rho_io[j];
+    }
+    for (int j = 0; j < nl - 2; ++j) {
+        const long long b = i + (long long)j * nc, lo = b + nc, lo2 = b + 2 * nc;
+        cvec[j] = th_int[j + 1] * gam[j + 1] * th_int[j]
+                  + 0.5 * (vg.exner_bg[lo] - vg.exner_bg[lo2]) * (alpha[j + 1] + beta[j + 1] * th_int[j])
+                  - (vg.z_scalar[lo] - vg.z_scalar[lo2]) / (iw * dt * C_D_P) * 0.5 * so.w[i + (long long)(j + 2) * nc]
+                        / (vg.volume[lo] * rho_io[j + 1]);
+        evec[j] = th_int[j] * gam[j + 1] * th_int[j + 1]
+                  - 0.5 * (vg.exner_bg[b] - vg.exner_bg[lo]) * (alpha[j + 1] + beta[j + 1] * th_int[j + 1])
+                  + (vg.z_scalar[b] - vg.z_scalar[lo]) / (iw * dt * C_D_P) * 0.5 * so.w[i + (long long)(j + 1) * nc]
+                        / (vg.volume[lo] * rho_io[j]);
+    }
+    thomas(cvec, dvec, evec, rvec, nl - 1);
+    double *sol = rvec;
+    /* Klemp (2008) upper damping layer */
+    const double ztop = vg.z_v[0];
+    for (int j = 0; j < nl - 1; ++j) {
+        const double zad = vg.z_v[i + (long long)(j + 1) * nc] - p.damping_start_height;
+        double dc;
+        if (zad < 0.0) {
+            dc = 0.0;
+        } else {
+            const double s = sin(0.5 * M_PI * zad / (ztop - p.damping_start_height));
+            dc = p.damping_coeff_max * (s * s);
+        }
+        sol[j] = sol[j] / (1.0 + dt * dc);
+    }
+    for (int j = 0; j < nl; ++j) {
+        const long long b = i + (long long)j * nc;
+        const double vol = vg.volume[b];
+        double r, rt;
+        if (j == 0) {
+            r = rho_expl[j] + dt * (sol[j]) / vol;
+            rt = rt_expl[j] + dt * (th_int[j] * sol[j]) / vol;
+        } else if (j == nl - 1) {
+            r = rho_expl[j] + dt * (-sol[j - 1]) / vol;
+            rt = rt_expl[j] + dt * (-th_int[j - 1] * sol[j - 1]) / vol;
+        } else {
+            r = rho_expl[j] + dt * (-sol[j - 1] + sol[j]) / vol;
+            rt = rt_expl[j] + dt * (-th_int[j - 1] * sol[j - 1] + th_int[j] * sol[j]) / vol;
+        }
+        sn.rho[gp + b] = r;
+        sn.rhotheta_v[b] = rt;
+    }
+    for (int j = 0; j < nl - 1; ++j) {
+        const long long b = i + (long long)j * nc, wi = i + (long long)(j + 1) * nc;
+        const double dint = 0.5 * (sn.rho[gp + b] + sn.rho[gp + b + nc]);
+        sn.w[wi] = (2.0 * sol[j] / vg.area_v[wi] - dint * so.w[wi]) / rho_io[j];
+    }
+    for (int j = 0; j < nl; ++j) {
+        const long long b = i + (long long)j * nc;
+        sn.theta_v_pert[b] = sn.rhotheta_v[b] / sn.rho[gp + b] - vg.theta_v_bg[b];
+        sn.exner_pert[b] = so.exner_pert[b] + vg.volume[b] * gam[j] * (sn.rhotheta_v[b] - so.rhotheta_v[b]);
+    }
+}
+
+/* vertical advection and sedimentation of every constituent except the main
+ * gas (column_solvers.c:385-639); one thread per column, constituents in the
+ * reference's order because the sedimentation heat accumulates over them */
+__global__ void k_vertical_tracers(VGrid vg, StepParams p, DState so, DState sn, DState st, const double *temperature,
+                                   double *sed_heat, int rk)
+{
+    const int i = (int)gtid();
+    if (i >= vg.nc) return;
+    const int nl = vg.nl, nc = vg.nc, cond = p.n_cond;
+    const long long ns = (long long)nl * nc;
+    const double dt = p.dt, iw = 0.5, ew = 1.0 - iw;
+    const long long bot = i + ns - nc;
+    const double a_sfc = vg.area_v[(long long)nl * nc + i];
+    for (int k = 0; k < p.n_const; ++k) {
+        if (k == cond) continue;
+        double vsink = 0.0;
+        bool has_sink = false;
+        if (k < cond / 4) { vsink = p.snow_velocity; has_sink = true; }
+        else if (k < cond / 2) { vsink = p.rain_velocity; has_sink = true; }
+        else if (k < cond) { vsink = p.cloud_velocity; has_sink = true; }
+        double cvec[MAX_L], dvec[MAX_L], evec[MAX_L], rvec[MAX_L], fi[MAX_L], fr[MAX_L], fe[MAX_L];
+        const double *ro = so.rho + k * ns;
+        for (int j = 0; j < nl - 1; ++j) {
+            if (rk == 0 && k == 0) sed_heat[(long long)j * nc + i] = 0.0;
+            const long long b = i + (long long)j * nc, lo = b + nc, wi = i + (long long)(j + 1) * nc;
+            double a_ = so.w[wi], b_ = sn.w[wi];
+            if (has_sink) { a_ -= vsink; b_ -= vsink; }
+            const double ar = vg.area_v[wi];
+            a_ = ar * a_;
+            b_ = ar * b_;
+            double dio, tio;
+            if (b_ >= 0.0) { dio = ro[lo]; tio = temperature[lo]; }
+            else { dio = ro[b]; tio = temperature[b]; }
+            fi[j] = a_;
+            fr[j] = dio * b_;
+            fe[j] = c_p_cond(k, tio) * tio * fr[j];
+        }
+        if (rk == 0 && k == 0) sed_heat[(long long)(nl - 1) * nc + i] = 0.0;
+        for (int j = 0; j < nl - 1; ++j) {
+            const long long b = i + (long long)j * nc;
+            if (fi[j] >= 0.0) { cvec[j] = 0.0; evec[j] = -iw * dt / vg.volume[b] * fi[j]; }
+            else { cvec[j] = iw * dt / vg.volume[b + nc] * fi[j]; evec[j] = 0.0; }
+        }
+        for (int j = 0; j < nl; ++j) {
+            const long long b = i + (long long)j * nc;
+            const double vol = vg.volume[b];
+            if (j == 0) {
+                dvec[j] = fi[0] >= 0.0 ? 1.0 : 1.0 - iw * dt / vol * fi[0];
+            } else if (j == nl - 1) {
+                dvec[j] = fi[j - 1] >= 0.0 ? 1.0 + iw * dt / vol * fi[j - 1] : 1.0;
+                if (has_sink) dvec[j] += iw * vsink * dt * a_sfc / vol;
+            } else {
+                dvec[j] = 1.0;
+                if (fi[j - 1] >= 0.0) dvec[j] += iw * dt / vol * fi[j - 1];
+                if (fi[j] < 0.0) dvec[j] -= iw * dt / vol * fi[j];
+            }
+            rvec[j] = ro[b] + dt * st.rho[k * ns + b];
+            if (j == 0) {
+                rvec[j] += ew * dt * fr[j] / vol;
+                if (rk == 0 && k < cond) sed_heat[b] += fe[j] / vol;
+            } else if (j == nl - 1) {
+                rvec[j] += -ew * dt * fr[j - 1] / vol;
+                if (rk == 0 && k < cond) sed_heat[b] += -fe[j - 1] / vol;
+                if (has_sink) {
+                    rvec[j] += -ew * vsink * dt * ro[bot] * a_sfc / vol;
+                    if (rk == 0)
+                        sed_heat[b] += -vsink * temperature[bot] * c_p_cond(k, temperature[bot]) * ro[bot] * a_sfc / vol;
+                }
+            } else {
+                rvec[j] += ew * dt * (-fr[j - 1] + fr[j]) / vol;
+                if (rk == 0 && k < cond) sed_heat[b] += (-fe[j - 1] + fe[j]) / vol;
+            }
+        }
+        thomas(cvec, dvec, evec, rvec, nl);
+        for (int j = 0; j < nl; ++j) {
+            double v = rvec[j];
+            if (v < 0.0) v = 0.0;
+            sn.rho[k * ns + i + (long long)j * nc] = v;
+        }
+    }
+}
+
+}  // namespace
+}  // namespace game
+

@@ -1,0 +1,122 @@
+/*
+ * game_gb300 -- GB300-native RKHEVI dynamical-core step of GAME
+ * (MHBalsmeier/GAME_archived) behind the reference's own C entry points.
+ *
+ * Drop-in boundary.  The functions in section 2 have exactly the names,
+ * argument lists and argument meaning of the reference routines they replace;
+ * a reference build links this library in place of its
+ * src/spatial_operators/*.o and src/time_stepping/*.o.  The reference's
+ * array typedefs (Scalar_field, Vector_field, Curl_field, Dual_vector_field)
+ * decay to double* in a parameter list and are written as double* here; the
+ * struct arguments are the reference's own structs (src/game_types.h:70-238),
+ * passed by pointer and never dereferenced by the caller's side of this
+ * header.  Their layout depends on the reference's compile-time enums
+ * RES_ID, NO_OF_LAYERS and MOISTURE_ON, which the caller hands to
+ * game_gpu_init once; the library computes every member offset at run time.
+ *
+ * Return values: 0 on success, nonzero on a CUDA or validation error
+ * (game_gpu_last_error() describes it).  The reference returns 0 and calls
+ * exit(1) on errors; this library never exits the process.
+ *
+ * Residency.  By default (resident = 0) every call reads its inputs from host
+ * memory and writes its results back to host memory before returning, as the
+ * reference does.  With game_gpu_set_resident(1), manage_rkhevi and
+ * linear_combine_two_states work on device mirrors of the State structs and
+ * touch host memory only through game_gpu_sync_to_device/_to_host.  The
+ * per-operator entry points (grad, divv_h, ...) always work host-in/host-out:
+ * the reference calls them on host arrays outside the time step.
+ *
+ * Threading: one context per process, not re-entrant; calls are synchronous.
+ */
+#ifndef GAME_GB300_H
+#define GAME_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct grid;
+struct dualgrid;
+struct state;
+struct diagnostics;
+struct forcings;
+struct irreversible_quantities;
+struct config;
+
+/* ------------------------------------------------------------------------
+ * 1. library control (no counterpart in the reference)
+ * ---------------------------------------------------------------------- */
+enum { GAME_GPU_FP64 = 0, GAME_GPU_MIXED = 1 };
+
+/* Uploads and renumbers the grid tables once, after the reference's
+ * set_grid_properties (src/io/set_grid_properties.c:21-255) has filled grid
+ * and dualgrid.  res_id, no_of_layers and moisture_on are the reference's
+ * RES_ID, NO_OF_LAYERS and MOISTURE_ON (src/game_types.h:12-20). */
+int game_gpu_init(int res_id, int no_of_layers, int moisture_on, struct grid *grid, struct dualgrid *dualgrid);
+int game_gpu_finalize(void);
+/* GAME_GPU_FP64: every operator in FP64 (results equal the reference's to
+ * rounding); GAME_GPU_MIXED: horizontal operators in FP32, vertical solves,
+ * density and mass-flux accumulation in FP64.  Set before the first step. */
+int game_gpu_set_precision(int precision);
+int game_gpu_set_resident(int resident);
+int game_gpu_set_graphs(int on);
+int game_gpu_sync_to_device(struct state *state);
+int game_gpu_sync_to_host(struct state *state);
+/* writes the library's copies of the lagged step fields back into the host
+ * structs: forcings->pressure_gradient_acc_neg_nl holds the decelerated sum
+ * nl + l and pressure_gradient_acc_neg_l holds 0 (their sum, the only form
+ * in which the step reads them, is exact); pot_vort_tend, v_squared_grad,
+ * diagnostics->temperature, irrev->phase_trans_rates, phase_trans_heating_rate,
+ * condensates_sediment_heat. */
+int game_gpu_sync_aux_to_host(struct diagnostics *diagnostics, struct forcings *forcings,
+                              struct irreversible_quantities *irrev);
+int game_gpu_synchronize(void);
+const char *game_gpu_last_error(void);
+int game_gpu_host_alloc(void **ptr, size_t bytes);
+int game_gpu_host_free(void *ptr);
+long long game_gpu_kernel_launches(int reset);
+
+/* ------------------------------------------------------------------------
+ * 2. drop-in entry points (reference signatures)
+ * ---------------------------------------------------------------------- */
+/* src/time_stepping/time_stepping.h:6 -> src/time_stepping/manage_rkhevi.c:20 */
+int manage_rkhevi(struct state *state_old, struct state *state_new, struct grid *grid, struct dualgrid *dualgrid,
+                  struct state *state_tendency, struct diagnostics *diagnostics, struct forcings *forcings,
+                  struct irreversible_quantities *irrev, struct config *config, double delta_t,
+                  double time_coordinate);
+/* src/spatial_operators/spatial_operators.h:24 -> linear_combine_two_states.c:14 */
+int linear_combine_two_states(struct state *state_0, struct state *state_1, struct state *state_out,
+                              double coeff_0, double coeff_1, struct grid *grid);
+/* spatial_operators.h:6-11 -> gradient_operators.c:14,35,56,66,76 */
+int grad_hor_cov(double *in_field, double *out_field, struct grid *grid);
+int grad_vert_cov(double *in_field, double *out_field, struct grid *grid);
+int vector_field_hor_cov_to_con(double *cov_to_con_field, struct grid *grid);
+int grad_cov(double *in_field, double *out_field, struct grid *grid);
+int grad(double *in_field, double *out_field, struct grid *grid);
+int grad_hor(double *in_field, double *out_field, struct grid *grid);
+/* spatial_operators.h:12-14 -> vorticities.c:18,87,104 */
+int calc_pot_vort(double *velocity_field, double *density_field, struct diagnostics *diagnostics, struct grid *grid,
+                  struct dualgrid *dualgrid);
+int add_f_to_rel_vort(double *rel_vort, double *out_field, struct dualgrid *dualgrid);
+int calc_rel_vort(double *velocity_field, struct diagnostics *diagnostics, struct grid *grid,
+                  struct dualgrid *dualgrid);
+/* spatial_operators.h:15 -> vorticity_flux.c:16 (pot_vorticity is a Curl_field) */
+int vorticity_flux(double *mass_flux_density, double *pot_vorticity, double *out_field, struct grid *grid,
+                   struct dualgrid *dualgrid);
+/* spatial_operators.h:16-17 -> divergences.c:14,66 */
+int divv_h(double *in_field, double *out_field, struct grid *grid);
+int divv_h_tracer(double *in_field, double *density_field, double *wind_field, double *out_field, struct grid *grid);
+/* spatial_operators.h:20-23 -> multiplications.c:35,45,68,98 */
+int scalar_times_vector(double *scalar_field, double *vector_field, double *out_field, struct grid *grid);
+int scalar_times_vector_h(double *in_field_h, double *vector_field, double *out_field, struct grid *grid);
+int scalar_times_vector_h_upstream(double *in_field_h, double *vector_field, double *out_field, struct grid *grid);
+int scalar_times_vector_v(double *in_field_v, double *vector_field, double *out_field, struct grid *grid);
+/* spatial_operators.h:25 -> inner_product.c:13 */
+int inner_product(double *in_field_0, double *in_field_1, double *out_field, struct grid *grid);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

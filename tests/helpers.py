@@ -1,0 +1,65 @@
+"""Shared test set-up: grids, initial states and comparisons.
+
+Initial states are built with the oracle's operators (tests may use the
+oracle); the GPU library is then compared with the oracle on identical inputs.
+"""
+import functools
+
+import numpy as np
+
+from game_archived_gb300 import cases, structs, tables
+from oracle.bind import Oracle
+
+MOUNTAIN = (2000.0, 1.5e6, 30.0, 90.0)   # 2 km Gaussian mountain, 1500 km half-width, 30N 90E
+FIELDS = ("rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind")
+
+
+@functools.lru_cache(maxsize=8)
+def grid_tables(res, mountain=False, n_lloyd=200):
+    return tables.GridTables(res, n_lloyd=n_lloyd, mountain=MOUNTAIN if mountain else None)
+
+
+def make_model(res, moist, case, mountain=False, n_lloyd=200):
+    tab = grid_tables(res, mountain, n_lloyd)
+    lay = structs.Layout(res, 26, moist)
+    m = structs.Model(lay)
+    tables.fill_grid(tab, m.grid, m.dualgrid)
+    cases.default_config(m)
+    cases.build_initial_state(m, tab, case, Oracle(m))
+    return tab, m
+
+
+def clone(model, buffers=None):
+    m2 = structs.Model(model.layout, buffers)
+    for k in structs.Model.KINDS:
+        getattr(m2, k).copy_from(getattr(model, k))
+    return m2
+
+
+def rel_err(a, b):
+    scale = np.max(np.abs(b))
+    if scale == 0:
+        return float(np.max(np.abs(a - b)))
+    return float(np.max(np.abs(a - b)) / scale)
+
+
+def state_errors(s_a, s_b, lay):
+    """norm-relative error max|a-b| / max|b| per prognostic field; the wind's
+    vertical and horizontal parts and each constituent separately"""
+    out = {}
+    ns = lay.n_scalars
+    for k in range(lay.n_const):
+        out[f"rho[{k}]"] = rel_err(s_a["rho"][k * ns:(k + 1) * ns], s_b["rho"][k * ns:(k + 1) * ns])
+    for f in ("rhotheta_v", "theta_v_pert", "exner_pert"):
+        out[f] = rel_err(s_a[f], s_b[f])
+    w_a, w_b = wind_parts(s_a["wind"], lay), wind_parts(s_b["wind"], lay)
+    out["wind_h"] = rel_err(w_a[1], w_b[1])
+    out["wind_v"] = rel_err(w_a[0], w_b[0])
+    return out
+
+
+def wind_parts(wind, lay):
+    nc, ne, vpl = lay.nc, lay.ne, lay.vpl
+    w = np.stack([wind[k * vpl:k * vpl + nc] for k in range(lay.nl + 1)])
+    u = np.stack([wind[k * vpl + nc:(k + 1) * vpl] for k in range(lay.nl)])
+    return w, u
