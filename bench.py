@@ -1,0 +1,459 @@
+#!/usr/bin/env python3
+"""RKHEVI step throughput on GB300.
+
+Workload: GAME's RKHEVI dynamical-core step at RES_ID=6 (40962 cells, 122880
+edges), 26 layers, moist build (6 constituents), flat, barotropic jet with
+70 % relative humidity below 8 km (synthetic, seeded), dt = 100 s.  A "step"
+is one pass of the reference's time loop (src/coordinator.c:302-324):
+linear_combine_two_states(new -> old) followed by manage_rkhevi, both through
+the library's C ABI.
+
+value     mixed-precision step (FP32 horizontal operators, FP64 vertical
+          solves / state), device-resident, steps/s, CUDA events on the
+          library's stream; the FP64 step is reported beside it.
+e2e       the same loop in the default host-in/host-out mode: every call
+          copies its State arguments from pinned host memory to the device and
+          its results back, as a reference driver linked against the library
+          would run it.
+roofline  dominant kernel of the step: algorithmic bytes per launch / its mean
+          launch time (events around every kernel in a separate profiled pass
+          of the same steps), against the measured HBM copy bandwidth.
+cpu_baseline  the oracle (C restatement of the reference, OpenMP over the same
+          loops as the reference) on this host's cores, bounded sample.
+
+--impl reference runs the CPU implementation of the same workload (the
+oracle port, all host threads) and prints the same metric.  Under torchrun
+(N > 1) every rank runs an independent replica (the path does not shard
+without a halo exchange, which the reference does not have); value is the
+total over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RKHEVI steps/s at RES_ID=6 L26: FP32-mixed vs FP64 GPU; adjoint/forward cost"
+L = 26
+
+
+# ------------------------------------------------------------------ sizes
+def grid_sizes(res, nl=L):
+    p4 = 4 ** res
+    nc, ne, nt = 10 * p4 + 2, 30 * p4, 20 * p4
+    s = nl * nc
+    vt = nl * ne + (nl + 1) * nc
+    dv = (nl + 1) * ne + nl * nt
+    return dict(nc=nc, ne=ne, nt=nt, s=s, vt=vt, dv=dv, nl=nl)
+
+
+def b_step(res, n_const, w_s, w_t, w_g, nl=L):
+    """Compulsory bytes of one RKHEVI step: every state, tendency and grid
+    array touched once per substage, B = 2 [3 B_state + 2 B_tend + B_grid]."""
+    g = grid_sizes(res, nl)
+    b_state = ((n_const + 3) * g["s"] + g["vt"]) * w_s
+    b_tend = ((n_const + 1) * g["s"] + nl * g["ne"]) * w_t
+    b_grid = (6 * g["vt"] + 12 * g["s"] + 16 * g["ne"] + 2 * g["dv"]) * w_g \
+        + (26 * g["ne"] + 12 * g["nc"] + 6 * g["nt"]) * 4
+    return 2 * (3 * b_state + 2 * b_tend + b_grid)
+
+
+def kernel_bytes(res, n_const, r, nl=L):
+    """Algorithmic bytes of one step's launches of each kernel (every array
+    a kernel reads or writes counted once per launch; r = bytes of the
+    horizontal-operator type, state 8, indices 4).  Returns name -> (bytes per
+    step, launches per step) for a non-first step."""
+    g = grid_sizes(res, nl)
+    nc, ne, nt, s = g["nc"], g["ne"], g["nt"], g["s"]
+    wl, ul, zl, tl = (nl + 1) * nc, nl * ne, (nl + 1) * ne, nl * nt
+    d, i = 8, 4
+    C = n_const
+    moist = C > 1
+    out = {}
+    out["k_cell_prepare"] = (((4 + C) * s + 7 * s) * d if moist else 5 * s * d, 1)
+    out["k_tri_vort"] = (ul * d + 6 * nt * i + ul * r + 2 * tl * r + ul * r + tl * r, 1)
+    out["k_edge_vort"] = ((ul + wl + s) * d + tl * r + 4 * ne * i + zl * r + ul * r + wl * r + ul * r + 2 * s * r
+                          + 6 * ne * r + 4 * ne * (r + i) + tl * r + zl * r + 2 * ul * r, 1)
+    out["k_cell_kinetic"] = ((ul + wl + s) * d + 8 * s * r + 6 * nc * i + s * r + wl * r, 1)
+    tables_h = 30 * ne * i + 2 * ne * i + 2 * s * r + ul * r + wl * r + ul * r
+    rk0_h = 3 * s * d + C * s * d + ul * r + tables_h + ul * r + 2 * ul * r + ul * d + 2 * ul * r + 2 * ul * d
+    rk1_h = (ul + wl + zl + ul + s) * r + 2 * ul * r + ul * d + ul * d + tables_h + 2 * ul * r + 2 * ul * d
+    out["k_momentum_h"] = (rk0_h + rk1_h, 2)
+    tables_v = 6 * nc * i + 6 * s * r + 2 * wl * r
+    rk0_v = 3 * s * d + C * s * d + wl * r + 3 * wl * r + wl * d + wl * r + wl * d
+    rk1_v = (ul + zl + s) * r + tables_v + 2 * wl * r + C * s * d + wl * r + 2 * wl * d
+    out["k_momentum_v"] = (rk0_v + rk1_v, 2)
+    out["k_theta"] = (2 * 3 * s * d, 2)
+    sc = C * s * d + ul * d + 2 * s * d + (8 * s * d if moist else 0) + 2 * s * d + 18 * nc * i + ul * r + 6 * s * r \
+        + ul * r + wl * r + s * r + (C + 1) * s * d
+    out["k_scalar_tend"] = (2 * sc + (C + 1) * s * d, 2)
+    vw = (4 * s + wl + 3 * s + 2 * s + wl + 4 * s + 2 * wl + 4 * s + wl) * d
+    out["k_vertical_waves"] = (2 * vw, 2)
+    if moist:
+        vt_ = ((C - 1) * 3 * s + 2 * wl + s + s + wl + 2 * s) * d
+        out["k_vertical_tracers"] = (2 * vt_, 2)
+    return out
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region"""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------ set-up
+def build_model(res, moist, n_lloyd, pinned):
+    from game_archived_gb300 import abi, cases, structs, tables
+    tab = tables.GridTables(res, n_lloyd=n_lloyd)
+    lay = structs.Layout(res, L, moist)
+    m = abi.pinned_model(lay) if pinned else structs.Model(lay)
+    tables.fill_grid(tab, m.grid, m.dualgrid)
+    cases.default_config(m)
+    return tab, m
+
+
+def copy_model(src, pinned):
+    from game_archived_gb300 import abi, structs
+    m = abi.pinned_model(src.layout) if pinned else structs.Model(src.layout)
+    for k in structs.Model.KINDS:
+        getattr(m, k).copy_from(getattr(src, k))
+    return m
+
+
+def read_ncu_traffic(kernel):
+    """per-launch DRAM traffic of a kernel from the committed ncu summary"""
+    path = os.path.join(ROOT, "profiles", "ncu_rkhevi_res6_mixed.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == "traffic_per_launch_bytes" and parts[1] == kernel:
+                try:
+                    return float(parts[2])
+                except ValueError:
+                    return None
+    return None
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ GPU arm
+def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, profile=False):
+    from game_archived_gb300 import abi, driver
+    m = copy_model(model0, pinned=False)
+    g = abi.GpuModel(m, precision, resident=True, graphs=True, device=device)
+    try:
+        for s in (m.state_old, m.state_new, m.state_tendency):
+            g.sync_to_device(s)
+        driver.start(m, g.linear_combine_two_states)
+        t = 0.0
+        for n in range(warmup):
+            driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
+            t += dt
+        g.synchronize()
+        g.kernel_launches(reset=True)
+        if sampler:
+            sampler.start()
+        g.event_record(0)
+        for n in range(steps):
+            driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
+            t += dt
+        g.event_record(1)
+        g.synchronize()
+        ms = g.event_elapsed_ms(0, 1)
+        clocks = sampler.stop() if sampler else None
+        launches = g.kernel_launches()
+        prof = None
+        if profile:
+            g.profile(True)
+            for n in range(steps):
+                driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
+                t += dt
+            g.profile(False)
+            prof = g.profile_results()
+        g.sync_to_host(m.state_new)
+        import numpy as np
+        finite = bool(np.isfinite(m.state_new["rho"]).all() and np.isfinite(m.state_new["wind"]).all())
+        return ms / steps, launches, clocks, prof, finite
+    finally:
+        g.close()
+
+
+def time_e2e(model0, precision, steps, warmup, dt, device):
+    from game_archived_gb300 import abi, driver
+    m = copy_model(model0, pinned=True)
+    g = abi.GpuModel(m, precision, resident=False, graphs=True, device=device)
+    try:
+        driver.start(m, g.linear_combine_two_states)
+        t = 0.0
+        for n in range(warmup):
+            driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
+            t += dt
+        g.synchronize()
+        g.transfer_bytes(reset=True)
+        t0 = time.perf_counter()
+        for n in range(steps):
+            driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
+            t += dt
+        g.synchronize()
+        sec = time.perf_counter() - t0
+        h2d, d2h = g.transfer_bytes()
+        return sec / steps, h2d // steps, d2h // steps
+    finally:
+        g.close()
+
+
+def cpu_baseline(model0, dt, max_seconds=25.0):
+    """oracle on all host threads; bounded number of steps"""
+    from game_archived_gb300 import driver
+    from oracle.bind import Oracle
+    m = copy_model(model0, pinned=False)
+    o = Oracle(m)
+    driver.start(m, o.linear_combine_two_states)
+    times = []
+    t = 0.0
+    t_start = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        driver.step(m, o.linear_combine_two_states, o.manage_rkhevi, dt, t)
+        times.append(time.perf_counter() - t0)
+        t += dt
+        if len(times) >= 2 and (time.perf_counter() - t_start > max_seconds or len(times) >= 8):
+            break
+    steady = times[1:] if len(times) > 1 else times
+    return statistics.median(steady), len(times)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_ours(args):
+    from game_archived_gb300 import abi, cases
+    from game_archived_gb300.ops import CAbiOps
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    res, dt = args.res, args.dt
+    tab, model0 = build_model(res, 1, args.n_lloyd, pinned=False)
+    g = abi.GpuModel(model0, abi.FP64, device=local)
+    try:
+        cases.build_initial_state(model0, tab, "jet_moist", CAbiOps(g.lib, model0))
+    finally:
+        g.close()
+    n_const = model0.layout.n_const
+
+    barrier(world)
+    ms64, _, _, _, ok64 = time_resident(model0, abi.FP64, args.steps, args.warmup, dt, local)
+    barrier(world)
+    sampler = ClockSampler(local)
+    ms32, launches, clocks, prof, ok32 = time_resident(model0, abi.MIXED, args.steps, args.warmup, dt, local,
+                                                       sampler=sampler, profile=True)
+    barrier(world)
+    ms32_max = allreduce_max(ms32, world)
+    ms64_max = allreduce_max(ms64, world)
+    e2e_sec, h2d, d2h = time_e2e(model0, abi.MIXED, max(2, args.steps // 4), min(args.warmup, 3), dt, local)
+    e2e_max = allreduce_max(e2e_sec, world)
+    if rank != 0:
+        barrier(world)
+        return
+    value = world * 1000.0 / ms32_max
+    peak, peak_kind = measured_peak()
+    # dominant kernel of the mixed step
+    kb = kernel_bytes(res, n_const, 4)
+    total_ms = sum(v[0] for v in prof.values())
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_n) = dom
+    dom_bytes_step, dom_launch_per_step = kb.get(dom_name, (None, 1))
+    avg_launch_ms = dom_ms / dom_n
+    bytes_per_launch = dom_bytes_step / dom_launch_per_step if dom_bytes_step else None
+    achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9 if bytes_per_launch else None
+    step_bytes = b_step(res, n_const, 8, 8, 4)
+    kernels = {k: {"ms_per_launch": v[0] / v[1], "share": v[0] / total_ms, "launches": v[1]} for k, v in prof.items()}
+    for k, v in kernels.items():
+        if k in kb:
+            bpl = kb[k][0] / kb[k][1]
+            v["algorithmic_bytes_per_launch"] = bpl
+            v["gbs"] = bpl / (v["ms_per_launch"] * 1e-3) / 1e9
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms32_max,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": f"RKHEVI step RES_ID={res} ({grid_sizes(res)['nc']} cells, {grid_sizes(res)['ne']} edges), "
+                               f"26 layers, moist (6 constituents), barotropic jet + RH 0.7, dt={dt:g} s",
+                   "precision": "mixed: FP32 horizontal operators, FP64 vertical solves and state",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "working set per step > L2 (state+tables+work >> 129 MB)"},
+        "fp64": {"steps_per_s": world * 1000.0 / ms64_max, "ms_per_step": ms64_max},
+        "mixed_over_fp64": ms64_max / ms32_max,
+        "roofline": {"bound": "hbm", "kernel": dom_name,
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": read_ncu_traffic(dom_name), "peak_source": peak_kind},
+        "roofline_step": {"algorithmic_bytes": step_bytes, "achieved": step_bytes / (ms32_max * 1e-3) / 1e9,
+                          "peak": peak, "unit": "GB/s", "frac": step_bytes / (ms32_max * 1e-3) / 1e9 / peak},
+        "kernels": kernels,
+        "e2e": {"value": world / e2e_max, "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "finite": bool(ok32 and ok64),
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        sec, n = cpu_baseline(model0, dt)
+        line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{n} RKHEVI steps of the same RES_ID={res} moist workload, FP64, "
+                                          f"median of steps after the first"}
+    print(json.dumps(line))
+    barrier(world)
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from game_archived_gb300 import cases, driver
+    from oracle.bind import Oracle
+    res, dt = args.res, args.dt
+    tab, m = build_model(res, 1, args.n_lloyd, pinned=False)
+    o = Oracle(m)
+    cases.build_initial_state(m, tab, "jet_moist", o)
+    driver.start(m, o.linear_combine_two_states)
+    t = 0.0
+    n_warm = min(args.warmup, 1)
+    n_steps = max(1, min(args.steps, 4))
+    for _ in range(n_warm):
+        driver.step(m, o.linear_combine_two_states, o.manage_rkhevi, dt, t)
+        t += dt
+    t0 = time.perf_counter()
+    for _ in range(n_steps):
+        driver.step(m, o.linear_combine_two_states, o.manage_rkhevi, dt, t)
+        t += dt
+    sec = (time.perf_counter() - t0) / n_steps
+    value = 1.0 / sec
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+        "steps": n_steps, "warmup": n_warm, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"RKHEVI step RES_ID={res}, 26 layers, moist, jet, dt={dt:g} s (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{n_steps} steps after {n_warm} warm-up, OpenMP over all host threads; the "
+                                   "reference's own build cannot run on this host (its sources are not here), so "
+                                   "the oracle port, bit-identical to it, stands in"},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--res", type=int, default=6)
+    ap.add_argument("--dt", type=float, default=100.0)
+    ap.add_argument("--n-lloyd", type=int, default=300)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

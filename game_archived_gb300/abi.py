@@ -25,6 +25,14 @@ SIGNATURES = {
     "game_gpu_host_alloc": ([ctypes.POINTER(vp), ctypes.c_size_t], cint),
     "game_gpu_host_free": ([vp], cint),
     "game_gpu_kernel_launches": ([cint], ctypes.c_longlong),
+    "game_gpu_set_device": ([cint], cint),
+    "game_gpu_event_record": ([cint], cint),
+    "game_gpu_event_elapsed": ([cint, cint, ctypes.POINTER(ctypes.c_float)], cint),
+    "game_gpu_profile": ([cint], cint),
+    "game_gpu_profile_count": ([], cint),
+    "game_gpu_profile_get": ([cint, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_longlong)], cint),
+    "game_gpu_transfer_bytes": ([ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), cint], cint),
     "manage_rkhevi": ([vp] * 9 + [dbl, dbl], cint),
     "linear_combine_two_states": ([vp, vp, vp, dbl, dbl, vp], cint),
     "grad_hor_cov": ([vp] * 3, cint),
@@ -67,10 +75,12 @@ class GpuError(RuntimeError):
 class GpuModel:
     """The CUDA library bound to a Model."""
 
-    def __init__(self, model, precision=FP64, resident=False, graphs=True):
+    def __init__(self, model, precision=FP64, resident=False, graphs=True, device=None):
         self.lib = native.gpu()
         self.m = model
         lay = model.layout
+        if device is not None:
+            self._check(self.lib.game_gpu_set_device(device), "game_gpu_set_device")
         self._check(self.lib.game_gpu_init(lay.res_id, lay.n_layers, lay.moisture_on, model.grid.ptr,
                                            model.dualgrid.ptr), "game_gpu_init")
         self._check(self.lib.game_gpu_set_precision(precision), "set_precision")
@@ -111,6 +121,32 @@ class GpuModel:
 
     def kernel_launches(self, reset=False):
         return int(self.lib.game_gpu_kernel_launches(1 if reset else 0))
+
+    def event_record(self, slot):
+        self._check(self.lib.game_gpu_event_record(slot), "event_record")
+
+    def event_elapsed_ms(self, a, b):
+        ms = ctypes.c_float()
+        self._check(self.lib.game_gpu_event_elapsed(a, b, ctypes.byref(ms)), "event_elapsed")
+        return float(ms.value)
+
+    def profile(self, on):
+        self._check(self.lib.game_gpu_profile(1 if on else 0), "profile")
+
+    def profile_results(self):
+        out = {}
+        name, ms, n = ctypes.c_char_p(), ctypes.c_double(), ctypes.c_longlong()
+        for i in range(self.lib.game_gpu_profile_count()):
+            self._check(self.lib.game_gpu_profile_get(i, ctypes.byref(name), ctypes.byref(ms), ctypes.byref(n)),
+                        "profile_get")
+            out[name.value.decode()] = (ms.value, n.value)
+        return out
+
+    def transfer_bytes(self, reset=False):
+        h, d = ctypes.c_longlong(), ctypes.c_longlong()
+        self._check(self.lib.game_gpu_transfer_bytes(ctypes.byref(h), ctypes.byref(d), 1 if reset else 0),
+                    "transfer_bytes")
+        return h.value, d.value
 
     # -- single operators on host arrays
     def grad(self, s, out):

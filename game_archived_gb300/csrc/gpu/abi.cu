@@ -118,7 +118,7 @@ int run_device_step(Context *c, const StepParams &p, StateMirror *so, StateMirro
     auto launch = [&]() {
         return c->precision == PREC_FP64 ? launch_step_f64(c, p, so, sn, st) : launch_step_mixed(c, p, so, sn, st);
     };
-    if (!c->use_graphs) return launch();
+    if (!c->use_graphs || c->profiling) return launch();
     Context::GraphKey key{p.first_step, c->precision, p.dt, so, sn, st};
     auto it = c->graphs.find(key);
     if (it == c->graphs.end()) {
@@ -278,6 +278,79 @@ long long game_gpu_kernel_launches(int reset)
     long long n = ctx()->kernel_launches;
     if (reset) ctx()->kernel_launches = 0;
     return n;
+}
+
+int game_gpu_set_device(int device)
+{
+    if (ctx()) return fail("game_gpu_set_device must precede game_gpu_init");
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+int game_gpu_event_record(int slot)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    if (slot < 0 || slot > 1 << 20) return fail("event slot out of range");
+    while ((int)c->user_events.size() <= slot) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        c->user_events.push_back(e);
+    }
+    CK(cudaEventRecord(c->user_events[slot], c->stream));
+    return 0;
+}
+
+int game_gpu_event_elapsed(int a, int b, float *ms)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    if (a < 0 || b < 0 || a >= (int)c->user_events.size() || b >= (int)c->user_events.size())
+        return fail("event slot not recorded");
+    CK(cudaEventSynchronize(c->user_events[b]));
+    CK(cudaEventElapsedTime(ms, c->user_events[a], c->user_events[b]));
+    return 0;
+}
+
+int game_gpu_profile(int on)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    if (!on && profile_flush(c)) return -1;
+    if (on) c->prof_totals.clear();
+    c->profiling = on ? 1 : 0;
+    return 0;
+}
+
+int game_gpu_profile_count(void)
+{
+    if (!ctx()) return 0;
+    profile_flush(ctx());
+    return (int)ctx()->prof_totals.size();
+}
+
+int game_gpu_profile_get(int i, const char **name, double *ms, long long *launches)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    if (i < 0 || i >= (int)c->prof_totals.size()) return fail("profile entry out of range");
+    auto it = c->prof_totals.begin();
+    std::advance(it, i);
+    *name = it->first.c_str();
+    *ms = it->second.first;
+    *launches = it->second.second;
+    return 0;
+}
+
+int game_gpu_transfer_bytes(long long *h2d, long long *d2h, int reset)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    *h2d = c->h2d_bytes;
+    *d2h = c->d2h_bytes;
+    if (reset) c->h2d_bytes = c->d2h_bytes = 0;
+    return 0;
 }
 
 /* ---------------------------------------------------------------- the step */

@@ -469,11 +469,29 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
 #undef DI
 }
 
+int profile_flush(Context *c)
+{
+    CK(cudaStreamSynchronize(c->stream));
+    for (auto &p : c->pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        auto &t = c->prof_totals[p.name];
+        t.first += ms;
+        t.second += 1;
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    c->pending.clear();
+    return 0;
+}
+
 int destroy_context()
 {
     Context *c = g_ctx;
     if (!c) return 0;
     cudaDeviceSynchronize();
+    profile_flush(c);
+    for (auto e : c->user_events) cudaEventDestroy(e);
     for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
     for (auto &kv : c->states) cudaFree(kv.second.dev);
     for (auto &b : c->owned) cudaFree(b.p);
@@ -514,6 +532,7 @@ int upload_state(const void *host_state, StateMirror *m)
     Context *c = g_ctx;
     const double *h = (const double *)((const char *)host_state + c->off_state_rho);
     CK(cudaMemcpyAsync(c->staging, h, (size_t)c->state_len * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    c->h2d_bytes += (long long)c->state_len * (long long)sizeof(double);
     launch_gather(m->dev, c->staging, c->map_state, c->state_len, c->stream);
     return 0;
 }
@@ -531,11 +550,14 @@ int download_state(const void *host_state, StateMirror *m, int which_mask)
         {8, (c->n_const + 2) * ns, ns}, {16, (c->n_const + 3) * ns, c->nv}, {32, soil0, c->state_len - soil0}};
     if (which_mask == 63) {
         CK(cudaMemcpyAsync(h, c->staging, (size_t)c->state_len * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        c->d2h_bytes += (long long)c->state_len * (long long)sizeof(double);
     } else {
         for (auto &p : parts)
-            if (which_mask & p.bit)
+            if (which_mask & p.bit) {
                 CK(cudaMemcpyAsync(h + p.lo, c->staging + p.lo, (size_t)p.n * sizeof(double), cudaMemcpyDeviceToHost,
                                    c->stream));
+                c->d2h_bytes += p.n * (long long)sizeof(double);
+            }
     }
     return 0;
 }
@@ -545,13 +567,14 @@ int upload_field(const double *host, double *dev, const int *map, long long n, l
 {
     Context *c = g_ctx;
     CK(cudaMemcpyAsync(c->staging, host, (size_t)host_len * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    c->h2d_bytes += host_len * (long long)sizeof(double);
     launch_gather(dev, c->staging, map, n, c->stream);
     return 0;
 }
 
-/* device layout -> staging -> host, copying back only reference positions
- * [host_lo, host_hi) (the range the operator writes); the staging buffer is
- * first filled from the host so untouched positions keep their values */
+/* device layout -> staging -> host for reference positions [host_lo, host_hi);
+ * the map is a bijection onto the field, so the scatter writes every staging
+ * position of that range */
 int download_field(double *host, const double *dev, const int *map, long long n, long long host_len,
                    long long host_lo, long long host_hi)
 {
@@ -560,6 +583,7 @@ int download_field(double *host, const double *dev, const int *map, long long n,
     launch_scatter(c->staging, dev, map, n, c->stream);
     CK(cudaMemcpyAsync(host + host_lo, c->staging + host_lo, (size_t)(host_hi - host_lo) * sizeof(double),
                        cudaMemcpyDeviceToHost, c->stream));
+    c->d2h_bytes += (host_hi - host_lo) * (long long)sizeof(double);
     return 0;
 }
 

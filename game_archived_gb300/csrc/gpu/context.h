@@ -97,7 +97,40 @@ struct Context {
     std::map<GraphKey, cudaGraphExec_t> graphs;
     int use_graphs = 1;
     int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */
+    long long h2d_bytes = 0, d2h_bytes = 0;
+
+    /* per-kernel timing: events around every step kernel while profiling */
+    int profiling = 0;
+    struct Pending {
+        const char *name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::map<std::string, std::pair<double, long long>> prof_totals; /* name -> (ms, launches) */
+    std::vector<cudaEvent_t> user_events;
 };
+
+/* brackets one kernel launch with events while the context is profiling */
+struct ProfScope {
+    Context *c;
+    cudaEvent_t b = nullptr;
+    const char *name;
+    ProfScope(Context *ctx_, const char *n) : c(ctx_), name(n)
+    {
+        if (c->profiling) {
+            cudaEvent_t a;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, c->stream);
+            c->pending.push_back({name, a, b});
+        }
+    }
+    ~ProfScope()
+    {
+        if (c->profiling) cudaEventRecord(b, c->stream);
+    }
+};
+int profile_flush(Context *c);
 
 Context *ctx();
 void set_error(const std::string &msg);

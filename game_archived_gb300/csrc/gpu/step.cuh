@@ -32,11 +32,17 @@ static void launch_momentum(Context *c, const StepParams &p, StateMirror *so, St
     HGrid<R> &g = hgrid<R>(c);
     Work<R> &w = work<R>(c);
     const int bs = 256;
-    k_momentum_v<R, ADV, PG><<<nblocks((long long)(c->nl + 1) * c->nc, bs), bs, 0, c->stream>>>(
-        g, p, sn->ds, c->vg.theta_v_bg, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w);
-    k_momentum_h<R, ADV, PG><<<nblocks((long long)c->nl * c->ne, bs), bs, 0, c->stream>>>(
-        g, p, sn->ds, so->ds.u, c->vg.theta_v_bg, st->ds.u, w.P_h, w.pg_old_h, w.pvt_h, w.v2g_h, w.flux_h, w.flux_v,
-        w.zh, w.zv, w.v2, new_w, old_w);
+    {
+        ProfScope ps(c, "k_momentum_v");
+        k_momentum_v<R, ADV, PG><<<nblocks((long long)(c->nl + 1) * c->nc, bs), bs, 0, c->stream>>>(
+            g, p, sn->ds, c->vg.theta_v_bg, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w);
+    }
+    {
+        ProfScope ps(c, "k_momentum_h");
+        k_momentum_h<R, ADV, PG><<<nblocks((long long)c->nl * c->ne, bs), bs, 0, c->stream>>>(
+            g, p, sn->ds, so->ds.u, c->vg.theta_v_bg, st->ds.u, w.P_h, w.pg_old_h, w.pvt_h, w.v2g_h, w.flux_h,
+            w.flux_v, w.zh, w.zv, w.v2, new_w, old_w);
+    }
     c->kernel_launches += 2;
 }
 
@@ -48,28 +54,53 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
     Work<R> &w = work<R>(c);
     const int bs = 256;
     const long long ns = c->ns;
-    k_cell_prepare<<<nblocks(ns, bs), bs, 0, c->stream>>>(c->vg, p, so->ds, c->temperature, c->pt_rates, c->pt_heat);
+    {
+        ProfScope ps(c, "k_cell_prepare");
+        k_cell_prepare<<<nblocks(ns, bs), bs, 0, c->stream>>>(c->vg, p, so->ds, c->temperature, c->pt_rates,
+                                                              c->pt_heat);
+    }
     c->kernel_launches++;
     for (int rk = 0; rk < 2; ++rk) {
         const bool adv = rk == 1 || p.first_step;
         const double new_w = rk == 1 ? 0.5 : 1.0, old_w = 1.0 - new_w;
         const double *rho_gas = sn->ds.rho + (long long)c->n_cond * ns;
         if (adv) {
-            k_tri_vort<R><<<nblocks((long long)c->nl * c->nt, bs), bs, 0, c->stream>>>(g, sn->ds.u, w.tri_vort);
-            k_edge_vort<R><<<nblocks((long long)(c->nl + 1) * c->ne, bs), bs, 0, c->stream>>>(
-                g, sn->ds.u, sn->ds.w, rho_gas, w.tri_vort, w.zh, w.zv, w.flux_h);
-            k_cell_kinetic<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(g, sn->ds.u, sn->ds.w, rho_gas, w.v2, w.flux_v);
+            {
+                ProfScope ps(c, "k_tri_vort");
+                k_tri_vort<R><<<nblocks((long long)c->nl * c->nt, bs), bs, 0, c->stream>>>(g, sn->ds.u, w.tri_vort);
+            }
+            {
+                ProfScope ps(c, "k_edge_vort");
+                k_edge_vort<R><<<nblocks((long long)(c->nl + 1) * c->ne, bs), bs, 0, c->stream>>>(
+                    g, sn->ds.u, sn->ds.w, rho_gas, w.tri_vort, w.zh, w.zv, w.flux_h);
+            }
+            {
+                ProfScope ps(c, "k_cell_kinetic");
+                k_cell_kinetic<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(g, sn->ds.u, sn->ds.w, rho_gas, w.v2,
+                                                                          w.flux_v);
+            }
             c->kernel_launches += 3;
         }
         if (rk == 0 && adv) launch_momentum<R, true, true>(c, p, so, sn, st, new_w, old_w);
         else if (rk == 0) launch_momentum<R, false, true>(c, p, so, sn, st, new_w, old_w);
         else launch_momentum<R, true, false>(c, p, so, sn, st, new_w, old_w);
-        k_theta<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(c->vg, p, sn->ds, c->theta);
-        k_scalar_tend<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(g, c->vg, p, sn->ds, st->ds, c->theta, c->temperature,
-                                                                 c->pt_rates, c->pt_heat, c->sed_heat, rk);
-        k_vertical_waves<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, rk);
+        {
+            ProfScope ps(c, "k_theta");
+            k_theta<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(c->vg, p, sn->ds, c->theta);
+        }
+        {
+            ProfScope ps(c, "k_scalar_tend");
+            k_scalar_tend<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(g, c->vg, p, sn->ds, st->ds, c->theta,
+                                                                     c->temperature, c->pt_rates, c->pt_heat,
+                                                                     c->sed_heat, rk);
+        }
+        {
+            ProfScope ps(c, "k_vertical_waves");
+            k_vertical_waves<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, rk);
+        }
         c->kernel_launches += 3;
         if (c->n_const > 1) {
+            ProfScope ps(c, "k_vertical_tracers");
             k_vertical_tracers<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds,
                                                                           c->temperature, c->sed_heat, rk);
             c->kernel_launches++;

@@ -77,6 +77,18 @@ const char *game_gpu_last_error(void);
 int game_gpu_host_alloc(void **ptr, size_t bytes);
 int game_gpu_host_free(void *ptr);
 long long game_gpu_kernel_launches(int reset);
+/* selects the CUDA device (one process per GPU); call before game_gpu_init */
+int game_gpu_set_device(int device);
+/* timing on the library's own stream: record event `slot`, elapsed a -> b */
+int game_gpu_event_record(int slot);
+int game_gpu_event_elapsed(int a, int b, float *ms);
+/* per-kernel timing: while on, every step kernel is bracketed by events
+ * (CUDA graphs are bypassed); entries are (kernel name, total ms, launches) */
+int game_gpu_profile(int on);
+int game_gpu_profile_count(void);
+int game_gpu_profile_get(int i, const char **name, double *ms, long long *launches);
+/* bytes copied host->device and device->host by the library */
+int game_gpu_transfer_bytes(long long *h2d, long long *d2h, int reset);
 
 /* ------------------------------------------------------------------------
  * 2. drop-in entry points (reference signatures)

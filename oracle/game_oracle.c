@@ -36,11 +36,20 @@
 #define NCURL ((long)g->nl * 2 * g->ne + g->ne)
 #define COND (g->n_cond)
 
+/* the loops the reference runs as OpenMP parallel loops; none is a reduction,
+ * so results do not depend on the thread count */
+#ifdef _OPENMP
+#define ORC_PAR _Pragma("omp parallel for schedule(static)")
+#else
+#define ORC_PAR
+#endif
+
 /* ------------------------------------------------------------ gradients
  * src/spatial_operators/gradient_operators.c */
 int orc_grad_hor_cov(const orc_grid *g, const double *in, double *out)
 {
     /* :14-33 */
+    ORC_PAR
     for (long e = 0; e < NE; ++e)
         for (long l = 0; l < NL; ++l) {
             long vi = NC + l * VPL + e;
@@ -52,6 +61,7 @@ int orc_grad_hor_cov(const orc_grid *g, const double *in, double *out)
 int orc_grad_vert_cov(const orc_grid *g, const double *in, double *out)
 {
     /* :35-54 (inner interfaces only; TOA and surface entries are left as they are) */
+    ORC_PAR
     for (long i = NC; i < (long)(NL + 1) * NC - NC; ++i) {
         long layer = i / NC, h = i - layer * NC;
         long lower = h + layer * NC, upper = h + (layer - 1) * NC, vi = h + layer * VPL;
@@ -80,6 +90,7 @@ int orc_grad_hor(const orc_grid *g, const double *in, double *out)
 {
     /* :76-91 */
     orc_grad(g, in, out);
+    ORC_PAR
     for (long i = 0; i < (long)(NL + 1) * NC; ++i) {
         long layer = i / NC, h = i - layer * NC;
         out[h + layer * VPL] = 0;
@@ -143,6 +154,7 @@ static double horizontal_covariant(const orc_grid *g, const double *f, long laye
 int orc_vector_field_hor_cov_to_con(const orc_grid *g, double *f)
 {
     /* :113-133 */
+    ORC_PAR
     for (long i = 0; i < (long)g->n_oro * NE; ++i) {
         long li = i / NE, e = i - li * NE;
         double vg = remap_verpri2horpri_vector(g, f, li + (NL - g->n_oro), e);
@@ -157,6 +169,7 @@ int orc_vector_field_hor_cov_to_con(const orc_grid *g, double *f)
 int orc_divv_h(const orc_grid *g, const double *in, double *out)
 {
     /* :14-64 */
+    ORC_PAR
     for (long h = 0; h < NC; ++h) {
         int n_edges = h < N_PENT ? 5 : 6;
         for (long l = 0; l < NL; ++l) {
@@ -187,6 +200,7 @@ int orc_divv_h(const orc_grid *g, const double *in, double *out)
 int orc_divv_h_tracer(const orc_grid *g, const double *in, const double *density, const double *wind, double *out)
 {
     /* :66-148 */
+    ORC_PAR
     for (long h = 0; h < NC; ++h) {
         int n_edges = h < N_PENT ? 5 : 6;
         for (long l = 0; l < NL; ++l) {
@@ -223,6 +237,7 @@ int orc_divv_h_tracer(const orc_grid *g, const double *in, const double *density
 int orc_scalar_times_vector_h(const orc_grid *g, const double *s, const double *v, double *out)
 {
     /* :45-66 */
+    ORC_PAR
     for (long e = 0; e < NE; ++e)
         for (long l = 0; l < NL; ++l) {
             long vi = NC + l * VPL + e;
@@ -235,6 +250,7 @@ int orc_scalar_times_vector_h(const orc_grid *g, const double *s, const double *
 int orc_scalar_times_vector_h_upstream(const orc_grid *g, const double *s, const double *v, double *out)
 {
     /* :68-96 */
+    ORC_PAR
     for (long e = 0; e < NE; ++e)
         for (long l = 0; l < NL; ++l) {
             long vi = NC + l * VPL + e;
@@ -247,6 +263,7 @@ int orc_scalar_times_vector_h_upstream(const orc_grid *g, const double *s, const
 int orc_scalar_times_vector_v(const orc_grid *g, const double *s, const double *v, double *out)
 {
     /* :98-117 (inner interfaces only) */
+    ORC_PAR
     for (long h = 0; h < NC; ++h)
         for (long l = 1; l < NL; ++l) {
             long i = l * VPL + h;
@@ -268,6 +285,7 @@ int orc_scalar_times_vector(const orc_grid *g, const double *s, const double *v,
  * src/spatial_operators/inner_product.c:13-43 */
 int orc_inner_product(const orc_grid *g, const double *a, const double *b, double *out)
 {
+    ORC_PAR
     for (long h = 0; h < NC; ++h) {
         int n_edges = h < N_PENT ? 5 : 6;
         for (long l = 0; l < NL; ++l) {
@@ -289,6 +307,7 @@ int orc_inner_product(const orc_grid *g, const double *a, const double *b, doubl
 int orc_calc_rel_vort_on_triangles(const orc_grid *g, const double *w, double *out)
 {
     /* :167-222 */
+    ORC_PAR
     for (long i = 0; i < (long)NL * NT; ++i) {
         long layer = i / NT, h = i - layer * NT;
         out[i] = 0;
@@ -318,6 +337,7 @@ int orc_calc_rel_vort(const orc_grid *g, const double *w, orc_diag *d)
 {
     /* :104-165 */
     orc_calc_rel_vort_on_triangles(g, w, d->rel_vort_on_triangles);
+    ORC_PAR
     for (long i = NE; i < NCURL; ++i) {
         long layer = i / (2 * NE), h = i - layer * 2 * NE;
         if (h >= NE) {
@@ -349,6 +369,7 @@ int orc_calc_rel_vort(const orc_grid *g, const double *w, orc_diag *d)
 int orc_add_f_to_rel_vort(const orc_grid *g, const double *rel, double *out)
 {
     /* :87-102 */
+    ORC_PAR
     for (long i = 0; i < NCURL; ++i) {
         long layer = i / (2 * NE), h = i - layer * 2 * NE;
         out[i] = rel[i] + g->f_vec[h];
@@ -374,6 +395,7 @@ int orc_calc_pot_vort(const orc_grid *g, const double *w, const double *rho, orc
     /* :18-85 */
     orc_calc_rel_vort(g, w, d);
     orc_add_f_to_rel_vort(g, d->rel_vort, d->pot_vort);
+    ORC_PAR
     for (long i = 0; i < NCURL; ++i) {
         long layer = i / (2 * NE), h = i - layer * 2 * NE;
         double dens;
@@ -409,6 +431,7 @@ int orc_calc_pot_vort(const orc_grid *g, const double *w, const double *rho, orc
  * src/spatial_operators/vorticity_flux.c:16-187 */
 int orc_vorticity_flux(const orc_grid *g, const double *mf, const double *pv, double *out)
 {
+    ORC_PAR
     for (long h = 0; h < VPL; ++h) {
         for (long l = 0; l < NL + 1; ++l) {
             long i = l * VPL + h;
@@ -463,6 +486,7 @@ int orc_vorticity_flux(const orc_grid *g, const double *mf, const double *pv, do
 int orc_linear_combine_two_states(const orc_grid *g, const orc_state *s0, const orc_state *s1, orc_state *o,
                                   double c0, double c1)
 {
+    ORC_PAR
     for (long i = 0; i < NS; ++i) {
         for (int j = 0; j < g->n_const; ++j)
             o->rho[j * NS + i] = c0 * s0->rho[j * NS + i] + c1 * s1->rho[j * NS + i];
@@ -470,6 +494,7 @@ int orc_linear_combine_two_states(const orc_grid *g, const orc_state *s0, const 
         o->theta_v_pert[i] = o->rhotheta_v[i] / o->rho[COND * NS + i] - g->theta_v_bg[i];
         o->exner_pert[i] = c0 * s0->exner_pert[i] + c1 * s1->exner_pert[i];
     }
+    ORC_PAR
     for (long i = 0; i < NV; ++i) o->wind[i] = c0 * s0->wind[i] + c1 * s1->wind[i];
     return 0;
 }
@@ -624,6 +649,7 @@ int orc_calc_h2otracers_source_rates(const orc_grid *g, const orc_state *s, orc_
     const double max_cloud_water = 0.2e-3;
     double *pr = ir->phase_trans_rates;
     if (c->sfc_phase_trans) return -1;
+    ORC_PAR
     for (long i = 0; i < NS; ++i) {
         double T = d->temperature[i], sat, wvp, dry, air, a, b, cc, p, q, ef, diff, ptd;
         sat = T >= T_0 ? saturation_pressure_over_water(T) : saturation_pressure_over_ice(T);
@@ -699,11 +725,14 @@ int orc_manage_pressure_gradient(const orc_grid *g, const orc_state *s, orc_diag
     /* :17-72 */
     if (c->totally_first_step_bool == 0)
         for (long i = 0; i < NV; ++i) f->pgrad_acc_old[i] = -f->pgrad_nl[i] - f->pgrad_l[i];
+    ORC_PAR
     for (long i = 0; i < NS; ++i) d->scalar_field_placeholder[i] = C_D_P * (g->theta_v_bg[i] + s->theta_v_pert[i]);
     orc_grad(g, s->exner_pert, f->pgrad_nl);
     orc_scalar_times_vector(g, d->scalar_field_placeholder, f->pgrad_nl, f->pgrad_nl);
+    ORC_PAR
     for (long i = 0; i < NS; ++i) d->scalar_field_placeholder[i] = C_D_P * s->theta_v_pert[i];
     orc_scalar_times_vector(g, d->scalar_field_placeholder, g->exner_bg_grad, f->pgrad_l);
+    ORC_PAR
     for (long i = 0; i < NS; ++i)
         ir->pressure_gradient_decel_factor[i] = s->rho[COND * NS + i] / density_total(g, s, i);
     orc_scalar_times_vector(g, ir->pressure_gradient_decel_factor, f->pgrad_nl, f->pgrad_nl);
@@ -716,6 +745,7 @@ int orc_manage_pressure_gradient(const orc_grid *g, const orc_state *s, orc_diag
 int orc_calc_pressure_grad_condensates_v(const orc_grid *g, const orc_state *s, orc_forcings *f, orc_irrev *ir)
 {
     /* :74-87 */
+    ORC_PAR
     for (long i = 0; i < NS; ++i)
         ir->pressure_gradient_decel_factor[i] = s->rho[COND * NS + i] / density_total(g, s, i) - 1.0;
     orc_scalar_times_vector_v(g, ir->pressure_gradient_decel_factor, g->gravity_m, f->pgrad_condensates_v);
@@ -737,6 +767,7 @@ int orc_vector_tendencies_expl(const orc_grid *g, const orc_state *s, orc_state 
     }
     double new_w = rk_step == 1 ? 0.5 : 1.0, old_w = 1.0 - new_w;
     double cur_hor = 0.5 + c->impl_thermo_weight, old_hor = 1.0 - cur_hor, cur_ver = 1.0 - c->impl_thermo_weight;
+    ORC_PAR
     for (long i = 0; i < NV; ++i) {
         long layer = i / VPL, h = i - layer * VPL;
         if (i < NC || i >= NV - NC) {
@@ -777,6 +808,7 @@ int orc_scalar_tendencies_expl(const orc_grid *g, const orc_state *s_old, const 
             orc_scalar_times_vector_h_upstream(g, &s->rho[shift], s->wind, d->flux_density);
             orc_divv_h_tracer(g, d->flux_density, &s->rho[shift], s->wind, d->flux_density_divv);
         }
+        ORC_PAR
         for (long j = 0; j < NS; ++j) {
             long si = shift + j;
             tend->rho[si] = old_w[k] * tend->rho[si]
@@ -827,6 +859,7 @@ int orc_three_band_solver_ver_waves(const orc_grid *g, const orc_state *so, orc_
     const double damp_start = c->damping_start_height_over_toa * g->z_vector[0];
     const double pdw = 0.5;
     const long gp = COND * NS;
+    ORC_PAR
     for (long i = 0; i < NC; ++i) {
         double cvec[64], dvec[64], evec[64], rvec[64], rho_expl[64], rt_expl[64], tp_expl[64], ep_expl[64];
         double th_int[64], sol[64], rho_io[64], rho_ie[64], alpha[64], beta[64], gam[64];
@@ -931,6 +964,7 @@ int orc_three_band_solver_gen_densities(const orc_grid *g, const orc_state *so, 
         if (k < COND / 4) { vsink = c->snow_velocity; has_sink = 1; }
         else if (k < COND / 2) { vsink = c->rain_velocity; has_sink = 1; }
         else if (k < COND) { vsink = c->cloud_droplets_velocity; has_sink = 1; }
+        ORC_PAR
         for (long i = 0; i < NC; ++i) {
             double cvec[64], dvec[64], evec[64], rvec[64], fi[64], fr[64], fe[64], sol[64];
             for (long j = 0; j < NL - 1; ++j) {
@@ -1011,6 +1045,7 @@ int orc_manage_rkhevi(const orc_grid *g, const orc_state *so, orc_state *sn, orc
         if (rk == 0) orc_manage_pressure_gradient(g, sn, d, f, ir, c);
         orc_calc_pressure_grad_condensates_v(g, sn, f, ir);
         orc_vector_tendencies_expl(g, sn, st, d, f, ir, c, rk, dt);
+        ORC_PAR
         for (long e = 0; e < NE; ++e)
             for (long l = 0; l < NL; ++l) {
                 long vi = NC + l * VPL + e;
@@ -1037,6 +1072,7 @@ int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *te
     /* src/io/write_output.c:105-121 with gas_constant_diagnostics
      * (src/constituents/derived_quantities.c:42-61) */
     const double lapse = 0.0065;
+    ORC_PAR
     for (long i = 0; i < NC; ++i) {
         long si = (NL - 1) * NC + i;
         double rgas;
