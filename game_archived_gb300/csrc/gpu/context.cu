@@ -445,6 +445,17 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     c->pt_rates = dalloc<double>(c, 5 * NS);
     c->pt_heat = dalloc<double>(c, NS);
     c->sed_heat = dalloc<double>(c, NS);
+    c->cp_ice = dalloc<double>(c, NS);
+    c->cp_water = dalloc<double>(c, NS);
+    c->wv_layer = dalloc<double>(c, 8 * (size_t)NS);
+    c->wv_rows = dalloc<double>(c, 7 * (size_t)(L - 1) * NC);
+    {
+        std::vector<double> iv(h_vol.size()), ia(h_areav.size());
+        for (size_t k = 0; k < iv.size(); ++k) iv[k] = 1.0 / h_vol[k];
+        for (size_t k = 0; k < ia.size(); ++k) ia[k] = h_areav[k] != 0.0 ? 1.0 / h_areav[k] : 0.0;
+        c->inv_vol = dupload(c, iv);
+        c->inv_area_v = dupload(c, ia);
+    }
     auto work = [&](auto &w, auto tag) {
         using R = decltype(tag);
         w.P_h = dalloc<R>(c, (size_t)L * NE); w.P_v = dalloc<R>(c, (size_t)(L + 1) * NC);

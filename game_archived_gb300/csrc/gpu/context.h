@@ -82,6 +82,12 @@ struct Context {
     double *pt_rates = nullptr;       /* [5][L][Nc] (moist) */
     double *pt_heat = nullptr;        /* [L][Nc] */
     double *sed_heat = nullptr;       /* [L][Nc] */
+    double *cp_ice = nullptr, *cp_water = nullptr; /* c_p of ice / liquid water at T, [L][Nc] */
+    double *inv_vol = nullptr;        /* 1 / volume [L][Nc] (mixed path) */
+    double *inv_area_v = nullptr;     /* 1 / area of the interfaces [L+1][Nc] (mixed path) */
+    /* vertical sound-wave solver: per-layer and per-interface work */
+    double *wv_layer = nullptr;       /* 8 x [L][Nc] */
+    double *wv_rows = nullptr;        /* 7 x [L-1][Nc] */
     Work<double> w64{};
     Work<float> w32{};
 

@@ -199,12 +199,14 @@ __device__ __forceinline__ double dsat_pressure_ice_dT(double t)
     return sat_pressure_ice(t) * (6545.8 / (a * a) - 2.0 / (tc + 868.0));
 }
 
-/* mass-weighted c_v (derived_quantities.c:97-115) */
+/* mass-weighted c_v (derived_quantities.c:97-115); cp_ice / cp_water are
+ * c_p_cond of the even (ice) and odd (liquid) condensates at the cell's
+ * temperature, evaluated once per step */
 __device__ __forceinline__ double c_v_mass_weighted(const double *rho, int n_cond, int moist, long long ns,
-                                                    long long i, double temperature)
+                                                    long long i, double cp_ice, double cp_water)
 {
     double r = 0.0;
-    for (int k = 0; k < n_cond; ++k) r += rho[k * ns + i] * c_p_cond(k, temperature);
+    for (int k = 0; k < n_cond; ++k) r += rho[k * ns + i] * ((k % 2 == 0) ? cp_ice : cp_water);
     r += rho[n_cond * ns + i] * C_D_V;
     if (moist) r += rho[(n_cond + 1) * ns + i] * C_V_V;
     return r;
@@ -214,7 +216,7 @@ __device__ __forceinline__ double c_v_mass_weighted(const double *rho, int n_con
  * temperature (derived_quantities.c:15-40) from state_old and, for the moist
  * build, phase-transition rates and heating (phase_trans.c:16-311) */
 __global__ void k_cell_prepare(VGrid vg, StepParams p, DState so, double *temperature, double *pt_rates,
-                               double *pt_heat)
+                               double *pt_heat, double *cp_ice_out, double *cp_water_out)
 {
     const long long ns = (long long)vg.nl * vg.nc;
     const long long i = gtid();
@@ -230,20 +232,40 @@ __global__ void k_cell_prepare(VGrid vg, StepParams p, DState so, double *temper
     T = (vg.theta_v_bg[i] + so.theta_v_pert[i]) * (vg.exner_bg[i] + so.exner_pert[i])
         / (1.0 + rho[(cond + 1) * ns + i] / rho[cond * ns + i] * (M_D / M_V - 1.0));
     temperature[i] = T;
+    const double cpi = c_p_ice(T), cpw = c_p_water(T);
+    cp_ice_out[i] = cpi;
+    cp_water_out[i] = cpw;
     const double dt = p.dt;
     const double max_cloud_water = 0.2e-3;
-    double sat = T >= T_0 ? sat_pressure_water(T) : sat_pressure_ice(T);
+    /* each transcendental evaluated once; reused values are the same numbers
+     * the reference recomputes */
+    const double sat0 = T >= T_0 ? sat_pressure_water(T) : sat_pressure_ice(T);
     double wvp = rho[(cond + 1) * ns + i] * R_V * T;
     double dry = (rho[cond * ns + i] - rho[(cond + 1) * ns + i]) * R_D * T;
     double air = dry + wvp;
     double ef = T >= T_0 ? 1.00071 * exp(0.000000045 * air) : 0.99882 * exp(0.00000008 * air);
-    sat = ef * sat;
+    double sat = ef * sat0;
     int dir = T >= T_0 ? 0 : 1;
-    double cv = c_v_mass_weighted(rho, cond, 1, ns, i, T);
-    double pth = phase_trans_heat(dir, T);
+    double dsat;
+    if (dir == 0) {
+        double tc = T - T_0;
+        if (tc > 100.0) tc = 100.0;
+        if (tc < 0.0) tc = 0.0;
+        const double q0 = tc + 237.1;
+        dsat = sat0 * (4924.99 / (q0 * q0) - 1.57 / (tc + 105.0));
+    } else {
+        double tc = T - T_0;
+        if (tc < -80.0) tc = -80.0;
+        if (tc > 0.0) tc = 0.0;
+        const double q0 = tc + 278.0;
+        dsat = sat0 * (6545.8 / (q0 * q0) - 2.0 / (tc + 868.0));
+    }
+    const double h_evap = enthalpy_evaporation(T), h_subl = enthalpy_sublimation(T);
+    const double h_melt = h_subl - h_evap;
+    double cv = c_v_mass_weighted(rho, cond, 1, ns, i, cpi, cpw);
+    double pth = dir == 0 ? h_evap : h_subl;
     double a = -R_V * pth / cv;
-    double b = R_V * T - R_V * rho[(cond + 1) * ns + i] * pth / cv
-               + ef * (dir == 0 ? dsat_pressure_water_dT(T) : dsat_pressure_ice_dT(T)) * pth / cv;
+    double b = R_V * T - R_V * rho[(cond + 1) * ns + i] * pth / cv + ef * dsat * pth / cv;
     double cc = wvp - sat;
     double pp = b / a;
     double q = cc / a;
@@ -255,25 +277,25 @@ __global__ void k_cell_prepare(VGrid vg, StepParams p, DState so, double *temper
             double ptd = fmin(rho[3 * ns + i], diff);
             r4 = ptd / dt;
             r3 = rho[2 * ns + i] / dt - ptd / dt;
-            heat = r2 * phase_trans_heat(2, T) - ptd * phase_trans_heat(0, T) / dt;
+            heat = r2 * h_melt - ptd * h_evap / dt;
         } else {
             r3 = -rho[3 * ns + i] / dt;
             double ptd = fmin(rho[2 * ns + i], diff);
             r4 = ptd / dt;
             r2 = rho[3 * ns + i] / dt - ptd / dt;
-            heat = -r3 * phase_trans_heat(2, T) - ptd * phase_trans_heat(1, T) / dt;
+            heat = -r3 * h_melt - ptd * h_subl / dt;
         }
     } else {
         if (T >= T_0) {
             r2 = -rho[2 * ns + i] / dt;
             r4 = diff / dt;
             r3 = rho[2 * ns + i] / dt - diff / dt;
-            heat = r2 * phase_trans_heat(2, T) - diff * phase_trans_heat(0, T) / dt;
+            heat = r2 * h_melt - diff * h_evap / dt;
         } else {
             r3 = -rho[3 * ns + i] / dt;
             r4 = diff / dt;
             r2 = rho[3 * ns + i] / dt - diff / dt;
-            heat = -r3 * phase_trans_heat(2, T) - diff * phase_trans_heat(1, T) / dt;
+            heat = -r3 * h_melt - diff * h_subl / dt;
         }
     }
     r0 = 0.0;
@@ -288,12 +310,12 @@ __global__ void k_cell_prepare(VGrid vg, StepParams p, DState so, double *temper
     if (T >= T_0 && rho[i] > 0.0) {
         r0 = -rho[i] / dt;
         r1 -= r0;
-        heat += r0 * phase_trans_heat(2, T);
+        heat += r0 * h_melt;
     }
     if (T < T_0 && rho[ns + i] > 0.0) {
         r1 = -rho[ns + i] / dt;
         r0 -= r1;
-        heat += -r1 * phase_trans_heat(2, T);
+        heat += -r1 * h_melt;
     }
     pt_rates[i] = r0;
     pt_rates[ns + i] = r1;
@@ -616,49 +638,9 @@ __global__ void k_momentum_v(HGrid<R> g, StepParams p, DState sn, const double *
     tend_w[i] = t;
 }
 
-/* ------------------------------------------------------ k_scalar_tend
+/* ------------------------------------------------------ k_scalar_tend2
  * explicit mass and rho*theta_v tendencies (scalar_tendencies_expl.c:90-178)
- * at (cell, layer).  Edge fluxes are recomputed from the neighbouring cells
- * instead of being stored; the divergence sums run in double. */
-template <typename R>
-__device__ __forceinline__ R flux_centred(const HGrid<R> &g, const double *f, const double *u, int l, int c, int j)
-{
-    const int nb = g.adj_nbr[j * g.nc + c], a = g.adj[j * g.nc + c];
-    const long long o = (long long)l * g.nc;
-    return (R(0.5) * (R(f[o + c]) + R(f[o + nb]))) * R(u[(long long)l * g.ne + a]);
-}
-
-template <typename R>
-__device__ __forceinline__ R flux_theta(const HGrid<R> &g, const double *rho, const double *theta, const double *u,
-                                        int l, int c, int j)
-{
-    const int nb = g.adj_nbr[j * g.nc + c];
-    const long long o = (long long)l * g.nc;
-    return (R(0.5) * (R(theta[o + c]) + R(theta[o + nb]))) * flux_centred(g, rho, u, l, c, j);
-}
-
-template <typename R>
-__device__ __forceinline__ R flux_upstream(const HGrid<R> &g, const double *f, const double *u, int l, int c, int j)
-{
-    const int nb = g.adj_nbr[j * g.nc + c], a = g.adj[j * g.nc + c], sg = g.adj_sign[j * g.nc + c];
-    const long long o = (long long)l * g.nc;
-    const R ue = R(u[(long long)l * g.ne + a]);
-    /* upstream: the edge's from cell where u >= 0 (multiplications.c:68-96) */
-    const bool self_is_from = sg > 0;
-    const double fs = (ue >= R(0)) == self_is_from ? f[o + c] : f[o + nb];
-    return R(fs) * ue;
-}
-
-enum FluxKind { FLUX_MAIN = 0, FLUX_THETA = 1, FLUX_TRACER = 2 };
-
-template <typename R, int KIND>
-__device__ __forceinline__ R edge_flux(const HGrid<R> &g, const double *f, const double *rho_gas, const double *theta,
-                                       const double *u, int l, int c, int j)
-{
-    if (KIND == FLUX_MAIN) return flux_centred(g, f, u, l, c, j);
-    if (KIND == FLUX_THETA) return flux_theta(g, rho_gas, theta, u, l, c, j);
-    return flux_upstream(g, f, u, l, c, j);
-}
+ * at (cell, layer) */
 
 /* vertical_contravariant_corr (averaging.c:41-95) of an edge field given
  * by the functor flux(l, j) at level k of cell c */
@@ -680,62 +662,6 @@ __device__ __forceinline__ R contra_corr(const HGrid<R> &g, int k, int c, int n_
     return r;
 }
 
-/* divergence (divv_h / divv_h_tracer, divergences.c:14-148) of one edge flux
- * at (cell c, layer l); horizontal sum accumulated in double */
-template <typename R, int KIND>
-__device__ __forceinline__ double divergence(const HGrid<R> &g, const double *f, const double *rho_gas,
-                                             const double *theta, const double *u, int l, int c)
-{
-    const int n_edges = c < N_PENT ? 5 : 6;
-    const int nl = g.nl, n_oro = g.n_oro;
-    const long long nc = g.nc;
-    double comp_h = 0.0;
-    for (int j = 0; j < n_edges; ++j) {
-        const int a = g.adj[j * nc + c];
-        const double fx = double(edge_flux<R, KIND>(g, f, rho_gas, theta, u, l, c, j));
-        const double ar = double(g.area_h[(long long)l * g.ne + a]);
-        comp_h += fx * double(g.adj_sign[j * nc + c]) * ar;
-    }
-    double comp_v = 0.0;
-    if (l >= nl - n_oro - 1) {
-        const int ne_ = n_edges;
-        if (KIND != FLUX_TRACER) {
-            auto fl = [&](int ll, int j) { return edge_flux<R, KIND>(g, f, rho_gas, theta, u, ll, c, j); };
-            if (l == nl - n_oro - 1) {
-                R lo = contra_corr(g, l + 1, c, ne_, fl);
-                comp_v = double(-lo * g.area_v[(long long)(l + 1) * nc + c]);
-            } else if (l == nl - 1) {
-                R up = contra_corr(g, l, c, ne_, fl);
-                comp_v = double(up * g.area_v[(long long)l * nc + c]);
-            } else {
-                R up = contra_corr(g, l, c, ne_, fl);
-                R lo = contra_corr(g, l + 1, c, ne_, fl);
-                comp_v = double(up * g.area_v[(long long)l * nc + c] - lo * g.area_v[(long long)(l + 1) * nc + c]);
-            }
-        } else {
-            auto fw = [&](int ll, int j) { return R(u[(long long)ll * g.ne + g.adj[j * nc + c]]); };
-            const long long i = (long long)l * nc + c;
-            if (l == nl - n_oro - 1) {
-                R lo = contra_corr(g, l + 1, c, ne_, fw);
-                R d_lo = lo <= R(0) ? R(f[i]) : R(f[i + nc]);
-                comp_v = double(-d_lo * lo * g.area_v[(long long)(l + 1) * nc + c]);
-            } else if (l == nl - 1) {
-                R up = contra_corr(g, l, c, ne_, fw);
-                R d_up = up <= R(0) ? R(f[i - nc]) : R(f[i]);
-                comp_v = double(d_up * up * g.area_v[(long long)l * nc + c]);
-            } else {
-                R up = contra_corr(g, l, c, ne_, fw);
-                R d_up = up <= R(0) ? R(f[i - nc]) : R(f[i]);
-                R lo = contra_corr(g, l + 1, c, ne_, fw);
-                R d_lo = lo <= R(0) ? R(f[i]) : R(f[i + nc]);
-                comp_v = double(d_up * up * g.area_v[(long long)l * nc + c]
-                                - d_lo * lo * g.area_v[(long long)(l + 1) * nc + c]);
-            }
-        }
-    }
-    return 1.0 / double(g.volume[(long long)l * nc + c]) * (comp_h + comp_v);
-}
-
 template <typename R>
 __global__ void k_theta(VGrid vg, StepParams p, DState sn, double *theta)
 {
@@ -745,22 +671,147 @@ __global__ void k_theta(VGrid vg, StepParams p, DState sn, double *theta)
     theta[i] = sn.rhotheta_v[i] / sn.rho[p.n_cond * ns + i];
 }
 
+/* Restructured explicit scalar tendencies (same arithmetic as k_scalar_tend):
+ * the cell's edge data are loaded once; the terrain correction of the wind
+ * (shared by every tracer) is computed once; the main mass flux is reused for
+ * the rho*theta_v flux.  Edge fluxes are products in R; each flux*area is
+ * converted to double and the divergence accumulated in double.  With
+ * R = double the sums and products are the reference's, bit for bit. */
 template <typename R>
-__global__ void k_scalar_tend(HGrid<R> g, VGrid vg, StepParams p, DState sn, DState st, const double *theta,
-                              const double *temperature, const double *pt_rates, const double *pt_heat,
-                              const double *sed_heat, int rk)
+__global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, VGrid vg, StepParams p, DState sn, DState st,
+                                                      const double *theta, const double *cp_ice,
+                                                      const double *cp_water, const double *pt_rates,
+                                                      const double *pt_heat, const double *sed_heat, int rk)
 {
     const long long ns = (long long)g.nl * g.nc;
     const long long i = gtid();
     if (i >= ns) return;
+    const int nl = g.nl, n_oro = g.n_oro;
     const int l = (int)(i / g.nc), c = (int)(i - (long long)l * g.nc);
+    const long long nc = g.nc, ne = g.ne;
+    const int n_edges = c < N_PENT ? 5 : 6;
     const int cond = p.n_cond;
-    const double *rho_gas = sn.rho + cond * ns;
+    /* layers whose edge values the terrain correction needs */
+    const bool oro = l >= nl - n_oro - 1;
+    const bool has_up_corr = oro && l >= nl - n_oro;            /* contra_corr at level l   */
+    const bool has_lo_corr = oro && l < nl - 1;                 /* contra_corr at level l+1 */
+    const int l_lo = l - 1 >= 0 ? l - 1 : l, l_hi = l + 1 < nl ? l + 1 : l;
+    int a[6], nb[6];
+    bool from_self[6];
+    R ar[6], uu[3][6], wc[3][6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        if (j < n_edges) {
+            a[j] = g.adj[j * nc + c];
+            nb[j] = g.adj_nbr[j * nc + c];
+            from_self[j] = g.adj_sign[j * nc + c] > 0;
+            ar[j] = g.area_h[(long long)l * ne + a[j]];
+            uu[1][j] = R(sn.u[(long long)l * ne + a[j]]);
+            uu[0][j] = R(sn.u[(long long)l_lo * ne + a[j]]);
+            uu[2][j] = R(sn.u[(long long)l_hi * ne + a[j]]);
+            if (oro) {
+                wc[0][j] = R(-0.5) * ipw_at(g, j, l_lo, c) * g.slope_h[(long long)l_lo * ne + a[j]];
+                wc[1][j] = R(-0.5) * ipw_at(g, j, l, c) * g.slope_h[(long long)l * ne + a[j]];
+                wc[2][j] = R(-0.5) * ipw_at(g, j, l_hi, c) * g.slope_h[(long long)l_hi * ne + a[j]];
+            }
+        }
+    }
+    const int lay[3] = {l_lo, l, l_hi};
+    /* vertical_contravariant_corr at level l (slots 0,1) and l+1 (slots 1,2)
+     * of an edge field f[slot][j] (averaging.c:41-95) */
+    auto corr_up = [&](const R (&f)[3][6]) {
+        R r = R(0);
+        if (l > nl - n_oro)
+            for (int j = 0; j < n_edges; ++j) r += wc[0][j] * f[0][j];
+        for (int j = 0; j < n_edges; ++j) r += wc[1][j] * f[1][j];
+        return r;
+    };
+    auto corr_lo = [&](const R (&f)[3][6]) {
+        R r = R(0);
+        if (l + 1 > nl - n_oro)
+            for (int j = 0; j < n_edges; ++j) r += wc[1][j] * f[1][j];
+        for (int j = 0; j < n_edges; ++j) r += wc[2][j] * f[2][j];
+        return r;
+    };
+    const double inv_vol = 1.0 / double(g.volume[i]);
+    const R area_up = g.area_v[(long long)l * nc + c], area_lo = g.area_v[(long long)(l + 1) * nc + c];
+    /* centred vertical part for a flux field with corrections up / lo */
+    auto comp_v_centred = [&](const R (&f)[3][6]) -> double {
+        if (!oro) return 0.0;
+        if (l == nl - n_oro - 1) {
+            R lo = corr_lo(f);
+            return double(-lo * area_lo);
+        }
+        if (l == nl - 1) {
+            R up = corr_up(f);
+            return double(up * area_up);
+        }
+        R up = corr_up(f);
+        R lo = corr_lo(f);
+        return double(up * area_up - lo * area_lo);
+    };
+    auto comp_h_of = [&](const R (&f)[3][6]) -> double {
+        double s = 0.0;
+        for (int j = 0; j < n_edges; ++j) {
+            const R fa = f[1][j] * ar[j];
+            s += from_self[j] ? double(fa) : -double(fa);
+        }
+        return s;
+    };
+    /* wind terrain correction, shared by the tracers */
+    R w_up = R(0), w_lo = R(0);
+    if (oro) {
+        if (has_up_corr) w_up = corr_up(uu);
+        if (has_lo_corr) w_lo = corr_lo(uu);
+    }
+    R fmain[3][6];
     for (int k = 0; k < p.n_const; ++k) {
         const double new_w = (rk == 1 && k != cond) ? 0.5 : 1.0, old_w = 1.0 - new_w;
         const double *f = sn.rho + k * ns;
-        double div = (k == cond) ? divergence<R, FLUX_MAIN>(g, f, rho_gas, theta, sn.u, l, c)
-                                 : divergence<R, FLUX_TRACER>(g, f, rho_gas, theta, sn.u, l, c);
+        R fx[3][6];
+        double comp_h, comp_v;
+        if (k == cond) {
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                if (s != 1 && !oro) continue;
+                const long long o = (long long)lay[s] * nc;
+                const R fs = R(f[o + c]);
+                for (int j = 0; j < n_edges; ++j) fx[s][j] = (R(0.5) * (fs + R(f[o + nb[j]]))) * uu[s][j];
+            }
+            comp_h = comp_h_of(fx);
+            comp_v = comp_v_centred(fx);
+#pragma unroll
+            for (int s = 0; s < 3; ++s)
+                for (int j = 0; j < 6; ++j) fmain[s][j] = fx[s][j];
+        } else {
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                if (s != 1) continue; /* the tracers' vertical part uses the wind, not the flux */
+                const long long o = (long long)lay[s] * nc;
+                const double fs = f[o + c];
+                for (int j = 0; j < n_edges; ++j) {
+                    const bool up_self = (uu[s][j] >= R(0)) == from_self[j];
+                    fx[s][j] = R(up_self ? fs : f[o + nb[j]]) * uu[s][j];
+                }
+            }
+            comp_h = comp_h_of(fx);
+            comp_v = 0.0;
+            if (oro) {
+                const R d_here = R(f[i]);
+                if (l == nl - n_oro - 1) {
+                    const R d_lo = w_lo <= R(0) ? d_here : R(f[i + nc]);
+                    comp_v = double(-d_lo * w_lo * area_lo);
+                } else if (l == nl - 1) {
+                    const R d_up = w_up <= R(0) ? R(f[i - nc]) : d_here;
+                    comp_v = double(d_up * w_up * area_up);
+                } else {
+                    const R d_up = w_up <= R(0) ? R(f[i - nc]) : d_here;
+                    const R d_lo = w_lo <= R(0) ? d_here : R(f[i + nc]);
+                    comp_v = double(d_up * w_up * area_up - d_lo * w_lo * area_lo);
+                }
+            }
+        }
+        const double div = inv_vol * (comp_h + comp_v);
         double y = -div;
         if (p.moist) {
             long long pt = k * ns;
@@ -769,10 +820,19 @@ __global__ void k_scalar_tend(HGrid<R> g, VGrid vg, StepParams p, DState sn, DSt
         }
         st.rho[k * ns + i] = (new_w == 1.0 && rk == 0) ? y : old_w * st.rho[k * ns + i] + new_w * y;
         if (k == cond) {
-            double div_t = divergence<R, FLUX_THETA>(g, f, rho_gas, theta, sn.u, l, c);
+            /* rho*theta_v flux: theta_v averaged to the edge times the mass flux */
+            R ft[3][6];
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                if (s != 1 && !oro) continue;
+                const long long o = (long long)lay[s] * nc;
+                const R ts = R(theta[o + c]);
+                for (int j = 0; j < n_edges; ++j) ft[s][j] = (R(0.5) * (ts + R(theta[o + nb[j]]))) * fmain[s][j];
+            }
+            const double div_t = inv_vol * (comp_h_of(ft) + comp_v_centred(ft));
             double yt = -div_t;
             if (p.moist) {
-                const double cv = c_v_mass_weighted(sn.rho, cond, 1, ns, i, temperature[i]);
+                const double cv = c_v_mass_weighted(sn.rho, cond, 1, ns, i, cp_ice[i], cp_water[i]);
                 yt = yt + C_D_V * sn.rho[cond * ns + i] / cv * (pt_heat[i] + sed_heat[i])
                               / (C_D_P * (vg.exner_bg[i] + sn.exner_pert[i]))
                      + pt_rates[cond * ns + i] * theta[i];
@@ -796,116 +856,6 @@ __device__ __forceinline__ void thomas(const double *cv, const double *dv, const
     rv[0] = rv[0] / dv[0];
     for (int j = 1; j < n; ++j) rv[j] = (rv[j] - rv[j - 1] * cv[j - 1]) / (dv[j] - ep[j - 1] * cv[j - 1]);
     for (int j = n - 2; j >= 0; --j) rv[j] = rv[j] - ep[j] * rv[j + 1];
-}
-
-/* vertical sound-wave solver (column_solvers.c:19-383; soil and surface
- * fluxes off) */
-__global__ void k_vertical_waves(VGrid vg, StepParams p, DState so, DState sn, DState st, int rk)
-{
-    const int i = (int)gtid();
-    if (i >= vg.nc) return;
-    const int nl = vg.nl, nc = vg.nc;
-    const long long ns = (long long)nl * nc;
-    const long long gp = p.n_cond * ns;
-    const double dt = p.dt, iw = p.impl_thermo_weight, pdw = 0.5;
-    double cvec[MAX_L], dvec[MAX_L], evec[MAX_L], rvec[MAX_L];
-    double rho_expl[MAX_L], rt_expl[MAX_L], tp_expl[MAX_L], ep_expl[MAX_L];
-    double th_int[MAX_L], rho_io[MAX_L], rho_ie[MAX_L], alpha[MAX_L], beta[MAX_L], gam[MAX_L];
-    for (int j = 0; j < nl; ++j) {
-        const long long b = i + (long long)j * nc;
-        const double vol = vg.volume[b];
-        rho_expl[j] = so.rho[gp + b] + dt * st.rho[gp + b];
-        rt_expl[j] = so.rhotheta_v[b] + dt * st.rhotheta_v[b];
-        if (rk == 0) {
-            const double ro = so.rho[gp + b];
-            alpha[j] = -so.rhotheta_v[b] / (ro * ro) / vol;
-            beta[j] = 1.0 / ro / vol;
-            gam[j] = R_D / (C_D_V * so.rhotheta_v[b]) * (vg.exner_bg[b] + so.exner_pert[b]) / vol;
-        } else {
-            const double ro = so.rho[gp + b], rn = sn.rho[gp + b];
-            const double ao = -so.rhotheta_v[b] / (ro * ro), bo = 1.0 / ro;
-            const double go = R_D / (C_D_V * so.rhotheta_v[b]) * (vg.exner_bg[b] + so.exner_pert[b]);
-            const double an = -sn.rhotheta_v[b] / (rn * rn), bn = 1.0 / rn;
-            const double gn = R_D / (C_D_V * sn.rhotheta_v[b]) * (vg.exner_bg[b] + sn.exner_pert[b]);
-            alpha[j] = ((1.0 - pdw) * ao + pdw * an) / vol;
-            beta[j] = ((1.0 - pdw) * bo + pdw * bn) / vol;
-            gam[j] = ((1.0 - pdw) * go + pdw * gn) / vol;
-        }
-        tp_expl[j] = so.theta_v_pert[b] + dt * vol * (alpha[j] * st.rho[gp + b] + beta[j] * st.rhotheta_v[b]);
-        ep_expl[j] = so.exner_pert[b] + dt * vol * gam[j] * st.rhotheta_v[b];
-    }
-    for (int j = 0; j < nl - 1; ++j) {
-        const long long b = i + (long long)j * nc, lo = b + nc;
-        rho_io[j] = 0.5 * (so.rho[gp + b] + so.rho[gp + lo]);
-        rho_ie[j] = 0.5 * (rho_expl[j] + rho_expl[j + 1]);
-        th_int[j] = 0.5 * (sn.rhotheta_v[b] / sn.rho[gp + b] + sn.rhotheta_v[lo] / sn.rho[gp + lo]);
-    }
-    const double dt2 = dt * dt;
-    for (int j = 0; j < nl - 1; ++j) {
-        const long long b = i + (long long)j * nc, lo = b + nc, wi = i + (long long)(j + 1) * nc;
-        const double dz = vg.z_scalar[b] - vg.z_scalar[lo], dpi = vg.exner_bg[b] - vg.exner_bg[lo];
-        const double wo = so.w[wi];
-        dvec[j] = -(th_int[j] * th_int[j]) * (gam[j] + gam[j + 1])
-                  + 0.5 * dpi * (alpha[j + 1] - alpha[j] + th_int[j] * (beta[j + 1] - beta[j]))
-                  - dz / (iw * dt2 * C_D_P * rho_io[j])
-                        * (2.0 / vg.area_v[wi] + dt * wo * 0.5 * (-1.0 / vg.volume[b] + 1.0 / vg.volume[lo]));
-        rvec[j] = -(wo + dt * st.w[wi]) * dz / (iw * dt2 * C_D_P) + th_int[j] * (ep_expl[j] - ep_expl[j + 1]) / dt
-                  + 0.5 / dt * (tp_expl[j] + tp_expl[j + 1]) * dpi
-                  - dz / (iw * dt2 * C_D_P) * wo * rho_ie[j] / rho_io[j];
-    }
-    for (int j = 0; j < nl - 2; ++j) {
-        const long long b = i + (long long)j * nc, lo = b + nc, lo2 = b + 2 * nc;
-        cvec[j] = th_int[j + 1] * gam[j + 1] * th_int[j]
-                  + 0.5 * (vg.exner_bg[lo] - vg.exner_bg[lo2]) * (alpha[j + 1] + beta[j + 1] * th_int[j])
-                  - (vg.z_scalar[lo] - vg.z_scalar[lo2]) / (iw * dt * C_D_P) * 0.5 * so.w[i + (long long)(j + 2) * nc]
-                        / (vg.volume[lo] * rho_io[j + 1]);
-        evec[j] = th_int[j] * gam[j + 1] * th_int[j + 1]
-                  - 0.5 * (vg.exner_bg[b] - vg.exner_bg[lo]) * (alpha[j + 1] + beta[j + 1] * th_int[j + 1])
-                  + (vg.z_scalar[b] - vg.z_scalar[lo]) / (iw * dt * C_D_P) * 0.5 * so.w[i + (long long)(j + 1) * nc]
-                        / (vg.volume[lo] * rho_io[j]);
-    }
-    thomas(cvec, dvec, evec, rvec, nl - 1);
-    double *sol = rvec;
-    /* Klemp (2008) upper damping layer */
-    const double ztop = vg.z_v[0];
-    for (int j = 0; j < nl - 1; ++j) {
-        const double zad = vg.z_v[i + (long long)(j + 1) * nc] - p.damping_start_height;
-        double dc;
-        if (zad < 0.0) {
-            dc = 0.0;
-        } else {
-            const double s = sin(0.5 * M_PI * zad / (ztop - p.damping_start_height));
-            dc = p.damping_coeff_max * (s * s);
-        }
-        sol[j] = sol[j] / (1.0 + dt * dc);
-    }
-    for (int j = 0; j < nl; ++j) {
-        const long long b = i + (long long)j * nc;
-        const double vol = vg.volume[b];
-        double r, rt;
-        if (j == 0) {
-            r = rho_expl[j] + dt * (sol[j]) / vol;
-            rt = rt_expl[j] + dt * (th_int[j] * sol[j]) / vol;
-        } else if (j == nl - 1) {
-            r = rho_expl[j] + dt * (-sol[j - 1]) / vol;
-            rt = rt_expl[j] + dt * (-th_int[j - 1] * sol[j - 1]) / vol;
-        } else {
-            r = rho_expl[j] + dt * (-sol[j - 1] + sol[j]) / vol;
-            rt = rt_expl[j] + dt * (-th_int[j - 1] * sol[j - 1] + th_int[j] * sol[j]) / vol;
-        }
-        sn.rho[gp + b] = r;
-        sn.rhotheta_v[b] = rt;
-    }
-    for (int j = 0; j < nl - 1; ++j) {
-        const long long b = i + (long long)j * nc, wi = i + (long long)(j + 1) * nc;
-        const double dint = 0.5 * (sn.rho[gp + b] + sn.rho[gp + b + nc]);
-        sn.w[wi] = (2.0 * sol[j] / vg.area_v[wi] - dint * so.w[wi]) / rho_io[j];
-    }
-    for (int j = 0; j < nl; ++j) {
-        const long long b = i + (long long)j * nc;
-        sn.theta_v_pert[b] = sn.rhotheta_v[b] / sn.rho[gp + b] - vg.theta_v_bg[b];
-        sn.exner_pert[b] = so.exner_pert[b] + vg.volume[b] * gam[j] * (sn.rhotheta_v[b] - so.rhotheta_v[b]);
-    }
 }
 
 /* vertical advection and sedimentation of every constituent except the main

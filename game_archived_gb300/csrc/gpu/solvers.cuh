@@ -1,0 +1,450 @@
+/*
+ * Vertical implicit solvers of the RKHEVI step (src/time_stepping/column_solvers.c),
+ * FP64, restructured for the GPU:
+ *
+ * sound waves (column_solvers.c:19-383) in four kernels
+ *   k_waves_layer   per (layer, column): explicit predictors and the
+ *                   partial derivatives alpha, beta, gamma (:102-139)
+ *   k_waves_rows    per (interface, column): the tridiagonal rows c, d, e, r
+ *                   (:142-189) and the Klemp damping denominator (:285-298)
+ *   k_waves_thomas  per column: the elimination, with the sweep held in
+ *                   registers (layer count a compile-time constant)
+ *   k_waves_apply   per (layer, column): back-substitution into rho, rho*theta_v,
+ *                   w, theta_v', Pi' (:305-370)
+ * tracers (column_solvers.c:385-639)
+ *   k_tracers_solve per (constituent, column): rows built on the fly, Thomas
+ *                   sweep in registers, clipping
+ *   k_tracers_sedheat per (layer, column): sedimentation enthalpy flux
+ *                   divergence, accumulated over the condensates in the
+ *                   reference's order
+ *
+ * EXACT = true keeps the reference's operation order bit for bit (FP64
+ * parity path); EXACT = false (mixed path) multiplies by precomputed
+ * reciprocals of the grid metrics and of repeated denominators, which moves
+ * results by a few ulps but removes most FP64 divisions.
+ */
+#pragma once
+
+#include "kernels.cuh"
+
+namespace game {
+namespace {
+
+struct WavesWork {
+    /* per layer [L][Nc] */
+    double *rho_expl, *rt_expl, *alpha, *beta, *gam, *tp_expl, *ep_expl, *thl;
+    /* per inner interface [L-1][Nc] */
+    double *c, *d, *e, *r, *th_int, *rho_io, *dden;
+    /* mixed path: reciprocal grid metrics */
+    const double *inv_vol;    /* [L][Nc] */
+    const double *inv_area_v; /* [L+1][Nc] */
+};
+
+template <bool EXACT>
+__global__ void k_waves_layer(VGrid vg, StepParams p, DState so, DState sn, DState st, WavesWork ww, int rk)
+{
+    const long long ns = (long long)vg.nl * vg.nc, b = gtid();
+    if (b >= ns) return;
+    const long long gp = p.n_cond * ns;
+    const double dt = p.dt, pdw = 0.5;
+    const double vol = vg.volume[b];
+    const double ro = so.rho[gp + b], rto = so.rhotheta_v[b];
+    double alpha, beta, gam;
+    if (EXACT) {
+        if (rk == 0) {
+            alpha = -rto / (ro * ro) / vol;
+            beta = 1.0 / ro / vol;
+            gam = R_D / (C_D_V * rto) * (vg.exner_bg[b] + so.exner_pert[b]) / vol;
+        } else {
+            const double rn = sn.rho[gp + b];
+            const double ao = -rto / (ro * ro), bo = 1.0 / ro;
+            const double go = R_D / (C_D_V * rto) * (vg.exner_bg[b] + so.exner_pert[b]);
+            const double an = -sn.rhotheta_v[b] / (rn * rn), bn = 1.0 / rn;
+            const double gn = R_D / (C_D_V * sn.rhotheta_v[b]) * (vg.exner_bg[b] + sn.exner_pert[b]);
+            alpha = ((1.0 - pdw) * ao + pdw * an) / vol;
+            beta = ((1.0 - pdw) * bo + pdw * bn) / vol;
+            gam = ((1.0 - pdw) * go + pdw * gn) / vol;
+        }
+    } else {
+        const double iv = ww.inv_vol[b], iro = 1.0 / ro;
+        const double go = (R_D / C_D_V) * (vg.exner_bg[b] + so.exner_pert[b]) / rto;
+        if (rk == 0) {
+            alpha = -rto * iro * iro * iv;
+            beta = iro * iv;
+            gam = go * iv;
+        } else {
+            const double irn = 1.0 / sn.rho[gp + b];
+            const double gn = (R_D / C_D_V) * (vg.exner_bg[b] + sn.exner_pert[b]) / sn.rhotheta_v[b];
+            alpha = 0.5 * (-rto * iro * iro - sn.rhotheta_v[b] * irn * irn) * iv;
+            beta = 0.5 * (iro + irn) * iv;
+            gam = 0.5 * (go + gn) * iv;
+        }
+    }
+    ww.alpha[b] = alpha;
+    ww.beta[b] = beta;
+    ww.gam[b] = gam;
+    ww.rho_expl[b] = ro + dt * st.rho[gp + b];
+    ww.rt_expl[b] = rto + dt * st.rhotheta_v[b];
+    ww.tp_expl[b] = so.theta_v_pert[b] + dt * vol * (alpha * st.rho[gp + b] + beta * st.rhotheta_v[b]);
+    ww.ep_expl[b] = so.exner_pert[b] + dt * vol * gam * st.rhotheta_v[b];
+    ww.thl[b] = sn.rhotheta_v[b] / sn.rho[gp + b];
+}
+
+template <bool EXACT>
+__global__ void k_waves_rows(VGrid vg, StepParams p, DState so, DState st, WavesWork ww)
+{
+    const int nc = vg.nc, nl = vg.nl;
+    const long long n = (long long)(nl - 1) * nc, q = gtid();
+    if (q >= n) return;
+    const int j = (int)(q / nc), i = (int)(q - (long long)j * nc);
+    const long long ns = (long long)nl * nc, gp = p.n_cond * ns;
+    const long long b = q, lo = q + nc, wi = q + nc;
+    const double dt = p.dt, iw = p.impl_thermo_weight, dt2 = dt * dt;
+    const double rho_io = 0.5 * (so.rho[gp + b] + so.rho[gp + lo]);
+    const double rho_ie = 0.5 * (ww.rho_expl[b] + ww.rho_expl[lo]);
+    const double th = 0.5 * (ww.thl[b] + ww.thl[lo]);
+    const double dz = vg.z_scalar[b] - vg.z_scalar[lo], dpi = vg.exner_bg[b] - vg.exner_bg[lo];
+    const double wo = so.w[wi];
+    const double a0 = ww.alpha[b], a1 = ww.alpha[lo], b0 = ww.beta[b], b1 = ww.beta[lo];
+    const double g0 = ww.gam[b], g1 = ww.gam[lo];
+    double dv, rv;
+    if (EXACT) {
+        dv = -(th * th) * (g0 + g1) + 0.5 * dpi * (a1 - a0 + th * (b1 - b0))
+             - dz / (iw * dt2 * C_D_P * rho_io) * (2.0 / vg.area_v[wi] + dt * wo * 0.5 * (-1.0 / vg.volume[b] + 1.0 / vg.volume[lo]));
+        rv = -(wo + dt * st.w[wi]) * dz / (iw * dt2 * C_D_P) + th * (ww.ep_expl[b] - ww.ep_expl[lo]) / dt
+             + 0.5 / dt * (ww.tp_expl[b] + ww.tp_expl[lo]) * dpi - dz / (iw * dt2 * C_D_P) * wo * rho_ie / rho_io;
+    } else {
+        const double k1 = dz / (iw * dt2 * C_D_P), irio = 1.0 / rho_io, idt = 1.0 / dt;
+        dv = -(th * th) * (g0 + g1) + 0.5 * dpi * (a1 - a0 + th * (b1 - b0))
+             - k1 * irio * (2.0 * ww.inv_area_v[wi] + dt * wo * 0.5 * (ww.inv_vol[lo] - ww.inv_vol[b]));
+        rv = -(wo + dt * st.w[wi]) * k1 + th * (ww.ep_expl[b] - ww.ep_expl[lo]) * idt
+             + 0.5 * idt * (ww.tp_expl[b] + ww.tp_expl[lo]) * dpi - k1 * wo * rho_ie * irio;
+    }
+    ww.d[q] = dv;
+    ww.r[q] = rv;
+    ww.th_int[q] = th;
+    ww.rho_io[q] = rho_io;
+    if (j < nl - 2) {
+        const long long lo2 = lo + nc;
+        const double th1 = 0.5 * (ww.thl[lo] + ww.thl[lo2]);
+        const double rho_io1 = 0.5 * (so.rho[gp + lo] + so.rho[gp + lo2]);
+        double cv, ev;
+        if (EXACT) {
+            cv = th1 * g1 * th + 0.5 * (vg.exner_bg[lo] - vg.exner_bg[lo2]) * (a1 + b1 * th)
+                 - (vg.z_scalar[lo] - vg.z_scalar[lo2]) / (iw * dt * C_D_P) * 0.5 * so.w[wi + nc] / (vg.volume[lo] * rho_io1);
+            ev = th * g1 * th1 - 0.5 * dpi * (a1 + b1 * th1)
+                 + dz / (iw * dt * C_D_P) * 0.5 * wo / (vg.volume[lo] * rho_io);
+        } else {
+            const double k2 = 0.5 / (iw * dt * C_D_P) * ww.inv_vol[lo];
+            cv = th1 * g1 * th + 0.5 * (vg.exner_bg[lo] - vg.exner_bg[lo2]) * (a1 + b1 * th)
+                 - (vg.z_scalar[lo] - vg.z_scalar[lo2]) * k2 * so.w[wi + nc] / rho_io1;
+            ev = th * g1 * th1 - 0.5 * dpi * (a1 + b1 * th1) + dz * k2 * wo / rho_io;
+        }
+        ww.c[q] = cv;
+        ww.e[q] = ev;
+    }
+    /* Klemp (2008) damping of the solution at interface j + 1 */
+    const double zad = vg.z_v[wi] - p.damping_start_height;
+    double dc;
+    if (zad < 0.0) {
+        dc = 0.0;
+    } else {
+        const double s = sin(0.5 * M_PI * zad / (vg.z_v[0] - p.damping_start_height));
+        dc = p.damping_coeff_max * (s * s);
+    }
+    ww.dden[q] = 1.0 + dt * dc;
+    (void)i;
+}
+
+/* tridiagonal elimination of one column (column_solvers.c:641-669), forward
+ * sweep kept in registers; solution divided by the damping denominator and
+ * written over r */
+template <int NL, bool EXACT>
+__global__ void k_waves_thomas(int nc, WavesWork ww)
+{
+    const int i = (int)gtid();
+    if (i >= nc) return;
+    constexpr int n = NL - 1;
+    double ep[n], rp[n];
+#pragma unroll
+    for (int j = 0; j < n; ++j) {
+        const long long q = (long long)j * nc + i;
+        const double dj = ww.d[q], rj = ww.r[q];
+        if (j == 0) {
+            if (EXACT) {
+                ep[0] = ww.e[q] / dj;
+                rp[0] = rj / dj;
+            } else {
+                const double inv = 1.0 / dj;
+                ep[0] = ww.e[q] * inv;
+                rp[0] = rj * inv;
+            }
+        } else {
+            const double cm = ww.c[q - nc];
+            const double den = dj - ep[j - 1] * cm;
+            if (EXACT) {
+                if (j < n - 1) ep[j] = ww.e[q] / den;
+                rp[j] = (rj - rp[j - 1] * cm) / den;
+            } else {
+                const double inv = 1.0 / den;
+                if (j < n - 1) ep[j] = ww.e[q] * inv;
+                rp[j] = (rj - rp[j - 1] * cm) * inv;
+            }
+        }
+    }
+    double x = rp[n - 1];
+    ww.r[(long long)(n - 1) * nc + i] = x / ww.dden[(long long)(n - 1) * nc + i];
+#pragma unroll
+    for (int j = n - 2; j >= 0; --j) {
+        x = rp[j] - ep[j] * x;
+        ww.r[(long long)j * nc + i] = x / ww.dden[(long long)j * nc + i];
+    }
+}
+
+/* generic layer count: the sweep in local memory */
+template <bool EXACT>
+__global__ void k_waves_thomas_any(int nc, int nl, WavesWork ww)
+{
+    const int i = (int)gtid();
+    if (i >= nc) return;
+    const int n = nl - 1;
+    double ep[MAX_L], rp[MAX_L];
+    for (int j = 0; j < n; ++j) {
+        const long long q = (long long)j * nc + i;
+        const double dj = ww.d[q], rj = ww.r[q];
+        if (j == 0) {
+            ep[0] = ww.e[q] / dj;
+            rp[0] = rj / dj;
+        } else {
+            const double cm = ww.c[q - nc];
+            const double den = dj - ep[j - 1] * cm;
+            if (j < n - 1) ep[j] = ww.e[q] / den;
+            rp[j] = (rj - rp[j - 1] * cm) / den;
+        }
+    }
+    double x = rp[n - 1];
+    ww.r[(long long)(n - 1) * nc + i] = x / ww.dden[(long long)(n - 1) * nc + i];
+    for (int j = n - 2; j >= 0; --j) {
+        x = rp[j] - ep[j] * x;
+        ww.r[(long long)j * nc + i] = x / ww.dden[(long long)j * nc + i];
+    }
+}
+
+template <bool EXACT>
+__global__ void k_waves_apply(VGrid vg, StepParams p, DState so, DState sn, WavesWork ww)
+{
+    const int nc = vg.nc, nl = vg.nl;
+    const long long ns = (long long)nl * nc, b = gtid();
+    if (b >= ns) return;
+    const int j = (int)(b / nc);
+    const long long gp = p.n_cond * ns;
+    const double dt = p.dt;
+    const double *sol = ww.r;
+    auto rho_new = [&](int jj, long long bb) {
+        const double ve = EXACT ? vg.volume[bb] : 0.0;
+        const double iv = EXACT ? 0.0 : ww.inv_vol[bb];
+        double num;
+        if (jj == 0) num = sol[bb];
+        else if (jj == nl - 1) num = -sol[bb - nc];
+        else num = -sol[bb - nc] + sol[bb];
+        return EXACT ? ww.rho_expl[bb] + dt * (num) / ve : ww.rho_expl[bb] + dt * num * iv;
+    };
+    const double r_new = rho_new(j, b);
+    double num;
+    if (j == 0) num = ww.th_int[b] * sol[b];
+    else if (j == nl - 1) num = -ww.th_int[b - nc] * sol[b - nc];
+    else num = -ww.th_int[b - nc] * sol[b - nc] + ww.th_int[b] * sol[b];
+    const double rt_new = EXACT ? ww.rt_expl[b] + dt * num / vg.volume[b] : ww.rt_expl[b] + dt * num * ww.inv_vol[b];
+    sn.rho[gp + b] = r_new;
+    sn.rhotheta_v[b] = rt_new;
+    sn.theta_v_pert[b] = rt_new / r_new - vg.theta_v_bg[b];
+    sn.exner_pert[b] = so.exner_pert[b] + vg.volume[b] * ww.gam[b] * (rt_new - so.rhotheta_v[b]);
+    if (j < nl - 1) {
+        const long long wi = b + nc;
+        const double r_below = rho_new(j + 1, b + nc);
+        const double dint = 0.5 * (r_new + r_below);
+        if (EXACT)
+            sn.w[wi] = (2.0 * sol[b] / vg.area_v[wi] - dint * so.w[wi]) / ww.rho_io[b];
+        else
+            sn.w[wi] = (2.0 * sol[b] * ww.inv_area_v[wi] - dint * so.w[wi]) / ww.rho_io[b];
+    }
+}
+
+/* ------------------------------------------------------------- tracers */
+struct TracerWork {
+    const double *cp_ice, *cp_water; /* c_p of ice / liquid water at the cell temperature [L][Nc] */
+    const double *inv_vol;           /* mixed path */
+};
+
+__device__ __forceinline__ double sink_velocity(const StepParams &p, int k, bool &has)
+{
+    const int cond = p.n_cond;
+    has = true;
+    if (k < cond / 4) return p.snow_velocity;
+    if (k < cond / 2) return p.rain_velocity;
+    if (k < cond) return p.cloud_velocity;
+    has = false;
+    return 0.0;
+}
+
+/* vertical advection + sedimentation of constituent k in one column
+ * (column_solvers.c:398-635); thread = (k-slot, column) */
+template <int NL, bool EXACT>
+__global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DState st, TracerWork tw)
+{
+    const int nc = vg.nc;
+    const long long ns = (long long)NL * nc;
+    const long long q = gtid();
+    const int n_tr = p.n_const - 1;
+    if (q >= (long long)n_tr * nc) return;
+    const int slot = (int)(q / nc), i = (int)(q - (long long)slot * nc);
+    const int k = slot < p.n_cond ? slot : slot + 1; /* skip the main gas */
+    bool has_sink;
+    const double vsink = sink_velocity(p, k, has_sink);
+    const double dt = p.dt, iw = 0.5, ew = 1.0 - iw;
+    const double *ro = so.rho + k * ns;
+    const double *tr = st.rho + k * ns;
+    const long long bot = i + ns - nc;
+    const double a_sfc = vg.area_v[(long long)NL * nc + i];
+    double ep[NL], rp[NL];
+    double fi_prev = 0.0, fr_prev = 0.0, c_prev = 0.0;
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+        const long long b = i + (long long)j * nc;
+        const double vol = vg.volume[b];
+        const double ivol = EXACT ? 0.0 : tw.inv_vol[b];
+        /* flux at interface j (below layer j) */
+        double fi = 0.0, fr = 0.0, cj = 0.0, ej = 0.0;
+        if (j < NL - 1) {
+            const long long wi = b + nc;
+            double a_ = so.w[wi], b_ = sn.w[wi];
+            if (has_sink) {
+                a_ -= vsink;
+                b_ -= vsink;
+            }
+            const double ar = vg.area_v[wi];
+            a_ = ar * a_;
+            b_ = ar * b_;
+            const double dio = b_ >= 0.0 ? ro[b + nc] : ro[b];
+            fi = a_;
+            fr = dio * b_;
+            if (EXACT) {
+                if (fi >= 0.0) ej = -iw * dt / vol * fi;
+                else cj = iw * dt / vg.volume[b + nc] * fi;
+            } else {
+                if (fi >= 0.0) ej = -iw * dt * ivol * fi;
+                else cj = iw * dt * tw.inv_vol[b + nc] * fi;
+            }
+        }
+        double dj, rj = ro[b] + dt * tr[b];
+        if (EXACT) {
+            if (j == 0) {
+                dj = fi >= 0.0 ? 1.0 : 1.0 - iw * dt / vol * fi;
+                rj += ew * dt * fr / vol;
+            } else if (j == NL - 1) {
+                dj = fi_prev >= 0.0 ? 1.0 + iw * dt / vol * fi_prev : 1.0;
+                if (has_sink) dj += iw * vsink * dt * a_sfc / vol;
+                rj += -ew * dt * fr_prev / vol;
+                if (has_sink) rj += -ew * vsink * dt * ro[bot] * a_sfc / vol;
+            } else {
+                dj = 1.0;
+                if (fi_prev >= 0.0) dj += iw * dt / vol * fi_prev;
+                if (fi < 0.0) dj -= iw * dt / vol * fi;
+                rj += ew * dt * (-fr_prev + fr) / vol;
+            }
+        } else {
+            if (j == 0) {
+                dj = fi >= 0.0 ? 1.0 : 1.0 - iw * dt * ivol * fi;
+                rj += ew * dt * fr * ivol;
+            } else if (j == NL - 1) {
+                dj = fi_prev >= 0.0 ? 1.0 + iw * dt * ivol * fi_prev : 1.0;
+                if (has_sink) dj += iw * vsink * dt * a_sfc * ivol;
+                rj += -ew * dt * fr_prev * ivol;
+                if (has_sink) rj += -ew * vsink * dt * ro[bot] * a_sfc * ivol;
+            } else {
+                dj = 1.0;
+                if (fi_prev >= 0.0) dj += iw * dt * ivol * fi_prev;
+                if (fi < 0.0) dj -= iw * dt * ivol * fi;
+                rj += ew * dt * (-fr_prev + fr) * ivol;
+            }
+        }
+        /* forward elimination */
+        if (j == 0) {
+            if (EXACT) {
+                ep[0] = ej / dj;
+                rp[0] = rj / dj;
+            } else {
+                const double inv = 1.0 / dj;
+                ep[0] = ej * inv;
+                rp[0] = rj * inv;
+            }
+        } else {
+            const double den = dj - ep[j - 1] * c_prev;
+            if (EXACT) {
+                if (j < NL - 1) ep[j] = ej / den;
+                rp[j] = (rj - rp[j - 1] * c_prev) / den;
+            } else {
+                const double inv = 1.0 / den;
+                if (j < NL - 1) ep[j] = ej * inv;
+                rp[j] = (rj - rp[j - 1] * c_prev) * inv;
+            }
+        }
+        fi_prev = fi;
+        fr_prev = fr;
+        c_prev = cj;
+    }
+    double *rn = sn.rho + k * ns;
+    double x = rp[NL - 1];
+    rn[(long long)(NL - 1) * nc + i] = x < 0.0 ? 0.0 : x;
+#pragma unroll
+    for (int j = NL - 2; j >= 0; --j) {
+        x = rp[j] - ep[j] * x;
+        rn[(long long)j * nc + i] = x < 0.0 ? 0.0 : x;
+    }
+}
+
+/* sedimentation heating (rk 0 only): per (layer, column), the condensates'
+ * contributions added in the reference's constituent order */
+template <bool EXACT>
+__global__ void k_tracers_sedheat(VGrid vg, StepParams p, DState so, DState sn, const double *temperature,
+                                  TracerWork tw, double *sed_heat)
+{
+    const int nc = vg.nc, nl = vg.nl;
+    const long long ns = (long long)nl * nc, b = gtid();
+    if (b >= ns) return;
+    const int j = (int)(b / nc), i = (int)(b - (long long)j * nc);
+    const double vol = vg.volume[b];
+    const long long bot = i + ns - nc;
+    const double a_sfc = vg.area_v[(long long)nl * nc + i];
+    /* enthalpy flux of constituent k at interface jj (below layer jj) */
+    auto fe = [&](int k, int jj, double vsink, bool has) {
+        const long long bb = i + (long long)jj * nc, wi = bb + nc;
+        double b_ = sn.w[wi];
+        if (has) b_ -= vsink;
+        b_ = vg.area_v[wi] * b_;
+        const long long up = b_ >= 0.0 ? bb + nc : bb;
+        const double dio = so.rho[k * ns + up], tio = temperature[up];
+        const double fr = dio * b_;
+        const double cp = (k % 2 == 0) ? tw.cp_ice[up] : tw.cp_water[up];
+        return cp * tio * fr;
+    };
+    double sh = 0.0;
+    for (int k = 0; k < p.n_cond; ++k) {
+        bool has;
+        const double vs = sink_velocity(p, k, has);
+        if (j == 0) {
+            sh += fe(k, j, vs, has) / vol;
+        } else if (j == nl - 1) {
+            sh += -fe(k, j - 1, vs, has) / vol;
+            const double tb = temperature[bot];
+            const double cp = (k % 2 == 0) ? tw.cp_ice[bot] : tw.cp_water[bot];
+            sh += -vs * tb * cp * so.rho[k * ns + bot] * a_sfc / vol;
+        } else {
+            sh += (-fe(k, j - 1, vs, has) + fe(k, j, vs, has)) / vol;
+        }
+    }
+    sed_heat[b] = sh;
+}
+
+}  // namespace
+}  // namespace game

@@ -1,12 +1,14 @@
 /*
  * One RKHEVI step on device mirrors (src/time_stepping/manage_rkhevi.c:20-100),
  * templated on the horizontal precision R.  Included by step_f64.cu (R =
- * double, compiled without FMA contraction) and step_mixed.cu (R = float).
+ * double, compiled without FMA contraction, every operation in the
+ * reference's order) and step_mixed.cu (R = float).
  */
 #pragma once
 
 #include "context.h"
 #include "kernels.cuh"
+#include "solvers.cuh"
 
 namespace game {
 
@@ -24,6 +26,25 @@ template <>
 inline Work<double> &work<double>(Context *c) { return c->w64; }
 template <>
 inline Work<float> &work<float>(Context *c) { return c->w32; }
+
+/* the layer count the register-resident column sweeps are compiled for
+ * (NO_OF_LAYERS of every GAME configuration); other counts use the generic
+ * local-memory sweeps */
+constexpr int NL_FIXED = 26;
+
+inline WavesWork waves_work(Context *c)
+{
+    WavesWork w;
+    const long long ns = c->ns, ni = (long long)(c->nl - 1) * c->nc;
+    double *a = c->wv_layer, *b = c->wv_rows;
+    w.rho_expl = a; w.rt_expl = a + ns; w.alpha = a + 2 * ns; w.beta = a + 3 * ns; w.gam = a + 4 * ns;
+    w.tp_expl = a + 5 * ns; w.ep_expl = a + 6 * ns; w.thl = a + 7 * ns;
+    w.c = b; w.d = b + ni; w.e = b + 2 * ni; w.r = b + 3 * ni; w.th_int = b + 4 * ni; w.rho_io = b + 5 * ni;
+    w.dden = b + 6 * ni;
+    w.inv_vol = c->inv_vol;
+    w.inv_area_v = c->inv_area_v;
+    return w;
+}
 
 template <typename R, bool ADV, bool PG>
 static void launch_momentum(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st,
@@ -46,10 +67,58 @@ static void launch_momentum(Context *c, const StepParams &p, StateMirror *so, St
     c->kernel_launches += 2;
 }
 
+template <bool EXACT>
+void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st, int rk)
+{
+    const long long ns = c->ns;
+    WavesWork ww = waves_work(c);
+    {
+        ProfScope ps(c, "k_waves_layer");
+        k_waves_layer<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, ww, rk);
+    }
+    {
+        ProfScope ps(c, "k_waves_rows");
+        k_waves_rows<EXACT><<<nblocks((long long)(c->nl - 1) * c->nc, 256), 256, 0, c->stream>>>(c->vg, p, so->ds,
+                                                                                                 st->ds, ww);
+    }
+    {
+        ProfScope ps(c, "k_waves_thomas");
+        if (c->nl == NL_FIXED)
+            k_waves_thomas<NL_FIXED, EXACT><<<nblocks(c->nc, 64), 64, 0, c->stream>>>(c->nc, ww);
+        else
+            k_waves_thomas_any<EXACT><<<nblocks(c->nc, 64), 64, 0, c->stream>>>(c->nc, c->nl, ww);
+    }
+    {
+        ProfScope ps(c, "k_waves_apply");
+        k_waves_apply<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, ww);
+    }
+    c->kernel_launches += 4;
+    if (c->n_const > 1) {
+        TracerWork tw{c->cp_ice, c->cp_water, c->inv_vol};
+        if (c->nl == NL_FIXED) {
+            if (rk == 0) {
+                ProfScope ps(c, "k_tracers_sedheat");
+                k_tracers_sedheat<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds,
+                                                                                 c->temperature, tw, c->sed_heat);
+                c->kernel_launches++;
+            }
+            ProfScope ps(c, "k_tracers_solve");
+            k_tracers_solve<NL_FIXED, EXACT><<<nblocks((long long)(c->n_const - 1) * c->nc, 64), 64, 0, c->stream>>>(
+                c->vg, p, so->ds, sn->ds, st->ds, tw);
+        } else {
+            ProfScope ps(c, "k_vertical_tracers");
+            k_vertical_tracers<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds,
+                                                                          c->temperature, c->sed_heat, rk);
+        }
+        c->kernel_launches++;
+    }
+}
+
 /* the kernel sequence of one step; everything on c->stream */
 template <typename R>
 void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st)
 {
+    constexpr bool EXACT = sizeof(R) == sizeof(double);
     HGrid<R> &g = hgrid<R>(c);
     Work<R> &w = work<R>(c);
     const int bs = 256;
@@ -57,7 +126,7 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
     {
         ProfScope ps(c, "k_cell_prepare");
         k_cell_prepare<<<nblocks(ns, bs), bs, 0, c->stream>>>(c->vg, p, so->ds, c->temperature, c->pt_rates,
-                                                              c->pt_heat);
+                                                              c->pt_heat, c->cp_ice, c->cp_water);
     }
     c->kernel_launches++;
     for (int rk = 0; rk < 2; ++rk) {
@@ -90,21 +159,12 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
         }
         {
             ProfScope ps(c, "k_scalar_tend");
-            k_scalar_tend<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(g, c->vg, p, sn->ds, st->ds, c->theta,
-                                                                     c->temperature, c->pt_rates, c->pt_heat,
-                                                                     c->sed_heat, rk);
+            k_scalar_tend2<R><<<nblocks(ns, 128), 128, 0, c->stream>>>(g, c->vg, p, sn->ds, st->ds, c->theta,
+                                                                        c->cp_ice, c->cp_water, c->pt_rates,
+                                                                        c->pt_heat, c->sed_heat, rk);
         }
-        {
-            ProfScope ps(c, "k_vertical_waves");
-            k_vertical_waves<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, rk);
-        }
-        c->kernel_launches += 3;
-        if (c->n_const > 1) {
-            ProfScope ps(c, "k_vertical_tracers");
-            k_vertical_tracers<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds,
-                                                                          c->temperature, c->sed_heat, rk);
-            c->kernel_launches++;
-        }
+        c->kernel_launches += 2;
+        launch_vertical<EXACT>(c, p, so, sn, st, rk);
     }
 }
 
