@@ -1,0 +1,73 @@
+"""Pins the oracle to the reference: the reference's own C (compiled from its
+sources into oracle/_ref by oracle/build_ref.py) and the oracle run the same
+driver loop on identical host structs; every byte of State, Diagnostics,
+Forcings and Irreversible_quantities must agree after every step.  Runs only
+where the reference sources exist (this build container)."""
+import numpy as np
+import pytest
+
+from game_archived_gb300 import driver
+from helpers import clone, make_model
+from oracle.bind import Oracle
+
+refbind = pytest.importorskip("refbind")
+pytestmark = pytest.mark.skipif(not refbind.available(), reason="reference sources not present")
+
+CASES = [
+    (3, 0, "std_wind", False, 400.0, 4),
+    (3, 1, "jet_moist", True, 300.0, 3),
+    (4, 0, "std_wind_tpert", True, 200.0, 3),
+    (4, 1, "tracers", False, 300.0, 2),
+]
+
+
+@pytest.mark.parametrize("cfg", CASES, ids=lambda c: f"R{c[0]}M{c[1]}-{c[2]}{'-oro' if c[3] else ''}")
+def test_oracle_bitwise_equals_reference(cfg):
+    res, moist, case, mountain, dt, steps = cfg
+    _, m_ref = make_model(res, moist, case, mountain)
+    m_orc = clone(m_ref)
+    ref = refbind.Reference(m_ref)
+    orc = Oracle(m_orc)
+    driver.start(m_ref, ref.linear_combine_two_states)
+    driver.start(m_orc, orc.linear_combine_two_states)
+    for n in range(steps):
+        driver.step(m_ref, ref.linear_combine_two_states, ref.manage_rkhevi, dt, n * dt)
+        driver.step(m_orc, orc.linear_combine_two_states, orc.manage_rkhevi, dt, n * dt)
+        for k in ("state_old", "state_new", "state_tendency", "diagnostics", "forcings", "irrev"):
+            a, b = getattr(m_ref, k).buf, getattr(m_orc, k).buf
+            assert np.array_equal(a, b), f"step {n}: {k} differs in {np.count_nonzero(a != b)} bytes"
+
+
+def test_reference_operators_equal_oracle():
+    """single operators called on host arrays, as the reference's
+    initialisation and output code call them"""
+    _, m = make_model(3, 1, "tracers", True)
+    ref = refbind.Reference(m)
+    import ctypes
+    vp = ctypes.c_void_p
+    lib = ref.lib
+    lay = m.layout
+    orc = Oracle(m)
+    rng = np.random.default_rng(11)
+    s = m.state_old["exner_pert"] + 1e-3 * rng.standard_normal(lay.n_scalars)
+    wind = m.state_old["wind"].copy()
+    for name, args_ref, args_orc, out_len in [
+        ("grad", None, None, lay.n_vectors),
+        ("inner_product", None, None, lay.n_scalars),
+        ("divv_h", None, None, lay.n_scalars),
+    ]:
+        a = np.zeros(out_len)
+        b = np.zeros(out_len)
+        if name == "grad":
+            getattr(lib, name).argtypes = [vp] * 3
+            lib.grad(s.ctypes.data, a.ctypes.data, m.grid.ptr)
+            orc.grad(s, b)
+        elif name == "inner_product":
+            lib.inner_product.argtypes = [vp] * 4
+            lib.inner_product(wind.ctypes.data, wind.ctypes.data, a.ctypes.data, m.grid.ptr)
+            orc.inner_product(wind, wind, b)
+        else:
+            lib.divv_h.argtypes = [vp] * 3
+            lib.divv_h(wind.ctypes.data, a.ctypes.data, m.grid.ptr)
+            orc.divv_h(wind, b)
+        assert np.array_equal(a, b), name
