@@ -52,6 +52,9 @@ SIGNATURES = {
     "scalar_times_vector_h_upstream": ([vp] * 4, cint),
     "scalar_times_vector_v": ([vp] * 4, cint),
     "inner_product": ([vp] * 4, cint),
+    "global_scalar_integrator": ([vp, vp], dbl),
+    "game_gpu_write_out_integral": ([vp, cint, vp], cint),
+    "game_gpu_surface_pressure": ([vp, vp, vp], cint),
 }
 
 FP64, MIXED = 0, 1
@@ -173,6 +176,35 @@ class GpuModel:
     def vorticity_flux(self, flux, pv, out):
         m = self.m
         self._check(self.lib.vorticity_flux(_p(flux), _p(pv), _p(out), m.grid.ptr, m.dualgrid.ptr), "vorticity_flux")
+
+    # -- integrals and surface pressure
+    def global_scalar_integrator(self, field):
+        import math
+        r = self.lib.global_scalar_integrator(_p(field), self.m.grid.ptr)
+        if math.isnan(r):
+            err = self.lib.game_gpu_last_error().decode()
+            if err:
+                raise GpuError(f"global_scalar_integrator: {err}")
+        return r
+
+    def write_out_integral(self, state, integral_id):
+        """masses (id 0), rho*theta_v (id 1) or (0.5 kinetic, potential,
+        c_v internal) energy (id 2) of a State"""
+        import numpy as np
+        n = {0: self.m.layout.n_const, 1: 1, 2: 3}[integral_id]
+        out = np.zeros(max(n, 1))
+        self._check(self.lib.game_gpu_write_out_integral(state.ptr, integral_id, _p(out)), "write_out_integral")
+        return out[:n]
+
+    def surface_pressure(self, state, with_mslp=False):
+        """surface pressure (and MSLP) per column, reference column order"""
+        import numpy as np
+        nc = self.m.layout.nc
+        ps = np.zeros(nc)
+        ms = np.zeros(nc) if with_mslp else None
+        self._check(self.lib.game_gpu_surface_pressure(state.ptr, _p(ps), _p(ms) if with_mslp else None),
+                    "surface_pressure")
+        return (ps, ms) if with_mslp else ps
 
 
 def pinned_model(layout):

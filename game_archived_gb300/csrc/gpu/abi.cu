@@ -4,7 +4,10 @@
 #include <cstring>
 #include <string>
 
+#include <cmath>
+
 #include "context.h"
+#include "diag.h"
 #include "game_gb300.h"
 #include "ops.h"
 
@@ -66,6 +69,9 @@ StepParams params_from_config(Context *c, const void *config, double dt)
     p.rain_velocity = *member<double>(config, GAME_CONFIG, "rain_velocity");
     p.cloud_velocity = *member<double>(config, GAME_CONFIG, "cloud_droplets_velocity");
     p.first_step = *member<int>(config, GAME_CONFIG, "totally_first_step_bool");
+    p.inv_dt = 1.0 / dt;
+    p.k_rows = 1.0 / (p.impl_thermo_weight * dt * dt * C_D_P);
+    p.k_rows2 = 0.5 / (p.impl_thermo_weight * dt * C_D_P);
     return p;
 }
 
@@ -111,15 +117,20 @@ int import_aux(const void *diag, const void *forc, const void *irrev)
     return 0;
 }
 
-long long g_graph_kernels = 0;
-
 int run_device_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st)
 {
+    /* the damping table is read by the step's kernels: bring it up to date
+     * outside any graph, before the first launch */
+    if (launch_damping_table(c, p)) return -1;
     auto launch = [&]() {
         return c->precision == PREC_FP64 ? launch_step_f64(c, p, so, sn, st) : launch_step_mixed(c, p, so, sn, st);
     };
-    if (!c->use_graphs || c->profiling) return launch();
-    Context::GraphKey key{p.first_step, c->precision, p.dt, so, sn, st};
+    if (!c->use_graphs || c->profiling) {
+        if (launch()) return -1;
+        c->temperature_from_step = 1;
+        return 0;
+    }
+    Context::GraphKey key{p, c->precision, so, sn, st};
     auto it = c->graphs.find(key);
     if (it == c->graphs.end()) {
         const int before = c->kernel_launches;
@@ -133,12 +144,12 @@ int run_device_step(Context *c, const StepParams &p, StateMirror *so, StateMirro
         e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return fail(std::string("graph instantiate: ") + cudaGetErrorString(e));
-        it = c->graphs.emplace(key, exec).first;
-        g_graph_kernels = c->kernel_launches - before;
+        it = c->graphs.emplace(key, Context::GraphEntry{exec, c->kernel_launches - before}).first;
         c->kernel_launches = before;
     }
-    CK(cudaGraphLaunch(it->second, c->stream));
-    c->kernel_launches += (int)g_graph_kernels;
+    CK(cudaGraphLaunch(it->second.exec, c->stream));
+    c->kernel_launches += it->second.launches;
+    c->temperature_from_step = 1;
     return 0;
 }
 
@@ -581,6 +592,102 @@ int vorticity_flux(double *mass_flux_density, double *pot_vorticity, double *out
     if (upload_field(pot_vorticity, pv, c->map_curl, c->ncurl, c->ncurl)) return -1;
     op_vorticity_flux(c, fl, pv, o);
     if (download_field(out_field, o, c->map_vec, c->nv, c->nv, 0, c->nv)) return -1;
+    return finish();
+}
+
+/* ------------------------------------------------ integrals, surface pressure */
+double global_scalar_integrator(double *density_gen, struct grid *grid)
+{
+    if (check_ready(grid)) return NAN;
+    Context *c = ctx();
+    if (cudaMemcpyAsync(c->staging, density_gen, (size_t)c->ns * sizeof(double), cudaMemcpyHostToDevice, c->stream) !=
+        cudaSuccess) {
+        fail("global_scalar_integrator: host-to-device copy failed");
+        return NAN;
+    }
+    c->h2d_bytes += c->ns * (long long)sizeof(double);
+    if (launch_integral(c->staging, 0, 1, c->ns, c->map_s, c->hg64.volume, c->red_partials, c->red_counters, c->red_out,
+                        c->stream))
+        return NAN;
+    c->kernel_launches++;
+    double r = NAN;
+    if (cudaMemcpyAsync(&r, c->red_out, sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
+        fail("global_scalar_integrator: device-to-host copy failed");
+        return NAN;
+    }
+    c->d2h_bytes += (long long)sizeof(double);
+    if (finish()) return NAN;
+    return r;
+}
+
+/* the device mirror of a State for a read-only diagnostic: in resident mode
+ * the mirror as it is, else a fresh upload of the host struct */
+static StateMirror *diag_mirror(struct state *state)
+{
+    Context *c = ctx();
+    if (c->resident) {
+        StateMirror *m = mirror(state, 0);
+        if (!m) fail("resident mode: this State has no device mirror (game_gpu_sync_to_device it first)");
+        return m;
+    }
+    StateMirror *m = mirror(state, 1);
+    if (m && upload_state(state, m)) return nullptr;
+    return m;
+}
+
+int game_gpu_write_out_integral(struct state *state, int integral_id, double *result)
+{
+    if (check_ready(nullptr)) return -1;
+    if (integral_id < 0 || integral_id > 2) return fail("integral_id must be 0 (masses), 1 (rho*theta_v) or 2 (energy)");
+    Context *c = ctx();
+    StateMirror *m = diag_mirror(state);
+    if (!m) return -1;
+    const long long ns = c->ns;
+    int n_out = 1;
+    if (integral_id == 0) {
+        n_out = c->n_const;
+        if (launch_integral(m->ds.rho, ns, n_out, ns, nullptr, c->hg64.volume, c->red_partials, c->red_counters,
+                            c->red_out, c->stream))
+            return -1;
+    } else if (integral_id == 1) {
+        if (launch_integral(m->ds.rhotheta_v, ns, 1, ns, nullptr, c->hg64.volume, c->red_partials, c->red_counters,
+                            c->red_out, c->stream))
+            return -1;
+    } else {
+        n_out = 3;
+        if (!c->temperature_from_step && diag_temperature(c, m, c->temperature)) return -1;
+        if (diag_energy_densities(c, m, c->temperature, c->energy_buf)) return -1;
+        if (launch_integral(c->energy_buf, ns, 3, ns, nullptr, c->hg64.volume, c->red_partials, c->red_counters,
+                            c->red_out, c->stream))
+            return -1;
+    }
+    c->kernel_launches++;
+    double r[INTEGRAL_MAX_FIELDS];
+    CK(cudaMemcpyAsync(r, c->red_out, (size_t)n_out * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    c->d2h_bytes += n_out * (long long)sizeof(double);
+    if (finish()) return -1;
+    if (integral_id == 2) {
+        result[0] = 0.5 * r[0];
+        result[1] = r[1];
+        result[2] = C_D_V * r[2];
+    } else {
+        for (int k = 0; k < n_out; ++k) result[k] = r[k];
+    }
+    return 0;
+}
+
+int game_gpu_surface_pressure(struct state *state, double *surface_p, double *mslp)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    StateMirror *m = diag_mirror(state);
+    if (!m) return -1;
+    double *ps = c->dev_tmp[0], *pm = c->dev_tmp[0] + c->nc;
+    if (diag_surface_pressure(c, m, ps, mslp ? pm : nullptr)) return -1;
+    if (download_field(surface_p, ps, c->map_s, c->nc, c->nc, 0, c->nc)) return -1;
+    /* same stream: the second scatter into the staging buffer runs after the
+     * first copy out of it */
+    if (mslp && download_field(mslp, pm, c->map_s, c->nc, c->nc, 0, c->nc)) return -1;
     return finish();
 }
 

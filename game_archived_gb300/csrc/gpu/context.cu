@@ -12,6 +12,7 @@
 #include <numeric>
 
 #include "context.h"
+#include "diag.h"
 
 namespace game {
 
@@ -29,12 +30,12 @@ const char *last_error() { return g_err.c_str(); }
 
 bool Context::GraphKey::operator<(const GraphKey &o) const
 {
-    if (first != o.first) return first < o.first;
     if (prec != o.prec) return prec < o.prec;
-    if (dt != o.dt) return dt < o.dt;
     if (so != o.so) return so < o.so;
     if (sn != o.sn) return sn < o.sn;
-    return st < o.st;
+    if (st != o.st) return st < o.st;
+    /* StepParams is plain data, value-initialised before it is filled */
+    return std::memcmp(&p, &o.p, sizeof(StepParams)) < 0;
 }
 
 /* ----------------------------------------------------------- gather/scatter */
@@ -377,16 +378,17 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
          t_ndh = dual_upload(c, h_ndh), t_areah = dual_upload(c, h_areah), t_zh = dual_upload(c, h_zh),
          t_slope = dual_upload(c, h_slope), t_ebggh = dual_upload(c, h_ebggh), t_tw = dual_upload(c, h_tw),
          t_rw = dual_upload(c, h_rw), t_fvec = dual_upload(c, h_fvec), t_dah = dual_upload(c, h_dah),
-         t_pvz = dual_upload(c, h_pvz), t_dat = dual_upload(c, h_dat), t_dzt = dual_upload(c, h_dzt);
+         t_pvz = dual_upload(c, h_pvz), t_dat = dual_upload(c, h_dat), t_dzt = dual_upload(c, h_dzt),
+         t_tbg = dual_upload(c, h_tbg), t_ebg = dual_upload(c, h_ebg);
     int *d_adj = dupload(c, h_adj), *d_sign = dupload(c, h_sign), *d_nbr = dupload(c, h_nbr);
     int *d_from = dupload(c, h_from), *d_to = dupload(c, h_to), *d_ti = dupload(c, h_ti), *d_tm = dupload(c, h_tm);
     int *d_ri = dupload(c, h_ri), *d_dfrom = dupload(c, h_dfrom), *d_dto = dupload(c, h_dto);
     int *d_vi = dupload(c, h_vi), *d_vs = dupload(c, h_vs);
-    double *d_zs = dupload(c, h_zs), *d_tbg = dupload(c, h_tbg), *d_ebg = dupload(c, h_ebg), *d_zv = dupload(c, h_zv);
+    double *d_zs = dupload(c, h_zs), *d_tbg = t_tbg.d, *d_ebg = t_ebg.d, *d_zv = dupload(c, h_zv);
 
     auto fill = [&](auto &hg, auto pick) {
         hg.nc = NC; hg.ne = NE; hg.nt = NT; hg.nl = L; hg.n_oro = c->n_oro;
-        hg.volume = pick(t_vol); hg.ipw = pick(t_ipw); hg.adj = d_adj; hg.adj_sign = d_sign; hg.adj_nbr = d_nbr;
+        hg.volume = pick(t_vol); hg.theta_v_bg = pick(t_tbg); hg.exner_bg = pick(t_ebg); hg.ipw = pick(t_ipw); hg.adj = d_adj; hg.adj_sign = d_sign; hg.adj_nbr = d_nbr;
         hg.nd_v = pick(t_ndv); hg.area_v = pick(t_areav); hg.exner_bg_grad_v = pick(t_ebggv); hg.gravity_m_v = pick(t_gmv);
         hg.from = d_from; hg.to = d_to; hg.nd_h = pick(t_ndh); hg.area_h = pick(t_areah); hg.z_h = pick(t_zh);
         hg.slope_h = pick(t_slope); hg.exner_bg_grad_h = pick(t_ebggh); hg.trsk_w = pick(t_tw); hg.trsk_i = d_ti;
@@ -447,8 +449,18 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     c->sed_heat = dalloc<double>(c, NS);
     c->cp_ice = dalloc<double>(c, NS);
     c->cp_water = dalloc<double>(c, NS);
+    c->shadow = dalloc<float>(c, (size_t)(c->n_const + 3) * NS + (size_t)(L + 1) * NC + (size_t)L * NE);
+    c->theta32 = dalloc<float>(c, NS);
+    c->cp32_ice = dalloc<float>(c, NS);
+    c->cp32_water = dalloc<float>(c, NS);
+    c->gravity_potential = dupload(c, cell_field(gpot));
+    c->red_partials = dalloc<double>(c, (size_t)2 * INTEGRAL_MAX_BLOCKS * INTEGRAL_MAX_FIELDS);
+    c->red_counters = dalloc<unsigned>(c, INTEGRAL_MAX_FIELDS);
+    c->red_out = dalloc<double>(c, INTEGRAL_MAX_FIELDS);
+    c->energy_buf = dalloc<double>(c, 3 * (size_t)NS);
     c->wv_layer = dalloc<double>(c, 8 * (size_t)NS);
     c->wv_rows = dalloc<double>(c, 7 * (size_t)(L - 1) * NC);
+    c->damp_dc = dalloc<double>(c, (size_t)(L - 1) * NC);
     {
         std::vector<double> iv(h_vol.size()), ia(h_areav.size());
         for (size_t k = 0; k < iv.size(); ++k) iv[k] = 1.0 / h_vol[k];
@@ -503,7 +515,7 @@ int destroy_context()
     cudaDeviceSynchronize();
     profile_flush(c);
     for (auto e : c->user_events) cudaEventDestroy(e);
-    for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
     for (auto &kv : c->states) cudaFree(kv.second.dev);
     for (auto &b : c->owned) cudaFree(b.p);
     if (c->stream) cudaStreamDestroy(c->stream);

@@ -83,6 +83,17 @@ struct Context {
     double *pt_heat = nullptr;        /* [L][Nc] */
     double *sed_heat = nullptr;       /* [L][Nc] */
     double *cp_ice = nullptr, *cp_water = nullptr; /* c_p of ice / liquid water at T, [L][Nc] */
+    /* mixed path: FP32 shadow of state_new and FP32 copies of per-step fields */
+    float *shadow = nullptr;          /* [rho C*S][rhotheta S][theta' S][Pi' S][w (L+1)Nc][u L*Ne] */
+    float *theta32 = nullptr, *cp32_ice = nullptr, *cp32_water = nullptr;
+    double *gravity_potential = nullptr; /* [L][Nc] */
+    /* global integrals: per-block (hi, lo) partial sums, one counter and one
+     * result per field, and three energy-density fields [3][L][Nc] */
+    double *red_partials = nullptr;
+    unsigned *red_counters = nullptr;
+    double *red_out = nullptr;
+    double *energy_buf = nullptr;
+    int temperature_from_step = 0;   /* temperature holds T(state_old) of the last step */
     double *inv_vol = nullptr;        /* 1 / volume [L][Nc] (mixed path) */
     double *inv_area_v = nullptr;     /* 1 / area of the interfaces [L+1][Nc] (mixed path) */
     /* vertical sound-wave solver: per-layer and per-interface work */
@@ -93,14 +104,24 @@ struct Context {
 
     std::map<const void *, StateMirror> states;
 
-    /* CUDA graphs of the device-side step, keyed by (first_step, precision, dt) */
+    /* CUDA graphs of the device-side step, keyed by every value the launches
+     * capture: the step parameters (time step, config values, first-step
+     * flag), the precision and the three state mirrors */
     struct GraphKey {
-        int first, prec;
-        double dt;
+        StepParams p;
+        int prec;
         const void *so, *sn, *st;
         bool operator<(const GraphKey &o) const;
     };
-    std::map<GraphKey, cudaGraphExec_t> graphs;
+    struct GraphEntry {
+        cudaGraphExec_t exec;
+        int launches; /* kernels in the graph */
+    };
+    std::map<GraphKey, GraphEntry> graphs;
+    /* Klemp damping coefficient of every inner interface [L-1][Nc] for the
+     * damping parameters in damp_key (start height, maximum coefficient) */
+    double *damp_dc = nullptr;
+    double damp_key[2] = {-1.0, -1.0};
     int use_graphs = 1;
     int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */
     long long h2d_bytes = 0, d2h_bytes = 0;

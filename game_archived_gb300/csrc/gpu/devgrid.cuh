@@ -42,6 +42,8 @@ struct HGrid {
     R radius;
     /* cells */
     const R *volume;        /* [L][Nc] */
+    const R *theta_v_bg;    /* [L][Nc] background virtual potential temperature */
+    const R *exner_bg;      /* [L][Nc] background Exner pressure */
     const R *ipw;           /* [8][L][Nc] inner-product weights */
     const int *adj;         /* [6][Nc] edges of the cell, reference order */
     const int *adj_sign;    /* [6][Nc] +1 cell is the edge's from cell, -1 to cell, 0 none */
@@ -91,13 +93,29 @@ struct DState {
     double *u;            /* [L][Ne] */
 };
 
-/* run configuration of one step */
+/* read view of the state in the horizontal precision R: the FP64 state itself
+ * on the FP64 path, its FP32 shadow on the mixed path */
+template <typename R>
+struct SView {
+    const R *rho, *rhotheta_v, *theta_v_pert, *exner_pert, *w, *u;
+};
+
+/* FP32 shadow of state_new (mixed path); kernels that write the FP64 state
+ * also write the shadow.  All pointers null on the FP64 path. */
+struct Shadow {
+    float *rho, *rhotheta_v, *theta_v_pert, *exner_pert, *w, *u;
+};
+
+/* run configuration of one step (no padding: compared bytewise as a key) */
 struct StepParams {
-    int n_const, n_cond, moist;
+    int n_const, n_cond, moist, first_step;
     double dt;
     double impl_thermo_weight, damping_start_height, damping_coeff_max, toa;
     double snow_velocity, rain_velocity, cloud_velocity;
-    int first_step;
+    /* derived on the host for the mixed path: 1/dt, 1/(w dt^2 c_p), 0.5/(w dt c_p)
+     * with w the implicit thermodynamic weight */
+    double inv_dt, k_rows, k_rows2;
 };
+static_assert(sizeof(StepParams) == 4 * sizeof(int) + 11 * sizeof(double), "StepParams has padding");
 
 }  // namespace game

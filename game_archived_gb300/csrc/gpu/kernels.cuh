@@ -71,8 +71,8 @@ __device__ __forceinline__ R grad_h(const HGrid<R> &g, const F *f, int l, int e)
 }
 
 /* horizontal covariant wind component (averaging.c:97-111) */
-template <typename R>
-__device__ __forceinline__ R hor_covariant(const HGrid<R> &g, const double *u, const double *w, int l, int e)
+template <typename R, typename F>
+__device__ __forceinline__ R hor_covariant(const HGrid<R> &g, const F *u, const F *w, int l, int e)
 {
     const long long le = (long long)l * g.ne + e;
     R r = R(u[le]);
@@ -325,10 +325,184 @@ __global__ void k_cell_prepare(VGrid vg, StepParams p, DState so, double *temper
     pt_heat[i] = heat;
 }
 
+/* ------------------------------------------------ k_cell_prepare_f32
+ * the same diagnostics and phase-transition rates in FP32 (mixed path).  The
+ * condensation quadratic's root -p/2 - sqrt(p^2/4 - q) is evaluated as
+ * q / (-p/2 + sqrt(p^2/4 - q)) when p < 0, the algebraically identical form
+ * without cancellation, which FP32 needs. */
+__device__ __forceinline__ float c_p_ice_f(float t)
+{
+    if (t > float(T_0)) t = float(T_0);
+    if (t < 20.f) t = 20.f;
+    const float q = t / 125.1f;
+    return (-2.0572f + 0.14644f * t + 0.06163f * t * expf(-(q * q))) / float(M_V);
+}
+__device__ __forceinline__ float c_p_water_f(float t)
+{
+    float tc = t - float(T_0), r;
+    if (tc >= 0.f) {
+        if (tc > 35.f) tc = 35.f;
+        const float a = tc - 35.f, a2 = a * a;
+        r = 0.9979f + 3.1e-6f * a2 + 3.8e-9f * (a2 * a2);
+    } else {
+        if (tc < -37.f) tc = -37.f;
+        const float t2 = tc * tc;
+        r = 1.000938f - 2.7052e-3f * tc - 2.3235e-5f * t2 + 4.3778e-6f * (t2 * tc) + 2.7136e-7f * (t2 * t2);
+    }
+    return 4186.8f * r;
+}
+__device__ __forceinline__ float enthalpy_evaporation_f(float t)
+{
+    if (t < float(T_0)) {
+        if (t < 30.f) t = 30.f;
+        return (56579.0f - 42.212f * t + expf(0.1149f * (281.6f - t))) / float(M_V);
+    }
+    if (t > float(T_0) + 100.f) t = float(T_0) + 100.f;
+    return 3151378.0f - 2386.0f * t;
+}
+__device__ __forceinline__ float enthalpy_sublimation_f(float t)
+{
+    if (t < 30.f) t = 30.f;
+    if (t > float(T_0)) t = float(T_0);
+    const float q = t / 123.75f;
+    return (46782.5f + 35.8925f * t - 0.07414f * (t * t) + 541.5f * expf(-(q * q))) / float(M_V);
+}
+
+__global__ void k_cell_prepare_f32(VGrid vg, StepParams p, DState so, double *temperature, double *pt_rates,
+                                   double *pt_heat, double *cp_ice_out, double *cp_water_out, float *cp32_ice,
+                                   float *cp32_water)
+{
+    const long long ns = (long long)vg.nl * vg.nc;
+    const long long i = gtid();
+    if (i >= ns) return;
+    const int cond = p.n_cond;
+    const double *rho = so.rho;
+    const float th = float(vg.theta_v_bg[i] + so.theta_v_pert[i]), pi = float(vg.exner_bg[i] + so.exner_pert[i]);
+    if (!p.moist) {
+        temperature[i] = double(th) * double(pi);
+        return;
+    }
+    float r[6];
+    for (int k = 0; k < 6; ++k) r[k] = float(rho[k * ns + i]);
+    const float rv = r[cond + 1], rg = r[cond];
+    const float T = th * pi / (1.f + rv / rg * float(M_D / M_V - 1.0));
+    temperature[i] = double(T);
+    const float cpi = c_p_ice_f(T), cpw = c_p_water_f(T);
+    cp_ice_out[i] = double(cpi);
+    cp_water_out[i] = double(cpw);
+    cp32_ice[i] = cpi;
+    cp32_water[i] = cpw;
+    const float dt = float(p.dt), T0 = float(T_0);
+    const bool warm = T >= T0;
+    float tc = T - T0, sat0, dsat_fac;
+    if (warm) {
+        float tw = tc > 100.f ? 100.f : tc;
+        if (tw > 0.f) {
+            sat0 = expf(34.494f - 4924.99f / (tw + 237.1f)) / powf(tw + 105.0f, 1.57f);
+        } else {
+            const float t2 = tw * tw;
+            sat0 = 100.f * (6.107799961f + 4.436518521e-1f * tw + 1.428945805e-2f * t2 + 2.650648471e-4f * t2 * tw
+                            + 3.031240396e-6f * t2 * t2 + 2.034080948e-8f * t2 * t2 * tw
+                            + 6.136820929e-11f * t2 * t2 * t2);
+        }
+        float td = tc > 100.f ? 100.f : (tc < 0.f ? 0.f : tc);
+        const float q0 = td + 237.1f;
+        dsat_fac = 4924.99f / (q0 * q0) - 1.57f / (td + 105.0f);
+    } else {
+        float ti = tc < -80.f ? -80.f : (tc > 0.f ? 0.f : tc);
+        const float a = ti + 868.0f;
+        sat0 = expf(43.494f - 6545.8f / (ti + 278.0f)) / (a * a);
+        const float q0 = ti + 278.0f;
+        dsat_fac = 6545.8f / (q0 * q0) - 2.0f / (ti + 868.0f);
+    }
+    const float wvp = rv * float(R_V) * T;
+    const float air = (rg - rv) * float(R_D) * T + wvp;
+    const float ef = warm ? 1.00071f * expf(0.000000045f * air) : 0.99882f * expf(0.00000008f * air);
+    const float sat = ef * sat0;
+    const float h_evap = enthalpy_evaporation_f(T), h_subl = enthalpy_sublimation_f(T), h_melt = h_subl - h_evap;
+    float cv = 0.f;
+    for (int k = 0; k < cond; ++k) cv += r[k] * ((k % 2 == 0) ? cpi : cpw);
+    cv += rg * float(C_D_V) + rv * float(C_V_V);
+    const float pth = warm ? h_evap : h_subl;
+    const float a = -float(R_V) * pth / cv;
+    const float b = float(R_V) * T - float(R_V) * rv * pth / cv + ef * (sat0 * dsat_fac) * pth / cv;
+    const float pp = b / a, q = (wvp - sat) / a;
+    const float sq = sqrtf(0.25f * (pp * pp) - q);
+    const float diff = pp < 0.f ? q / (-0.5f * pp + sq) : -0.5f * pp - sq;
+    float r0, r1, r2, r3, r4, heat;
+    if (sat >= wvp) {
+        if (warm) {
+            r2 = -r[2] / dt;
+            const float ptd = fminf(r[3], diff);
+            r4 = ptd / dt;
+            r3 = r[2] / dt - ptd / dt;
+            heat = r2 * h_melt - ptd * h_evap / dt;
+        } else {
+            r3 = -r[3] / dt;
+            const float ptd = fminf(r[2], diff);
+            r4 = ptd / dt;
+            r2 = r[3] / dt - ptd / dt;
+            heat = -r3 * h_melt - ptd * h_subl / dt;
+        }
+    } else {
+        if (warm) {
+            r2 = -r[2] / dt;
+            r4 = diff / dt;
+            r3 = r[2] / dt - diff / dt;
+            heat = r2 * h_melt - diff * h_evap / dt;
+        } else {
+            r3 = -r[3] / dt;
+            r4 = diff / dt;
+            r2 = r[3] / dt - diff / dt;
+            heat = -r3 * h_melt - diff * h_subl / dt;
+        }
+    }
+    r0 = 0.f;
+    r1 = 0.f;
+    const float max_cloud_water = 0.2e-3f;
+    if (!warm) {
+        r0 = fmaxf(r[2] - max_cloud_water * r[4], 0.f) / 1000.f;
+        r2 -= r0;
+    } else {
+        r1 = fmaxf(r[3] - max_cloud_water * r[4], 0.f) / 1000.f;
+        r3 -= r1;
+    }
+    if (warm && r[0] > 0.f) {
+        r0 = -r[0] / dt;
+        r1 -= r0;
+        heat += r0 * h_melt;
+    }
+    if (!warm && r[1] > 0.f) {
+        r1 = -r[1] / dt;
+        r0 -= r1;
+        heat += -r1 * h_melt;
+    }
+    pt_rates[i] = r0;
+    pt_rates[ns + i] = r1;
+    pt_rates[2 * ns + i] = r2;
+    pt_rates[3 * ns + i] = r3;
+    pt_rates[4 * ns + i] = r4;
+    pt_heat[i] = heat;
+}
+
+/* FP32 shadow of the state at the start of a mixed step */
+__global__ void k_make_shadow(long long n_rho, long long ns, long long nw, long long nu, DState s, Shadow sh)
+{
+    const long long i = gtid();
+    if (i < n_rho) sh.rho[i] = float(s.rho[i]);
+    if (i < ns) {
+        sh.rhotheta_v[i] = float(s.rhotheta_v[i]);
+        sh.theta_v_pert[i] = float(s.theta_v_pert[i]);
+        sh.exner_pert[i] = float(s.exner_pert[i]);
+    }
+    if (i < nw) sh.w[i] = float(s.w[i]);
+    if (i < nu) sh.u[i] = float(s.u[i]);
+}
+
 /* ------------------------------------------------------- k_tri_vort
  * vertical relative vorticity on triangles (vorticities.c:167-222) */
 template <typename R>
-__global__ void k_tri_vort(HGrid<R> g, const double *u, R *tri_vort)
+__global__ void k_tri_vort(HGrid<R> g, const R *u, R *tri_vort)
 {
     const long long n = (long long)g.nl * g.nt;
     const long long i = gtid();
@@ -338,7 +512,7 @@ __global__ void k_tri_vort(HGrid<R> g, const double *u, R *tri_vort)
     for (int j = 0; j < 3; ++j) {
         const int e = g.vort_i[j * g.nt + t];
         const long long le = (long long)l * g.ne + e;
-        R vel = R(u[le]);
+        R vel = u[le];
         R rescale = R(1);
         if (l >= g.nl - g.n_oro) {
             const R zt = g.dual_z_t[i];
@@ -349,7 +523,7 @@ __global__ void k_tri_vort(HGrid<R> g, const double *u, R *tri_vort)
             else if (l == g.nl - 1) lo = l - 1;
             else lo = l + 1;
             const long long lo_e = (long long)lo * g.ne + e;
-            R vgrad = (R(u[le]) - R(u[lo_e])) / (g.z_h[le] - g.z_h[lo_e]);
+            R vgrad = (u[le] - u[lo_e]) / (g.z_h[le] - g.z_h[lo_e]);
             vel += dz * vgrad;
         }
         acc += rescale * g.nd_h[le] * R(g.vort_s[j * g.nt + t]) * vel;
@@ -357,10 +531,9 @@ __global__ void k_tri_vort(HGrid<R> g, const double *u, R *tri_vort)
     tri_vort[i] = acc / g.dual_area_t[i];
 }
 
-/* relative vorticity of level k (tangential) or layer k (rhombus) at edge e
- * (vorticities.c:104-165) */
+/* tangential relative vorticity at level k, edge e (vorticities.c:104-165) */
 template <typename R>
-__device__ __forceinline__ R rel_vort_tangential(const HGrid<R> &g, const double *u, const double *w, int k, int e)
+__device__ __forceinline__ R rel_vort_tangential(const HGrid<R> &g, const R *u, const R *w, int k, int e)
 {
     const int nl = g.nl;
     if (k == 0) k = 1; /* no vertical shear of the tangential vorticity at the TOA */
@@ -373,17 +546,17 @@ __device__ __forceinline__ R rel_vort_tangential(const HGrid<R> &g, const double
     R c0 = hor_covariant(g, u, w, k, e);
     R c2 = hor_covariant(g, u, w, k - 1, e);
     return inv_area * (-g.nd_h[(long long)k * g.ne + e] * c0
-                       + g.nd_v[(long long)k * g.nc + fr] * R(w[(long long)k * g.nc + fr])
+                       + g.nd_v[(long long)k * g.nc + fr] * w[(long long)k * g.nc + fr]
                        + g.nd_h[(long long)(k - 1) * g.ne + e] * c2
-                       - g.nd_v[(long long)k * g.nc + to] * R(w[(long long)k * g.nc + to]));
+                       - g.nd_v[(long long)k * g.nc + to] * w[(long long)k * g.nc + to]);
 }
 
 /* --------------------------------------------------------- k_edge_vort
  * potential vorticity (vorticities.c:18-85) and the horizontal mass flux
  * density (multiplications.c:45-66), one thread per (edge, level 0..L) */
 template <typename R>
-__global__ void k_edge_vort(HGrid<R> g, const double *u, const double *w, const double *rho_gas, const R *tri_vort,
-                            R *zh, R *zv, R *flux_h)
+__global__ void k_edge_vort(HGrid<R> g, const R *u, const R *w, const R *rho_gas, const R *tri_vort, R *zh, R *zv,
+                            R *flux_h)
 {
     const long long n = (long long)(g.nl + 1) * g.ne;
     const long long i = gtid();
@@ -397,17 +570,17 @@ __global__ void k_edge_vort(HGrid<R> g, const double *u, const double *w, const 
         R pv = rel + g.f_vec[e];
         R dens;
         if (k == 0) {
-            R top = R(0.5) * (R(rho_gas[fr]) + R(rho_gas[to]));
-            R below = R(0.5) * (R(rho_gas[nc + fr]) + R(rho_gas[nc + to]));
+            R top = R(0.5) * (rho_gas[fr] + rho_gas[to]);
+            R below = R(0.5) * (rho_gas[nc + fr] + rho_gas[nc + to]);
             dens = top + (top - below) / g.pvz[ne + e] * g.pvz[e];
         } else if (k == nl) {
             long long a = (long long)(nl - 1) * nc, b = (long long)(nl - 2) * nc;
-            R low = R(0.5) * (R(rho_gas[a + fr]) + R(rho_gas[a + to]));
-            R above = R(0.5) * (R(rho_gas[b + fr]) + R(rho_gas[b + to]));
+            R low = R(0.5) * (rho_gas[a + fr] + rho_gas[a + to]);
+            R above = R(0.5) * (rho_gas[b + fr] + rho_gas[b + to]);
             dens = low + (above - low) / g.pvz[3 * (long long)ne + e] * g.pvz[2 * (long long)ne + e];
         } else {
             long long uf = (long long)(k - 1) * nc + fr, ut = (long long)(k - 1) * nc + to;
-            dens = R(0.25) * (R(rho_gas[uf]) + R(rho_gas[ut]) + R(rho_gas[uf + nc]) + R(rho_gas[ut + nc]));
+            dens = R(0.25) * (rho_gas[uf] + rho_gas[ut] + rho_gas[uf + nc] + rho_gas[ut + nc]);
         }
         zh[i] = pv / dens;
     }
@@ -421,11 +594,11 @@ __global__ void k_edge_vort(HGrid<R> g, const double *u, const double *w, const 
         R pv = rel + g.f_vec[ne + e];
         R dens = R(0);
         for (int j = 0; j < 4; ++j)
-            dens += g.rhombi_w[j * (long long)ne + e] * R(rho_gas[(long long)k * nc + g.rhombi_i[j * (long long)ne + e]]);
+            dens += g.rhombi_w[j * (long long)ne + e] * rho_gas[(long long)k * nc + g.rhombi_i[j * (long long)ne + e]];
         zv[le] = pv / dens;
         /* mass flux density */
-        R sv = R(0.5) * (R(rho_gas[(long long)k * nc + to]) + R(rho_gas[(long long)k * nc + fr]));
-        flux_h[le] = sv * R(u[le]);
+        R sv = R(0.5) * (rho_gas[(long long)k * nc + to] + rho_gas[(long long)k * nc + fr]);
+        flux_h[le] = sv * u[le];
     }
 }
 
@@ -433,8 +606,7 @@ __global__ void k_edge_vort(HGrid<R> g, const double *u, const double *w, const 
  * kinetic energy v^2 (inner_product.c:13-43) at (cell, layer) and the vertical
  * mass flux density (multiplications.c:98-117) at the inner interfaces */
 template <typename R>
-__global__ void k_cell_kinetic(HGrid<R> g, const double *u, const double *w, const double *rho_gas, R *v2,
-                               R *flux_v)
+__global__ void k_cell_kinetic(HGrid<R> g, const R *u, const R *w, const R *rho_gas, R *v2, R *flux_v)
 {
     const long long ns = (long long)g.nl * g.nc;
     const long long i = gtid();
@@ -443,15 +615,15 @@ __global__ void k_cell_kinetic(HGrid<R> g, const double *u, const double *w, con
     const int n_edges = c < N_PENT ? 5 : 6;
     R acc = R(0);
     for (int j = 0; j < n_edges; ++j) {
-        R ue = R(u[(long long)l * g.ne + g.adj[j * g.nc + c]]);
+        R ue = u[(long long)l * g.ne + g.adj[j * g.nc + c]];
         acc += ipw_at(g, j, l, c) * ue * ue;
     }
-    R wu = R(w[i]), wl = R(w[i + g.nc]);
+    R wu = w[i], wl = w[i + g.nc];
     acc += ipw_at(g, 6, l, c) * wu * wu;
     acc += ipw_at(g, 7, l, c) * wl * wl;
     v2[i] = acc;
     if (l >= 1) {
-        R sv = R(0.5) * (R(rho_gas[i - g.nc]) + R(rho_gas[i]));
+        R sv = R(0.5) * (rho_gas[i - g.nc] + rho_gas[i]);
         flux_v[i] = sv * wu;
     }
 }
@@ -497,22 +669,30 @@ __device__ __forceinline__ R vorticity_flux_h(const HGrid<R> &g, const R *flux_h
     return out;
 }
 
+/* sum of all constituent densities in R (derived_quantities.c:83-95) */
+template <typename R>
+__device__ __forceinline__ R density_total_r(const R *rho, int n_const, long long ns, long long i)
+{
+    R r = R(0);
+    for (int k = 0; k < n_const; ++k) r += rho[k * ns + i];
+    return r;
+}
+
 /* decelerated pressure-gradient sum nl + l at edge e, layer l
  * (manage_pressure_gradient.c:17-72) */
 template <typename R>
-__device__ __forceinline__ R pgrad_h(const HGrid<R> &g, const StepParams &p, const DState &s, const double *theta_bg,
-                                     int l, int e)
+__device__ __forceinline__ R pgrad_h(const HGrid<R> &g, const StepParams &p, const SView<R> &s, int l, int e)
 {
     const long long ns = (long long)g.nl * g.nc;
     const int fr = g.from[e], to = g.to[e];
     const long long cf = (long long)l * g.nc + fr, ct = (long long)l * g.nc + to;
+    const R cdp = R(C_D_P);
     R nl = grad_h(g, s.exner_pert, l, e);
-    R s_to = R(C_D_P * (theta_bg[ct] + s.theta_v_pert[ct])), s_fr = R(C_D_P * (theta_bg[cf] + s.theta_v_pert[cf]));
+    R s_to = cdp * (g.theta_v_bg[ct] + s.theta_v_pert[ct]), s_fr = cdp * (g.theta_v_bg[cf] + s.theta_v_pert[cf]);
     nl = (R(0.5) * (s_to + s_fr)) * nl;
-    R l_term = (R(0.5) * (R(C_D_P * s.theta_v_pert[ct]) + R(C_D_P * s.theta_v_pert[cf])))
-               * g.exner_bg_grad_h[(long long)l * g.ne + e];
-    R d_to = R(s.rho[p.n_cond * ns + ct] / density_total(s.rho, p.n_const, ns, ct));
-    R d_fr = R(s.rho[p.n_cond * ns + cf] / density_total(s.rho, p.n_const, ns, cf));
+    R l_term = (R(0.5) * (cdp * s.theta_v_pert[ct] + cdp * s.theta_v_pert[cf])) * g.exner_bg_grad_h[(long long)l * g.ne + e];
+    R d_to = s.rho[p.n_cond * ns + ct] / density_total_r(s.rho, p.n_const, ns, ct);
+    R d_fr = s.rho[p.n_cond * ns + cf] / density_total_r(s.rho, p.n_const, ns, cf);
     R dec = R(0.5) * (d_to + d_fr);
     nl = dec * nl;
     l_term = dec * l_term;
@@ -521,18 +701,17 @@ __device__ __forceinline__ R pgrad_h(const HGrid<R> &g, const StepParams &p, con
 
 /* the same at the inner interface k of cell c */
 template <typename R>
-__device__ __forceinline__ R pgrad_v(const HGrid<R> &g, const StepParams &p, const DState &s, const double *theta_bg,
-                                     int k, int c)
+__device__ __forceinline__ R pgrad_v(const HGrid<R> &g, const StepParams &p, const SView<R> &s, int k, int c)
 {
     const long long ns = (long long)g.nl * g.nc;
     const long long up = (long long)(k - 1) * g.nc + c, lo = (long long)k * g.nc + c;
+    const R cdp = R(C_D_P);
     R nl = grad_v(g, s.exner_pert, k, c);
-    R s_up = R(C_D_P * (theta_bg[up] + s.theta_v_pert[up])), s_lo = R(C_D_P * (theta_bg[lo] + s.theta_v_pert[lo]));
+    R s_up = cdp * (g.theta_v_bg[up] + s.theta_v_pert[up]), s_lo = cdp * (g.theta_v_bg[lo] + s.theta_v_pert[lo]);
     nl = (R(0.5) * (s_up + s_lo)) * nl;
-    R l_term = (R(0.5) * (R(C_D_P * s.theta_v_pert[up]) + R(C_D_P * s.theta_v_pert[lo])))
-               * g.exner_bg_grad_v[(long long)k * g.nc + c];
-    R d_up = R(s.rho[p.n_cond * ns + up] / density_total(s.rho, p.n_const, ns, up));
-    R d_lo = R(s.rho[p.n_cond * ns + lo] / density_total(s.rho, p.n_const, ns, lo));
+    R l_term = (R(0.5) * (cdp * s.theta_v_pert[up] + cdp * s.theta_v_pert[lo])) * g.exner_bg_grad_v[(long long)k * g.nc + c];
+    R d_up = s.rho[p.n_cond * ns + up] / density_total_r(s.rho, p.n_const, ns, up);
+    R d_lo = s.rho[p.n_cond * ns + lo] / density_total_r(s.rho, p.n_const, ns, lo);
     R dec = R(0.5) * (d_up + d_lo);
     nl = dec * nl;
     l_term = dec * l_term;
@@ -542,9 +721,10 @@ __device__ __forceinline__ R pgrad_v(const HGrid<R> &g, const StepParams &p, con
 /* ------------------------------------------------------- k_momentum_h
  * horizontal momentum: explicit tendency (vector_tendencies_expl.c:74-131) and
  * the wind update (manage_rkhevi.c:67-75).  ADV: the advection terms are
- * recomputed in this substage; PG: the pressure gradient is recomputed. */
+ * recomputed in this substage; PG: the pressure gradient is recomputed.
+ * The wind update is FP64; u_shadow (mixed path) receives its FP32 copy. */
 template <typename R, bool ADV, bool PG>
-__global__ void k_momentum_h(HGrid<R> g, StepParams p, DState sn, const double *u_old, const double *theta_bg,
+__global__ void k_momentum_h(HGrid<R> g, StepParams p, SView<R> sv, double *u_new, float *u_shadow, const double *u_old,
                              double *tend_u, R *P_h, R *pg_old_h, R *pvt_h, R *v2g_h, const R *flux_h,
                              const R *flux_v, const R *zh, const R *zv, const R *v2, double new_w, double old_w)
 {
@@ -554,7 +734,7 @@ __global__ void k_momentum_h(HGrid<R> g, StepParams p, DState sn, const double *
     const int l = (int)(i / g.ne), e = (int)(i - (long long)l * g.ne);
     R P, pgo;
     if (PG) {
-        P = pgrad_h(g, p, sn, theta_bg, l, e);
+        P = pgrad_h(g, p, sv, l, e);
         pgo = p.first_step ? -P : -P_h[i];
         P_h[i] = P;
         pg_old_h[i] = pgo;
@@ -576,15 +756,17 @@ __global__ void k_momentum_h(HGrid<R> g, StepParams p, DState sn, const double *
     R y = old_hor * pgo - cur_hor * P + pvt - R(0.5) * v2g;
     double t = (new_w == 1.0) ? double(y) : old_w * tend_u[i] + new_w * double(y);
     tend_u[i] = t;
-    sn.u[i] = u_old[i] + p.dt * t;
+    const double un = u_old[i] + p.dt * t;
+    u_new[i] = un;
+    if (u_shadow) u_shadow[i] = float(un);
 }
 
 /* ------------------------------------------------------- k_momentum_v
  * vertical momentum at interface k of cell c: tendency including the
  * condensate term (manage_pressure_gradient.c:74-87) */
 template <typename R, bool ADV, bool PG>
-__global__ void k_momentum_v(HGrid<R> g, StepParams p, DState sn, const double *theta_bg, double *tend_w, R *P_v,
-                             R *pvt_v, R *v2g_v, const R *flux_h, const R *zh, const R *v2, double new_w, double old_w)
+__global__ void k_momentum_v(HGrid<R> g, StepParams p, SView<R> sv, double *tend_w, R *P_v, R *pvt_v, R *v2g_v,
+                             const R *flux_h, const R *zh, const R *v2, double new_w, double old_w)
 {
     const long long n = (long long)(g.nl + 1) * g.nc;
     const long long i = gtid();
@@ -615,7 +797,7 @@ __global__ void k_momentum_v(HGrid<R> g, StepParams p, DState sn, const double *
     }
     R P, v2g;
     if (PG) {
-        P = pgrad_v(g, p, sn, theta_bg, k, c);
+        P = pgrad_v(g, p, sv, k, c);
         P_v[i] = P;
     } else {
         P = P_v[i];
@@ -629,8 +811,8 @@ __global__ void k_momentum_v(HGrid<R> g, StepParams p, DState sn, const double *
     }
     const long long ns = (long long)nl * g.nc;
     const long long up = (long long)(k - 1) * g.nc + c, lo = (long long)k * g.nc + c;
-    R d_up = R(sn.rho[p.n_cond * ns + up] / density_total(sn.rho, p.n_const, ns, up) - 1.0);
-    R d_lo = R(sn.rho[p.n_cond * ns + lo] / density_total(sn.rho, p.n_const, ns, lo) - 1.0);
+    R d_up = sv.rho[p.n_cond * ns + up] / density_total_r(sv.rho, p.n_const, ns, up) - R(1);
+    R d_lo = sv.rho[p.n_cond * ns + lo] / density_total_r(sv.rho, p.n_const, ns, lo) - R(1);
     R pgc = (R(0.5) * (d_up + d_lo)) * g.gravity_m_v[i];
     const R cur_ver = R(1.0 - p.impl_thermo_weight);
     R y = -cur_ver * P + pvt - R(0.5) * v2g + pgc;
@@ -663,25 +845,53 @@ __device__ __forceinline__ R contra_corr(const HGrid<R> &g, int k, int c, int n_
 }
 
 template <typename R>
-__global__ void k_theta(VGrid vg, StepParams p, DState sn, double *theta)
+__global__ void k_theta(int nl, int nc, int n_cond, SView<R> sv, R *theta)
 {
-    const long long ns = (long long)vg.nl * vg.nc;
+    const long long ns = (long long)nl * nc;
     const long long i = gtid();
     if (i >= ns) return;
-    theta[i] = sn.rhotheta_v[i] / sn.rho[p.n_cond * ns + i];
+    theta[i] = sv.rhotheta_v[i] / sv.rho[n_cond * ns + i];
 }
 
-/* Restructured explicit scalar tendencies (same arithmetic as k_scalar_tend):
- * the cell's edge data are loaded once; the terrain correction of the wind
- * (shared by every tracer) is computed once; the main mass flux is reused for
- * the rho*theta_v flux.  Edge fluxes are products in R; each flux*area is
- * converted to double and the divergence accumulated in double.  With
- * R = double the sums and products are the reference's, bit for bit. */
+/* Sum of edge fluxes of one cell.  R = double: plain double accumulation
+ * (the reference's).  R = float: Knuth's TwoSum keeps the exact rounding
+ * error of every FP32 addition in a second FP32 word, so the pair (hi, lo)
+ * carries the sum to ~2^-48 relative before being rounded once to double --
+ * FP64-class accumulation of the mass fluxes at FP32 instruction cost. */
 template <typename R>
-__global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, VGrid vg, StepParams p, DState sn, DState st,
-                                                      const double *theta, const double *cp_ice,
-                                                      const double *cp_water, const double *pt_rates,
-                                                      const double *pt_heat, const double *sed_heat, int rk)
+struct FluxSum {
+    double s = 0.0;
+    __device__ __forceinline__ void add(R x) { s += double(x); }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct FluxSum<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x)
+    {
+        const float t = hi + x;
+        const float bp = t - hi;
+        const float err = (hi - (t - bp)) + (x - bp);
+        hi = t;
+        lo += err;
+    }
+    __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
+};
+
+/* Explicit mass and rho*theta_v tendencies (scalar_tendencies_expl.c:90-178)
+ * at (cell, layer).  The cell's edges are streamed one layer at a time
+ * (layer l-1, l, l+1) so that only one layer's fluxes are live; every
+ * accumulator still receives its terms in the reference's order (layer
+ * l-1 before l, edges j = 0..5), so with R = double every sum and product is
+ * the reference's, bit for bit.  The main mass flux is reused for the
+ * rho*theta_v flux; the terrain correction of the wind is computed once for
+ * all tracers.  Edge fluxes are products in R, divergences accumulate in
+ * double (FluxSum) and tendencies are formed in double. */
+template <typename R>
+__global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, SView<R> sv, DState st,
+                                                      const R *theta, const R *cp_ice, const R *cp_water,
+                                                      const double *pt_rates, const double *pt_heat,
+                                                      const double *sed_heat, const double *inv_vol_tab, int rk)
 {
     const long long ns = (long long)g.nl * g.nc;
     const long long i = gtid();
@@ -691,153 +901,131 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, VGrid vg, Step
     const long long nc = g.nc, ne = g.ne;
     const int n_edges = c < N_PENT ? 5 : 6;
     const int cond = p.n_cond;
-    /* layers whose edge values the terrain correction needs */
     const bool oro = l >= nl - n_oro - 1;
-    const bool has_up_corr = oro && l >= nl - n_oro;            /* contra_corr at level l   */
-    const bool has_lo_corr = oro && l < nl - 1;                 /* contra_corr at level l+1 */
-    const int l_lo = l - 1 >= 0 ? l - 1 : l, l_hi = l + 1 < nl ? l + 1 : l;
-    int a[6], nb[6];
-    bool from_self[6];
-    R ar[6], uu[3][6], wc[3][6];
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-        if (j < n_edges) {
-            a[j] = g.adj[j * nc + c];
-            nb[j] = g.adj_nbr[j * nc + c];
-            from_self[j] = g.adj_sign[j * nc + c] > 0;
-            ar[j] = g.area_h[(long long)l * ne + a[j]];
-            uu[1][j] = R(sn.u[(long long)l * ne + a[j]]);
-            uu[0][j] = R(sn.u[(long long)l_lo * ne + a[j]]);
-            uu[2][j] = R(sn.u[(long long)l_hi * ne + a[j]]);
-            if (oro) {
-                wc[0][j] = R(-0.5) * ipw_at(g, j, l_lo, c) * g.slope_h[(long long)l_lo * ne + a[j]];
-                wc[1][j] = R(-0.5) * ipw_at(g, j, l, c) * g.slope_h[(long long)l * ne + a[j]];
-                wc[2][j] = R(-0.5) * ipw_at(g, j, l_hi, c) * g.slope_h[(long long)l_hi * ne + a[j]];
-            }
-        }
-    }
-    const int lay[3] = {l_lo, l, l_hi};
-    /* vertical_contravariant_corr at level l (slots 0,1) and l+1 (slots 1,2)
-     * of an edge field f[slot][j] (averaging.c:41-95) */
-    auto corr_up = [&](const R (&f)[3][6]) {
-        R r = R(0);
-        if (l > nl - n_oro)
-            for (int j = 0; j < n_edges; ++j) r += wc[0][j] * f[0][j];
-        for (int j = 0; j < n_edges; ++j) r += wc[1][j] * f[1][j];
-        return r;
-    };
-    auto corr_lo = [&](const R (&f)[3][6]) {
-        R r = R(0);
-        if (l + 1 > nl - n_oro)
-            for (int j = 0; j < n_edges; ++j) r += wc[1][j] * f[1][j];
-        for (int j = 0; j < n_edges; ++j) r += wc[2][j] * f[2][j];
-        return r;
-    };
-    const double inv_vol = 1.0 / double(g.volume[i]);
+    const bool up_corr = oro && l >= nl - n_oro;            /* contra_corr at level l needed   */
+    const bool lo_corr = oro && l < nl - 1;                 /* contra_corr at level l+1 needed */
+    const bool up_has_prev = up_corr && l > nl - n_oro;     /* level l sums layer l-1, then l  */
+    const bool lo_has_curr = lo_corr && l + 1 > nl - n_oro; /* level l+1 sums layer l, then l+1 */
+    const double inv_vol = sizeof(R) == sizeof(double) ? 1.0 / double(g.volume[i]) : inv_vol_tab[i];
     const R area_up = g.area_v[(long long)l * nc + c], area_lo = g.area_v[(long long)(l + 1) * nc + c];
-    /* centred vertical part for a flux field with corrections up / lo */
-    auto comp_v_centred = [&](const R (&f)[3][6]) -> double {
-        if (!oro) return 0.0;
-        if (l == nl - n_oro - 1) {
-            R lo = corr_lo(f);
-            return double(-lo * area_lo);
-        }
-        if (l == nl - 1) {
-            R up = corr_up(f);
-            return double(up * area_up);
-        }
-        R up = corr_up(f);
-        R lo = corr_lo(f);
-        return double(up * area_up - lo * area_lo);
+    auto edge = [&](int j) { return g.adj[j * nc + c]; };
+    auto wcorr = [&](int ll, int j) {
+        return R(-0.5) * ipw_at(g, j, ll, c) * g.slope_h[(long long)ll * ne + edge(j)];
     };
-    auto comp_h_of = [&](const R (&f)[3][6]) -> double {
-        double s = 0.0;
-        for (int j = 0; j < n_edges; ++j) {
-            const R fa = f[1][j] * ar[j];
-            s += from_self[j] ? double(fa) : -double(fa);
-        }
-        return s;
-    };
-    /* wind terrain correction, shared by the tracers */
+    auto uval = [&](int ll, int j) { return sv.u[(long long)ll * ne + edge(j)]; };
+    /* terrain correction of the wind at levels l and l+1 (shared by the tracers) */
     R w_up = R(0), w_lo = R(0);
     if (oro) {
-        if (has_up_corr) w_up = corr_up(uu);
-        if (has_lo_corr) w_lo = corr_lo(uu);
+        if (up_has_prev)
+            for (int j = 0; j < n_edges; ++j) w_up += wcorr(l - 1, j) * uval(l - 1, j);
+        for (int j = 0; j < n_edges; ++j) {
+            const R t = wcorr(l, j) * uval(l, j);
+            if (up_corr) w_up += t;
+            if (lo_has_curr) w_lo += t;
+        }
+        if (lo_corr)
+            for (int j = 0; j < n_edges; ++j) w_lo += wcorr(l + 1, j) * uval(l + 1, j);
     }
-    R fmain[3][6];
     for (int k = 0; k < p.n_const; ++k) {
         const double new_w = (rk == 1 && k != cond) ? 0.5 : 1.0, old_w = 1.0 - new_w;
-        const double *f = sn.rho + k * ns;
-        R fx[3][6];
-        double comp_h, comp_v;
+        const R *f = sv.rho + k * ns;
         if (k == cond) {
-#pragma unroll
-            for (int s = 0; s < 3; ++s) {
-                if (s != 1 && !oro) continue;
-                const long long o = (long long)lay[s] * nc;
-                const R fs = R(f[o + c]);
-                for (int j = 0; j < n_edges; ++j) fx[s][j] = (R(0.5) * (fs + R(f[o + nb[j]]))) * uu[s][j];
-            }
-            comp_h = comp_h_of(fx);
-            comp_v = comp_v_centred(fx);
-#pragma unroll
-            for (int s = 0; s < 3; ++s)
-                for (int j = 0; j < 6; ++j) fmain[s][j] = fx[s][j];
-        } else {
-#pragma unroll
-            for (int s = 0; s < 3; ++s) {
-                if (s != 1) continue; /* the tracers' vertical part uses the wind, not the flux */
-                const long long o = (long long)lay[s] * nc;
-                const double fs = f[o + c];
+            /* centred mass flux and, from it, the rho*theta_v flux */
+            FluxSum<R> hm, ht;
+            R um = R(0), ut = R(0), lm = R(0), lt = R(0);
+            auto layer_pass = [&](int ll, bool to_h, bool to_up, bool to_lo) {
+                const long long o = (long long)ll * nc;
+                const R fs = f[o + c], ts = theta[o + c];
                 for (int j = 0; j < n_edges; ++j) {
-                    const bool up_self = (uu[s][j] >= R(0)) == from_self[j];
-                    fx[s][j] = R(up_self ? fs : f[o + nb[j]]) * uu[s][j];
+                    const int nb = g.adj_nbr[j * nc + c];
+                    const R fm = (R(0.5) * (fs + f[o + nb])) * uval(ll, j);
+                    const R ft = (R(0.5) * (ts + theta[o + nb])) * fm;
+                    if (to_h) {
+                        const R ar = g.area_h[(long long)ll * ne + edge(j)];
+                        const bool self_from = g.adj_sign[j * nc + c] > 0;
+                        const R am = fm * ar, at = ft * ar;
+                        hm.add(self_from ? am : -am);
+                        ht.add(self_from ? at : -at);
+                    }
+                    if (to_up || to_lo) {
+                        const R wc = wcorr(ll, j);
+                        if (to_up) {
+                            um += wc * fm;
+                            ut += wc * ft;
+                        }
+                        if (to_lo) {
+                            lm += wc * fm;
+                            lt += wc * ft;
+                        }
+                    }
+                }
+            };
+            if (up_has_prev) layer_pass(l - 1, false, true, false);
+            layer_pass(l, true, up_corr, lo_has_curr);
+            if (lo_corr) layer_pass(l + 1, false, false, true);
+            auto comp_v = [&](R up, R lo) -> double {
+                if (!oro) return 0.0;
+                if (l == nl - n_oro - 1) return double(-lo * area_lo);
+                if (l == nl - 1) return double(up * area_up);
+                return double(up * area_up - lo * area_lo);
+            };
+            const double div = inv_vol * (hm.value() + comp_v(um, lm));
+            double y = -div;
+            if (p.moist) y = y + pt_rates[cond * ns + i];
+            st.rho[k * ns + i] = rk == 0 ? y : old_w * st.rho[k * ns + i] + new_w * y;
+            const double div_t = inv_vol * (ht.value() + comp_v(ut, lt));
+            double yt = -div_t;
+            if (p.moist) {
+                /* diabatic heating: c_v-weighted, divided by c_p * Pi */
+                R cv = R(0);
+                for (int kk = 0; kk < cond; ++kk) cv += sv.rho[kk * ns + i] * ((kk % 2 == 0) ? cp_ice[i] : cp_water[i]);
+                cv += sv.rho[cond * ns + i] * R(C_D_V);
+                cv += sv.rho[(cond + 1) * ns + i] * R(C_V_V);
+                if (sizeof(R) == sizeof(double)) {
+                    yt = yt + C_D_V * double(sv.rho[cond * ns + i]) / double(cv) * (pt_heat[i] + sed_heat[i])
+                                  / (C_D_P * (double(g.exner_bg[i]) + double(sv.exner_pert[i])))
+                         + pt_rates[cond * ns + i] * double(theta[i]);
+                } else {
+                    const R fac = R(C_D_V) * sv.rho[cond * ns + i] / cv / (R(C_D_P) * (g.exner_bg[i] + sv.exner_pert[i]));
+                    yt = yt + double(fac) * (pt_heat[i] + sed_heat[i]) + pt_rates[cond * ns + i] * double(theta[i]);
                 }
             }
-            comp_h = comp_h_of(fx);
-            comp_v = 0.0;
+            st.rhotheta_v[i] = rk == 0 ? yt : old_w * st.rhotheta_v[i] + new_w * yt;
+        } else {
+            /* upstream tracer flux; vertical part from the wind correction */
+            FluxSum<R> h;
+            const long long o = (long long)l * nc;
+            const R fs = f[o + c];
+            for (int j = 0; j < n_edges; ++j) {
+                const R ue = uval(l, j);
+                const bool self_from = g.adj_sign[j * nc + c] > 0;
+                const R fv = ((ue >= R(0)) == self_from ? fs : f[o + g.adj_nbr[j * nc + c]]) * ue;
+                const R a = fv * g.area_h[(long long)l * ne + edge(j)];
+                h.add(self_from ? a : -a);
+            }
+            double comp_v = 0.0;
             if (oro) {
-                const R d_here = R(f[i]);
+                const R d_here = f[i];
                 if (l == nl - n_oro - 1) {
-                    const R d_lo = w_lo <= R(0) ? d_here : R(f[i + nc]);
+                    const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
                     comp_v = double(-d_lo * w_lo * area_lo);
                 } else if (l == nl - 1) {
-                    const R d_up = w_up <= R(0) ? R(f[i - nc]) : d_here;
+                    const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
                     comp_v = double(d_up * w_up * area_up);
                 } else {
-                    const R d_up = w_up <= R(0) ? R(f[i - nc]) : d_here;
-                    const R d_lo = w_lo <= R(0) ? d_here : R(f[i + nc]);
+                    const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
+                    const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
                     comp_v = double(d_up * w_up * area_up - d_lo * w_lo * area_lo);
                 }
             }
-        }
-        const double div = inv_vol * (comp_h + comp_v);
-        double y = -div;
-        if (p.moist) {
-            long long pt = k * ns;
-            if (k == cond + 1) pt -= ns;
-            y = y + pt_rates[pt + i];
-        }
-        st.rho[k * ns + i] = (new_w == 1.0 && rk == 0) ? y : old_w * st.rho[k * ns + i] + new_w * y;
-        if (k == cond) {
-            /* rho*theta_v flux: theta_v averaged to the edge times the mass flux */
-            R ft[3][6];
-#pragma unroll
-            for (int s = 0; s < 3; ++s) {
-                if (s != 1 && !oro) continue;
-                const long long o = (long long)lay[s] * nc;
-                const R ts = R(theta[o + c]);
-                for (int j = 0; j < n_edges; ++j) ft[s][j] = (R(0.5) * (ts + R(theta[o + nb[j]]))) * fmain[s][j];
-            }
-            const double div_t = inv_vol * (comp_h_of(ft) + comp_v_centred(ft));
-            double yt = -div_t;
+            const double div = inv_vol * (h.value() + comp_v);
+            double y = -div;
             if (p.moist) {
-                const double cv = c_v_mass_weighted(sn.rho, cond, 1, ns, i, cp_ice[i], cp_water[i]);
-                yt = yt + C_D_V * sn.rho[cond * ns + i] / cv * (pt_heat[i] + sed_heat[i])
-                              / (C_D_P * (vg.exner_bg[i] + sn.exner_pert[i]))
-                     + pt_rates[cond * ns + i] * theta[i];
+                long long pt = k * ns;
+                if (k == cond + 1) pt -= ns;
+                y = y + pt_rates[pt + i];
             }
-            st.rhotheta_v[i] = (rk == 0) ? yt : old_w * st.rhotheta_v[i] + new_w * yt;
+            st.rho[k * ns + i] = (new_w == 1.0 && rk == 0) ? y : old_w * st.rho[k * ns + i] + new_w * y;
         }
     }
 }

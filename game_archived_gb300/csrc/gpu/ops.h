@@ -20,6 +20,9 @@ void op_linear_combine(Context *c, StateMirror *a, StateMirror *b, StateMirror *
 
 int launch_step_f64(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st);
 int launch_step_mixed(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st);
+/* recomputes the damping table when the damping parameters changed (not
+ * inside a stream capture) */
+int launch_damping_table(Context *c, const StepParams &p);
 
 const char *last_error();
 

@@ -38,7 +38,27 @@ struct WavesWork {
     /* mixed path: reciprocal grid metrics */
     const double *inv_vol;    /* [L][Nc] */
     const double *inv_area_v; /* [L+1][Nc] */
+    /* Klemp damping coefficient of the inner interfaces [L-1][Nc] */
+    const double *damp_dc;
 };
+
+/* Klemp (2008) damping coefficient at inner interface j + 1 of every column
+ * (column_solvers.c:285-298).  It depends on the grid and the two damping
+ * parameters only, so it is tabulated once per parameter pair instead of
+ * once per substage. */
+__global__ void k_damping_table(VGrid vg, double start_height, double coeff_max, double *dc)
+{
+    const long long n = (long long)(vg.nl - 1) * vg.nc, q = gtid();
+    if (q >= n) return;
+    const long long wi = q + vg.nc;
+    const double zad = vg.z_v[wi] - start_height;
+    double r = 0.0;
+    if (zad >= 0.0) {
+        const double s = sin(0.5 * M_PI * zad / (vg.z_v[0] - start_height));
+        r = coeff_max * (s * s);
+    }
+    dc[q] = r;
+}
 
 template <bool EXACT>
 __global__ void k_waves_layer(VGrid vg, StepParams p, DState so, DState sn, DState st, WavesWork ww, int rk)
@@ -114,7 +134,7 @@ __global__ void k_waves_rows(VGrid vg, StepParams p, DState so, DState st, Waves
         rv = -(wo + dt * st.w[wi]) * dz / (iw * dt2 * C_D_P) + th * (ww.ep_expl[b] - ww.ep_expl[lo]) / dt
              + 0.5 / dt * (ww.tp_expl[b] + ww.tp_expl[lo]) * dpi - dz / (iw * dt2 * C_D_P) * wo * rho_ie / rho_io;
     } else {
-        const double k1 = dz / (iw * dt2 * C_D_P), irio = 1.0 / rho_io, idt = 1.0 / dt;
+        const double k1 = dz * p.k_rows, irio = 1.0 / rho_io, idt = p.inv_dt;
         dv = -(th * th) * (g0 + g1) + 0.5 * dpi * (a1 - a0 + th * (b1 - b0))
              - k1 * irio * (2.0 * ww.inv_area_v[wi] + dt * wo * 0.5 * (ww.inv_vol[lo] - ww.inv_vol[b]));
         rv = -(wo + dt * st.w[wi]) * k1 + th * (ww.ep_expl[b] - ww.ep_expl[lo]) * idt
@@ -135,7 +155,7 @@ __global__ void k_waves_rows(VGrid vg, StepParams p, DState so, DState st, Waves
             ev = th * g1 * th1 - 0.5 * dpi * (a1 + b1 * th1)
                  + dz / (iw * dt * C_D_P) * 0.5 * wo / (vg.volume[lo] * rho_io);
         } else {
-            const double k2 = 0.5 / (iw * dt * C_D_P) * ww.inv_vol[lo];
+            const double k2 = p.k_rows2 * ww.inv_vol[lo];
             cv = th1 * g1 * th + 0.5 * (vg.exner_bg[lo] - vg.exner_bg[lo2]) * (a1 + b1 * th)
                  - (vg.z_scalar[lo] - vg.z_scalar[lo2]) * k2 * so.w[wi + nc] / rho_io1;
             ev = th * g1 * th1 - 0.5 * dpi * (a1 + b1 * th1) + dz * k2 * wo / rho_io;
@@ -143,16 +163,8 @@ __global__ void k_waves_rows(VGrid vg, StepParams p, DState so, DState st, Waves
         ww.c[q] = cv;
         ww.e[q] = ev;
     }
-    /* Klemp (2008) damping of the solution at interface j + 1 */
-    const double zad = vg.z_v[wi] - p.damping_start_height;
-    double dc;
-    if (zad < 0.0) {
-        dc = 0.0;
-    } else {
-        const double s = sin(0.5 * M_PI * zad / (vg.z_v[0] - p.damping_start_height));
-        dc = p.damping_coeff_max * (s * s);
-    }
-    ww.dden[q] = 1.0 + dt * dc;
+    /* Klemp (2008) damping denominator of the solution at interface j + 1 */
+    ww.dden[q] = 1.0 + dt * ww.damp_dc[q];
     (void)i;
 }
 
@@ -231,7 +243,7 @@ __global__ void k_waves_thomas_any(int nc, int nl, WavesWork ww)
 }
 
 template <bool EXACT>
-__global__ void k_waves_apply(VGrid vg, StepParams p, DState so, DState sn, WavesWork ww)
+__global__ void k_waves_apply(VGrid vg, StepParams p, DState so, DState sn, WavesWork ww, Shadow sh)
 {
     const int nc = vg.nc, nl = vg.nl;
     const long long ns = (long long)nl * nc, b = gtid();
@@ -255,18 +267,29 @@ __global__ void k_waves_apply(VGrid vg, StepParams p, DState so, DState sn, Wave
     else if (j == nl - 1) num = -ww.th_int[b - nc] * sol[b - nc];
     else num = -ww.th_int[b - nc] * sol[b - nc] + ww.th_int[b] * sol[b];
     const double rt_new = EXACT ? ww.rt_expl[b] + dt * num / vg.volume[b] : ww.rt_expl[b] + dt * num * ww.inv_vol[b];
+    const double tp_new = rt_new / r_new - vg.theta_v_bg[b];
+    const double ep_new = so.exner_pert[b] + vg.volume[b] * ww.gam[b] * (rt_new - so.rhotheta_v[b]);
     sn.rho[gp + b] = r_new;
     sn.rhotheta_v[b] = rt_new;
-    sn.theta_v_pert[b] = rt_new / r_new - vg.theta_v_bg[b];
-    sn.exner_pert[b] = so.exner_pert[b] + vg.volume[b] * ww.gam[b] * (rt_new - so.rhotheta_v[b]);
+    sn.theta_v_pert[b] = tp_new;
+    sn.exner_pert[b] = ep_new;
+    if (sh.rho) {
+        sh.rho[gp + b] = float(r_new);
+        sh.rhotheta_v[b] = float(rt_new);
+        sh.theta_v_pert[b] = float(tp_new);
+        sh.exner_pert[b] = float(ep_new);
+    }
     if (j < nl - 1) {
         const long long wi = b + nc;
         const double r_below = rho_new(j + 1, b + nc);
         const double dint = 0.5 * (r_new + r_below);
+        double wn;
         if (EXACT)
-            sn.w[wi] = (2.0 * sol[b] / vg.area_v[wi] - dint * so.w[wi]) / ww.rho_io[b];
+            wn = (2.0 * sol[b] / vg.area_v[wi] - dint * so.w[wi]) / ww.rho_io[b];
         else
-            sn.w[wi] = (2.0 * sol[b] * ww.inv_area_v[wi] - dint * so.w[wi]) / ww.rho_io[b];
+            wn = (2.0 * sol[b] * ww.inv_area_v[wi] - dint * so.w[wi]) / ww.rho_io[b];
+        sn.w[wi] = wn;
+        if (sh.w) sh.w[wi] = float(wn);
     }
 }
 
@@ -290,7 +313,7 @@ __device__ __forceinline__ double sink_velocity(const StepParams &p, int k, bool
 /* vertical advection + sedimentation of constituent k in one column
  * (column_solvers.c:398-635); thread = (k-slot, column) */
 template <int NL, bool EXACT>
-__global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DState st, TracerWork tw)
+__global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DState st, TracerWork tw, float *sh_rho)
 {
     const int nc = vg.nc;
     const long long ns = (long long)NL * nc;
@@ -394,12 +417,19 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
         c_prev = cj;
     }
     double *rn = sn.rho + k * ns;
+    float *rs = sh_rho ? sh_rho + k * ns : nullptr;
     double x = rp[NL - 1];
-    rn[(long long)(NL - 1) * nc + i] = x < 0.0 ? 0.0 : x;
+    {
+        const double v = x < 0.0 ? 0.0 : x;
+        rn[(long long)(NL - 1) * nc + i] = v;
+        if (rs) rs[(long long)(NL - 1) * nc + i] = float(v);
+    }
 #pragma unroll
     for (int j = NL - 2; j >= 0; --j) {
         x = rp[j] - ep[j] * x;
-        rn[(long long)j * nc + i] = x < 0.0 ? 0.0 : x;
+        const double v = x < 0.0 ? 0.0 : x;
+        rn[(long long)j * nc + i] = v;
+        if (rs) rs[(long long)j * nc + i] = float(v);
     }
 }
 
@@ -414,6 +444,7 @@ __global__ void k_tracers_sedheat(VGrid vg, StepParams p, DState so, DState sn, 
     if (b >= ns) return;
     const int j = (int)(b / nc), i = (int)(b - (long long)j * nc);
     const double vol = vg.volume[b];
+    const double ivol = EXACT ? 0.0 : tw.inv_vol[b];
     const long long bot = i + ns - nc;
     const double a_sfc = vg.area_v[(long long)nl * nc + i];
     /* enthalpy flux of constituent k at interface jj (below layer jj) */
@@ -428,19 +459,20 @@ __global__ void k_tracers_sedheat(VGrid vg, StepParams p, DState so, DState sn, 
         const double cp = (k % 2 == 0) ? tw.cp_ice[up] : tw.cp_water[up];
         return cp * tio * fr;
     };
+    auto per_vol = [&](double x) { return EXACT ? x / vol : x * ivol; };
     double sh = 0.0;
     for (int k = 0; k < p.n_cond; ++k) {
         bool has;
         const double vs = sink_velocity(p, k, has);
         if (j == 0) {
-            sh += fe(k, j, vs, has) / vol;
+            sh += per_vol(fe(k, j, vs, has));
         } else if (j == nl - 1) {
-            sh += -fe(k, j - 1, vs, has) / vol;
+            sh += per_vol(-fe(k, j - 1, vs, has));
             const double tb = temperature[bot];
             const double cp = (k % 2 == 0) ? tw.cp_ice[bot] : tw.cp_water[bot];
-            sh += -vs * tb * cp * so.rho[k * ns + bot] * a_sfc / vol;
+            sh += per_vol(-vs * tb * cp * so.rho[k * ns + bot] * a_sfc);
         } else {
-            sh += (-fe(k, j - 1, vs, has) + fe(k, j, vs, has)) / vol;
+            sh += per_vol(-fe(k, j - 1, vs, has) + fe(k, j, vs, has));
         }
     }
     sed_heat[b] = sh;

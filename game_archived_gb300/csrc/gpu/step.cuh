@@ -43,12 +43,45 @@ inline WavesWork waves_work(Context *c)
     w.dden = b + 6 * ni;
     w.inv_vol = c->inv_vol;
     w.inv_area_v = c->inv_area_v;
+    w.damp_dc = c->damp_dc;
     return w;
 }
 
+/* read view of state_new in precision R and the FP32 shadow (mixed path) */
+template <typename R>
+struct Views {
+    SView<R> sv;
+    Shadow sh;
+};
+template <typename R>
+Views<R> views(Context *c, StateMirror *sn);
+template <>
+inline Views<double> views<double>(Context *c, StateMirror *sn)
+{
+    Views<double> v{};
+    v.sv = {sn->ds.rho, sn->ds.rhotheta_v, sn->ds.theta_v_pert, sn->ds.exner_pert, sn->ds.w, sn->ds.u};
+    v.sh = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return v;
+}
+template <>
+inline Views<float> views<float>(Context *c, StateMirror *sn)
+{
+    Views<float> v{};
+    const long long ns = c->ns;
+    float *b = c->shadow;
+    v.sh.rho = b;
+    v.sh.rhotheta_v = b + (long long)c->n_const * ns;
+    v.sh.theta_v_pert = v.sh.rhotheta_v + ns;
+    v.sh.exner_pert = v.sh.theta_v_pert + ns;
+    v.sh.w = v.sh.exner_pert + ns;
+    v.sh.u = v.sh.w + (long long)(c->nl + 1) * c->nc;
+    v.sv = {v.sh.rho, v.sh.rhotheta_v, v.sh.theta_v_pert, v.sh.exner_pert, v.sh.w, v.sh.u};
+    return v;
+}
+
 template <typename R, bool ADV, bool PG>
-static void launch_momentum(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st,
-                            double new_w, double old_w)
+static void launch_momentum(Context *c, const StepParams &p, const Views<R> &v, StateMirror *so, StateMirror *sn,
+                            StateMirror *st, double new_w, double old_w)
 {
     HGrid<R> &g = hgrid<R>(c);
     Work<R> &w = work<R>(c);
@@ -56,19 +89,20 @@ static void launch_momentum(Context *c, const StepParams &p, StateMirror *so, St
     {
         ProfScope ps(c, "k_momentum_v");
         k_momentum_v<R, ADV, PG><<<nblocks((long long)(c->nl + 1) * c->nc, bs), bs, 0, c->stream>>>(
-            g, p, sn->ds, c->vg.theta_v_bg, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w);
+            g, p, v.sv, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w);
     }
     {
         ProfScope ps(c, "k_momentum_h");
         k_momentum_h<R, ADV, PG><<<nblocks((long long)c->nl * c->ne, bs), bs, 0, c->stream>>>(
-            g, p, sn->ds, so->ds.u, c->vg.theta_v_bg, st->ds.u, w.P_h, w.pg_old_h, w.pvt_h, w.v2g_h, w.flux_h,
-            w.flux_v, w.zh, w.zv, w.v2, new_w, old_w);
+            g, p, v.sv, sn->ds.u, v.sh.u, so->ds.u, st->ds.u, w.P_h, w.pg_old_h, w.pvt_h, w.v2g_h, w.flux_h, w.flux_v,
+            w.zh, w.zv, w.v2, new_w, old_w);
     }
     c->kernel_launches += 2;
 }
 
 template <bool EXACT>
-void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st, int rk)
+void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st, int rk,
+                     const Shadow &sh)
 {
     const long long ns = c->ns;
     WavesWork ww = waves_work(c);
@@ -90,7 +124,7 @@ void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirr
     }
     {
         ProfScope ps(c, "k_waves_apply");
-        k_waves_apply<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, ww);
+        k_waves_apply<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, ww, sh);
     }
     c->kernel_launches += 4;
     if (c->n_const > 1) {
@@ -104,7 +138,7 @@ void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirr
             }
             ProfScope ps(c, "k_tracers_solve");
             k_tracers_solve<NL_FIXED, EXACT><<<nblocks((long long)(c->n_const - 1) * c->nc, 64), 64, 0, c->stream>>>(
-                c->vg, p, so->ds, sn->ds, st->ds, tw);
+                c->vg, p, so->ds, sn->ds, st->ds, tw, sh.rho);
         } else {
             ProfScope ps(c, "k_vertical_tracers");
             k_vertical_tracers<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds,
@@ -123,48 +157,72 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
     Work<R> &w = work<R>(c);
     const int bs = 256;
     const long long ns = c->ns;
+    const Views<R> v = views<R>(c, sn);
+    R *theta = EXACT ? (R *)c->theta : (R *)c->theta32;
+    const R *cpi = EXACT ? (const R *)c->cp_ice : (const R *)c->cp32_ice;
+    const R *cpw = EXACT ? (const R *)c->cp_water : (const R *)c->cp32_water;
+    if (!EXACT) {
+        ProfScope ps(c, "k_make_shadow");
+        const long long n_rho = (long long)c->n_const * ns, nw = (long long)(c->nl + 1) * c->nc,
+                        nu = (long long)c->nl * c->ne;
+        k_make_shadow<<<nblocks(std::max(std::max(n_rho, nw), nu), bs), bs, 0, c->stream>>>(n_rho, ns, nw, nu, sn->ds,
+                                                                                            v.sh);
+        c->kernel_launches++;
+    }
     {
         ProfScope ps(c, "k_cell_prepare");
-        k_cell_prepare<<<nblocks(ns, bs), bs, 0, c->stream>>>(c->vg, p, so->ds, c->temperature, c->pt_rates,
-                                                              c->pt_heat, c->cp_ice, c->cp_water);
+        if (EXACT)
+            k_cell_prepare<<<nblocks(ns, bs), bs, 0, c->stream>>>(c->vg, p, so->ds, c->temperature, c->pt_rates,
+                                                                  c->pt_heat, c->cp_ice, c->cp_water);
+        else
+            k_cell_prepare_f32<<<nblocks(ns, bs), bs, 0, c->stream>>>(c->vg, p, so->ds, c->temperature, c->pt_rates,
+                                                                      c->pt_heat, c->cp_ice, c->cp_water, c->cp32_ice,
+                                                                      c->cp32_water);
     }
     c->kernel_launches++;
+    const R *rho_gas = v.sv.rho + (long long)c->n_cond * ns;
     for (int rk = 0; rk < 2; ++rk) {
         const bool adv = rk == 1 || p.first_step;
         const double new_w = rk == 1 ? 0.5 : 1.0, old_w = 1.0 - new_w;
-        const double *rho_gas = sn->ds.rho + (long long)c->n_cond * ns;
         if (adv) {
             {
                 ProfScope ps(c, "k_tri_vort");
-                k_tri_vort<R><<<nblocks((long long)c->nl * c->nt, bs), bs, 0, c->stream>>>(g, sn->ds.u, w.tri_vort);
+                k_tri_vort<R><<<nblocks((long long)c->nl * c->nt, bs), bs, 0, c->stream>>>(g, v.sv.u, w.tri_vort);
             }
             {
                 ProfScope ps(c, "k_edge_vort");
                 k_edge_vort<R><<<nblocks((long long)(c->nl + 1) * c->ne, bs), bs, 0, c->stream>>>(
-                    g, sn->ds.u, sn->ds.w, rho_gas, w.tri_vort, w.zh, w.zv, w.flux_h);
+                    g, v.sv.u, v.sv.w, rho_gas, w.tri_vort, w.zh, w.zv, w.flux_h);
             }
             {
                 ProfScope ps(c, "k_cell_kinetic");
-                k_cell_kinetic<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(g, sn->ds.u, sn->ds.w, rho_gas, w.v2,
-                                                                          w.flux_v);
+                k_cell_kinetic<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(g, v.sv.u, v.sv.w, rho_gas, w.v2, w.flux_v);
             }
             c->kernel_launches += 3;
         }
-        if (rk == 0 && adv) launch_momentum<R, true, true>(c, p, so, sn, st, new_w, old_w);
-        else if (rk == 0) launch_momentum<R, false, true>(c, p, so, sn, st, new_w, old_w);
-        else launch_momentum<R, true, false>(c, p, so, sn, st, new_w, old_w);
+        if (rk == 0 && adv) launch_momentum<R, true, true>(c, p, v, so, sn, st, new_w, old_w);
+        else if (rk == 0) launch_momentum<R, false, true>(c, p, v, so, sn, st, new_w, old_w);
+        else launch_momentum<R, true, false>(c, p, v, so, sn, st, new_w, old_w);
         {
             ProfScope ps(c, "k_theta");
-            k_theta<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(c->vg, p, sn->ds, c->theta);
+            k_theta<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(c->nl, c->nc, c->n_cond, v.sv, theta);
         }
         {
             ProfScope ps(c, "k_scalar_tend");
-            k_scalar_tend2<R><<<nblocks(ns, 128), 128, 0, c->stream>>>(g, c->vg, p, sn->ds, st->ds, c->theta,
-                                                                        c->cp_ice, c->cp_water, c->pt_rates,
-                                                                        c->pt_heat, c->sed_heat, rk);
+            k_scalar_tend2<R><<<nblocks(ns, 128), 128, 0, c->stream>>>(g, p, v.sv, st->ds, theta, cpi, cpw,
+                                                                        c->pt_rates, c->pt_heat, c->sed_heat,
+                                                                        c->inv_vol, rk);
         }
         c->kernel_launches += 2;
-        launch_vertical<EXACT>(c, p, so, sn, st, rk);
+        launch_vertical<EXACT>(c, p, so, sn, st, rk, v.sh);
+        if (!EXACT && c->nl != NL_FIXED && c->n_const > 1) {
+            /* the generic tracer sweep does not write the shadow: refresh it */
+            const long long n_rho = (long long)c->n_const * ns, nw = (long long)(c->nl + 1) * c->nc,
+                            nu = (long long)c->nl * c->ne;
+            k_make_shadow<<<nblocks(std::max(std::max(n_rho, nw), nu), bs), bs, 0, c->stream>>>(n_rho, ns, nw, nu,
+                                                                                                sn->ds, v.sh);
+            c->kernel_launches++;
+        }
     }
 }
 

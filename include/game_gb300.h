@@ -128,6 +128,34 @@ int scalar_times_vector_v(double *in_field_v, double *vector_field, double *out_
 /* spatial_operators.h:25 -> inner_product.c:13 */
 int inner_product(double *in_field_0, double *in_field_1, double *out_field, struct grid *grid);
 
+/* ---- 3. integrals and surface pressure (the model's monitoring output) ---- */
+
+/* src/io/write_output.c:28 -> :1659-1668: sum of density_gen * volume over all
+ * grid boxes.  Summed on the device with compensated (double-word)
+ * accumulation of the exact products, so the result is the exact sum
+ * rounded once, where the reference's serial loop carries up to
+ * NO_OF_SCALARS roundings.  Returns NaN on error (game_gpu_last_error). */
+double global_scalar_integrator(double *density_gen, struct grid *grid);
+
+/* The values write_out_integral (src/io/write_output.c:1515-1596) appends to
+ * its files, without the file: integral_id 0 -> result[NO_OF_CONSTITUENTS],
+ * the mass of every constituent; 1 -> result[0], the integral of
+ * rho*theta_v; 2 -> result[0..2] = 0.5 * kinetic, potential and
+ * C_D_V * internal energy of the gas phase.  The temperature of id 2 is the
+ * one the reference's diagnostics hold at that point: T(state_old) of the
+ * last manage_rkhevi call, or T(state) before the first step
+ * (coordinator.c:250 and :280-284).  Reads the device mirror in resident
+ * mode, else uploads state first.  No counterpart function in the reference
+ * (write_out_integral also writes files). */
+int game_gpu_write_out_integral(struct state *state, int integral_id, double *result);
+
+/* Surface pressure and mean-sea-level pressure of every column
+ * (src/io/write_output.c:105-121, with temperature_diagnostics of state as
+ * write_out computes it at :83): surface_p[NO_OF_SCALARS_H] and, when mslp
+ * is not NULL, mslp[NO_OF_SCALARS_H], in the reference's column order.
+ * No counterpart function in the reference (the loop is inside write_out). */
+int game_gpu_surface_pressure(struct state *state, double *surface_p, double *mslp);
+
 #ifdef __cplusplus
 }
 #endif

@@ -158,11 +158,41 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle manage_rkhevi returned {rc}")
 
-    def surface_pressure(self, state, temperature):
+    def surface_pressure(self, state, temperature, with_mslp=False):
         out = np.zeros(self.m.layout.nc)
+        ms = np.zeros(self.m.layout.nc) if with_mslp else None
         s = self.state(state)
-        self.lib.orc_surface_pressure(ctypes.byref(self.g), ctypes.byref(s), _d(temperature), _d(out))
-        return out
+        self.lib.orc_surface_pressure(ctypes.byref(self.g), ctypes.byref(s), _d(temperature), _d(out),
+                                      _d(ms) if with_mslp else None)
+        return (out, ms) if with_mslp else out
+
+    def temperature(self, state):
+        """temperature_diagnostics of a State (derived_quantities.c:15-40)"""
+        t = np.zeros(self.m.layout.n_scalars)
+        d = OrcDiag()
+        d.temperature = _d(t)
+        s = self.state(state)
+        self.lib.orc_temperature_diagnostics(ctypes.byref(self.g), ctypes.byref(s), ctypes.byref(d))
+        return t
 
     def integral(self, field):
         return self.lib.orc_global_scalar_integrator(ctypes.byref(self.g), _d(field))
+
+    def write_out_integral(self, state, integral_id, temperature):
+        """the numbers write_out_integral (src/io/write_output.c:1515-1596)
+        writes: serial sums as in the reference"""
+        lay = self.m.layout
+        ns = lay.n_scalars
+        rho = state["rho"]
+        if integral_id == 0:
+            return np.array([self.integral(np.ascontiguousarray(rho[k * ns:(k + 1) * ns]))
+                             for k in range(lay.n_const)])
+        if integral_id == 1:
+            return np.array([self.integral(np.ascontiguousarray(state["rhotheta_v"]))])
+        rho_g = np.ascontiguousarray(rho[lay.n_cond * ns:(lay.n_cond + 1) * ns])
+        ekin = np.zeros(ns)
+        self.inner_product(state["wind"], state["wind"], ekin)
+        ekin = rho_g * ekin
+        pot = rho_g * self.m.grid["gravity_potential"]
+        internal = rho_g * temperature
+        return np.array([0.5 * self.integral(ekin), self.integral(pot), 717.942189 * self.integral(internal)])

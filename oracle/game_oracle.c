@@ -1067,7 +1067,8 @@ double orc_global_scalar_integrator(const orc_grid *g, const double *field)
     return r;
 }
 
-int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *temperature, double *p_sfc)
+int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *temperature, double *p_sfc,
+                         double *mslp)
 {
     /* src/io/write_output.c:105-121 with gas_constant_diagnostics
      * (src/constituents/derived_quantities.c:42-61) */
@@ -1083,6 +1084,10 @@ int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *te
         }
         double t_low = temperature[si];
         double p = s->rho[COND * NS + si] * rgas * t_low;
+        if (mslp) {
+            double t_mslp = t_low + lapse * g->z_scalar[i + (NL - 1) * NC];
+            mslp[i] = p / pow(1 - (t_mslp - t_low) / t_mslp, g->gravity_m[(NL - 1) * VPL + i] / (rgas * lapse));
+        }
         double t_sfc = t_low + lapse * (g->z_scalar[i + (NL - 1) * NC] - g->z_vector[NV - NC + i]);
         double fac = pow(1.0 - (t_sfc - t_low) / t_sfc, g->gravity_m[(NL - 1) * VPL + i] / (rgas * lapse));
         p_sfc[i] = p / fac;

@@ -99,6 +99,8 @@ int orc_manage_rkhevi(const orc_grid *g, const orc_state *s_old, orc_state *s_ne
 
 /* output metrics (src/io/write_output.c:105-121, 1515-1668) */
 double orc_global_scalar_integrator(const orc_grid *g, const double *field);
-int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *temperature, double *p_sfc);
+/* mslp may be NULL */
+int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *temperature, double *p_sfc,
+                         double *mslp);
 
 #endif
