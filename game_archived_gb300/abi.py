@@ -55,6 +55,7 @@ SIGNATURES = {
     "global_scalar_integrator": ([vp, vp], dbl),
     "game_gpu_write_out_integral": ([vp, cint, vp], cint),
     "game_gpu_surface_pressure": ([vp, vp, vp], cint),
+    "game_gpu_weighted_sums_noalloc": ([vp, cint, ctypes.c_longlong, vp, vp, vp], cint),
 }
 
 FP64, MIXED = 0, 1

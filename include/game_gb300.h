@@ -156,6 +156,32 @@ int game_gpu_write_out_integral(struct state *state, int integral_id, double *re
  * No counterpart function in the reference (the loop is inside write_out). */
 int game_gpu_surface_pressure(struct state *state, double *surface_p, double *mslp);
 
+/* ---- 4. the weighted-sum reduction without any allocation ---- */
+
+/* sums[k] = sum over i < n of fields[k*n + i] * weights[i], for k < n_fields,
+ * with the compensated accumulation of global_scalar_integrator.  All four
+ * arrays are DEVICE pointers; sums is written on the device in stream order
+ * (stream: a cudaStream_t, NULL for the default stream), and the call returns
+ * without waiting for it.  No game_gpu_init is needed.
+ *
+ * Allocates nothing: no cudaMalloc, no cudaFree, no library routine that
+ * allocates.  Its scratch is a fixed 77,856-byte device array inside the
+ * library, which limits n_fields to 1..8 (larger counts are rejected with an
+ * error); n is unlimited.  For callers that cannot allocate device memory at
+ * the point of the call: hosts that keep several streams busy and cannot take
+ * the device-wide synchronisation of cudaMalloc/cudaFree, and hosts that have
+ * given all device memory to their own pool.
+ *
+ * The first call on each device (with that device current) looks up the
+ * scratch array and zeroes its counters, synchronously; make it before any
+ * stream capture begins.  Calls on one device share the scratch: calls whose
+ * kernels may overlap (different streams without ordering, several host
+ * threads) race and return wrong sums; keep them in one stream.
+ *
+ * No counterpart in the reference. */
+int game_gpu_weighted_sums_noalloc(const double *fields, int n_fields, long long n, const double *weights,
+                                   double *sums, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
