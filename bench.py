@@ -65,40 +65,64 @@ def b_step(res, n_const, w_s, w_t, w_g, nl=L):
 
 
 def kernel_bytes(res, n_const, r, nl=L):
-    """Algorithmic bytes of one step's launches of each kernel (every array
-    a kernel reads or writes counted once per launch; r = bytes of the
-    horizontal-operator type, state 8, indices 4).  Returns name -> (bytes per
-    step, launches per step) for a non-first step."""
+    """Algorithmic bytes of one non-first step's launches of each kernel of
+    the mixed path: every array a kernel reads or writes, counted once per
+    launch (r = bytes of the horizontal type and of the FP32 state shadow,
+    FP64 state / tendencies / solver work 8, indices 4).  The extra terrain
+    terms of the orography layers are left out, so these are lower bounds.
+    Returns name -> (bytes per step, launches per step)."""
     g = grid_sizes(res, nl)
     nc, ne, nt, s = g["nc"], g["ne"], g["nt"], g["s"]
     wl, ul, zl, tl = (nl + 1) * nc, nl * ne, (nl + 1) * ne, nl * nt
+    wi = (nl - 1) * nc          # inner interfaces
     d, i = 8, 4
     C = n_const
     moist = C > 1
     out = {}
-    out["k_cell_prepare"] = (((4 + C) * s + 7 * s) * d if moist else 5 * s * d, 1)
-    out["k_tri_vort"] = (ul * d + 6 * nt * i + ul * r + 2 * tl * r + ul * r + tl * r, 1)
-    out["k_edge_vort"] = ((ul + wl + s) * d + tl * r + 4 * ne * i + zl * r + ul * r + wl * r + ul * r + 2 * s * r
-                          + 6 * ne * r + 4 * ne * (r + i) + tl * r + zl * r + 2 * ul * r, 1)
-    out["k_cell_kinetic"] = ((ul + wl + s) * d + 8 * s * r + 6 * nc * i + s * r + wl * r, 1)
-    tables_h = 30 * ne * i + 2 * ne * i + 2 * s * r + ul * r + wl * r + ul * r
-    rk0_h = 3 * s * d + C * s * d + ul * r + tables_h + ul * r + 2 * ul * r + ul * d + 2 * ul * r + 2 * ul * d
-    rk1_h = (ul + wl + zl + ul + s) * r + 2 * ul * r + ul * d + ul * d + tables_h + 2 * ul * r + 2 * ul * d
+    out["k_make_shadow"] = (((C + 3) * s + wl + ul) * (d + r), 1)
+    out["k_cell_prepare"] = (((C + 4) * s + 9 * s) * d + 2 * s * r if moist else 5 * s * d, 1)
+    # rk 1 only (advection recomputed in the second substage)
+    out["k_tri_vort"] = (3 * ul * r + 6 * nt * i + 3 * tl * r, 1)
+    out["k_edge_vort"] = ((ul + wl + s) * r + tl * r + 4 * ne * i + zl * r + ul * r + wl * r + 6 * ne * r
+                          + 4 * ne * (r + i) + tl * r + zl * r + 2 * ul * r, 1)
+    out["k_cell_kinetic"] = ((ul + wl + s) * r + 8 * s * r + 6 * nc * i + s * r + wl * r, 1)
+    rk0_h = (3 + C) * s * r + 3 * ul * r + 2 * ne * i + 3 * ul * r + 2 * ul * r + 3 * ul * d + ul * r
+    rk1_h = (2 * ul + zl) * r + 10 * ne * (r + 2 * i) + 2 * ne * i + 2 * s * r + wl * r + s * r + ul * r \
+        + 4 * ul * r + 2 * ul * d + ul * d + ul * d + ul * r
     out["k_momentum_h"] = (rk0_h + rk1_h, 2)
-    tables_v = 6 * nc * i + 6 * s * r + 2 * wl * r
-    rk0_v = 3 * s * d + C * s * d + wl * r + 3 * wl * r + wl * d + wl * r + wl * d
-    rk1_v = (ul + zl + s) * r + tables_v + 2 * wl * r + C * s * d + wl * r + 2 * wl * d
+    rk0_v = (3 + C) * s * r + 2 * wl * r + wl * r + 2 * wl * r + wl * r + wl * d
+    rk1_v = 6 * nc * i + 6 * s * r + ul * r + zl * r + 4 * wl * r + s * r + C * s * r + wl * r + 2 * wl * d
     out["k_momentum_v"] = (rk0_v + rk1_v, 2)
-    out["k_theta"] = (2 * 3 * s * d, 2)
-    sc = C * s * d + ul * d + 2 * s * d + (8 * s * d if moist else 0) + 2 * s * d + 18 * nc * i + ul * r + 6 * s * r \
-        + ul * r + wl * r + s * r + (C + 1) * s * d
-    out["k_scalar_tend"] = (2 * sc + (C + 1) * s * d, 2)
-    vw = (4 * s + wl + 3 * s + 2 * s + wl + 4 * s + 2 * wl + 4 * s + wl) * d
-    out["k_vertical_waves"] = (2 * vw, 2)
+    out["k_theta"] = (2 * 3 * s * r, 2)
+    sc = C * s * r + s * r + 2 * ul * r + 18 * nc * i + s * d + wl * r + (C + 1) * s * d
     if moist:
-        vt_ = ((C - 1) * 3 * s + 2 * wl + s + s + wl + 2 * s) * d
-        out["k_vertical_tracers"] = (2 * vt_, 2)
+        sc += 7 * s * d + 4 * s * r
+    out["k_scalar_tend"] = (2 * sc + (C + 1) * s * d, 2)
+    out["k_waves_layer"] = ((11 + 12 + 16) * s * d, 2)
+    out["k_waves_rows"] = (2 * (14 * wi + 8 * s) * d, 2)
+    out["k_waves_thomas"] = (2 * 6 * wi * d, 2)
+    out["k_waves_apply"] = (2 * ((4 * wi + 12 * s + 2 * wl) * d + (4 * s + wi) * r), 2)
+    if moist:
+        out["k_tracers_solve"] = (2 * ((3 * (C - 1) * s + 3 * wl + s) * d + (C - 1) * s * r), 2)
+        out["k_tracers_sedheat"] = ((((C - 2) + 5) * s + 2 * wl) * d, 1)
     return out
+
+
+def read_ncu_summary(kernel, key):
+    """a per-kernel figure from the committed ncu summary (lines
+    '<key> <kernel> <value>')"""
+    path = os.path.join(ROOT, "profiles", "ncu_rkhevi_res6_mixed.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) == 3 and parts[0] == key and parts[1] == kernel:
+                try:
+                    return float(parts[2])
+                except ValueError:
+                    return None
+    return None
 
 
 # ------------------------------------------------------------------ clocks
@@ -120,7 +144,7 @@ class ClockSampler:
             os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -173,22 +197,6 @@ def copy_model(src, pinned):
     for k in structs.Model.KINDS:
         getattr(m, k).copy_from(getattr(src, k))
     return m
-
-
-def read_ncu_traffic(kernel):
-    """per-launch DRAM traffic of a kernel from the committed ncu summary"""
-    path = os.path.join(ROOT, "profiles", "ncu_rkhevi_res6_mixed.md")
-    if not os.path.exists(path):
-        return None
-    with open(path) as f:
-        for line in f:
-            parts = line.split()
-            if len(parts) >= 3 and parts[0] == "traffic_per_launch_bytes" and parts[1] == kernel:
-                try:
-                    return float(parts[2])
-                except ValueError:
-                    return None
-    return None
 
 
 def measured_peak():
@@ -381,7 +389,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dom_name,
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
-                     "traffic": read_ncu_traffic(dom_name), "peak_source": peak_kind},
+                     "traffic": read_ncu_summary(dom_name, "traffic_per_launch_bytes"), "peak_source": peak_kind,
+                     "fp64_pipe_pct_ncu": read_ncu_summary(dom_name, "fp64_pipe_pct")},
         "roofline_step": {"algorithmic_bytes": step_bytes, "achieved": step_bytes / (ms32_max * 1e-3) / 1e9,
                           "peak": peak, "unit": "GB/s", "frac": step_bytes / (ms32_max * 1e-3) / 1e9 / peak},
         "kernels": kernels,
@@ -439,7 +448,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--res", type=int, default=6)

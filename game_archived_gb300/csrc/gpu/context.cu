@@ -461,12 +461,27 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     c->wv_layer = dalloc<double>(c, 8 * (size_t)NS);
     c->wv_rows = dalloc<double>(c, 7 * (size_t)(L - 1) * NC);
     c->damp_dc = dalloc<double>(c, (size_t)(L - 1) * NC);
+    c->damp_inv = dalloc<double>(c, (size_t)(L - 1) * NC);
     {
         std::vector<double> iv(h_vol.size()), ia(h_areav.size());
         for (size_t k = 0; k < iv.size(); ++k) iv[k] = 1.0 / h_vol[k];
         for (size_t k = 0; k < ia.size(); ++k) ia[k] = h_areav[k] != 0.0 ? 1.0 / h_areav[k] : 0.0;
         c->inv_vol = dupload(c, iv);
         c->inv_area_v = dupload(c, ia);
+        /* mixed-path sound-wave rows: dz, H, G1, G2, Cz, Ez per inner interface */
+        const size_t ni = (size_t)(L - 1) * NC;
+        std::vector<double> geo(6 * ni);
+        for (size_t q = 0; q < ni; ++q) {
+            const size_t b = q, lo = q + NC, wi = q + NC;
+            const double dz = h_zs[b] - h_zs[lo];
+            geo[q] = dz;
+            geo[ni + q] = 0.5 * (h_ebg[b] - h_ebg[lo]);
+            geo[2 * ni + q] = 2.0 * ia[wi];
+            geo[3 * ni + q] = 0.5 * (iv[lo] - iv[b]);
+            geo[4 * ni + q] = dz * iv[b];
+            geo[5 * ni + q] = dz * iv[lo];
+        }
+        c->wv_geo = dupload(c, geo);
     }
     auto work = [&](auto &w, auto tag) {
         using R = decltype(tag);

@@ -118,10 +118,13 @@ struct Context {
         int launches; /* kernels in the graph */
     };
     std::map<GraphKey, GraphEntry> graphs;
-    /* Klemp damping coefficient of every inner interface [L-1][Nc] for the
-     * damping parameters in damp_key (start height, maximum coefficient) */
-    double *damp_dc = nullptr;
-    double damp_key[2] = {-1.0, -1.0};
+    /* Klemp damping coefficient of every inner interface [L-1][Nc] and
+     * 1 / (1 + dt * coefficient) for the values in damp_key (start height,
+     * maximum coefficient, dt) */
+    double *damp_dc = nullptr, *damp_inv = nullptr;
+    double damp_key[3] = {-1.0, -1.0, -1.0};
+    /* grid terms of the mixed-path sound-wave rows [6][L-1][Nc] */
+    double *wv_geo = nullptr;
     int use_graphs = 1;
     int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */
     long long h2d_bytes = 0, d2h_bytes = 0;

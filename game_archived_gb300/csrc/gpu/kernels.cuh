@@ -34,6 +34,25 @@ namespace {
 /* ------------------------------------------------------------ utilities */
 __device__ __forceinline__ long long gtid() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
 
+/* FP64 reciprocal for the mixed path (the FP64 path divides exactly as the
+ * reference).  The seed is the hardware's approximate reciprocal (PTX
+ * rcp.approx.ftz.f64; relative error below 2^-20, measured on GB300 over
+ * 2^20 inputs spanning 1e-300..1e300), refined by Newton-Raphson steps
+ * r <- r + r (1 - x r), each of which squares the relative error: one step
+ * leaves about 2^-40, two steps gave the correctly rounded reciprocal on every
+ * sampled input.  One multiply-add pair per step instead of the several FP64
+ * operations of an IEEE division, on a GPU whose FP64 rate is 1/64 of FP32.
+ * x must be a normal number whose reciprocal is normal (ftz). */
+template <int STEPS>
+__device__ __forceinline__ double rcp_nr(double x)
+{
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+#pragma unroll
+    for (int s = 0; s < STEPS; ++s) r = fma(r, fma(-x, r, 1.0), r);
+    return r;
+}
+
 template <typename R>
 __device__ __forceinline__ R ipw_at(const HGrid<R> &g, int j, int l, int c)
 {
@@ -913,6 +932,12 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
         return R(-0.5) * ipw_at(g, j, ll, c) * g.slope_h[(long long)ll * ne + edge(j)];
     };
     auto uval = [&](int ll, int j) { return sv.u[(long long)ll * ne + edge(j)]; };
+    auto comp_v = [&](R up, R lo) -> double {
+        if (!oro) return 0.0;
+        if (l == nl - n_oro - 1) return double(-lo * area_lo);
+        if (l == nl - 1) return double(up * area_up);
+        return double(up * area_up - lo * area_lo);
+    };
     /* terrain correction of the wind at levels l and l+1 (shared by the tracers) */
     R w_up = R(0), w_lo = R(0);
     if (oro) {
@@ -926,107 +951,119 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
         if (lo_corr)
             for (int j = 0; j < n_edges; ++j) w_lo += wcorr(l + 1, j) * uval(l + 1, j);
     }
-    for (int k = 0; k < p.n_const; ++k) {
-        const double new_w = (rk == 1 && k != cond) ? 0.5 : 1.0, old_w = 1.0 - new_w;
-        const R *f = sv.rho + k * ns;
-        if (k == cond) {
-            /* centred mass flux and, from it, the rho*theta_v flux */
-            FluxSum<R> hm, ht;
-            R um = R(0), ut = R(0), lm = R(0), lt = R(0);
-            auto layer_pass = [&](int ll, bool to_h, bool to_up, bool to_lo) {
-                const long long o = (long long)ll * nc;
-                const R fs = f[o + c], ts = theta[o + c];
-                for (int j = 0; j < n_edges; ++j) {
-                    const int nb = g.adj_nbr[j * nc + c];
-                    const R fm = (R(0.5) * (fs + f[o + nb])) * uval(ll, j);
-                    const R ft = (R(0.5) * (ts + theta[o + nb])) * fm;
-                    if (to_h) {
-                        const R ar = g.area_h[(long long)ll * ne + edge(j)];
-                        const bool self_from = g.adj_sign[j * nc + c] > 0;
-                        const R am = fm * ar, at = ft * ar;
-                        hm.add(self_from ? am : -am);
-                        ht.add(self_from ? at : -at);
-                    }
-                    if (to_up || to_lo) {
-                        const R wc = wcorr(ll, j);
-                        if (to_up) {
-                            um += wc * fm;
-                            ut += wc * ft;
-                        }
-                        if (to_lo) {
-                            lm += wc * fm;
-                            lt += wc * ft;
-                        }
-                    }
-                }
-            };
-            if (up_has_prev) layer_pass(l - 1, false, true, false);
-            layer_pass(l, true, up_corr, lo_has_curr);
-            if (lo_corr) layer_pass(l + 1, false, false, true);
-            auto comp_v = [&](R up, R lo) -> double {
-                if (!oro) return 0.0;
-                if (l == nl - n_oro - 1) return double(-lo * area_lo);
-                if (l == nl - 1) return double(up * area_up);
-                return double(up * area_up - lo * area_lo);
-            };
-            const double div = inv_vol * (hm.value() + comp_v(um, lm));
-            double y = -div;
-            if (p.moist) y = y + pt_rates[cond * ns + i];
-            st.rho[k * ns + i] = rk == 0 ? y : old_w * st.rho[k * ns + i] + new_w * y;
-            const double div_t = inv_vol * (ht.value() + comp_v(ut, lt));
-            double yt = -div_t;
-            if (p.moist) {
-                /* diabatic heating: c_v-weighted, divided by c_p * Pi */
-                R cv = R(0);
-                for (int kk = 0; kk < cond; ++kk) cv += sv.rho[kk * ns + i] * ((kk % 2 == 0) ? cp_ice[i] : cp_water[i]);
-                cv += sv.rho[cond * ns + i] * R(C_D_V);
-                cv += sv.rho[(cond + 1) * ns + i] * R(C_V_V);
-                if (sizeof(R) == sizeof(double)) {
-                    yt = yt + C_D_V * double(sv.rho[cond * ns + i]) / double(cv) * (pt_heat[i] + sed_heat[i])
-                                  / (C_D_P * (double(g.exner_bg[i]) + double(sv.exner_pert[i])))
-                         + pt_rates[cond * ns + i] * double(theta[i]);
-                } else {
-                    const R fac = R(C_D_V) * sv.rho[cond * ns + i] / cv / (R(C_D_P) * (g.exner_bg[i] + sv.exner_pert[i]));
-                    yt = yt + double(fac) * (pt_heat[i] + sed_heat[i]) + pt_rates[cond * ns + i] * double(theta[i]);
-                }
-            }
-            st.rhotheta_v[i] = rk == 0 ? yt : old_w * st.rhotheta_v[i] + new_w * yt;
-        } else {
-            /* upstream tracer flux; vertical part from the wind correction */
-            FluxSum<R> h;
-            const long long o = (long long)l * nc;
-            const R fs = f[o + c];
+    /* the main gas: centred mass flux and, from it, the rho*theta_v flux
+     * (new weight 1 in both substages) */
+    {
+        const R *f = sv.rho + cond * ns;
+        FluxSum<R> hm, ht;
+        R um = R(0), ut = R(0), lm = R(0), lt = R(0);
+        auto layer_pass = [&](int ll, bool to_h, bool to_up, bool to_lo) {
+            const long long o = (long long)ll * nc;
+            const R fs = f[o + c], ts = theta[o + c];
             for (int j = 0; j < n_edges; ++j) {
-                const R ue = uval(l, j);
-                const bool self_from = g.adj_sign[j * nc + c] > 0;
-                const R fv = ((ue >= R(0)) == self_from ? fs : f[o + g.adj_nbr[j * nc + c]]) * ue;
-                const R a = fv * g.area_h[(long long)l * ne + edge(j)];
-                h.add(self_from ? a : -a);
-            }
-            double comp_v = 0.0;
-            if (oro) {
-                const R d_here = f[i];
-                if (l == nl - n_oro - 1) {
-                    const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
-                    comp_v = double(-d_lo * w_lo * area_lo);
-                } else if (l == nl - 1) {
-                    const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
-                    comp_v = double(d_up * w_up * area_up);
-                } else {
-                    const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
-                    const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
-                    comp_v = double(d_up * w_up * area_up - d_lo * w_lo * area_lo);
+                const int nb = g.adj_nbr[j * nc + c];
+                const R fm = (R(0.5) * (fs + f[o + nb])) * uval(ll, j);
+                const R ft = (R(0.5) * (ts + theta[o + nb])) * fm;
+                if (to_h) {
+                    const R ar = g.area_h[(long long)ll * ne + edge(j)];
+                    const bool self_from = g.adj_sign[j * nc + c] > 0;
+                    const R am = fm * ar, at = ft * ar;
+                    hm.add(self_from ? am : -am);
+                    ht.add(self_from ? at : -at);
+                }
+                if (to_up || to_lo) {
+                    const R wc = wcorr(ll, j);
+                    if (to_up) {
+                        um += wc * fm;
+                        ut += wc * ft;
+                    }
+                    if (to_lo) {
+                        lm += wc * fm;
+                        lt += wc * ft;
+                    }
                 }
             }
-            const double div = inv_vol * (h.value() + comp_v);
-            double y = -div;
-            if (p.moist) {
-                long long pt = k * ns;
-                if (k == cond + 1) pt -= ns;
-                y = y + pt_rates[pt + i];
+        };
+        if (up_has_prev) layer_pass(l - 1, false, true, false);
+        layer_pass(l, true, up_corr, lo_has_curr);
+        if (lo_corr) layer_pass(l + 1, false, false, true);
+        const double div = inv_vol * (hm.value() + comp_v(um, lm));
+        double y = -div;
+        if (p.moist) y = y + pt_rates[cond * ns + i];
+        st.rho[cond * ns + i] = rk == 0 ? y : 0.0 * st.rho[cond * ns + i] + 1.0 * y;
+        const double div_t = inv_vol * (ht.value() + comp_v(ut, lt));
+        double yt = -div_t;
+        if (p.moist) {
+            /* diabatic heating: c_v-weighted, divided by c_p * Pi */
+            R cv = R(0);
+            for (int kk = 0; kk < cond; ++kk) cv += sv.rho[kk * ns + i] * ((kk % 2 == 0) ? cp_ice[i] : cp_water[i]);
+            cv += sv.rho[cond * ns + i] * R(C_D_V);
+            cv += sv.rho[(cond + 1) * ns + i] * R(C_V_V);
+            if (sizeof(R) == sizeof(double)) {
+                yt = yt + C_D_V * double(sv.rho[cond * ns + i]) / double(cv) * (pt_heat[i] + sed_heat[i])
+                              / (C_D_P * (double(g.exner_bg[i]) + double(sv.exner_pert[i])))
+                     + pt_rates[cond * ns + i] * double(theta[i]);
+            } else {
+                const R fac = R(C_D_V) * sv.rho[cond * ns + i] / cv / (R(C_D_P) * (g.exner_bg[i] + sv.exner_pert[i]));
+                yt = yt + double(fac) * (pt_heat[i] + sed_heat[i]) + pt_rates[cond * ns + i] * double(theta[i]);
             }
-            st.rho[k * ns + i] = (new_w == 1.0 && rk == 0) ? y : old_w * st.rho[k * ns + i] + new_w * y;
         }
+        st.rhotheta_v[i] = rk == 0 ? yt : 0.0 * st.rhotheta_v[i] + 1.0 * yt;
+    }
+    if (p.n_const == 1) return;
+    /* the other constituents: upstream flux.  The cell's edges, neighbours,
+     * orientation and layer-l wind and face areas are loaded once for all
+     * of them. */
+    int ej[6], nbj[6];
+    bool sfj[6];
+    R uj[6], arj[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        const bool on = j < n_edges;
+        ej[j] = on ? g.adj[j * nc + c] : 0;
+        nbj[j] = on ? g.adj_nbr[j * nc + c] : c;
+        sfj[j] = on && g.adj_sign[j * nc + c] > 0;
+        uj[j] = on ? sv.u[(long long)l * ne + ej[j]] : R(0);
+        arj[j] = on ? g.area_h[(long long)l * ne + ej[j]] : R(0);
+    }
+    const long long o = (long long)l * nc;
+    for (int k = 0; k < p.n_const; ++k) {
+        if (k == cond) continue;
+        const double new_w = rk == 1 ? 0.5 : 1.0, old_w = 1.0 - new_w;
+        const R *f = sv.rho + k * ns;
+        FluxSum<R> h;
+        const R fs = f[o + c];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            if (j >= n_edges) continue;
+            const R ue = uj[j];
+            const R fv = ((ue >= R(0)) == sfj[j] ? fs : f[o + nbj[j]]) * ue;
+            const R a = fv * arj[j];
+            h.add(sfj[j] ? a : -a);
+        }
+        double cv = 0.0;
+        if (oro) {
+            const R d_here = f[i];
+            if (l == nl - n_oro - 1) {
+                const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
+                cv = double(-d_lo * w_lo * area_lo);
+            } else if (l == nl - 1) {
+                const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
+                cv = double(d_up * w_up * area_up);
+            } else {
+                const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
+                const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
+                cv = double(d_up * w_up * area_up - d_lo * w_lo * area_lo);
+            }
+        }
+        const double div = inv_vol * (h.value() + cv);
+        double y = -div;
+        if (p.moist) {
+            long long pt = k * ns;
+            if (k == cond + 1) pt -= ns;
+            y = y + pt_rates[pt + i];
+        }
+        st.rho[k * ns + i] = rk == 0 ? y : old_w * st.rho[k * ns + i] + new_w * y;
     }
 }
 

@@ -6,7 +6,8 @@
  *   k_waves_layer   per (layer, column): explicit predictors and the
  *                   partial derivatives alpha, beta, gamma (:102-139)
  *   k_waves_rows    per (interface, column): the tridiagonal rows c, d, e, r
- *                   (:142-189) and the Klemp damping denominator (:285-298)
+ *                   (:142-189) and the Klemp damping denominator (:285-298);
+ *                   k_waves_rows_mixed is its mixed-path rearrangement
  *   k_waves_thomas  per column: the elimination, with the sweep held in
  *                   registers (layer count a compile-time constant)
  *   k_waves_apply   per (layer, column): back-substitution into rho, rho*theta_v,
@@ -38,15 +39,22 @@ struct WavesWork {
     /* mixed path: reciprocal grid metrics */
     const double *inv_vol;    /* [L][Nc] */
     const double *inv_area_v; /* [L+1][Nc] */
-    /* Klemp damping coefficient of the inner interfaces [L-1][Nc] */
-    const double *damp_dc;
+    /* Klemp damping coefficient of the inner interfaces [L-1][Nc]; mixed
+     * path: 1 / (1 + dt * coefficient) for the current dt */
+    const double *damp_dc, *damp_inv;
+    /* mixed path: grid terms of the rows of inner interface j [6][L-1][Nc]:
+     * dz = z(j) - z(j+1), H = (Pi_bg(j) - Pi_bg(j+1)) / 2, G1 = 2 / A_v,
+     * G2 = (1/V(j+1) - 1/V(j)) / 2, Cz = dz / V(j), Ez = dz / V(j+1)
+     * (layers j, j+1 above and below the interface) */
+    const double *geo;
 };
 
 /* Klemp (2008) damping coefficient at inner interface j + 1 of every column
  * (column_solvers.c:285-298).  It depends on the grid and the two damping
  * parameters only, so it is tabulated once per parameter pair instead of
  * once per substage. */
-__global__ void k_damping_table(VGrid vg, double start_height, double coeff_max, double *dc)
+__global__ void k_damping_table(VGrid vg, double start_height, double coeff_max, double dt, double *dc,
+                                double *inv_den)
 {
     const long long n = (long long)(vg.nl - 1) * vg.nc, q = gtid();
     if (q >= n) return;
@@ -58,6 +66,7 @@ __global__ void k_damping_table(VGrid vg, double start_height, double coeff_max,
         r = coeff_max * (s * s);
     }
     dc[q] = r;
+    inv_den[q] = 1.0 / (1.0 + dt * r);
 }
 
 template <bool EXACT>
@@ -86,19 +95,29 @@ __global__ void k_waves_layer(VGrid vg, StepParams p, DState so, DState sn, DSta
             gam = ((1.0 - pdw) * go + pdw * gn) / vol;
         }
     } else {
-        const double iv = ww.inv_vol[b], iro = 1.0 / ro;
-        const double go = (R_D / C_D_V) * (vg.exner_bg[b] + so.exner_pert[b]) / rto;
+        const double iv = ww.inv_vol[b], iro = rcp_nr<1>(ro);
+        const double rn = sn.rho[gp + b], rtn = sn.rhotheta_v[b], irn = rk == 0 ? 0.0 : rcp_nr<1>(rn);
+        const double go = (R_D / C_D_V) * (vg.exner_bg[b] + so.exner_pert[b]) * rcp_nr<1>(rto);
         if (rk == 0) {
             alpha = -rto * iro * iro * iv;
             beta = iro * iv;
             gam = go * iv;
         } else {
-            const double irn = 1.0 / sn.rho[gp + b];
-            const double gn = (R_D / C_D_V) * (vg.exner_bg[b] + sn.exner_pert[b]) / sn.rhotheta_v[b];
-            alpha = 0.5 * (-rto * iro * iro - sn.rhotheta_v[b] * irn * irn) * iv;
+            const double gn = (R_D / C_D_V) * (vg.exner_bg[b] + sn.exner_pert[b]) * rcp_nr<1>(rtn);
+            alpha = 0.5 * (-rto * iro * iro - rtn * irn * irn) * iv;
             beta = 0.5 * (iro + irn) * iv;
             gam = 0.5 * (go + gn) * iv;
         }
+        const double str = st.rho[gp + b], strt = st.rhotheta_v[b];
+        ww.alpha[b] = alpha;
+        ww.beta[b] = beta;
+        ww.gam[b] = gam;
+        ww.rho_expl[b] = ro + dt * str;
+        ww.rt_expl[b] = rto + dt * strt;
+        ww.tp_expl[b] = so.theta_v_pert[b] + dt * vol * (alpha * str + beta * strt);
+        ww.ep_expl[b] = so.exner_pert[b] + dt * vol * gam * strt;
+        ww.thl[b] = rtn * (rk == 0 ? rcp_nr<1>(rn) : irn);
+        return;
     }
     ww.alpha[b] = alpha;
     ww.beta[b] = beta;
@@ -110,13 +129,13 @@ __global__ void k_waves_layer(VGrid vg, StepParams p, DState so, DState sn, DSta
     ww.thl[b] = sn.rhotheta_v[b] / sn.rho[gp + b];
 }
 
-template <bool EXACT>
+/* FP64 path: the rows in the reference's operation order */
 __global__ void k_waves_rows(VGrid vg, StepParams p, DState so, DState st, WavesWork ww)
 {
     const int nc = vg.nc, nl = vg.nl;
     const long long n = (long long)(nl - 1) * nc, q = gtid();
     if (q >= n) return;
-    const int j = (int)(q / nc), i = (int)(q - (long long)j * nc);
+    const int j = (int)(q / nc);
     const long long ns = (long long)nl * nc, gp = p.n_cond * ns;
     const long long b = q, lo = q + nc, wi = q + nc;
     const double dt = p.dt, iw = p.impl_thermo_weight, dt2 = dt * dt;
@@ -127,45 +146,66 @@ __global__ void k_waves_rows(VGrid vg, StepParams p, DState so, DState st, Waves
     const double wo = so.w[wi];
     const double a0 = ww.alpha[b], a1 = ww.alpha[lo], b0 = ww.beta[b], b1 = ww.beta[lo];
     const double g0 = ww.gam[b], g1 = ww.gam[lo];
-    double dv, rv;
-    if (EXACT) {
-        dv = -(th * th) * (g0 + g1) + 0.5 * dpi * (a1 - a0 + th * (b1 - b0))
-             - dz / (iw * dt2 * C_D_P * rho_io) * (2.0 / vg.area_v[wi] + dt * wo * 0.5 * (-1.0 / vg.volume[b] + 1.0 / vg.volume[lo]));
-        rv = -(wo + dt * st.w[wi]) * dz / (iw * dt2 * C_D_P) + th * (ww.ep_expl[b] - ww.ep_expl[lo]) / dt
-             + 0.5 / dt * (ww.tp_expl[b] + ww.tp_expl[lo]) * dpi - dz / (iw * dt2 * C_D_P) * wo * rho_ie / rho_io;
-    } else {
-        const double k1 = dz * p.k_rows, irio = 1.0 / rho_io, idt = p.inv_dt;
-        dv = -(th * th) * (g0 + g1) + 0.5 * dpi * (a1 - a0 + th * (b1 - b0))
-             - k1 * irio * (2.0 * ww.inv_area_v[wi] + dt * wo * 0.5 * (ww.inv_vol[lo] - ww.inv_vol[b]));
-        rv = -(wo + dt * st.w[wi]) * k1 + th * (ww.ep_expl[b] - ww.ep_expl[lo]) * idt
-             + 0.5 * idt * (ww.tp_expl[b] + ww.tp_expl[lo]) * dpi - k1 * wo * rho_ie * irio;
-    }
-    ww.d[q] = dv;
-    ww.r[q] = rv;
+    ww.d[q] = -(th * th) * (g0 + g1) + 0.5 * dpi * (a1 - a0 + th * (b1 - b0))
+              - dz / (iw * dt2 * C_D_P * rho_io) * (2.0 / vg.area_v[wi] + dt * wo * 0.5 * (-1.0 / vg.volume[b] + 1.0 / vg.volume[lo]));
+    ww.r[q] = -(wo + dt * st.w[wi]) * dz / (iw * dt2 * C_D_P) + th * (ww.ep_expl[b] - ww.ep_expl[lo]) / dt
+              + 0.5 / dt * (ww.tp_expl[b] + ww.tp_expl[lo]) * dpi - dz / (iw * dt2 * C_D_P) * wo * rho_ie / rho_io;
     ww.th_int[q] = th;
     ww.rho_io[q] = rho_io;
     if (j < nl - 2) {
         const long long lo2 = lo + nc;
         const double th1 = 0.5 * (ww.thl[lo] + ww.thl[lo2]);
         const double rho_io1 = 0.5 * (so.rho[gp + lo] + so.rho[gp + lo2]);
-        double cv, ev;
-        if (EXACT) {
-            cv = th1 * g1 * th + 0.5 * (vg.exner_bg[lo] - vg.exner_bg[lo2]) * (a1 + b1 * th)
-                 - (vg.z_scalar[lo] - vg.z_scalar[lo2]) / (iw * dt * C_D_P) * 0.5 * so.w[wi + nc] / (vg.volume[lo] * rho_io1);
-            ev = th * g1 * th1 - 0.5 * dpi * (a1 + b1 * th1)
-                 + dz / (iw * dt * C_D_P) * 0.5 * wo / (vg.volume[lo] * rho_io);
-        } else {
-            const double k2 = p.k_rows2 * ww.inv_vol[lo];
-            cv = th1 * g1 * th + 0.5 * (vg.exner_bg[lo] - vg.exner_bg[lo2]) * (a1 + b1 * th)
-                 - (vg.z_scalar[lo] - vg.z_scalar[lo2]) * k2 * so.w[wi + nc] / rho_io1;
-            ev = th * g1 * th1 - 0.5 * dpi * (a1 + b1 * th1) + dz * k2 * wo / rho_io;
-        }
-        ww.c[q] = cv;
-        ww.e[q] = ev;
+        ww.c[q] = th1 * g1 * th + 0.5 * (vg.exner_bg[lo] - vg.exner_bg[lo2]) * (a1 + b1 * th)
+                  - (vg.z_scalar[lo] - vg.z_scalar[lo2]) / (iw * dt * C_D_P) * 0.5 * so.w[wi + nc] / (vg.volume[lo] * rho_io1);
+        ww.e[q] = th * g1 * th1 - 0.5 * dpi * (a1 + b1 * th1)
+                  + dz / (iw * dt * C_D_P) * 0.5 * wo / (vg.volume[lo] * rho_io);
     }
     /* Klemp (2008) damping denominator of the solution at interface j + 1 */
     ww.dden[q] = 1.0 + dt * ww.damp_dc[q];
-    (void)i;
+}
+
+/* Mixed path: the rows of column_solvers.c:142-189 rearranged so that every
+ * inner interface needs one reciprocal.  Thread (interface j, column) forms
+ * d_j, r_j, the super-diagonal e_j of row j and the sub-diagonal c_{j-1} of
+ * row j-1: c_{j-1} depends on the quantities of interface j (theta_v, rho,
+ * w, heights) and on layer j, so the thread of interface j owns it.  Grid
+ * terms come from the geo tables; 1/rho at the interface is kept in rho_io
+ * for k_waves_apply. */
+__global__ void k_waves_rows_mixed(VGrid vg, StepParams p, DState so, DState st, WavesWork ww)
+{
+    const int nc = vg.nc, nl = vg.nl;
+    const long long n = (long long)(nl - 1) * nc, q = gtid();
+    if (q >= n) return;
+    const int j = (int)(q / nc);
+    const long long ns = (long long)nl * nc, gp = p.n_cond * ns;
+    const long long b = q, lo = q + nc, wi = q + nc;
+    const double dt = p.dt;
+    const double *geo = ww.geo;
+    const double dz = geo[q], H = geo[n + q], G1 = geo[2 * n + q], G2 = geo[3 * n + q];
+    const double rho_io = 0.5 * (so.rho[gp + b] + so.rho[gp + lo]);
+    const double irio = rcp_nr<1>(rho_io);
+    const double rho_ie = 0.5 * (ww.rho_expl[b] + ww.rho_expl[lo]);
+    const double tl_b = ww.thl[b], tl_lo = ww.thl[lo];
+    const double th = 0.5 * (tl_b + tl_lo);
+    const double wo = so.w[wi];
+    const double a0 = ww.alpha[b], a1 = ww.alpha[lo], b0 = ww.beta[b], b1 = ww.beta[lo];
+    const double g0 = ww.gam[b], g1 = ww.gam[lo];
+    const double k1 = dz * p.k_rows;
+    ww.d[q] = -(th * th) * (g0 + g1) + H * (a1 - a0 + th * (b1 - b0)) - k1 * irio * (G1 + dt * wo * G2);
+    ww.r[q] = -(wo + dt * st.w[wi]) * k1 + th * (ww.ep_expl[b] - ww.ep_expl[lo]) * p.inv_dt
+              + p.inv_dt * (ww.tp_expl[b] + ww.tp_expl[lo]) * H - k1 * wo * rho_ie * irio;
+    ww.th_int[q] = th;
+    ww.rho_io[q] = irio;
+    const double sw = p.k_rows2 * wo * irio;
+    if (j < nl - 2) {
+        const double th_next = 0.5 * (tl_lo + ww.thl[lo + nc]);
+        ww.e[q] = th * g1 * th_next - H * (a1 + b1 * th_next) + geo[5 * n + q] * sw;
+    }
+    if (j > 0) {
+        const double th_prev = 0.5 * (ww.thl[b - nc] + tl_b);
+        ww.c[q - nc] = th * g0 * th_prev + H * (a0 + b0 * th_prev) - geo[4 * n + q] * sw;
+    }
 }
 
 /* tridiagonal elimination of one column (column_solvers.c:641-669), forward
@@ -187,7 +227,7 @@ __global__ void k_waves_thomas(int nc, WavesWork ww)
                 ep[0] = ww.e[q] / dj;
                 rp[0] = rj / dj;
             } else {
-                const double inv = 1.0 / dj;
+                const double inv = rcp_nr<2>(dj);
                 ep[0] = ww.e[q] * inv;
                 rp[0] = rj * inv;
             }
@@ -198,18 +238,21 @@ __global__ void k_waves_thomas(int nc, WavesWork ww)
                 if (j < n - 1) ep[j] = ww.e[q] / den;
                 rp[j] = (rj - rp[j - 1] * cm) / den;
             } else {
-                const double inv = 1.0 / den;
+                const double inv = rcp_nr<2>(den);
                 if (j < n - 1) ep[j] = ww.e[q] * inv;
                 rp[j] = (rj - rp[j - 1] * cm) * inv;
             }
         }
     }
+    /* damping: divide by 1 + dt * coefficient (mixed path: multiply by the
+     * tabulated reciprocal) */
+    auto damp = [&](double x, long long q) { return EXACT ? x / ww.dden[q] : x * ww.damp_inv[q]; };
     double x = rp[n - 1];
-    ww.r[(long long)(n - 1) * nc + i] = x / ww.dden[(long long)(n - 1) * nc + i];
+    ww.r[(long long)(n - 1) * nc + i] = damp(x, (long long)(n - 1) * nc + i);
 #pragma unroll
     for (int j = n - 2; j >= 0; --j) {
         x = rp[j] - ep[j] * x;
-        ww.r[(long long)j * nc + i] = x / ww.dden[(long long)j * nc + i];
+        ww.r[(long long)j * nc + i] = damp(x, (long long)j * nc + i);
     }
 }
 
@@ -234,11 +277,12 @@ __global__ void k_waves_thomas_any(int nc, int nl, WavesWork ww)
             rp[j] = (rj - rp[j - 1] * cm) / den;
         }
     }
+    auto damp = [&](double x, long long q) { return EXACT ? x / ww.dden[q] : x * ww.damp_inv[q]; };
     double x = rp[n - 1];
-    ww.r[(long long)(n - 1) * nc + i] = x / ww.dden[(long long)(n - 1) * nc + i];
+    ww.r[(long long)(n - 1) * nc + i] = damp(x, (long long)(n - 1) * nc + i);
     for (int j = n - 2; j >= 0; --j) {
         x = rp[j] - ep[j] * x;
-        ww.r[(long long)j * nc + i] = x / ww.dden[(long long)j * nc + i];
+        ww.r[(long long)j * nc + i] = damp(x, (long long)j * nc + i);
     }
 }
 
@@ -267,7 +311,7 @@ __global__ void k_waves_apply(VGrid vg, StepParams p, DState so, DState sn, Wave
     else if (j == nl - 1) num = -ww.th_int[b - nc] * sol[b - nc];
     else num = -ww.th_int[b - nc] * sol[b - nc] + ww.th_int[b] * sol[b];
     const double rt_new = EXACT ? ww.rt_expl[b] + dt * num / vg.volume[b] : ww.rt_expl[b] + dt * num * ww.inv_vol[b];
-    const double tp_new = rt_new / r_new - vg.theta_v_bg[b];
+    const double tp_new = (EXACT ? rt_new / r_new : rt_new * rcp_nr<1>(r_new)) - vg.theta_v_bg[b];
     const double ep_new = so.exner_pert[b] + vg.volume[b] * ww.gam[b] * (rt_new - so.rhotheta_v[b]);
     sn.rho[gp + b] = r_new;
     sn.rhotheta_v[b] = rt_new;
@@ -286,8 +330,8 @@ __global__ void k_waves_apply(VGrid vg, StepParams p, DState so, DState sn, Wave
         double wn;
         if (EXACT)
             wn = (2.0 * sol[b] / vg.area_v[wi] - dint * so.w[wi]) / ww.rho_io[b];
-        else
-            wn = (2.0 * sol[b] * ww.inv_area_v[wi] - dint * so.w[wi]) / ww.rho_io[b];
+        else /* rho_io holds 1 / rho at the interface on the mixed path */
+            wn = (2.0 * sol[b] * ww.inv_area_v[wi] - dint * so.w[wi]) * ww.rho_io[b];
         sn.w[wi] = wn;
         if (sh.w) sh.w[wi] = float(wn);
     }
@@ -324,7 +368,7 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
     const int k = slot < p.n_cond ? slot : slot + 1; /* skip the main gas */
     bool has_sink;
     const double vsink = sink_velocity(p, k, has_sink);
-    const double dt = p.dt, iw = 0.5, ew = 1.0 - iw;
+    const double dt = p.dt, iw = 0.5, ew = 1.0 - iw, half_dt = 0.5 * dt;
     const double *ro = so.rho + k * ns;
     const double *tr = st.rho + k * ns;
     const long long bot = i + ns - nc;
@@ -334,8 +378,10 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
 #pragma unroll
     for (int j = 0; j < NL; ++j) {
         const long long b = i + (long long)j * nc;
-        const double vol = vg.volume[b];
-        const double ivol = EXACT ? 0.0 : tw.inv_vol[b];
+        const double vol = EXACT ? vg.volume[b] : 0.0;
+        /* mixed path: implicit and explicit weights are both 1/2, so every
+         * flux term of row j carries the factor g = dt / (2 V_j) */
+        const double g = EXACT ? 0.0 : half_dt * tw.inv_vol[b];
         /* flux at interface j (below layer j) */
         double fi = 0.0, fr = 0.0, cj = 0.0, ej = 0.0;
         if (j < NL - 1) {
@@ -354,11 +400,12 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
             if (EXACT) {
                 if (fi >= 0.0) ej = -iw * dt / vol * fi;
                 else cj = iw * dt / vg.volume[b + nc] * fi;
-            } else {
-                if (fi >= 0.0) ej = -iw * dt * ivol * fi;
-                else cj = iw * dt * tw.inv_vol[b + nc] * fi;
+            } else if (fi >= 0.0) {
+                ej = -g * fi;
             }
         }
+        if (!EXACT) /* sub-diagonal of row j - 1, formed with row j's factor */
+            c_prev = fi_prev < 0.0 ? g * fi_prev : 0.0;
         double dj, rj = ro[b] + dt * tr[b];
         if (EXACT) {
             if (j == 0) {
@@ -377,18 +424,19 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
             }
         } else {
             if (j == 0) {
-                dj = fi >= 0.0 ? 1.0 : 1.0 - iw * dt * ivol * fi;
-                rj += ew * dt * fr * ivol;
+                dj = fi >= 0.0 ? 1.0 : 1.0 - g * fi;
+                rj += g * fr;
             } else if (j == NL - 1) {
-                dj = fi_prev >= 0.0 ? 1.0 + iw * dt * ivol * fi_prev : 1.0;
-                if (has_sink) dj += iw * vsink * dt * a_sfc * ivol;
-                rj += -ew * dt * fr_prev * ivol;
-                if (has_sink) rj += -ew * vsink * dt * ro[bot] * a_sfc * ivol;
+                dj = fi_prev >= 0.0 ? 1.0 + g * fi_prev : 1.0;
+                rj -= g * fr_prev;
+                if (has_sink) {
+                    const double gs = g * vsink * a_sfc;
+                    dj += gs;
+                    rj -= gs * ro[bot];
+                }
             } else {
-                dj = 1.0;
-                if (fi_prev >= 0.0) dj += iw * dt * ivol * fi_prev;
-                if (fi < 0.0) dj -= iw * dt * ivol * fi;
-                rj += ew * dt * (-fr_prev + fr) * ivol;
+                dj = 1.0 + (fi_prev >= 0.0 ? g * fi_prev : 0.0) - (fi < 0.0 ? g * fi : 0.0);
+                rj += g * (fr - fr_prev);
             }
         }
         /* forward elimination */
@@ -397,7 +445,7 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
                 ep[0] = ej / dj;
                 rp[0] = rj / dj;
             } else {
-                const double inv = 1.0 / dj;
+                const double inv = rcp_nr<2>(dj);
                 ep[0] = ej * inv;
                 rp[0] = rj * inv;
             }
@@ -407,14 +455,14 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
                 if (j < NL - 1) ep[j] = ej / den;
                 rp[j] = (rj - rp[j - 1] * c_prev) / den;
             } else {
-                const double inv = 1.0 / den;
+                const double inv = rcp_nr<2>(den);
                 if (j < NL - 1) ep[j] = ej * inv;
                 rp[j] = (rj - rp[j - 1] * c_prev) * inv;
             }
         }
         fi_prev = fi;
         fr_prev = fr;
-        c_prev = cj;
+        if (EXACT) c_prev = cj;
     }
     double *rn = sn.rho + k * ns;
     float *rs = sh_rho ? sh_rho + k * ns : nullptr;

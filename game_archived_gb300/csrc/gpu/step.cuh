@@ -44,6 +44,8 @@ inline WavesWork waves_work(Context *c)
     w.inv_vol = c->inv_vol;
     w.inv_area_v = c->inv_area_v;
     w.damp_dc = c->damp_dc;
+    w.damp_inv = c->damp_inv;
+    w.geo = c->wv_geo;
     return w;
 }
 
@@ -112,8 +114,11 @@ void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirr
     }
     {
         ProfScope ps(c, "k_waves_rows");
-        k_waves_rows<EXACT><<<nblocks((long long)(c->nl - 1) * c->nc, 256), 256, 0, c->stream>>>(c->vg, p, so->ds,
-                                                                                                 st->ds, ww);
+        const unsigned nb = nblocks((long long)(c->nl - 1) * c->nc, 256);
+        if (EXACT)
+            k_waves_rows<<<nb, 256, 0, c->stream>>>(c->vg, p, so->ds, st->ds, ww);
+        else
+            k_waves_rows_mixed<<<nb, 256, 0, c->stream>>>(c->vg, p, so->ds, st->ds, ww);
     }
     {
         ProfScope ps(c, "k_waves_thomas");
