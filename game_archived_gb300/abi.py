@@ -35,6 +35,12 @@ SIGNATURES = {
     "game_gpu_transfer_bytes": ([ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), cint], cint),
     "manage_rkhevi": ([vp] * 9 + [dbl, dbl], cint),
     "linear_combine_two_states": ([vp, vp, vp, dbl, dbl, vp], cint),
+    "manage_pressure_gradient": ([vp] * 7, cint),
+    "calc_pressure_grad_condensates_v": ([vp] * 4, cint),
+    "vector_tendencies_expl": ([vp] * 8 + [cint, dbl], cint),
+    "scalar_tendencies_expl": ([vp] * 5 + [dbl] + [vp] * 4 + [cint], cint),
+    "three_band_solver_ver_waves": ([vp] * 6 + [dbl, vp, cint], cint),
+    "three_band_solver_gen_densities": ([vp] * 6 + [dbl, cint, vp], cint),
     "grad_hor_cov": ([vp] * 3, cint),
     "grad_vert_cov": ([vp] * 3, cint),
     "vector_field_hor_cov_to_con": ([vp] * 2, cint),
@@ -109,6 +115,42 @@ class GpuModel:
     def linear_combine_two_states(self, s0, s1, out, c0, c1):
         self._check(self.lib.linear_combine_two_states(s0.ptr, s1.ptr, out.ptr, c0, c1, self.m.grid.ptr),
                     "linear_combine_two_states")
+
+    # -- the sub-steps of manage_rkhevi (reference argument order)
+    def manage_pressure_gradient(self, state):
+        m = self.m
+        self._check(self.lib.manage_pressure_gradient(state.ptr, m.grid.ptr, m.dualgrid.ptr, m.diagnostics.ptr,
+                                                      m.forcings.ptr, m.irrev.ptr, m.config.ptr),
+                    "manage_pressure_gradient")
+
+    def calc_pressure_grad_condensates_v(self, state):
+        m = self.m
+        self._check(self.lib.calc_pressure_grad_condensates_v(state.ptr, m.grid.ptr, m.forcings.ptr, m.irrev.ptr),
+                    "calc_pressure_grad_condensates_v")
+
+    def vector_tendencies_expl(self, state, tend, rk, dt):
+        m = self.m
+        self._check(self.lib.vector_tendencies_expl(state.ptr, tend.ptr, m.grid.ptr, m.dualgrid.ptr, m.diagnostics.ptr,
+                                                    m.forcings.ptr, m.irrev.ptr, m.config.ptr, rk, dt),
+                    "vector_tendencies_expl")
+
+    def scalar_tendencies_expl(self, s_old, s_new, tend, dt, rk):
+        m = self.m
+        self._check(self.lib.scalar_tendencies_expl(s_old.ptr, s_new.ptr, tend.ptr, m.grid.ptr, m.dualgrid.ptr, dt,
+                                                    m.diagnostics.ptr, m.forcings.ptr, m.irrev.ptr, m.config.ptr, rk),
+                    "scalar_tendencies_expl")
+
+    def three_band_solver_ver_waves(self, s_old, s_new, tend, dt, rk):
+        m = self.m
+        self._check(self.lib.three_band_solver_ver_waves(s_old.ptr, s_new.ptr, tend.ptr, m.diagnostics.ptr,
+                                                         m.forcings.ptr, m.config.ptr, dt, m.grid.ptr, rk),
+                    "three_band_solver_ver_waves")
+
+    def three_band_solver_gen_densities(self, s_old, s_new, tend, dt, rk):
+        m = self.m
+        self._check(self.lib.three_band_solver_gen_densities(s_old.ptr, s_new.ptr, tend.ptr, m.diagnostics.ptr,
+                                                             m.irrev.ptr, m.config.ptr, dt, rk, m.grid.ptr),
+                    "three_band_solver_gen_densities")
 
     def sync_to_device(self, s):
         self._check(self.lib.game_gpu_sync_to_device(s.ptr), "sync_to_device")

@@ -10,6 +10,7 @@
 #include "diag.h"
 #include "game_gb300.h"
 #include "ops.h"
+#include "substeps.h"
 
 using namespace game;
 
@@ -688,6 +689,204 @@ int game_gpu_surface_pressure(struct state *state, double *surface_p, double *ms
     /* same stream: the second scatter into the staging buffer runs after the
      * first copy out of it */
     if (mslp && download_field(mslp, pm, c->map_s, c->nc, c->nc, 0, c->nc)) return -1;
+    return finish();
+}
+
+/* -------------------------------------------------------- the sub-steps
+ * Host-in/host-out in every residency mode, on private device buffers: they
+ * never read or write the device mirrors or the lagged fields of the
+ * device-resident step.  FP64 path, reference operation order.  Scratch
+ * members of Diagnostics that the reference overwrites as work space
+ * (scalar_field_placeholder, flux_density_divv, and flux_density inside
+ * scalar_tendencies_expl) are not written. */
+static double *vec_of(void *base, int sid, const char *name) { return member<double>(base, sid, name); }
+
+static int up_vec(void *base, int sid, const char *name, double *dev)
+{
+    Context *c = ctx();
+    return upload_field(vec_of(base, sid, name), dev, c->map_vec, c->nv, c->nv);
+}
+static int down_vec(void *base, int sid, const char *name, const double *dev)
+{
+    Context *c = ctx();
+    return download_field(vec_of(base, sid, name), dev, c->map_vec, c->nv, c->nv, 0, c->nv);
+}
+static int up_scal(void *base, int sid, const char *name, double *dev, int n_fields = 1)
+{
+    Context *c = ctx();
+    for (int k = 0; k < n_fields; ++k)
+        if (upload_field(vec_of(base, sid, name) + (long long)k * c->ns, dev + (long long)k * c->ns, c->map_s, c->ns,
+                         c->ns))
+            return -1;
+    return 0;
+}
+static int down_scal(void *base, int sid, const char *name, const double *dev)
+{
+    Context *c = ctx();
+    return download_field(vec_of(base, sid, name), dev, c->map_s, c->ns, c->ns, 0, c->ns);
+}
+
+int manage_pressure_gradient(struct state *state, struct grid *grid, struct dualgrid *dualgrid,
+                             struct diagnostics *diagnostics, struct forcings *forcings,
+                             struct irreversible_quantities *irrev, struct config *config)
+{
+    (void)dualgrid;
+    (void)diagnostics;
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    double *nl = b.vec[0], *l = b.vec[1], *old = b.vec[2];
+    if (upload_state(state, &b.sn)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_nl", nl)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_l", l)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "pgrad_acc_old", old)) return -1;
+    StepParams p = params_from_config(c, config, 1.0);
+    sub_pressure_gradient(c, p, &b.sn, nl, l, old, b.decel);
+    if (down_vec(forcings, GAME_FORCINGS, "pgrad_acc_old", old)) return -1;
+    if (down_vec(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_nl", nl)) return -1;
+    if (down_vec(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_l", l)) return -1;
+    if (down_scal(irrev, GAME_IRREV, "pressure_gradient_decel_factor", b.decel)) return -1;
+    return finish();
+}
+
+int calc_pressure_grad_condensates_v(struct state *state, struct grid *grid, struct forcings *forcings,
+                                     struct irreversible_quantities *irrev)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    if (upload_state(state, &b.sn)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "pressure_grad_condensates_v", b.vec[0])) return -1;
+    sub_condensates_v(c, &b.sn, b.decel, b.vec[0]);
+    if (down_vec(forcings, GAME_FORCINGS, "pressure_grad_condensates_v", b.vec[0])) return -1;
+    if (down_scal(irrev, GAME_IRREV, "pressure_gradient_decel_factor", b.decel)) return -1;
+    return finish();
+}
+
+int vector_tendencies_expl(struct state *state, struct state *state_tendency, struct grid *grid,
+                           struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,
+                           struct irreversible_quantities *irrev, struct config *config, int rk_step, double delta_t)
+{
+    (void)dualgrid;
+    if (check_ready(grid)) return -1;
+    if (check_config(config)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    const long long ns = c->ns, ncurl = c->ncurl, ntri = (long long)c->nl * c->nt;
+    double *pg_old = b.vec[0], *nl = b.vec[1], *l = b.vec[2], *cond_v = b.vec[3], *fric = b.vec[4];
+    double *flux = b.vec[5], *pvt = b.vec[6], *v2g = b.vec[7], *rel = b.vec[8], *pv = b.vec[9];
+    if (upload_state(state, &b.sn)) return -1;
+    if (upload_state(state_tendency, &b.st)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "pgrad_acc_old", pg_old)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_nl", nl)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_l", l)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "pressure_grad_condensates_v", cond_v)) return -1;
+    if (up_vec(irrev, GAME_IRREV, "friction_acc", fric)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "pot_vort_tend", pvt)) return -1;
+    if (up_vec(forcings, GAME_FORCINGS, "v_squared_grad", v2g)) return -1;
+    const int first = *member<int>(config, GAME_CONFIG, "totally_first_step_bool");
+    if (rk_step == 1 || first == 1) {
+        /* vector_tendencies_expl.c:24-35; entries the reference's operators
+         * leave alone keep the caller's values */
+        double *wind = b.sn.ds.w, *rho_gas = b.sn.ds.rho + (long long)c->n_cond * ns;
+        if (up_vec(diagnostics, GAME_DIAGNOSTICS, "flux_density", flux)) return -1;
+        op_scalar_times_vector(c, rho_gas, wind, flux, OP_STV_H | OP_STV_V);
+        op_rel_vort(c, wind, b.tri, rel);
+        op_pot_vort(c, rel, rho_gas, pv);
+        op_vorticity_flux(c, flux, pv, pvt);
+        op_inner_product(c, wind, wind, b.v2);
+        op_grad(c, b.v2, v2g, OP_GRAD_H | OP_GRAD_V | OP_GRAD_CON);
+        if (down_vec(diagnostics, GAME_DIAGNOSTICS, "flux_density", flux)) return -1;
+        if (download_field(vec_of(diagnostics, GAME_DIAGNOSTICS, "rel_vort_on_triangles"), b.tri, c->map_tri, ntri,
+                           ntri, 0, ntri))
+            return -1;
+        if (download_field(vec_of(diagnostics, GAME_DIAGNOSTICS, "rel_vort"), rel, c->map_curl, ncurl, ncurl, 0,
+                           ncurl))
+            return -1;
+        if (download_field(vec_of(diagnostics, GAME_DIAGNOSTICS, "pot_vort"), pv, c->map_curl, ncurl, ncurl, 0, ncurl))
+            return -1;
+        if (down_scal(diagnostics, GAME_DIAGNOSTICS, "v_squared", b.v2)) return -1;
+        if (down_vec(forcings, GAME_FORCINGS, "pot_vort_tend", pvt)) return -1;
+        if (down_vec(forcings, GAME_FORCINGS, "v_squared_grad", v2g)) return -1;
+    }
+    StepParams p = params_from_config(c, config, delta_t);
+    sub_vector_tendency(c, p, rk_step, b.st.ds.w, pg_old, nl, l, pvt, v2g, fric, cond_v);
+    if (download_state(state_tendency, &b.st, 16)) return -1;
+    return finish();
+}
+
+int scalar_tendencies_expl(struct state *state_old, struct state *state, struct state *state_tendency,
+                           struct grid *grid, struct dualgrid *dualgrid, double delta_t,
+                           struct diagnostics *diagnostics, struct forcings *forcings,
+                           struct irreversible_quantities *irrev, struct config *config, int rk_step)
+{
+    (void)state_old;
+    (void)dualgrid;
+    (void)forcings;
+    if (check_ready(grid)) return -1;
+    if (check_config(config)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    if (upload_state(state, &b.sn)) return -1;
+    if (upload_state(state_tendency, &b.st)) return -1;
+    if (c->moist) {
+        if (up_scal(diagnostics, GAME_DIAGNOSTICS, "temperature", b.temperature)) return -1;
+        sub_cp_tables(c, b.temperature, b.cp_ice, b.cp_water);
+        if (up_scal(irrev, GAME_IRREV, "phase_trans_rates", b.pt_rates, c->n_cond + 1)) return -1;
+        if (up_scal(irrev, GAME_IRREV, "phase_trans_heating_rate", b.pt_heat)) return -1;
+        if (up_scal(irrev, GAME_IRREV, "condensates_sediment_heat", b.sed_heat)) return -1;
+    }
+    StepParams p = params_from_config(c, config, delta_t);
+    sub_scalar_tendencies(c, p, &b.sn, &b.st, rk_step, b.theta, b.cp_ice, b.cp_water, b.pt_rates, b.pt_heat,
+                          b.sed_heat);
+    if (download_state(state_tendency, &b.st, 1 | 2)) return -1;
+    return finish();
+}
+
+int three_band_solver_ver_waves(struct state *state_old, struct state *state_new, struct state *state_tendency,
+                                struct diagnostics *diagnostics, struct forcings *forcings, struct config *config,
+                                double delta_t, struct grid *grid, int rk_step)
+{
+    (void)diagnostics;
+    (void)forcings;
+    if (check_ready(grid)) return -1;
+    if (check_config(config)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    if (upload_state(state_old, &b.so)) return -1;
+    if (upload_state(state_new, &b.sn)) return -1;
+    if (upload_state(state_tendency, &b.st)) return -1;
+    StepParams p = params_from_config(c, config, delta_t);
+    if (sub_ver_waves(c, p, &b.so, &b.sn, &b.st, rk_step)) return -1;
+    if (download_state(state_new, &b.sn, 1 | 2 | 4 | 8 | 16)) return -1;
+    return finish();
+}
+
+int three_band_solver_gen_densities(struct state *state_old, struct state *state_new, struct state *state_tendency,
+                                    struct diagnostics *diagnostics, struct irreversible_quantities *irrev,
+                                    struct config *config, double delta_t, int rk_step, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    if (check_config(config)) return -1;
+    Context *c = ctx();
+    if (c->n_const <= 1) return finish();
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    if (upload_state(state_old, &b.so)) return -1;
+    if (upload_state(state_new, &b.sn)) return -1;
+    if (upload_state(state_tendency, &b.st)) return -1;
+    if (up_scal(diagnostics, GAME_DIAGNOSTICS, "temperature", b.temperature)) return -1;
+    sub_cp_tables(c, b.temperature, b.cp_ice, b.cp_water);
+    if (up_scal(irrev, GAME_IRREV, "condensates_sediment_heat", b.sed_heat)) return -1;
+    StepParams p = params_from_config(c, config, delta_t);
+    sub_gen_densities(c, p, &b.so, &b.sn, &b.st, rk_step, b.temperature, b.cp_ice, b.cp_water, b.sed_heat);
+    if (download_state(state_new, &b.sn, 1)) return -1;
+    if (rk_step == 0 && down_scal(irrev, GAME_IRREV, "condensates_sediment_heat", b.sed_heat)) return -1;
     return finish();
 }
 

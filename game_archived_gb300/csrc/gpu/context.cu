@@ -540,6 +540,18 @@ int destroy_context()
 }
 
 /* --------------------------------------------------------- state mirrors */
+/* device layout pointers of a state block */
+static void set_mirror_views(Context *c, StateMirror &m)
+{
+    const long long ns = c->ns;
+    m.ds.rho = m.dev;
+    m.ds.rhotheta_v = m.dev + c->n_const * ns;
+    m.ds.theta_v_pert = m.ds.rhotheta_v + ns;
+    m.ds.exner_pert = m.ds.theta_v_pert + ns;
+    m.ds.w = m.ds.exner_pert + ns;
+    m.ds.u = m.ds.w + (long long)(c->nl + 1) * c->nc;
+}
+
 StateMirror *mirror(const void *host_state, int create)
 {
     Context *c = g_ctx;
@@ -552,15 +564,30 @@ StateMirror *mirror(const void *host_state, int create)
         return nullptr;
     }
     cudaMemset(m.dev, 0, (size_t)c->state_len * sizeof(double));
-    const long long ns = c->ns;
-    m.ds.rho = m.dev;
-    m.ds.rhotheta_v = m.dev + c->n_const * ns;
-    m.ds.theta_v_pert = m.ds.rhotheta_v + ns;
-    m.ds.exner_pert = m.ds.theta_v_pert + ns;
-    m.ds.w = m.ds.exner_pert + ns;
-    m.ds.u = m.ds.w + (long long)(c->nl + 1) * c->nc;
+    set_mirror_views(c, m);
     c->states[host_state] = m;
     return &c->states[host_state];
+}
+
+int ensure_sub_buffers(Context *c)
+{
+    Context::SubBuffers &b = c->sub;
+    if (b.ready) return 0;
+    const size_t NS = (size_t)c->ns, nvec = (size_t)std::max<long long>(c->nv, c->ncurl);
+    for (StateMirror *m : {&b.so, &b.sn, &b.st}) {
+        m->dev = dalloc<double>(c, (size_t)c->state_len);
+        if (!m->dev) return fail("device allocation of the sub-step buffers failed");
+        set_mirror_views(c, *m);
+    }
+    for (auto &v : b.vec)
+        if (!(v = dalloc<double>(c, nvec))) return fail("device allocation of the sub-step buffers failed");
+    double **scal[] = {&b.temperature, &b.cp_ice, &b.cp_water, &b.theta, &b.pt_heat, &b.sed_heat, &b.decel, &b.v2};
+    for (double **p : scal)
+        if (!(*p = dalloc<double>(c, NS))) return fail("device allocation of the sub-step buffers failed");
+    if (!(b.pt_rates = dalloc<double>(c, 5 * NS))) return fail("device allocation of the sub-step buffers failed");
+    if (!(b.tri = dalloc<double>(c, (size_t)c->nl * c->nt))) return fail("device allocation of the sub-step buffers failed");
+    b.ready = true;
+    return 0;
 }
 
 /* the State members rho .. wind are contiguous in the reference struct:

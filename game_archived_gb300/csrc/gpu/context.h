@@ -104,6 +104,18 @@ struct Context {
 
     std::map<const void *, StateMirror> states;
 
+    /* private buffers of the sub-step entry points (three_band_solver_*,
+     * *_tendencies_expl, ...), allocated on their first call; never the
+     * mirrors or the lagged fields of the device-resident step */
+    struct SubBuffers {
+        bool ready = false;
+        StateMirror so, sn, st;
+        double *vec[10] = {}; /* each max(Vt, curl field) */
+        double *temperature = nullptr, *cp_ice = nullptr, *cp_water = nullptr, *theta = nullptr;
+        double *pt_rates = nullptr; /* 5 S */
+        double *pt_heat = nullptr, *sed_heat = nullptr, *decel = nullptr, *v2 = nullptr, *tri = nullptr;
+    } sub;
+
     /* CUDA graphs of the device-side step, keyed by every value the launches
      * capture: the step parameters (time step, config values, first-step
      * flag), the precision and the three state mirrors */
@@ -174,6 +186,7 @@ int fail(const std::string &msg);
 int init_context(int res_id, int n_layers, int moisture_on, const void *grid, const void *dualgrid);
 int destroy_context();
 StateMirror *mirror(const void *host_state, int create);
+int ensure_sub_buffers(Context *c);
 int upload_state(const void *host_state, StateMirror *m);
 int download_state(const void *host_state, StateMirror *m, int which_mask);
 int upload_field(const double *host, double *dev, const int *map, long long n, long long host_len);

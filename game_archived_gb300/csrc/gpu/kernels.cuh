@@ -700,40 +700,57 @@ __device__ __forceinline__ R density_total_r(const R *rho, int n_const, long lon
 /* decelerated pressure-gradient sum nl + l at edge e, layer l
  * (manage_pressure_gradient.c:17-72) */
 template <typename R>
-__device__ __forceinline__ R pgrad_h(const HGrid<R> &g, const StepParams &p, const SView<R> &s, int l, int e)
+__device__ __forceinline__ void pgrad_h_parts(const HGrid<R> &g, const StepParams &p, const SView<R> &s, int l, int e,
+                                              R &nl, R &l_term)
 {
     const long long ns = (long long)g.nl * g.nc;
     const int fr = g.from[e], to = g.to[e];
     const long long cf = (long long)l * g.nc + fr, ct = (long long)l * g.nc + to;
     const R cdp = R(C_D_P);
-    R nl = grad_h(g, s.exner_pert, l, e);
+    nl = grad_h(g, s.exner_pert, l, e);
     R s_to = cdp * (g.theta_v_bg[ct] + s.theta_v_pert[ct]), s_fr = cdp * (g.theta_v_bg[cf] + s.theta_v_pert[cf]);
     nl = (R(0.5) * (s_to + s_fr)) * nl;
-    R l_term = (R(0.5) * (cdp * s.theta_v_pert[ct] + cdp * s.theta_v_pert[cf])) * g.exner_bg_grad_h[(long long)l * g.ne + e];
+    l_term = (R(0.5) * (cdp * s.theta_v_pert[ct] + cdp * s.theta_v_pert[cf])) * g.exner_bg_grad_h[(long long)l * g.ne + e];
     R d_to = s.rho[p.n_cond * ns + ct] / density_total_r(s.rho, p.n_const, ns, ct);
     R d_fr = s.rho[p.n_cond * ns + cf] / density_total_r(s.rho, p.n_const, ns, cf);
     R dec = R(0.5) * (d_to + d_fr);
     nl = dec * nl;
     l_term = dec * l_term;
+}
+
+/* the sum nl + l, the only form the step reads */
+template <typename R>
+__device__ __forceinline__ R pgrad_h(const HGrid<R> &g, const StepParams &p, const SView<R> &s, int l, int e)
+{
+    R nl, l_term;
+    pgrad_h_parts(g, p, s, l, e, nl, l_term);
     return nl + l_term;
 }
 
 /* the same at the inner interface k of cell c */
 template <typename R>
-__device__ __forceinline__ R pgrad_v(const HGrid<R> &g, const StepParams &p, const SView<R> &s, int k, int c)
+__device__ __forceinline__ void pgrad_v_parts(const HGrid<R> &g, const StepParams &p, const SView<R> &s, int k, int c,
+                                              R &nl, R &l_term)
 {
     const long long ns = (long long)g.nl * g.nc;
     const long long up = (long long)(k - 1) * g.nc + c, lo = (long long)k * g.nc + c;
     const R cdp = R(C_D_P);
-    R nl = grad_v(g, s.exner_pert, k, c);
+    nl = grad_v(g, s.exner_pert, k, c);
     R s_up = cdp * (g.theta_v_bg[up] + s.theta_v_pert[up]), s_lo = cdp * (g.theta_v_bg[lo] + s.theta_v_pert[lo]);
     nl = (R(0.5) * (s_up + s_lo)) * nl;
-    R l_term = (R(0.5) * (cdp * s.theta_v_pert[up] + cdp * s.theta_v_pert[lo])) * g.exner_bg_grad_v[(long long)k * g.nc + c];
+    l_term = (R(0.5) * (cdp * s.theta_v_pert[up] + cdp * s.theta_v_pert[lo])) * g.exner_bg_grad_v[(long long)k * g.nc + c];
     R d_up = s.rho[p.n_cond * ns + up] / density_total_r(s.rho, p.n_const, ns, up);
     R d_lo = s.rho[p.n_cond * ns + lo] / density_total_r(s.rho, p.n_const, ns, lo);
     R dec = R(0.5) * (d_up + d_lo);
     nl = dec * nl;
     l_term = dec * l_term;
+}
+
+template <typename R>
+__device__ __forceinline__ R pgrad_v(const HGrid<R> &g, const StepParams &p, const SView<R> &s, int k, int c)
+{
+    R nl, l_term;
+    pgrad_v_parts(g, p, s, k, c, nl, l_term);
     return nl + l_term;
 }
 

@@ -102,9 +102,10 @@ static void launch_momentum(Context *c, const StepParams &p, const Views<R> &v, 
     c->kernel_launches += 2;
 }
 
+/* implicit vertical sound waves (column_solvers.c:19-383) */
 template <bool EXACT>
-void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st, int rk,
-                     const Shadow &sh)
+void launch_waves(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st, int rk,
+                  const Shadow &sh)
 {
     const long long ns = c->ns;
     WavesWork ww = waves_work(c);
@@ -132,25 +133,43 @@ void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirr
         k_waves_apply<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, ww, sh);
     }
     c->kernel_launches += 4;
-    if (c->n_const > 1) {
-        TracerWork tw{c->cp_ice, c->cp_water, c->inv_vol};
-        if (c->nl == NL_FIXED) {
-            if (rk == 0) {
-                ProfScope ps(c, "k_tracers_sedheat");
-                k_tracers_sedheat<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds,
-                                                                                 c->temperature, tw, c->sed_heat);
-                c->kernel_launches++;
-            }
-            ProfScope ps(c, "k_tracers_solve");
-            k_tracers_solve<NL_FIXED, EXACT><<<nblocks((long long)(c->n_const - 1) * c->nc, 64), 64, 0, c->stream>>>(
-                c->vg, p, so->ds, sn->ds, st->ds, tw, sh.rho);
-        } else {
-            ProfScope ps(c, "k_vertical_tracers");
-            k_vertical_tracers<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds,
-                                                                          c->temperature, c->sed_heat, rk);
+}
+
+/* implicit vertical advection and sedimentation of the non-main constituents
+ * (column_solvers.c:385-639); temperature and its c_p tables as of the start
+ * of the step, sedimentation heat written at rk 0 */
+template <bool EXACT>
+void launch_tracers(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st, int rk,
+                    const Shadow &sh, const double *temperature, const double *cp_ice, const double *cp_water,
+                    double *sed_heat)
+{
+    if (c->n_const <= 1) return;
+    const long long ns = c->ns;
+    TracerWork tw{cp_ice, cp_water, c->inv_vol};
+    if (c->nl == NL_FIXED) {
+        if (rk == 0) {
+            ProfScope ps(c, "k_tracers_sedheat");
+            k_tracers_sedheat<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, temperature,
+                                                                             tw, sed_heat);
+            c->kernel_launches++;
         }
-        c->kernel_launches++;
+        ProfScope ps(c, "k_tracers_solve");
+        k_tracers_solve<NL_FIXED, EXACT><<<nblocks((long long)(c->n_const - 1) * c->nc, 64), 64, 0, c->stream>>>(
+            c->vg, p, so->ds, sn->ds, st->ds, tw, sh.rho);
+    } else {
+        ProfScope ps(c, "k_vertical_tracers");
+        k_vertical_tracers<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, temperature,
+                                                                      sed_heat, rk);
     }
+    c->kernel_launches++;
+}
+
+template <bool EXACT>
+void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st, int rk,
+                     const Shadow &sh)
+{
+    launch_waves<EXACT>(c, p, so, sn, st, rk, sh);
+    launch_tracers<EXACT>(c, p, so, sn, st, rk, sh, c->temperature, c->cp_ice, c->cp_water, c->sed_heat);
 }
 
 /* the kernel sequence of one step; everything on c->stream */

@@ -101,6 +101,39 @@ int manage_rkhevi(struct state *state_old, struct state *state_new, struct grid 
 /* src/spatial_operators/spatial_operators.h:24 -> linear_combine_two_states.c:14 */
 int linear_combine_two_states(struct state *state_0, struct state *state_1, struct state *state_out,
                               double coeff_0, double coeff_1, struct grid *grid);
+
+/* The sub-steps of manage_rkhevi (time_stepping.h:7-12), for drivers that call
+ * them one by one.  FP64, host-in/host-out in every residency mode, on private
+ * device buffers (they never touch the device mirrors of a resident run).
+ * They write the reference's output members; Diagnostics members the
+ * reference uses as scratch (scalar_field_placeholder, flux_density_divv,
+ * and flux_density inside scalar_tendencies_expl) are left alone.  Like
+ * manage_rkhevi they return an error when a diffusion, radiation, PBL, soil
+ * or surface-flux switch is on. */
+/* time_stepping.h:7 -> src/time_stepping/manage_pressure_gradient.c:17 */
+int manage_pressure_gradient(struct state *state, struct grid *grid, struct dualgrid *dualgrid,
+                             struct diagnostics *diagnostics, struct forcings *forcings,
+                             struct irreversible_quantities *irrev, struct config *config);
+/* time_stepping.h:8 -> manage_pressure_gradient.c:74 */
+int calc_pressure_grad_condensates_v(struct state *state, struct grid *grid, struct forcings *forcings,
+                                     struct irreversible_quantities *irrev);
+/* time_stepping.h:9 -> src/time_stepping/vector_tendencies_expl.c:18 */
+int vector_tendencies_expl(struct state *state, struct state *state_tendency, struct grid *grid,
+                           struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,
+                           struct irreversible_quantities *irrev, struct config *config, int rk_step, double delta_t);
+/* time_stepping.h:10 -> src/time_stepping/scalar_tendencies_expl.c:17 */
+int scalar_tendencies_expl(struct state *state_old, struct state *state, struct state *state_tendency,
+                           struct grid *grid, struct dualgrid *dualgrid, double delta_t,
+                           struct diagnostics *diagnostics, struct forcings *forcings,
+                           struct irreversible_quantities *irrev, struct config *config, int rk_step);
+/* time_stepping.h:11 -> src/time_stepping/column_solvers.c:19 */
+int three_band_solver_ver_waves(struct state *state_old, struct state *state_new, struct state *state_tendency,
+                                struct diagnostics *diagnostics, struct forcings *forcings, struct config *config,
+                                double delta_t, struct grid *grid, int rk_step);
+/* time_stepping.h:12 -> column_solvers.c:385 */
+int three_band_solver_gen_densities(struct state *state_old, struct state *state_new, struct state *state_tendency,
+                                    struct diagnostics *diagnostics, struct irreversible_quantities *irrev,
+                                    struct config *config, double delta_t, int rk_step, struct grid *grid);
 /* spatial_operators.h:6-11 -> gradient_operators.c:14,35,56,66,76 */
 int grad_hor_cov(double *in_field, double *out_field, struct grid *grid);
 int grad_vert_cov(double *in_field, double *out_field, struct grid *grid);

@@ -148,6 +148,57 @@ class Oracle:
         self.lib.orc_linear_combine_two_states(ctypes.byref(self.g), ctypes.byref(a), ctypes.byref(b),
                                                ctypes.byref(o), ctypes.c_double(c0), ctypes.c_double(c1))
 
+    # ---- the sub-steps of manage_rkhevi (reference argument meaning)
+    def step_prelude(self, state, dt):
+        """temperature diagnostics and phase-transition rates of a State, as
+        manage_rkhevi computes them first (manage_rkhevi.c:29-41)"""
+        m = self.m
+        s, d, r, c = self.state(state), self.diag(), self.irrev(), self.config()
+        self.lib.orc_temperature_diagnostics(ctypes.byref(self.g), ctypes.byref(s), ctypes.byref(d))
+        if m.layout.moisture_on:
+            self.lib.orc_calc_h2otracers_source_rates(ctypes.byref(self.g), ctypes.byref(s), ctypes.byref(d),
+                                                      ctypes.byref(c), ctypes.byref(r), ctypes.c_double(dt))
+
+    def manage_pressure_gradient(self, state):
+        s, d, f, r, c = self.state(state), self.diag(), self.forcings(), self.irrev(), self.config()
+        self.lib.orc_manage_pressure_gradient(ctypes.byref(self.g), ctypes.byref(s), ctypes.byref(d), ctypes.byref(f),
+                                              ctypes.byref(r), ctypes.byref(c))
+
+    def calc_pressure_grad_condensates_v(self, state):
+        s, f, r = self.state(state), self.forcings(), self.irrev()
+        self.lib.orc_calc_pressure_grad_condensates_v(ctypes.byref(self.g), ctypes.byref(s), ctypes.byref(f),
+                                                      ctypes.byref(r))
+
+    def vector_tendencies_expl(self, state, tend, rk, dt):
+        s, t, d, f, r, c = (self.state(state), self.state(tend), self.diag(), self.forcings(), self.irrev(),
+                            self.config())
+        self.lib.orc_vector_tendencies_expl(ctypes.byref(self.g), ctypes.byref(s), ctypes.byref(t), ctypes.byref(d),
+                                            ctypes.byref(f), ctypes.byref(r), ctypes.byref(c), int(rk),
+                                            ctypes.c_double(dt))
+
+    def scalar_tendencies_expl(self, s_old, s_new, tend, dt, rk):
+        so, sn, t = self.state(s_old), self.state(s_new), self.state(tend)
+        d, f, r, c = self.diag(), self.forcings(), self.irrev(), self.config()
+        rc = self.lib.orc_scalar_tendencies_expl(ctypes.byref(self.g), ctypes.byref(so), ctypes.byref(sn),
+                                                 ctypes.byref(t), ctypes.c_double(dt), ctypes.byref(d),
+                                                 ctypes.byref(f), ctypes.byref(r), ctypes.byref(c), int(rk))
+        if rc != 0:
+            raise RuntimeError(f"oracle scalar_tendencies_expl returned {rc}")
+
+    def three_band_solver_ver_waves(self, s_old, s_new, tend, dt, rk):
+        so, sn, t, c = self.state(s_old), self.state(s_new), self.state(tend), self.config()
+        rc = self.lib.orc_three_band_solver_ver_waves(ctypes.byref(self.g), ctypes.byref(so), ctypes.byref(sn),
+                                                      ctypes.byref(t), ctypes.byref(c), ctypes.c_double(dt), int(rk))
+        if rc != 0:
+            raise RuntimeError(f"oracle three_band_solver_ver_waves returned {rc}")
+
+    def three_band_solver_gen_densities(self, s_old, s_new, tend, dt, rk):
+        so, sn, t = self.state(s_old), self.state(s_new), self.state(tend)
+        d, r, c = self.diag(), self.irrev(), self.config()
+        self.lib.orc_three_band_solver_gen_densities(ctypes.byref(self.g), ctypes.byref(so), ctypes.byref(sn),
+                                                     ctypes.byref(t), ctypes.byref(d), ctypes.byref(r),
+                                                     ctypes.byref(c), ctypes.c_double(dt), int(rk))
+
     def manage_rkhevi(self, dt, t=0.0):
         m = self.m
         so, sn, st = self.state(m.state_old), self.state(m.state_new), self.state(m.state_tendency)
