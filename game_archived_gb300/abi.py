@@ -62,6 +62,10 @@ SIGNATURES = {
     "game_gpu_write_out_integral": ([vp, cint, vp], cint),
     "game_gpu_surface_pressure": ([vp, vp, vp], cint),
     "game_gpu_weighted_sums_noalloc": ([vp, cint, ctypes.c_longlong, vp, vp, vp], cint),
+    "rkhevi_window_forward": ([vp] * 8 + [dbl, cint], cint),
+    "rkhevi_window_tl": ([vp, vp], cint),
+    "rkhevi_window_backward": ([vp, vp], cint),
+    "game_gpu_sfc_pressure_objective": ([vp, vp, ctypes.POINTER(ctypes.c_double), vp], cint),
 }
 
 FP64, MIXED = 0, 1
@@ -219,6 +223,28 @@ class GpuModel:
     def vorticity_flux(self, flux, pv, out):
         m = self.m
         self._check(self.lib.vorticity_flux(_p(flux), _p(pv), _p(out), m.grid.ptr, m.dualgrid.ptr), "vorticity_flux")
+
+    # -- adjoint / tangent-linear windows (dry build)
+    def window_forward(self, s_init, s_final, dt, n_steps):
+        m = self.m
+        self._check(self.lib.rkhevi_window_forward(s_init.ptr, s_final.ptr, m.grid.ptr, m.dualgrid.ptr,
+                                                   m.diagnostics.ptr, m.forcings.ptr, m.irrev.ptr, m.config.ptr,
+                                                   dt, n_steps), "rkhevi_window_forward")
+
+    def window_tl(self, s_dot, s_final_dot):
+        self._check(self.lib.rkhevi_window_tl(s_dot.ptr, s_final_dot.ptr), "rkhevi_window_tl")
+
+    def window_backward(self, s_final_bar, s_init_bar):
+        self._check(self.lib.rkhevi_window_backward(s_final_bar.ptr, s_init_bar.ptr), "rkhevi_window_backward")
+
+    def sfc_pressure_objective(self, state, weights, state_bar=None):
+        import numpy as np
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        J = ctypes.c_double()
+        self._check(self.lib.game_gpu_sfc_pressure_objective(state.ptr, _p(w), ctypes.byref(J),
+                                                             state_bar.ptr if state_bar is not None else None),
+                    "sfc_pressure_objective")
+        return J.value
 
     # -- integrals and surface pressure
     def global_scalar_integrator(self, field):

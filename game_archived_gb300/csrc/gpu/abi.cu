@@ -11,6 +11,7 @@
 #include "game_gb300.h"
 #include "ops.h"
 #include "substeps.h"
+#include "adj.h"
 
 using namespace game;
 
@@ -887,6 +888,84 @@ int three_band_solver_gen_densities(struct state *state_old, struct state *state
     sub_gen_densities(c, p, &b.so, &b.sn, &b.st, rk_step, b.temperature, b.cp_ice, b.cp_water, b.sed_heat);
     if (download_state(state_new, &b.sn, 1)) return -1;
     if (rk_step == 0 && down_scal(irrev, GAME_IRREV, "condensates_sediment_heat", b.sed_heat)) return -1;
+    return finish();
+}
+
+/* ----------------------------------------------- adjoint / tangent-linear */
+/* copy a device state block into a private mirror and download it */
+static int adj_download(struct state *host, StateMirror *m, const double *blk)
+{
+    Context *c = ctx();
+    if (blk != m->dev)
+        CK(cudaMemcpyAsync(m->dev, blk, (size_t)adj_block_len(c) * sizeof(double), cudaMemcpyDeviceToDevice,
+                           c->stream));
+    if (download_state(host, m, 1 | 2 | 4 | 8 | 16)) return -1;
+    return finish();
+}
+
+int rkhevi_window_forward(struct state *state_init, struct state *state_final, struct grid *grid,
+                          struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,
+                          struct irreversible_quantities *irrev, struct config *config, double delta_t, int n_steps)
+{
+    (void)dualgrid;
+    (void)irrev;
+    if (check_ready(grid)) return -1;
+    if (check_config(config)) return -1;
+    Context *c = ctx();
+    if (c->n_const != 1) return fail("rkhevi_window_forward: the adjoint model covers the dry build (MOISTURE_ON = 0)");
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    if (upload_state(state_init, &b.so)) return -1;
+    StepParams p = params_from_config(c, config, delta_t);
+    double *auxP = b.vec[0], *auxV = b.vec[1], *auxG = b.vec[2], *fl = b.vec[3];
+    if (up_vec(diagnostics, GAME_DIAGNOSTICS, "flux_density", fl)) return -1;
+    if (!p.first_step) {
+        if (up_vec(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_nl", auxP)) return -1;
+        if (up_vec(forcings, GAME_FORCINGS, "pressure_gradient_acc_neg_l", b.vec[4])) return -1;
+        if (up_vec(forcings, GAME_FORCINGS, "pot_vort_tend", auxV)) return -1;
+        if (up_vec(forcings, GAME_FORCINGS, "v_squared_grad", auxG)) return -1;
+        adj_add_into(c, auxP, b.vec[4], c->nv); /* the step reads nl + l */
+    }
+    if (adj_window_forward(c, &b.so, p, n_steps, auxP, auxV, auxG, fl, &b.sn)) return -1;
+    return adj_download(state_final, &b.sn, b.sn.dev);
+}
+
+int rkhevi_window_tl(struct state *state_init_dot, struct state *state_final_dot)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    if (upload_state(state_init_dot, &b.st)) return -1;
+    if (adj_window_tl(c, b.st.dev, b.sn.dev)) return -1;
+    return adj_download(state_final_dot, &b.sn, b.sn.dev);
+}
+
+int rkhevi_window_backward(struct state *state_final_bar, struct state *state_init_bar)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    if (upload_state(state_final_bar, &b.st)) return -1;
+    if (adj_window_backward(c, b.st.dev, b.sn.dev)) return -1;
+    return adj_download(state_init_bar, &b.sn, b.sn.dev);
+}
+
+int game_gpu_sfc_pressure_objective(struct state *state, const double *weights, double *objective,
+                                    struct state *state_bar)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    if (c->n_const != 1) return fail("game_gpu_sfc_pressure_objective: dry build only (MOISTURE_ON = 0)");
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    double *w = adj_obj_weights(c);
+    if (!w) return -1;
+    if (upload_state(state, &b.st)) return -1;
+    if (upload_field(weights, w, c->map_s, c->nc, c->nc)) return -1;
+    if (adj_objective(c, &b.st, w, objective, state_bar ? b.sn.dev : nullptr)) return -1;
+    if (state_bar) return adj_download(state_bar, &b.sn, b.sn.dev);
     return finish();
 }
 

@@ -1,0 +1,550 @@
+/*
+ * Adjoint and tangent-linear models of the dry RKHEVI step over multi-step
+ * windows (compiled with --fmad=false, like the FP64 step).
+ *
+ * Window forward: the initial State and, unless the window starts with the
+ * model's first step, the lagged fields of the previous step (pressure
+ * gradient nl + l, vorticity flux, kinetic-energy gradient) are
+ * checkpointed; every step is run with the differentiable kernels of
+ * adj_fwd.cuh (the same operations as the fused FP64 step) and its end state
+ * and lagged fields are checkpointed.
+ * Window backward (reverse mode): from the last step to the first, the step
+ * is recomputed from its checkpoint with every intermediate field kept (both
+ * RK stage states, the momentum, scalar and solver work of both substages),
+ * then the hand-written adjoint kernels of adj_bwd.cuh run in reverse order.
+ * The bars of the lagged fields carry over to the earlier step.
+ * Window tangent-linear: the same forward kernels instantiated with dual
+ * numbers.
+ *
+ * The control is the State at the window start: rho, rho theta_v, Pi', w and
+ * u.  theta_v' is rediagnosed from rho theta_v / rho at every step start
+ * (linear_combine_two_states, src/coordinator.c:305), so its input bar is 0.
+ */
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "adj_bwd.cuh"
+#include "adj.h"
+#include "diag.h"
+#include "ops.h"
+
+namespace game {
+namespace {
+
+/* --------------------------------------------------------------- utilities */
+template <class T>
+__global__ void ku_copy(long long n, const T *src, T *dst)
+{
+    const long long i = gtid();
+    if (i < n) dst[i] = src[i];
+}
+template <class T>
+__global__ void ku_neg(long long n, const T *src, T *dst)
+{
+    const long long i = gtid();
+    if (i < n) dst[i] = -src[i];
+}
+__global__ void ku_axpy(long long n, double a, const double *x, double *y)
+{
+    const long long i = gtid();
+    if (i < n) y[i] += a * x[i];
+}
+__global__ void ku_to_dual(long long n, const double *v, const double *d, Dual *out)
+{
+    const long long i = gtid();
+    if (i < n) out[i] = Dual{v[i], d ? d[i] : 0.0};
+}
+__global__ void ku_dual_part(long long n, const Dual *in, double *d)
+{
+    const long long i = gtid();
+    if (i < n) d[i] = in[i].d;
+}
+__global__ void ku_dden(long long n, double dt, const double *dc, double *dden)
+{
+    const long long i = gtid();
+    if (i < n) dden[i] = 1.0 + dt * dc[i];
+}
+/* flux_v levels 0 and L (never written by the step) */
+template <class T>
+__global__ void ku_fv_bounds(int nc, int nl, const double *src, T *fv)
+{
+    const int i = (int)gtid();
+    if (i >= nc) return;
+    fv[i] = tconst<T>(src[i]);
+    fv[(long long)nl * nc + i] = tconst<T>(src[(long long)nl * nc + i]);
+}
+
+inline unsigned nbk(long long n, int bs = 256) { return (unsigned)((n + bs - 1) / bs); }
+
+/* ------------------------------------------------------------- step buffers */
+template <class T>
+struct StepBufs {
+    T *so = nullptr, *sn1 = nullptr, *sn2 = nullptr;
+    T *P = nullptr, *pgo = nullptr;
+    T *tri[2] = {}, *zh[2] = {}, *zv[2] = {}, *fh[2] = {}, *fv[2] = {}, *v2[2] = {};
+    T *pvt[2] = {}, *v2g[2] = {}, *tend[2] = {};
+    T *theta[2] = {}, *str[2] = {}, *strt[2] = {};
+    T *wl[2] = {}, *wr[2] = {};
+};
+
+}  // namespace
+
+struct AdjState {
+    std::vector<void *> owned;
+    long long ns = 0, nw = 0, nu = 0, nv = 0, nblk = 0, ntri = 0, nzh = 0, nwi = 0;
+    StepBufs<double> B;          /* forward tape of one step */
+    StepBufs<double> Z;          /* bars of one step */
+    StepBufs<Dual> D;            /* tangent-linear run */
+    double *rn_b = nullptr, *rtn_b = nullptr;
+    double *dden = nullptr, *fv_bounds = nullptr; /* (L+1) Nc */
+    double *ck = nullptr;        /* checkpoints: (n_steps + 1) x (state block + 3 Vt) */
+    int ck_cap = -1;
+    double *obj_w = nullptr, *obj_p = nullptr, *obj_out = nullptr; /* objective work */
+    Dual *tl_aux[3] = {};        /* lagged fields between tangent-linear steps */
+    double *bar_state = nullptr; /* bar of the current step-end state */
+    double *bar_aux[3] = {}, *bar_aux_prev[3] = {}; /* bars of the lagged fields */
+    /* the window of the last forward run */
+    int n_steps = 0, first = 0, have = 0;
+    AParams ap{};
+    StepParams p{};
+};
+
+namespace {
+
+template <class T>
+T *aalloc(AdjState *a, long long n)
+{
+    void *p = nullptr;
+    if (cudaMalloc(&p, (size_t)(n > 0 ? n : 1) * sizeof(T)) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, (size_t)(n > 0 ? n : 1) * sizeof(T));
+    a->owned.push_back(p);
+    return (T *)p;
+}
+
+template <class T>
+bool alloc_step(AdjState *a, StepBufs<T> &S)
+{
+    bool ok = true;
+    auto A = [&](T *&p, long long n) {
+        p = aalloc<T>(a, n);
+        ok = ok && p;
+    };
+    A(S.so, a->nblk);
+    A(S.sn1, a->nblk);
+    A(S.sn2, a->nblk);
+    A(S.P, a->nv);
+    A(S.pgo, a->nv);
+    for (int r = 0; r < 2; ++r) {
+        A(S.tri[r], a->ntri);
+        A(S.zh[r], a->nzh);
+        A(S.zv[r], a->nu);
+        A(S.fh[r], a->nu);
+        A(S.fv[r], a->nw);
+        A(S.v2[r], a->ns);
+        A(S.pvt[r], a->nv);
+        A(S.v2g[r], a->nv);
+        A(S.tend[r], a->nv);
+        A(S.theta[r], a->ns);
+        A(S.str[r], a->ns);
+        A(S.strt[r], a->ns);
+        A(S.wl[r], WL_N * a->ns);
+        A(S.wr[r], WR_N * a->nwi);
+    }
+    return ok;
+}
+
+void adj_release_fn(Context *c)
+{
+    if (!c->adj) return;
+    for (void *p : c->adj->owned) cudaFree(p);
+    delete c->adj;
+    c->adj = nullptr;
+}
+
+int ensure_adj(Context *c)
+{
+    if (c->adj) return 0;
+    if (c->n_const != 1) return fail("adjoint: the adjoint and tangent-linear models cover the dry build (MOISTURE_ON = 0)");
+    if (c->nl > MAX_L) return fail("adjoint: more layers than the column solvers support");
+    AdjState *a = new AdjState();
+    c->adj = a;
+    c->adj_release = adj_release_fn;
+    a->ns = c->ns;
+    a->nw = (long long)(c->nl + 1) * c->nc;
+    a->nu = (long long)c->nl * c->ne;
+    a->nv = a->nw + a->nu;
+    a->nblk = 4 * a->ns + a->nv;
+    a->ntri = (long long)c->nl * c->nt;
+    a->nzh = (long long)(c->nl + 1) * c->ne;
+    a->nwi = (long long)(c->nl - 1) * c->nc;
+    bool ok = alloc_step(a, a->B) && alloc_step(a, a->Z) && alloc_step(a, a->D);
+    ok = ok && (a->rn_b = aalloc<double>(a, a->ns)) && (a->rtn_b = aalloc<double>(a, a->ns));
+    ok = ok && (a->dden = aalloc<double>(a, a->nwi)) && (a->fv_bounds = aalloc<double>(a, a->nw));
+    ok = ok && (a->obj_w = aalloc<double>(a, c->nc)) && (a->obj_p = aalloc<double>(a, c->nc))
+         && (a->obj_out = aalloc<double>(a, 1)) && (a->bar_state = aalloc<double>(a, a->nblk));
+    for (int k = 0; k < 3; ++k)
+        ok = ok && (a->tl_aux[k] = aalloc<Dual>(a, a->nv)) && (a->bar_aux[k] = aalloc<double>(a, a->nv))
+             && (a->bar_aux_prev[k] = aalloc<double>(a, a->nv));
+    if (!ok) {
+        adj_release_fn(c);
+        return fail("adjoint: device allocation failed");
+    }
+    return 0;
+}
+
+template <class T>
+AState<T> view(const AdjState *a, T *blk)
+{
+    AState<T> s;
+    s.rho = blk;
+    s.rt = blk + a->ns;
+    s.tp = blk + 2 * a->ns;
+    s.ep = blk + 3 * a->ns;
+    s.w = blk + 4 * a->ns;
+    s.u = s.w + a->nw;
+    return s;
+}
+
+long long ck_stride(const AdjState *a) { return a->nblk + 3 * a->nv; }
+
+/* ----------------------------------------------------------- step forward */
+template <class T>
+void step_fwd(Context *c, AdjState *a, StepBufs<T> &B, const T *P_prev, const T *pvt_prev, const T *v2g_prev,
+              bool first)
+{
+    const HGrid<double> &g = c->hg64;
+    const VGrid &vg = c->vg;
+    const AParams ap = a->ap;
+    cudaStream_t st = c->stream;
+    const long long ns = a->ns, nv = a->nv;
+    AState<T> so = view(a, B.so), s1 = view(a, B.sn1), s2 = view(a, B.sn2);
+    /* substage 0 (state_new = state_old) */
+    fa_pgrad<T><<<nbk(nv), 256, 0, st>>>(g, so, B.P);
+    ku_neg<T><<<nbk(nv), 256, 0, st>>>(nv, first ? B.P : P_prev, B.pgo);
+    if (first) {
+        fa_tri<T><<<nbk(a->ntri), 256, 0, st>>>(g, so.u, B.tri[0]);
+        fa_edge<T><<<nbk(a->nzh), 256, 0, st>>>(g, so.u, so.w, so.rho, B.tri[0], B.zh[0], B.zv[0], B.fh[0]);
+        fa_kin<T><<<nbk(ns), 256, 0, st>>>(g, so.u, so.w, so.rho, B.v2[0], B.fv[0]);
+    } else {
+        ku_copy<T><<<nbk(nv), 256, 0, st>>>(nv, pvt_prev, B.pvt[0]);
+        ku_copy<T><<<nbk(nv), 256, 0, st>>>(nv, v2g_prev, B.v2g[0]);
+    }
+    fa_mom_v<T><<<nbk(a->nw), 256, 0, st>>>(g, ap, first, 1.0, 0.0, B.P, B.fh[0], B.zh[0], B.v2[0], B.pvt[0],
+                                            B.v2g[0], B.tend[0], B.tend[0]);
+    fa_mom_h<T><<<nbk(a->nu), 256, 0, st>>>(g, ap, first, 1.0, 0.0, B.P, B.pgo, B.fh[0], B.fv[0], B.zh[0], B.zv[0],
+                                            B.v2[0], B.pvt[0], B.v2g[0], B.tend[0], B.tend[0], so.u, s1.u);
+    fa_theta<T><<<nbk(ns), 256, 0, st>>>(ns, so.rho, so.rt, B.theta[0]);
+    fa_scalar<T><<<nbk(ns, 128), 128, 0, st>>>(g, so.rho, B.theta[0], s1.u, B.str[0], B.strt[0]);
+    fa_waves_layer<T><<<nbk(ns), 256, 0, st>>>(vg, ap, 0, so, so, B.str[0], B.strt[0], B.wl[0]);
+    fa_waves_rows<T><<<nbk(a->nwi), 256, 0, st>>>(vg, ap, so, B.tend[0], B.wl[0], B.wr[0]);
+    fa_waves_thomas<T><<<nbk(c->nc, 64), 64, 0, st>>>(c->nc, c->nl, a->dden, B.wr[0]);
+    fa_waves_apply<T><<<nbk(ns), 256, 0, st>>>(vg, ap, so, B.wl[0], B.wr[0], s1);
+    /* substage 1 */
+    fa_tri<T><<<nbk(a->ntri), 256, 0, st>>>(g, s1.u, B.tri[1]);
+    fa_edge<T><<<nbk(a->nzh), 256, 0, st>>>(g, s1.u, s1.w, s1.rho, B.tri[1], B.zh[1], B.zv[1], B.fh[1]);
+    fa_kin<T><<<nbk(ns), 256, 0, st>>>(g, s1.u, s1.w, s1.rho, B.v2[1], B.fv[1]);
+    fa_mom_v<T><<<nbk(a->nw), 256, 0, st>>>(g, ap, 1, 0.5, 0.5, B.P, B.fh[1], B.zh[1], B.v2[1], B.pvt[1], B.v2g[1],
+                                            B.tend[0], B.tend[1]);
+    fa_mom_h<T><<<nbk(a->nu), 256, 0, st>>>(g, ap, 1, 0.5, 0.5, B.P, B.pgo, B.fh[1], B.fv[1], B.zh[1], B.zv[1],
+                                            B.v2[1], B.pvt[1], B.v2g[1], B.tend[0], B.tend[1], so.u, s2.u);
+    fa_theta<T><<<nbk(ns), 256, 0, st>>>(ns, s1.rho, s1.rt, B.theta[1]);
+    fa_scalar<T><<<nbk(ns, 128), 128, 0, st>>>(g, s1.rho, B.theta[1], s2.u, B.str[1], B.strt[1]);
+    fa_waves_layer<T><<<nbk(ns), 256, 0, st>>>(vg, ap, 1, so, s1, B.str[1], B.strt[1], B.wl[1]);
+    fa_waves_rows<T><<<nbk(a->nwi), 256, 0, st>>>(vg, ap, so, B.tend[1], B.wl[1], B.wr[1]);
+    fa_waves_thomas<T><<<nbk(c->nc, 64), 64, 0, st>>>(c->nc, c->nl, a->dden, B.wr[1]);
+    fa_waves_apply<T><<<nbk(ns), 256, 0, st>>>(vg, ap, so, B.wl[1], B.wr[1], s2);
+    c->kernel_launches += first ? 27 : 26;
+}
+
+/* ---------------------------------------------------------- step backward
+ * s2b: bar of the step's end state (modified); P_next_b, pvt_next_b,
+ * v2g_next_b: bars of this step's lagged outputs from the next step (may be
+ * null); writes sob (bar of the step-start state, theta_v' bar consumed) and,
+ * for a step that is not the model's first, the bars of the lagged inputs. */
+void step_bwd(Context *c, AdjState *a, bool first, double *s2b, const double *P_next_b, const double *pvt_next_b,
+              const double *v2g_next_b, double *sob, double *P_prev_b, double *pvt_prev_b, double *v2g_prev_b)
+{
+    const HGrid<double> &g = c->hg64;
+    const VGrid &vg = c->vg;
+    const AParams ap = a->ap;
+    cudaStream_t st = c->stream;
+    const long long ns = a->ns, nv = a->nv, nw = a->nw;
+    StepBufs<double> &B = a->B, &Z = a->Z;
+    /* zero all bars of the step */
+    auto zero = [&](double *p, long long n) { cudaMemsetAsync(p, 0, (size_t)n * sizeof(double), st); };
+    zero(sob, a->nblk);
+    zero(Z.sn1, a->nblk);
+    zero(Z.P, nv);
+    zero(Z.pgo, nv);
+    for (int r = 0; r < 2; ++r) {
+        zero(Z.tri[r], a->ntri);
+        zero(Z.zh[r], a->nzh);
+        zero(Z.zv[r], a->nu);
+        zero(Z.fh[r], a->nu);
+        zero(Z.fv[r], a->nw);
+        zero(Z.v2[r], ns);
+        zero(Z.pvt[r], nv);
+        zero(Z.v2g[r], nv);
+        zero(Z.tend[r], nv);
+        zero(Z.theta[r], ns);
+        zero(Z.str[r], ns);
+        zero(Z.strt[r], ns);
+        zero(Z.wl[r], WL_N * ns);
+        zero(Z.wr[r], WR_N * a->nwi);
+    }
+    if (pvt_next_b) ku_copy<double><<<nbk(nv), 256, 0, st>>>(nv, pvt_next_b, Z.pvt[1]);
+    if (v2g_next_b) ku_copy<double><<<nbk(nv), 256, 0, st>>>(nv, v2g_next_b, Z.v2g[1]);
+    AState<double> so = view(a, B.so), s1 = view(a, B.sn1), s2 = view(a, B.sn2);
+    AState<double> sob_v = view(a, sob), s1b = view(a, Z.sn1), s2b_v = view(a, s2b);
+    /* substage 1: sound waves */
+    for (int rk = 1; rk >= 0; --rk) {
+        AState<double> out = rk ? s2 : s1, out_b = rk ? s2b_v : s1b;
+        AState<double> sn = rk ? s1 : so, sn_b = rk ? s1b : sob_v;
+        ba_apply_layer<<<nbk(ns), 256, 0, st>>>(vg, so, B.wl[rk], out, out_b, a->rn_b, a->rtn_b, sob_v, Z.wl[rk]);
+        ba_apply_w<<<nbk(a->nwi), 256, 0, st>>>(vg, so, B.wr[rk], out, out_b, a->rn_b, sob_v, Z.wr[rk]);
+        ba_apply_rho<<<nbk(ns), 256, 0, st>>>(vg, ap, B.wr[rk], a->rn_b, a->rtn_b, Z.wl[rk], Z.wr[rk]);
+        ba_thomas<<<nbk(c->nc, 64), 64, 0, st>>>(c->nc, c->nl, a->dden, B.wr[rk], Z.wr[rk]);
+        ba_waves_rows<<<nbk(a->nwi), 256, 0, st>>>(vg, ap, so, B.wl[rk], B.wr[rk], Z.wr[rk], Z.wl[rk], sob_v,
+                                                   Z.tend[rk]);
+        ba_waves_layer<<<nbk(ns), 256, 0, st>>>(vg, ap, rk, so, sn, B.str[rk], B.strt[rk], B.wl[rk], Z.wl[rk], sob_v,
+                                                sn_b, Z.str[rk], Z.strt[rk]);
+        /* scalar tendencies: density and theta_v of sn, the wind of out */
+        ba_scalar<<<nbk(ns, 128), 128, 0, st>>>(g, sn.rho, B.theta[rk], out.u, Z.str[rk], Z.strt[rk], sn_b.rho,
+                                           Z.theta[rk], out_b.u);
+        ba_theta<<<nbk(ns), 256, 0, st>>>(ns, sn.rho, sn.rt, Z.theta[rk], sn_b.rho, sn_b.rt);
+        /* momentum */
+        const int adv = rk == 1 || first;
+        const double new_w = rk ? 0.5 : 1.0, old_w = 1.0 - new_w;
+        double *tend_in_b = rk ? Z.tend[0] : nullptr;
+        ba_mom_v<<<nbk(nw), 256, 0, st>>>(g, ap, adv, new_w, old_w, B.fh[rk], B.zh[rk], Z.tend[rk], tend_in_b, Z.P,
+                                          Z.pvt[rk], Z.v2g[rk], Z.fh[rk], Z.zh[rk], Z.v2[rk]);
+        ba_mom_h<<<nbk(a->nu), 256, 0, st>>>(g, ap, adv, new_w, old_w, B.fh[rk], B.fv[rk], B.zh[rk], B.zv[rk],
+                                             Z.tend[rk], out_b.u, sob_v.u, tend_in_b, Z.P, Z.pgo, Z.pvt[rk], Z.v2g[rk],
+                                             Z.fh[rk], Z.fv[rk], Z.zh[rk], Z.zv[rk], Z.v2[rk]);
+        if (adv) {
+            ba_kin<<<nbk(ns), 256, 0, st>>>(g, sn.u, sn.w, sn.rho, Z.v2[rk], Z.fv[rk], sn_b.u, sn_b.w, sn_b.rho);
+            ba_edge<<<nbk(a->nzh), 256, 0, st>>>(g, sn.u, sn.rho, B.zh[rk], B.zv[rk], Z.zh[rk], Z.zv[rk], Z.fh[rk],
+                                                 sn_b.u, sn_b.w, sn_b.rho, Z.tri[rk]);
+            ba_tri<<<nbk(a->ntri), 256, 0, st>>>(g, Z.tri[rk], sn_b.u);
+        }
+    }
+    if (!first) {
+        ku_copy<double><<<nbk(nv), 256, 0, st>>>(nv, Z.pvt[0], pvt_prev_b);
+        ku_copy<double><<<nbk(nv), 256, 0, st>>>(nv, Z.v2g[0], v2g_prev_b);
+    }
+    /* pressure gradient: its use in the next step, then pg_old = -P or -P_prev */
+    if (P_next_b) ku_axpy<<<nbk(nv), 256, 0, st>>>(nv, 1.0, P_next_b, Z.P);
+    if (first)
+        ku_axpy<<<nbk(nv), 256, 0, st>>>(nv, -1.0, Z.pgo, Z.P);
+    else
+        ku_neg<double><<<nbk(nv), 256, 0, st>>>(nv, Z.pgo, P_prev_b);
+    ba_pgrad<<<nbk(nv), 256, 0, st>>>(g, so, Z.P, sob_v.tp, sob_v.ep);
+    ba_rediag<<<nbk(ns), 256, 0, st>>>(ns, so.rho, so.rt, sob_v.tp, sob_v.rho, sob_v.rt);
+    c->kernel_launches += 40;
+}
+
+/* the step-start state of step n from its checkpoint: theta_v' rediagnosed */
+template <class T>
+void load_start(Context *c, AdjState *a, int n, T *so_blk)
+{
+    const double *ck = a->ck + (long long)n * ck_stride(a);
+    if constexpr (sizeof(T) == sizeof(double))
+        ku_copy<double><<<nbk(a->nblk), 256, 0, c->stream>>>(a->nblk, ck, (double *)so_blk);
+    fa_rediag<T><<<nbk(a->ns), 256, 0, c->stream>>>(c->vg, view(a, so_blk));
+}
+
+const double *ck_aux(const AdjState *a, int n, int which) /* 0 P, 1 pvt, 2 v2g */
+{
+    return a->ck + (long long)n * ck_stride(a) + a->nblk + (long long)which * a->nv;
+}
+
+/* --------------------------------------------------------------- objective */
+/* surface pressure of a column (write_output.c:105-121, dry) and its partial
+ * derivatives by rho, theta_v' and Pi' of the lowest layer */
+__device__ __forceinline__ double sfc_p_dry(const VGrid &vg, const double *gm_v, const double *rho, const double *tp,
+                                            const double *ep, int i, double *d_rho, double *d_tp, double *d_ep)
+{
+    const int nc = vg.nc, nl = vg.nl;
+    const long long si = (long long)(nl - 1) * nc + i;
+    const double lapse = 0.0065, rgas = R_D;
+    const double th = vg.theta_v_bg[si] + tp[si], pe = vg.exner_bg[si] + ep[si];
+    const double t_low = th * pe;
+    const double p = rho[si] * rgas * t_low;
+    const double t_sfc = t_low + lapse * (vg.z_scalar[si] - vg.z_v[(long long)nl * nc + i]);
+    const double q = 1.0 - (t_sfc - t_low) / t_sfc;
+    const double ex = gm_v[(long long)(nl - 1) * nc + i] / (rgas * lapse);
+    const double fac = pow(q, ex);
+    const double ps = p / fac;
+    if (d_rho) {
+        const double k = t_sfc - t_low;
+        const double dfac_dt = ex * pow(q, ex - 1.0) * (k / (t_sfc * t_sfc));
+        const double dps_dt = rho[si] * rgas / fac - ps / fac * dfac_dt;
+        *d_rho = rgas * t_low / fac;
+        *d_tp = dps_dt * pe;
+        *d_ep = dps_dt * th;
+    }
+    return ps;
+}
+
+__global__ void k_obj(VGrid vg, const double *gm_v, AState<double> s, const double *w, double *p2, AState<double> sb)
+{
+    const int i = (int)gtid();
+    if (i >= vg.nc) return;
+    double dr, dt_, de;
+    const double ps = sfc_p_dry(vg, gm_v, s.rho, s.tp, s.ep, i, sb.rho ? &dr : nullptr, &dt_, &de);
+    p2[i] = ps * ps;
+    if (sb.rho) {
+        const long long si = (long long)(vg.nl - 1) * vg.nc + i;
+        const double pb = 2.0 * w[i] * ps;
+        sb.rho[si] += pb * dr;
+        sb.tp[si] += pb * dt_;
+        sb.ep[si] += pb * de;
+    }
+}
+
+/* ---------------------------------------------------------- host helpers */
+int set_params(Context *c, AdjState *a, const StepParams &p)
+{
+    a->p = p;
+    a->ap.dt = p.dt;
+    a->ap.impl_thermo_weight = p.impl_thermo_weight;
+    if (launch_damping_table(c, p)) return -1;
+    ku_dden<<<nbk(a->nwi), 256, 0, c->stream>>>(a->nwi, p.dt, c->damp_dc, a->dden);
+    return 0;
+}
+
+}  // namespace
+
+/* ---------------------------------------------------------------- API */
+int adj_window_forward(Context *c, StateMirror *init, const StepParams &p, int n_steps, const double *aux_P,
+                       const double *aux_pvt, const double *aux_v2g, const double *fv_bounds, StateMirror *final_out)
+{
+    if (ensure_adj(c)) return -1;
+    AdjState *a = c->adj;
+    if (n_steps < 1) return fail("adjoint window: n_steps must be at least 1");
+    if (a->ck_cap < n_steps) {
+        double *ck = aalloc<double>(a, (long long)(n_steps + 1) * ck_stride(a));
+        if (!ck) return fail("adjoint window: device allocation of the checkpoints failed");
+        a->ck = ck;
+        a->ck_cap = n_steps;
+    }
+    if (set_params(c, a, p)) return -1;
+    a->n_steps = n_steps;
+    a->first = p.first_step ? 1 : 0;
+    cudaStream_t st = c->stream;
+    ku_copy<double><<<nbk(a->nw), 256, 0, st>>>(a->nw, fv_bounds, a->fv_bounds);
+    for (StepBufs<double> *S : {&a->B})
+        for (int r = 0; r < 2; ++r) ku_fv_bounds<double><<<nbk(c->nc), 256, 0, st>>>(c->nc, c->nl, a->fv_bounds, S->fv[r]);
+    /* checkpoint 0: the initial state and the lagged inputs */
+    double *ck0 = a->ck;
+    ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, init->dev, ck0);
+    if (!a->first) {
+        ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, aux_P, ck0 + a->nblk);
+        ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, aux_pvt, ck0 + a->nblk + a->nv);
+        ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, aux_v2g, ck0 + a->nblk + 2 * a->nv);
+    }
+    for (int n = 0; n < n_steps; ++n) {
+        load_start<double>(c, a, n, a->B.so);
+        const bool first = a->first && n == 0;
+        step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2), first);
+        double *ckn = a->ck + (long long)(n + 1) * ck_stride(a);
+        ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->B.sn2, ckn);
+        ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.P, ckn + a->nblk);
+        ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.pvt[1], ckn + a->nblk + a->nv);
+        ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.v2g[1], ckn + a->nblk + 2 * a->nv);
+    }
+    a->have = 1;
+    if (final_out)
+        ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->ck + (long long)n_steps * ck_stride(a),
+                                                      final_out->dev);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int adj_window_tl(Context *c, const double *init_dot, double *final_dot)
+{
+    AdjState *a = c->adj;
+    if (!a || !a->have) return fail("adjoint window: run the window forward first");
+    cudaStream_t st = c->stream;
+    StepBufs<Dual> &D = a->D;
+    for (int r = 0; r < 2; ++r) ku_fv_bounds<Dual><<<nbk(c->nc), 256, 0, st>>>(c->nc, c->nl, a->fv_bounds, D.fv[r]);
+    /* lagged inputs of the window's first step: values from checkpoint 0,
+     * derivative 0 (they are not part of the control) */
+    for (int k = 0; k < 3; ++k)
+        ku_to_dual<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, 0, k), nullptr, a->tl_aux[k]);
+    ku_to_dual<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->ck, init_dot, D.so);
+    for (int n = 0; n < a->n_steps; ++n) {
+        if (n > 0) ku_copy<Dual><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, D.sn2, D.so);
+        fa_rediag<Dual><<<nbk(a->ns), 256, 0, st>>>(c->vg, view(a, D.so));
+        step_fwd<Dual>(c, a, D, a->tl_aux[0], a->tl_aux[1], a->tl_aux[2], a->first && n == 0);
+        ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.P, a->tl_aux[0]);
+        ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.pvt[1], a->tl_aux[1]);
+        ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.v2g[1], a->tl_aux[2]);
+    }
+    ku_dual_part<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, D.sn2, final_dot);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int adj_window_backward(Context *c, const double *final_bar, double *init_bar)
+{
+    AdjState *a = c->adj;
+    if (!a || !a->have) return fail("adjoint window: run the window forward first");
+    cudaStream_t st = c->stream;
+    const long long nv = a->nv;
+    ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, final_bar, a->bar_state);
+    bool have_next = false;
+    for (int n = a->n_steps - 1; n >= 0; --n) {
+        const bool first = a->first && n == 0;
+        /* recompute the step from its checkpoint, keeping the tape */
+        load_start<double>(c, a, n, a->B.so);
+        step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2), first);
+        step_bwd(c, a, first, a->bar_state, have_next ? a->bar_aux[0] : nullptr,
+                 have_next ? a->bar_aux[1] : nullptr, have_next ? a->bar_aux[2] : nullptr, init_bar,
+                 a->bar_aux_prev[0], a->bar_aux_prev[1], a->bar_aux_prev[2]);
+        /* the step-start bar is the previous step's end-state bar */
+        ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, init_bar, a->bar_state);
+        for (int k = 0; k < 3; ++k) std::swap(a->bar_aux[k], a->bar_aux_prev[k]);
+        have_next = !first;
+    }
+    (void)nv;
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int adj_objective(Context *c, StateMirror *s, const double *w_dev, double *J, double *bar_blk)
+{
+    if (ensure_adj(c)) return -1;
+    AdjState *a = c->adj;
+    AState<double> sv = view(a, s->dev);
+    AState<double> sb{};
+    if (bar_blk) {
+        cudaMemsetAsync(bar_blk, 0, (size_t)a->nblk * sizeof(double), c->stream);
+        sb = view(a, bar_blk);
+    }
+    k_obj<<<nbk(c->nc, 128), 128, 0, c->stream>>>(c->vg, c->hg64.gravity_m_v, sv, w_dev, a->obj_p, sb);
+    if (launch_integral(a->obj_p, 0, 1, c->nc, nullptr, w_dev, c->red_partials, c->red_counters, a->obj_out,
+                        c->stream))
+        return -1;
+    c->kernel_launches += 2;
+    CK(cudaMemcpyAsync(J, a->obj_out, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+double *adj_obj_weights(Context *c)
+{
+    if (ensure_adj(c)) return nullptr;
+    return c->adj->obj_w;
+}
+
+void adj_add_into(Context *c, double *y, const double *x, long long n)
+{
+    ku_axpy<<<nbk(n), 256, 0, c->stream>>>(n, 1.0, x, y);
+    c->kernel_launches++;
+}
+
+long long adj_block_len(Context *c) { return 4 * c->ns + (long long)(c->nl + 1) * c->nc + (long long)c->nl * c->ne; }
+
+}  // namespace game

@@ -530,6 +530,7 @@ int destroy_context()
     cudaDeviceSynchronize();
     profile_flush(c);
     for (auto e : c->user_events) cudaEventDestroy(e);
+    if (c->adj_release) c->adj_release(c);
     for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
     for (auto &kv : c->states) cudaFree(kv.second.dev);
     for (auto &b : c->owned) cudaFree(b.p);

@@ -17,6 +17,8 @@
 
 namespace game {
 
+struct AdjState;
+
 /* device buffer owned by the context */
 struct DBuf {
     void *p = nullptr;
@@ -103,6 +105,10 @@ struct Context {
     Work<float> w32{};
 
     std::map<const void *, StateMirror> states;
+
+    /* adjoint / tangent-linear window state (adj_f64.cu), created on first use */
+    struct AdjState *adj = nullptr;
+    void (*adj_release)(Context *) = nullptr;
 
     /* private buffers of the sub-step entry points (three_band_solver_*,
      * *_tendencies_expl, ...), allocated on their first call; never the

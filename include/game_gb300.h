@@ -189,7 +189,47 @@ int game_gpu_write_out_integral(struct state *state, int integral_id, double *re
  * No counterpart function in the reference (the loop is inside write_out). */
 int game_gpu_surface_pressure(struct state *state, double *surface_p, double *mslp);
 
-/* ---- 4. the weighted-sum reduction without any allocation ---- */
+/* ---- 4. adjoint and tangent-linear models of the step (dry build) ----
+ *
+ * A window of n_steps RKHEVI steps of the FP64 dry step, with hand-written
+ * adjoint kernels for every operator of the step (pressure gradient,
+ * vorticities, vorticity flux, kinetic energy and its gradient, momentum
+ * tendencies, flux divergences, the sound-wave rows, the tridiagonal solve and
+ * its back-substitution).  No counterpart in the reference.
+ *
+ * rkhevi_window_forward runs the window from state_init as the reference's
+ * time loop would (src/coordinator.c:302-324: each step starts with
+ * linear_combine_two_states(new -> old) and calls manage_rkhevi), stores one
+ * checkpoint per step on the device and writes the end state to state_final.
+ * With config->totally_first_step_bool = 1 the window depends on state_init
+ * only; otherwise the lagged fields of forcings (pressure gradient, vorticity
+ * flux, kinetic-energy gradient) and the flux_density boundary values of
+ * diagnostics enter as fixed inputs.  The control variables are rho,
+ * rhotheta_v, exner_pert and wind of state_init; theta_v_pert is rediagnosed
+ * from rhotheta_v / rho at every step start, so its derivative is 0.
+ *
+ * rkhevi_window_tl: the tangent-linear model of the last forward window,
+ * d(state_final) for a perturbation state_init_dot (State structs holding
+ * perturbations).  rkhevi_window_backward: its adjoint, the gradient with
+ * respect to state_init of <state_final_bar, state_final> (State structs
+ * holding bars); each step is recomputed from its checkpoint, keeping both
+ * RK stage states, then differentiated in reverse.
+ *
+ * game_gpu_sfc_pressure_objective: J = sum_i weights[i] p_sfc,i^2 over the
+ * columns (surface pressure of src/io/write_output.c:105-121, reference
+ * column order) and, when state_bar is not NULL, dJ/dstate written to
+ * state_bar (nonzero on the lowest layer's rho, theta_v_pert, exner_pert).
+ *
+ * Dry build only (MOISTURE_ON = 0): other builds return an error. */
+int rkhevi_window_forward(struct state *state_init, struct state *state_final, struct grid *grid,
+                          struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,
+                          struct irreversible_quantities *irrev, struct config *config, double delta_t, int n_steps);
+int rkhevi_window_tl(struct state *state_init_dot, struct state *state_final_dot);
+int rkhevi_window_backward(struct state *state_final_bar, struct state *state_init_bar);
+int game_gpu_sfc_pressure_objective(struct state *state, const double *weights, double *objective,
+                                    struct state *state_bar);
+
+/* ---- 5. the weighted-sum reduction without any allocation ---- */
 
 /* sums[k] = sum over i < n of fields[k*n + i] * weights[i], for k < n_fields,
  * with the compensated accumulation of global_scalar_integrator.  All four
