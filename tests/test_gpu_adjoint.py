@@ -181,3 +181,44 @@ def test_finite_differences_of_the_surface_pressure_objective():
     finally:
         g.close()
     print(f"FD vs adjoint over {n_dir} directions: worst relative difference {worst:.3g}, J = {J0:.6g}")
+
+
+def test_adjoint_matches_the_torch_cpu_adjoint():
+    """the gradient of the surface-pressure objective after a 3-step window
+    (RES_ID=3, mountain): hand-written GPU adjoint vs reverse-mode automatic
+    differentiation of the FP64 PyTorch restatement on the CPU (itself pinned
+    to the oracle in test_torch_adjoint.py); every control field within 1e-9
+    relative"""
+    torch = pytest.importorskip("torch")
+    import torch_dry_step as tds
+    from helpers import rel_err
+    _, m = make_model(3, 0, "std_wind_tpert", mountain=True)
+    n, dt = 3, 300.0
+    w = cap_weights(m)
+    m_g = clone(m)
+    g = abi.GpuModel(m_g, abi.FP64)
+    try:
+        m_g.config["totally_first_step_bool"][0] = 1
+        out = _state_like(m.layout)
+        g.window_forward(m_g.state_old, out, dt, n)
+        jb = _state_like(m.layout)
+        J_gpu = g.sfc_pressure_objective(out, w, jb)
+        grad = _state_like(m.layout)
+        g.window_backward(jb, grad)
+    finally:
+        g.close()
+    step = tds.make_step(m, dt)
+    x = tds.state_tensors(m, m.state_old)
+    for k in ("rho", "rt", "ep", "w", "u"):
+        x[k].requires_grad_(True)
+    s = step.window(x, n)
+    ps = step.sfc_pressure(s)
+    J = (torch.tensor(w) * ps * ps).sum()
+    J.backward()
+    ref = _state_like(m.layout)
+    tds.tensors_to_state(m, {"rho": x["rho"].grad, "rt": x["rt"].grad, "tp": None, "ep": x["ep"].grad,
+                             "w": x["w"].grad, "u": x["u"].grad}, ref)
+    assert abs(J_gpu - float(J)) <= 1e-12 * abs(float(J))
+    errs = {f: rel_err(grad[f], ref[f]) for f in ("rho", "rhotheta_v", "exner_pert", "wind")}
+    print(f"GPU adjoint vs CPU (torch) adjoint, max |diff| / max |ref| per field: {errs}")
+    assert max(errs.values()) <= 1e-9, errs
