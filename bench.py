@@ -181,9 +181,12 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ set-up
-def build_model(res, moist, n_lloyd, pinned):
+MOUNTAIN = (2000.0, 1.5e6, 30.0, 90.0)   # 2 km Gaussian mountain, 1500 km half-width, 30N 90E
+
+
+def build_model(res, moist, n_lloyd, pinned, mountain=None):
     from game_archived_gb300 import abi, cases, structs, tables
-    tab = tables.GridTables(res, n_lloyd=n_lloyd)
+    tab = tables.GridTables(res, n_lloyd=n_lloyd, mountain=mountain)
     lay = structs.Layout(res, L, moist)
     m = abi.pinned_model(lay) if pinned else structs.Model(lay)
     tables.fill_grid(tab, m.grid, m.dualgrid)
@@ -272,6 +275,68 @@ def time_e2e(model0, precision, steps, warmup, dt, device):
         return sec / steps, h2d // steps, d2h // steps
     finally:
         g.close()
+
+
+def cap_weights(m, lat0=45.0, lon0=0.0, radius_deg=20.0):
+    """area_sfc of the columns within radius_deg of (lat0, lon0), else 0"""
+    import numpy as np
+    lay = m.layout
+    lat, lon = m.grid["latitude_scalar"][:lay.nc], m.grid["longitude_scalar"][:lay.nc]
+    p0, l0 = np.radians(lat0), np.radians(lon0)
+    cosd = np.sin(lat) * np.sin(p0) + np.cos(lat) * np.cos(p0) * np.cos(lon - l0)
+    area_sfc = m.grid["area"][lay.n_vectors - lay.nc:lay.n_vectors]
+    return np.where(cosd >= np.cos(np.radians(radius_deg)), area_sfc, 0.0)
+
+
+def time_adjoint(res, n_lloyd, n_steps, dt, device, repeats=3):
+    """Cost of the adjoint relative to the forward step on the adjoint
+    configuration: dry, 2 km mountain, standard atmosphere with 1 K noise,
+    a window of n_steps at dt, objective sum over a 20-degree cap at 45N/0E
+    of area_sfc * p_sfc^2.  Forward: the fused FP64 step, device-resident,
+    CUDA graphs.  Window forward / backward: the C-ABI calls (the backward
+    recomputes every step from its checkpoint), CUDA events on the library
+    stream around each call, mean over the repeats."""
+    from game_archived_gb300 import abi, cases, structs
+    from game_archived_gb300.ops import CAbiOps
+    tab, m = build_model(res, 0, n_lloyd, pinned=False, mountain=MOUNTAIN)
+    g = abi.GpuModel(m, abi.FP64, device=device)
+    try:
+        cases.build_initial_state(m, tab, "std_wind_tpert", CAbiOps(g.lib, m))
+    finally:
+        g.close()
+    ms_fwd = time_resident(m, abi.FP64, n_steps, 3, dt, device)[0]
+    mm = copy_model(m, pinned=False)
+    g = abi.GpuModel(mm, abi.FP64, device=device)
+    try:
+        mm.config["totally_first_step_bool"][0] = 1
+        lay = mm.layout
+        out, bar, grad = (structs.HostStruct(lay, "state") for _ in range(3))
+        w = cap_weights(mm)
+        g.window_forward(mm.state_old, out, dt, n_steps)
+        J = g.sfc_pressure_objective(out, w, bar)
+        g.window_backward(bar, grad)
+        tf, tb = [], []
+        for _ in range(repeats):
+            g.event_record(0)
+            g.window_forward(mm.state_old, out, dt, n_steps)
+            g.event_record(1)
+            g.window_backward(bar, grad)
+            g.event_record(2)
+            g.synchronize()
+            tf.append(g.event_elapsed_ms(0, 1))
+            tb.append(g.event_elapsed_ms(1, 2))
+    finally:
+        g.close()
+    wf, wb = statistics.mean(tf) / n_steps, statistics.mean(tb) / n_steps
+    return {"config": f"RES_ID={res} ({grid_sizes(res)['nc']} cells), 26 layers, dry, 2 km mountain, "
+                      f"{n_steps}-step window, dt={dt:g} s, objective: area-weighted p_sfc^2 over a 20-degree cap",
+            "forward_fused_fp64_ms_per_step": ms_fwd,
+            "window_forward_ms_per_step": wf,
+            "window_backward_ms_per_step": wb,
+            "adjoint_over_forward": wb / ms_fwd,
+            "objective": J,
+            "note": "backward recomputes each step from its checkpoint (both RK stage states kept) and runs the "
+                    "hand-written adjoint kernels; window times include the host-in/host-out copy of one State"}
 
 
 def cpu_baseline(model0, dt, max_seconds=25.0):
@@ -400,6 +465,8 @@ def run_ours(args):
         "clocks": clocks,
         "finite": bool(ok32 and ok64),
     }
+    if not args.no_adjoint:
+        line["adjoint"] = time_adjoint(args.adjoint_res, args.n_lloyd, 12, 200.0, local)
     if world == 1 and not args.no_cpu_baseline:
         sec, n = cpu_baseline(model0, dt)
         line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
@@ -455,6 +522,8 @@ def main():
     ap.add_argument("--dt", type=float, default=100.0)
     ap.add_argument("--n-lloyd", type=int, default=300)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-res", type=int, default=5)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
