@@ -62,6 +62,13 @@ SIGNATURES = {
     "game_gpu_write_out_integral": ([vp, cint, vp], cint),
     "game_gpu_surface_pressure": ([vp, vp, vp], cint),
     "game_gpu_weighted_sums_noalloc": ([vp, cint, ctypes.c_longlong, vp, vp, vp], cint),
+    "grad_adj": ([vp] * 3, cint),
+    "divv_h_adj": ([vp] * 3, cint),
+    "scalar_times_vector_adj": ([vp] * 6, cint),
+    "inner_product_adj": ([vp] * 6, cint),
+    "calc_pot_vort_adj": ([vp] * 7, cint),
+    "vorticity_flux_adj": ([vp] * 7, cint),
+    "three_band_solver_ver_waves_adj": ([vp] * 6 + [dbl, vp, cint, vp, vp, vp], cint),
     "rkhevi_window_forward": ([vp] * 8 + [dbl, cint], cint),
     "rkhevi_window_tl": ([vp, vp], cint),
     "rkhevi_window_backward": ([vp, vp], cint),
@@ -223,6 +230,38 @@ class GpuModel:
     def vorticity_flux(self, flux, pv, out):
         m = self.m
         self._check(self.lib.vorticity_flux(_p(flux), _p(pv), _p(out), m.grid.ptr, m.dualgrid.ptr), "vorticity_flux")
+
+    # -- operator adjoints (bars of inputs accumulated)
+    def grad_adj(self, out_bar, in_bar):
+        self._check(self.lib.grad_adj(_p(out_bar), _p(in_bar), self.m.grid.ptr), "grad_adj")
+
+    def divv_h_adj(self, out_bar, in_bar):
+        self._check(self.lib.divv_h_adj(_p(out_bar), _p(in_bar), self.m.grid.ptr), "divv_h_adj")
+
+    def scalar_times_vector_adj(self, s, v, out_bar, s_bar, v_bar):
+        self._check(self.lib.scalar_times_vector_adj(_p(s), _p(v), _p(out_bar), _p(s_bar), _p(v_bar),
+                                                     self.m.grid.ptr), "scalar_times_vector_adj")
+
+    def inner_product_adj(self, a, b, out_bar, a_bar, b_bar):
+        self._check(self.lib.inner_product_adj(_p(a), _p(b), _p(out_bar), _p(a_bar), _p(b_bar), self.m.grid.ptr),
+                    "inner_product_adj")
+
+    def calc_pot_vort_adj(self, wind, rho, pv_bar, wind_bar, rho_bar):
+        m = self.m
+        self._check(self.lib.calc_pot_vort_adj(_p(wind), _p(rho), _p(pv_bar), _p(wind_bar), _p(rho_bar), m.grid.ptr,
+                                               m.dualgrid.ptr), "calc_pot_vort_adj")
+
+    def vorticity_flux_adj(self, flux, pv, out_bar, flux_bar, pv_bar):
+        m = self.m
+        self._check(self.lib.vorticity_flux_adj(_p(flux), _p(pv), _p(out_bar), _p(flux_bar), _p(pv_bar), m.grid.ptr,
+                                                m.dualgrid.ptr), "vorticity_flux_adj")
+
+    def three_band_solver_ver_waves_adj(self, s_old, s_new, tend, dt, rk, so_bar, sn_bar, st_bar):
+        m = self.m
+        self._check(self.lib.three_band_solver_ver_waves_adj(s_old.ptr, s_new.ptr, tend.ptr, m.diagnostics.ptr,
+                                                             m.forcings.ptr, m.config.ptr, dt, m.grid.ptr, rk,
+                                                             so_bar.ptr, sn_bar.ptr, st_bar.ptr),
+                    "three_band_solver_ver_waves_adj")
 
     # -- adjoint / tangent-linear windows (dry build)
     def window_forward(self, s_init, s_final, dt, n_steps):

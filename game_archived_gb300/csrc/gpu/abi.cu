@@ -12,6 +12,7 @@
 #include "ops.h"
 #include "substeps.h"
 #include "adj.h"
+#include "adj_ops.h"
 
 using namespace game;
 
@@ -966,6 +967,137 @@ int game_gpu_sfc_pressure_objective(struct state *state, const double *weights, 
     if (upload_field(weights, w, c->map_s, c->nc, c->nc)) return -1;
     if (adj_objective(c, &b.st, w, objective, state_bar ? b.sn.dev : nullptr)) return -1;
     if (state_bar) return adj_download(state_bar, &b.sn, b.sn.dev);
+    return finish();
+}
+
+/* ------------------------------------------------- operator adjoints
+ * Host arrays in the reference layout.  Bars of a forward's inputs are
+ * accumulated (x_bar += (dy/dx)^T y_bar); bars of its outputs are read. */
+static int up(const double *h, double *d, const int *map, long long n) { return upload_field(h, d, map, n, n); }
+static int down(double *h, const double *d, const int *map, long long n) { return download_field(h, d, map, n, n, 0, n); }
+
+int grad_adj(double *out_field_bar, double *in_field_bar, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    double *ob = c->sub.vec[0], *ib = c->sub.vec[1];
+    if (up(out_field_bar, ob, c->map_vec, c->nv) || up(in_field_bar, ib, c->map_s, c->ns)) return -1;
+    op_grad_adj(c, ob, ib);
+    if (down(in_field_bar, ib, c->map_s, c->ns)) return -1;
+    return finish();
+}
+
+int divv_h_adj(double *out_field_bar, double *in_field_bar, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    double *ob = c->sub.vec[0], *ib = c->sub.vec[1];
+    if (up(out_field_bar, ob, c->map_s, c->ns) || up(in_field_bar, ib, c->map_vec, c->nv)) return -1;
+    op_divv_adj(c, ob, ib);
+    if (down(in_field_bar, ib, c->map_vec, c->nv)) return -1;
+    return finish();
+}
+
+int scalar_times_vector_adj(double *scalar_field, double *vector_field, double *out_field_bar,
+                            double *scalar_field_bar, double *vector_field_bar, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    double **v = c->sub.vec;
+    if (up(scalar_field, v[0], c->map_s, c->ns) || up(vector_field, v[1], c->map_vec, c->nv)
+        || up(out_field_bar, v[2], c->map_vec, c->nv) || up(scalar_field_bar, v[3], c->map_s, c->ns)
+        || up(vector_field_bar, v[4], c->map_vec, c->nv))
+        return -1;
+    op_stv_adj(c, v[0], v[1], v[2], v[3], v[4]);
+    if (down(scalar_field_bar, v[3], c->map_s, c->ns) || down(vector_field_bar, v[4], c->map_vec, c->nv)) return -1;
+    return finish();
+}
+
+int inner_product_adj(double *in_field_0, double *in_field_1, double *out_field_bar, double *in_field_0_bar,
+                      double *in_field_1_bar, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    double **v = c->sub.vec;
+    if (up(in_field_0, v[0], c->map_vec, c->nv) || up(in_field_1, v[1], c->map_vec, c->nv)
+        || up(out_field_bar, v[2], c->map_s, c->ns) || up(in_field_0_bar, v[3], c->map_vec, c->nv)
+        || up(in_field_1_bar, v[4], c->map_vec, c->nv))
+        return -1;
+    op_inner_adj(c, v[0], v[1], v[2], v[3], v[4]);
+    if (down(in_field_0_bar, v[3], c->map_vec, c->nv) || down(in_field_1_bar, v[4], c->map_vec, c->nv)) return -1;
+    return finish();
+}
+
+int calc_pot_vort_adj(double *velocity_field, double *density_field, double *pot_vort_bar,
+                      double *velocity_field_bar, double *density_field_bar, struct grid *grid,
+                      struct dualgrid *dualgrid)
+{
+    (void)dualgrid;
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    double **v = c->sub.vec;
+    double *wind = v[0], *rho = v[1], *rel = v[2], *pv = v[3], *pvb = v[4], *zero_u = v[5], *wb = v[6], *rb = v[7],
+           *trib = v[8];
+    if (up(velocity_field, wind, c->map_vec, c->nv) || up(density_field, rho, c->map_s, c->ns)) return -1;
+    op_rel_vort(c, wind, c->sub.tri, rel);
+    op_pot_vort(c, rel, rho, pv);
+    if (up(pot_vort_bar, pvb, c->map_curl, c->ncurl) || up(velocity_field_bar, wb, c->map_vec, c->nv)
+        || up(density_field_bar, rb, c->map_s, c->ns))
+        return -1;
+    CK(cudaMemsetAsync(zero_u, 0, (size_t)c->nl * c->ne * sizeof(double), c->stream));
+    CK(cudaMemsetAsync(trib, 0, (size_t)c->nl * c->nt * sizeof(double), c->stream));
+    op_pot_vort_adj(c, wind, rho, pv, pvb, zero_u, wb, rb, trib);
+    if (down(velocity_field_bar, wb, c->map_vec, c->nv) || down(density_field_bar, rb, c->map_s, c->ns)) return -1;
+    return finish();
+}
+
+int vorticity_flux_adj(double *mass_flux_density, double *pot_vorticity, double *out_field_bar,
+                       double *mass_flux_density_bar, double *pot_vorticity_bar, struct grid *grid,
+                       struct dualgrid *dualgrid)
+{
+    (void)dualgrid;
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    double **v = c->sub.vec;
+    if (up(mass_flux_density, v[0], c->map_vec, c->nv) || up(pot_vorticity, v[1], c->map_curl, c->ncurl)
+        || up(out_field_bar, v[2], c->map_vec, c->nv) || up(mass_flux_density_bar, v[3], c->map_vec, c->nv)
+        || up(pot_vorticity_bar, v[4], c->map_curl, c->ncurl))
+        return -1;
+    op_vflux_adj(c, v[0], v[1], v[2], v[3], v[4]);
+    if (down(mass_flux_density_bar, v[3], c->map_vec, c->nv) || down(pot_vorticity_bar, v[4], c->map_curl, c->ncurl))
+        return -1;
+    return finish();
+}
+
+int three_band_solver_ver_waves_adj(struct state *state_old, struct state *state_new, struct state *state_tendency,
+                                    struct diagnostics *diagnostics, struct forcings *forcings, struct config *config,
+                                    double delta_t, struct grid *grid, int rk_step, struct state *state_old_bar,
+                                    struct state *state_new_bar, struct state *state_tendency_bar)
+{
+    (void)diagnostics;
+    (void)forcings;
+    if (check_ready(grid)) return -1;
+    if (check_config(config)) return -1;
+    Context *c = ctx();
+    if (c->n_const != 1) return fail("three_band_solver_ver_waves_adj: dry build only (MOISTURE_ON = 0)");
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    if (upload_state(state_old, &b.so) || upload_state(state_new, &b.sn) || upload_state(state_tendency, &b.st))
+        return -1;
+    if (upload_state(state_old_bar, &b.bso) || upload_state(state_new_bar, &b.bsn)
+        || upload_state(state_tendency_bar, &b.bst))
+        return -1;
+    StepParams p = params_from_config(c, config, delta_t);
+    if (adj_waves_backward(c, &b.so, &b.sn, &b.st, p, rk_step, &b.bso, &b.bsn, &b.bst)) return -1;
+    if (download_state(state_old_bar, &b.bso, 31) || download_state(state_new_bar, &b.bsn, 31)
+        || download_state(state_tendency_bar, &b.bst, 31))
+        return -1;
     return finish();
 }
 

@@ -26,6 +26,7 @@
 
 #include "adj_bwd.cuh"
 #include "adj.h"
+#include "adj_ops.h"
 #include "diag.h"
 #include "ops.h"
 
@@ -543,6 +544,67 @@ void adj_add_into(Context *c, double *y, const double *x, long long n)
 {
     ku_axpy<<<nbk(n), 256, 0, c->stream>>>(n, 1.0, x, y);
     c->kernel_launches++;
+}
+
+namespace {
+/* pass-through bars of the column solver: wind_h and the TOA / surface w of
+ * the output are the input's */
+__global__ void ku_waves_passthrough(int nc, int nl, long long nu, double *out_b_w, double *out_b_u, double *in_b_w,
+                                     double *in_b_u)
+{
+    const long long i = gtid();
+    if (i < nc) {
+        in_b_w[i] += out_b_w[i];
+        out_b_w[i] = 0.0;
+        in_b_w[(long long)nl * nc + i] += out_b_w[(long long)nl * nc + i];
+        out_b_w[(long long)nl * nc + i] = 0.0;
+    }
+    if (i < nu) {
+        in_b_u[i] += out_b_u[i];
+        out_b_u[i] = 0.0;
+    }
+}
+}  // namespace
+
+int adj_waves_backward(Context *c, StateMirror *so_m, StateMirror *sn_m, StateMirror *st_m, const StepParams &p, int rk,
+                       StateMirror *so_bar, StateMirror *sn_bar, StateMirror *st_bar)
+{
+    if (ensure_adj(c)) return -1;
+    AdjState *a = c->adj;
+    if (set_params(c, a, p)) return -1;
+    cudaStream_t st = c->stream;
+    const HGrid<double> &g = c->hg64;
+    (void)g;
+    const VGrid &vg = c->vg;
+    const AParams ap = a->ap;
+    const long long ns = a->ns;
+    AState<double> so = view(a, so_m->dev), sn = view(a, sn_m->dev), out = view(a, a->B.sn2);
+    double *wl = a->B.wl[0], *wr = a->B.wr[0], *wl_b = a->Z.wl[0], *wr_b = a->Z.wr[0];
+    /* forward of the solver, keeping its work */
+    fa_waves_layer<double><<<nbk(ns), 256, 0, st>>>(vg, ap, rk, so, sn, st_m->ds.rho, st_m->ds.rhotheta_v, wl);
+    fa_waves_rows<double><<<nbk(a->nwi), 256, 0, st>>>(vg, ap, so, st_m->ds.w, wl, wr);
+    fa_waves_thomas<double><<<nbk(c->nc, 64), 64, 0, st>>>(c->nc, c->nl, a->dden, wr);
+    fa_waves_apply<double><<<nbk(ns), 256, 0, st>>>(vg, ap, so, wl, wr, out);
+    /* bars: the output bar moves to a work block, the input bar starts with
+     * the pass-through fields */
+    double *ob = a->Z.sn2, *ib = sn_bar->dev;
+    ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, ib, ob);
+    cudaMemsetAsync(ib, 0, (size_t)a->nblk * sizeof(double), st);
+    AState<double> out_b = view(a, ob), in_b = view(a, ib), so_b = view(a, so_bar->dev);
+    ku_waves_passthrough<<<nbk(std::max<long long>(a->nu, c->nc)), 256, 0, st>>>(c->nc, c->nl, a->nu, out_b.w,
+                                                                                   out_b.u, in_b.w, in_b.u);
+    cudaMemsetAsync(wl_b, 0, (size_t)WL_N * ns * sizeof(double), st);
+    cudaMemsetAsync(wr_b, 0, (size_t)WR_N * a->nwi * sizeof(double), st);
+    ba_apply_layer<<<nbk(ns), 256, 0, st>>>(vg, so, wl, out, out_b, a->rn_b, a->rtn_b, so_b, wl_b);
+    ba_apply_w<<<nbk(a->nwi), 256, 0, st>>>(vg, so, wr, out, out_b, a->rn_b, so_b, wr_b);
+    ba_apply_rho<<<nbk(ns), 256, 0, st>>>(vg, ap, wr, a->rn_b, a->rtn_b, wl_b, wr_b);
+    ba_thomas<<<nbk(c->nc, 64), 64, 0, st>>>(c->nc, c->nl, a->dden, wr, wr_b);
+    ba_waves_rows<<<nbk(a->nwi), 256, 0, st>>>(vg, ap, so, wl, wr, wr_b, wl_b, so_b, st_bar->ds.w);
+    ba_waves_layer<<<nbk(ns), 256, 0, st>>>(vg, ap, rk, so, sn, st_m->ds.rho, st_m->ds.rhotheta_v, wl, wl_b, so_b,
+                                            in_b, st_bar->ds.rho, st_bar->ds.rhotheta_v);
+    c->kernel_launches += 12;
+    CK(cudaGetLastError());
+    return 0;
 }
 
 long long adj_block_len(Context *c) { return 4 * c->ns + (long long)(c->nl + 1) * c->nc + (long long)c->nl * c->ne; }

@@ -575,7 +575,7 @@ int ensure_sub_buffers(Context *c)
     Context::SubBuffers &b = c->sub;
     if (b.ready) return 0;
     const size_t NS = (size_t)c->ns, nvec = (size_t)std::max<long long>(c->nv, c->ncurl);
-    for (StateMirror *m : {&b.so, &b.sn, &b.st}) {
+    for (StateMirror *m : {&b.so, &b.sn, &b.st, &b.bso, &b.bsn, &b.bst}) {
         m->dev = dalloc<double>(c, (size_t)c->state_len);
         if (!m->dev) return fail("device allocation of the sub-step buffers failed");
         set_mirror_views(c, *m);

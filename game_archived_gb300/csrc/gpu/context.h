@@ -116,6 +116,7 @@ struct Context {
     struct SubBuffers {
         bool ready = false;
         StateMirror so, sn, st;
+        StateMirror bso, bsn, bst; /* bars of the adjoint entry points */
         double *vec[10] = {}; /* each max(Vt, curl field) */
         double *temperature = nullptr, *cp_ice = nullptr, *cp_water = nullptr, *theta = nullptr;
         double *pt_rates = nullptr; /* 5 S */

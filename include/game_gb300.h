@@ -221,6 +221,41 @@ int game_gpu_surface_pressure(struct state *state, double *surface_p, double *ms
  * state_bar (nonzero on the lowest layer's rho, theta_v_pert, exner_pert).
  *
  * Dry build only (MOISTURE_ON = 0): other builds return an error. */
+/* Adjoints of the single operators, the reverse half of each forward/backward
+ * pair.  Host arrays in the reference layouts of the forward call.  Bars of
+ * the forward's inputs are accumulated (in_bar += (d out / d in)^T out_bar),
+ * the bar of its output is read; operators that are not linear also take the
+ * forward's inputs, the point of linearisation.  Entries of an output the
+ * forward does not write (the TOA and surface w of grad and
+ * scalar_times_vector) carry no bar.  No counterpart in the reference. */
+/* gradient_operators.c:66 (grad) */
+int grad_adj(double *out_field_bar, double *in_field_bar, struct grid *grid);
+/* divergences.c:14 (divv_h) */
+int divv_h_adj(double *out_field_bar, double *in_field_bar, struct grid *grid);
+/* multiplications.c:35 (scalar_times_vector) */
+int scalar_times_vector_adj(double *scalar_field, double *vector_field, double *out_field_bar,
+                            double *scalar_field_bar, double *vector_field_bar, struct grid *grid);
+/* inner_product.c:13 (inner_product; with both inputs the wind it is the kinetic energy) */
+int inner_product_adj(double *in_field_0, double *in_field_1, double *out_field_bar, double *in_field_0_bar,
+                      double *in_field_1_bar, struct grid *grid);
+/* vorticities.c:18 (calc_pot_vort): bar of diagnostics->pot_vort (curl layout) */
+int calc_pot_vort_adj(double *velocity_field, double *density_field, double *pot_vort_bar,
+                      double *velocity_field_bar, double *density_field_bar, struct grid *grid,
+                      struct dualgrid *dualgrid);
+/* vorticity_flux.c:16 (vorticity_flux) */
+int vorticity_flux_adj(double *mass_flux_density, double *pot_vorticity, double *out_field_bar,
+                       double *mass_flux_density_bar, double *pot_vorticity_bar, struct grid *grid,
+                       struct dualgrid *dualgrid);
+/* column_solvers.c:19 (three_band_solver_ver_waves, dry build): the adjoint
+ * of the column solve with its tridiagonal elimination.  state_new_bar holds
+ * on entry the bar of the state_new the forward returns and on return the bar
+ * of the state_new it receives (fields the solver does not write pass their
+ * bars through); state_old_bar and state_tendency_bar are accumulated. */
+int three_band_solver_ver_waves_adj(struct state *state_old, struct state *state_new, struct state *state_tendency,
+                                    struct diagnostics *diagnostics, struct forcings *forcings, struct config *config,
+                                    double delta_t, struct grid *grid, int rk_step, struct state *state_old_bar,
+                                    struct state *state_new_bar, struct state *state_tendency_bar);
+
 int rkhevi_window_forward(struct state *state_init, struct state *state_final, struct grid *grid,
                           struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,
                           struct irreversible_quantities *irrev, struct config *config, double delta_t, int n_steps);
