@@ -75,6 +75,12 @@ StepParams params_from_config(Context *c, const void *config, double dt)
     p.inv_dt = 1.0 / dt;
     p.k_rows = 1.0 / (p.impl_thermo_weight * dt * dt * C_D_P);
     p.k_rows2 = 0.5 / (p.impl_thermo_weight * dt * C_D_P);
+    p.cur_hor = 0.5 + p.impl_thermo_weight;
+    p.old_hor = 1.0 - (0.5 + p.impl_thermo_weight);
+    p.cur_ver = 1.0 - p.impl_thermo_weight;
+    p.cur_hor_f = (float)p.cur_hor;
+    p.old_hor_f = (float)p.old_hor;
+    p.cur_ver_f = (float)p.cur_ver;
     return p;
 }
 

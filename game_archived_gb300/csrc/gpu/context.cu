@@ -498,6 +498,9 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     for (auto &b : c->owned)
         if (!b.p) return fail("device allocation failed");
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     CK(cudaDeviceSynchronize());
     CK(cudaGetLastError());
     return 0;
@@ -535,6 +538,9 @@ int destroy_context()
     for (auto &kv : c->states) cudaFree(kv.second.dev);
     for (auto &b : c->owned) cudaFree(b.p);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
     g_ctx = nullptr;
     return 0;

@@ -54,6 +54,8 @@ struct Context {
     int precision = PREC_FP64;
     int resident = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;                   /* second branch of the step */
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr; /* fork / join of the branches */
 
     /* host struct offsets (bytes) */
     size_t off_grid_z_vector = 0;

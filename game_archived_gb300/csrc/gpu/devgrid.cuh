@@ -115,7 +115,13 @@ struct StepParams {
     /* derived on the host for the mixed path: 1/dt, 1/(w dt^2 c_p), 0.5/(w dt c_p)
      * with w the implicit thermodynamic weight */
     double inv_dt, k_rows, k_rows2;
+    /* pressure-gradient weights of the momentum tendencies
+     * (vector_tendencies_expl.c:79-83): 0.5 + w, 1 - (0.5 + w), 1 - w, in
+     * double and rounded to float */
+    double cur_hor, old_hor, cur_ver;
+    float cur_hor_f, old_hor_f, cur_ver_f, pad_f;
 };
-static_assert(sizeof(StepParams) == 4 * sizeof(int) + 11 * sizeof(double), "StepParams has padding");
+static_assert(sizeof(StepParams) == 4 * sizeof(int) + 14 * sizeof(double) + 4 * sizeof(float),
+              "StepParams has padding");
 
 }  // namespace game

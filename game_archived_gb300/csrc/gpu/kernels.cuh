@@ -788,9 +788,12 @@ __global__ void k_momentum_h(HGrid<R> g, StepParams p, SView<R> sv, double *u_ne
         pvt = pvt_h[i];
         v2g = v2g_h[i];
     }
-    const R cur_hor = R(0.5 + p.impl_thermo_weight), old_hor = R(1.0 - (0.5 + p.impl_thermo_weight));
+    constexpr bool F = sizeof(R) == sizeof(float);
+    const R cur_hor = F ? R(p.cur_hor_f) : R(p.cur_hor), old_hor = F ? R(p.old_hor_f) : R(p.old_hor);
     R y = old_hor * pgo - cur_hor * P + pvt - R(0.5) * v2g;
-    double t = (new_w == 1.0) ? double(y) : old_w * tend_u[i] + new_w * double(y);
+    /* the pressure gradient is recomputed in substage 0 only, where the new
+     * weight is 1 */
+    double t = PG ? double(y) : old_w * tend_u[i] + new_w * double(y);
     tend_u[i] = t;
     const double un = u_old[i] + p.dt * t;
     u_new[i] = un;
@@ -850,9 +853,9 @@ __global__ void k_momentum_v(HGrid<R> g, StepParams p, SView<R> sv, double *tend
     R d_up = sv.rho[p.n_cond * ns + up] / density_total_r(sv.rho, p.n_const, ns, up) - R(1);
     R d_lo = sv.rho[p.n_cond * ns + lo] / density_total_r(sv.rho, p.n_const, ns, lo) - R(1);
     R pgc = (R(0.5) * (d_up + d_lo)) * g.gravity_m_v[i];
-    const R cur_ver = R(1.0 - p.impl_thermo_weight);
+    const R cur_ver = sizeof(R) == sizeof(float) ? R(p.cur_ver_f) : R(p.cur_ver);
     R y = -cur_ver * P + pvt - R(0.5) * v2g + pgc;
-    double t = (new_w == 1.0) ? double(y) : old_w * tend_w[i] + new_w * double(y);
+    double t = PG ? double(y) : old_w * tend_w[i] + new_w * double(y);
     tend_w[i] = t;
 }
 

@@ -82,24 +82,36 @@ inline Views<float> views<float>(Context *c, StateMirror *sn)
 }
 
 template <typename R, bool ADV, bool PG>
-static void launch_momentum(Context *c, const StepParams &p, const Views<R> &v, StateMirror *so, StateMirror *sn,
-                            StateMirror *st, double new_w, double old_w)
+static void launch_momentum_v(Context *c, const StepParams &p, const Views<R> &v, StateMirror *st, double new_w,
+                              double old_w)
 {
     HGrid<R> &g = hgrid<R>(c);
     Work<R> &w = work<R>(c);
-    const int bs = 256;
-    {
-        ProfScope ps(c, "k_momentum_v");
-        k_momentum_v<R, ADV, PG><<<nblocks((long long)(c->nl + 1) * c->nc, bs), bs, 0, c->stream>>>(
-            g, p, v.sv, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w);
-    }
-    {
-        ProfScope ps(c, "k_momentum_h");
-        k_momentum_h<R, ADV, PG><<<nblocks((long long)c->nl * c->ne, bs), bs, 0, c->stream>>>(
-            g, p, v.sv, sn->ds.u, v.sh.u, so->ds.u, st->ds.u, w.P_h, w.pg_old_h, w.pvt_h, w.v2g_h, w.flux_h, w.flux_v,
-            w.zh, w.zv, w.v2, new_w, old_w);
-    }
-    c->kernel_launches += 2;
+    ProfScope ps(c, "k_momentum_v");
+    k_momentum_v<R, ADV, PG><<<nblocks((long long)(c->nl + 1) * c->nc, 256), 256, 0, c->stream>>>(
+        g, p, v.sv, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w);
+    c->kernel_launches++;
+}
+
+template <typename R, bool ADV, bool PG>
+static void launch_momentum_h(Context *c, const StepParams &p, const Views<R> &v, StateMirror *so, StateMirror *sn,
+                              StateMirror *st, double new_w, double old_w)
+{
+    HGrid<R> &g = hgrid<R>(c);
+    Work<R> &w = work<R>(c);
+    ProfScope ps(c, "k_momentum_h");
+    k_momentum_h<R, ADV, PG><<<nblocks((long long)c->nl * c->ne, 256), 256, 0, c->stream>>>(
+        g, p, v.sv, sn->ds.u, v.sh.u, so->ds.u, st->ds.u, w.P_h, w.pg_old_h, w.pvt_h, w.v2g_h, w.flux_h, w.flux_v,
+        w.zh, w.zv, w.v2, new_w, old_w);
+    c->kernel_launches++;
+}
+
+template <typename R, bool ADV, bool PG>
+static void launch_momentum(Context *c, const StepParams &p, const Views<R> &v, StateMirror *so, StateMirror *sn,
+                            StateMirror *st, double new_w, double old_w)
+{
+    launch_momentum_v<R, ADV, PG>(c, p, v, st, new_w, old_w);
+    launch_momentum_h<R, ADV, PG>(c, p, v, so, sn, st, new_w, old_w);
 }
 
 /* implicit vertical sound waves (column_solvers.c:19-383) */
@@ -141,38 +153,31 @@ void launch_waves(Context *c, const StepParams &p, StateMirror *so, StateMirror 
 template <bool EXACT>
 void launch_tracers(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st, int rk,
                     const Shadow &sh, const double *temperature, const double *cp_ice, const double *cp_water,
-                    double *sed_heat)
+                    double *sed_heat, cudaStream_t strm = nullptr)
 {
     if (c->n_const <= 1) return;
+    if (!strm) strm = c->stream;
     const long long ns = c->ns;
     TracerWork tw{cp_ice, cp_water, c->inv_vol};
     if (c->nl == NL_FIXED) {
         if (rk == 0) {
             ProfScope ps(c, "k_tracers_sedheat");
-            k_tracers_sedheat<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, temperature,
+            k_tracers_sedheat<EXACT><<<nblocks(ns, 256), 256, 0, strm>>>(c->vg, p, so->ds, sn->ds, temperature,
                                                                              tw, sed_heat);
             c->kernel_launches++;
         }
         ProfScope ps(c, "k_tracers_solve");
-        k_tracers_solve<NL_FIXED, EXACT><<<nblocks((long long)(c->n_const - 1) * c->nc, 64), 64, 0, c->stream>>>(
+        k_tracers_solve<NL_FIXED, EXACT><<<nblocks((long long)(c->n_const - 1) * c->nc, 64), 64, 0, strm>>>(
             c->vg, p, so->ds, sn->ds, st->ds, tw, sh.rho);
     } else {
         ProfScope ps(c, "k_vertical_tracers");
-        k_vertical_tracers<<<nblocks(c->nc, 128), 128, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, temperature,
+        k_vertical_tracers<<<nblocks(c->nc, 128), 128, 0, strm>>>(c->vg, p, so->ds, sn->ds, st->ds, temperature,
                                                                       sed_heat, rk);
     }
     c->kernel_launches++;
 }
 
-template <bool EXACT>
-void launch_vertical(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st, int rk,
-                     const Shadow &sh)
-{
-    launch_waves<EXACT>(c, p, so, sn, st, rk, sh);
-    launch_tracers<EXACT>(c, p, so, sn, st, rk, sh, c->temperature, c->cp_ice, c->cp_water, c->sed_heat);
-}
-
-/* the kernel sequence of one step; everything on c->stream */
+/* the kernel sequence of one step on c->stream (and c->stream2 for the tracer branch) */
 template <typename R>
 void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st)
 {
@@ -205,6 +210,15 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
     }
     c->kernel_launches++;
     const R *rho_gas = v.sv.rho + (long long)c->n_cond * ns;
+    /* Substage 0's tracer solve (FP64-bound) and substage 1's advection and
+     * horizontal momentum (FP32, memory-bound) read and write disjoint
+     * fields: the tracer solve runs on a second stream (a parallel branch of
+     * the captured graph) and joins before substage 1's vertical momentum,
+     * whose condensate term reads the tracer densities.  Serial while
+     * profiling, and for the generic layer count (its shadow refresh reads
+     * every density). */
+    const bool fork = c->n_const > 1 && !c->profiling && c->nl == NL_FIXED;
+    bool join_pending = false;
     for (int rk = 0; rk < 2; ++rk) {
         const bool adv = rk == 1 || p.first_step;
         const double new_w = rk == 1 ? 0.5 : 1.0, old_w = 1.0 - new_w;
@@ -224,9 +238,19 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             }
             c->kernel_launches += 3;
         }
-        if (rk == 0 && adv) launch_momentum<R, true, true>(c, p, v, so, sn, st, new_w, old_w);
-        else if (rk == 0) launch_momentum<R, false, true>(c, p, v, so, sn, st, new_w, old_w);
-        else launch_momentum<R, true, false>(c, p, v, so, sn, st, new_w, old_w);
+        if (rk == 0 && adv) {
+            launch_momentum<R, true, true>(c, p, v, so, sn, st, new_w, old_w);
+        } else if (rk == 0) {
+            launch_momentum<R, false, true>(c, p, v, so, sn, st, new_w, old_w);
+        } else {
+            launch_momentum_h<R, true, false>(c, p, v, so, sn, st, new_w, old_w);
+            if (join_pending) {
+                cudaEventRecord(c->ev_join, c->stream2);
+                cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+                join_pending = false;
+            }
+            launch_momentum_v<R, true, false>(c, p, v, st, new_w, old_w);
+        }
         {
             ProfScope ps(c, "k_theta");
             k_theta<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(c->nl, c->nc, c->n_cond, v.sv, theta);
@@ -238,7 +262,16 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
                                                                         c->inv_vol, rk);
         }
         c->kernel_launches += 2;
-        launch_vertical<EXACT>(c, p, so, sn, st, rk, v.sh);
+        launch_waves<EXACT>(c, p, so, sn, st, rk, v.sh);
+        if (rk == 0 && fork) {
+            cudaEventRecord(c->ev_fork, c->stream);
+            cudaStreamWaitEvent(c->stream2, c->ev_fork, 0);
+            launch_tracers<EXACT>(c, p, so, sn, st, rk, v.sh, c->temperature, c->cp_ice, c->cp_water, c->sed_heat,
+                                  c->stream2);
+            join_pending = true;
+        } else {
+            launch_tracers<EXACT>(c, p, so, sn, st, rk, v.sh, c->temperature, c->cp_ice, c->cp_water, c->sed_heat);
+        }
         if (!EXACT && c->nl != NL_FIXED && c->n_const > 1) {
             /* the generic tracer sweep does not write the shadow: refresh it */
             const long long n_rho = (long long)c->n_const * ns, nw = (long long)(c->nl + 1) * c->nc,

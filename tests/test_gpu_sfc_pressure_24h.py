@@ -14,6 +14,7 @@ import pytest
 
 from game_archived_gb300 import abi, cases, driver, structs, tables
 from game_archived_gb300.ops import CAbiOps
+from helpers import state_errors
 
 pytestmark = pytest.mark.gpu
 
@@ -34,16 +35,26 @@ def _initial_model():
     return m
 
 
+SNAPSHOTS = (1, 72, STEPS)
+
+
 def _run(m0, precision):
     m = structs.Model(m0.layout)
     for k in structs.Model.KINDS:
         getattr(m, k).copy_from(getattr(m0, k))
     g = abi.GpuModel(m, precision, resident=True, graphs=True)
+    snaps = {}
+
+    def snapshot(i, model):
+        if i + 1 in SNAPSHOTS:
+            g.sync_to_host(model.state_new)
+            snaps[i + 1] = model.state_new.clone()
+
     try:
         for s in (m.state_old, m.state_new, m.state_tendency):
             g.sync_to_device(s)
         mass0 = g.write_out_integral(m.state_old, 0)
-        driver.run(m, STEPS, DT, g.linear_combine_two_states, g.manage_rkhevi)
+        driver.run(m, STEPS, DT, g.linear_combine_two_states, g.manage_rkhevi, callback=snapshot)
         g.synchronize()
         ps = g.surface_pressure(m.state_new)
         mass = g.write_out_integral(m.state_new, 0)
@@ -51,14 +62,19 @@ def _run(m0, precision):
         finite = bool(np.isfinite(m.state_new["rho"]).all() and np.isfinite(m.state_new["wind"]).all())
     finally:
         g.close()
-    return ps, mass0, mass, finite
+    return ps, mass0, mass, finite, snaps
 
 
 def test_mixed_surface_pressure_within_0p1_pa_after_24h():
     m0 = _initial_model()
-    ps64, mass0_64, mass64, ok64 = _run(m0, abi.FP64)
-    ps32, mass0_32, mass32, ok32 = _run(m0, abi.MIXED)
+    ps64, mass0_64, mass64, ok64, sn64 = _run(m0, abi.FP64)
+    ps32, mass0_32, mass32, ok32, sn32 = _run(m0, abi.MIXED)
     assert ok64 and ok32
+    # per-field error of the mixed path against the FP64 path (max |diff| / max |fp64|)
+    for n in SNAPSHOTS:
+        e = state_errors(sn32[n], sn64[n], m0.layout)
+        print(f"mixed vs FP64 after {n} steps: " + ", ".join(f"{k} {v:.2e}" for k, v in e.items()))
+        assert max(e.values()) < 1e-2, (n, e)
     err = np.abs(ps32 - ps64)
     print(f"24 h surface pressure: max |mixed - fp64| = {err.max():.4g} Pa, rms {np.sqrt(np.mean(err ** 2)):.4g} Pa, "
           f"p_sfc range {ps64.min():.1f}..{ps64.max():.1f} Pa")
