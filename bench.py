@@ -184,10 +184,10 @@ class ClockSampler:
 MOUNTAIN = (2000.0, 1.5e6, 30.0, 90.0)   # 2 km Gaussian mountain, 1500 km half-width, 30N 90E
 
 
-def build_model(res, moist, n_lloyd, pinned, mountain=None):
+def build_model(res, moist, n_lloyd, pinned, mountain=None, n_layers=L):
     from game_archived_gb300 import abi, cases, structs, tables
-    tab = tables.GridTables(res, n_lloyd=n_lloyd, mountain=mountain)
-    lay = structs.Layout(res, L, moist)
+    tab = tables.GridTables(res, n_layers=n_layers, n_lloyd=n_lloyd, mountain=mountain)
+    lay = structs.Layout(res, n_layers, moist)
     m = abi.pinned_model(lay) if pinned else structs.Model(lay)
     tables.fill_grid(tab, m.grid, m.dualgrid)
     cases.default_config(m)
@@ -212,10 +212,10 @@ def measured_peak():
 
 
 # ------------------------------------------------------------------ GPU arm
-def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, profile=False):
+def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, profile=False, column_solver=0):
     from game_archived_gb300 import abi, driver
     m = copy_model(model0, pinned=False)
-    g = abi.GpuModel(m, precision, resident=True, graphs=True, device=device)
+    g = abi.GpuModel(m, precision, resident=True, graphs=True, device=device, column_solver=column_solver)
     try:
         for s in (m.state_old, m.state_new, m.state_tendency):
             g.sync_to_device(s)
@@ -476,6 +476,51 @@ def run_ours(args):
     barrier(world)
 
 
+COLUMN_SOLVERS = {0: "auto", 1: "sweeps", 2: "pcr"}
+SOLVER_KERNELS = ("k_waves_thomas", "k_tracers_solve", "k_tracers_sedheat", "k_vertical_tracers")
+
+
+STUDY = ((6, 26, (0, 2)), (6, 64, (1, 2)), (6, 128, (1, 2)),
+         (5, 128, (1, 2)), (4, 128, (0, 1, 2)), (4, 256, (0, 1, 2)), (3, 256, (1, 2)))
+
+
+def column_study(args):
+    """Column solvers against grid size and layer count (--column-study): the
+    headline workload (moist jet) at the (RES_ID, layers) pairs of STUDY, each
+    with registers (per-thread Thomas sweep in registers, 26 layers), sweeps
+    (per-thread sweep in local memory, any other count), pcr (warp-
+    cooperative parallel cyclic reduction) and, where it is a mix of the two,
+    auto (the library's default choice); dt = --dt up to 128 layers and
+    shortened in proportion above.  One JSON line per (grid, layers, solver,
+    precision): device-resident steps/s and the per-step time of the
+    vertical-solver kernels from the profiled pass."""
+    from game_archived_gb300 import abi, cases
+    from game_archived_gb300.ops import CAbiOps
+    _, _, local = dist_env()
+    for res, nl, solvers in STUDY:
+        dt = args.dt * min(1.0, 128.0 / nl)
+        tab, m = build_model(res, 1, args.n_lloyd, pinned=False, n_layers=nl)
+        g = abi.GpuModel(m, abi.FP64, device=local)
+        try:
+            cases.build_initial_state(m, tab, "jet_moist", CAbiOps(g.lib, m))
+        finally:
+            g.close()
+        for solver in solvers:
+            for prec, name in ((abi.MIXED, "mixed"), (abi.FP64, "fp64")):
+                ms, launches, _, prof, ok = time_resident(m, prec, args.steps, args.warmup, dt, local,
+                                                          profile=True, column_solver=solver)
+                total = sum(v[0] for v in prof.values())
+                solve = {k: prof[k][0] / args.steps for k in SOLVER_KERNELS if k in prof}
+                print(json.dumps({
+                    "study": "column solvers", "res": res, "columns": grid_sizes(res)["nc"], "layers": nl,
+                    "solver": "registers" if (solver == 0 and nl == L) else COLUMN_SOLVERS[solver],
+                    "precision": name, "dt": dt,
+                    "steps_per_s": 1000.0 / ms, "ms_per_step": ms, "steps": args.steps,
+                    "vertical_solver_ms_per_step_profiled": solve,
+                    "vertical_solver_share": sum(solve.values()) * args.steps / total,
+                    "gpu_launches": int(launches), "finite": bool(ok)}), flush=True)
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -524,10 +569,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--adjoint-res", type=int, default=5)
+    ap.add_argument("--column-study", action="store_true",
+                    help="time the column solvers at 26, 64 and 128 layers instead of the headline line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.column_study:
+        column_study(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -17,6 +17,7 @@ SIGNATURES = {
     "game_gpu_set_precision": ([cint], cint),
     "game_gpu_set_resident": ([cint], cint),
     "game_gpu_set_graphs": ([cint], cint),
+    "game_gpu_set_column_solver": ([cint], cint),
     "game_gpu_sync_to_device": ([vp], cint),
     "game_gpu_sync_to_host": ([vp], cint),
     "game_gpu_sync_aux_to_host": ([vp, vp, vp], cint),
@@ -96,7 +97,7 @@ class GpuError(RuntimeError):
 class GpuModel:
     """The CUDA library bound to a Model."""
 
-    def __init__(self, model, precision=FP64, resident=False, graphs=True, device=None):
+    def __init__(self, model, precision=FP64, resident=False, graphs=True, device=None, column_solver=0):
         self.lib = native.gpu()
         self.m = model
         lay = model.layout
@@ -104,9 +105,14 @@ class GpuModel:
             self._check(self.lib.game_gpu_set_device(device), "game_gpu_set_device")
         self._check(self.lib.game_gpu_init(lay.res_id, lay.n_layers, lay.moisture_on, model.grid.ptr,
                                            model.dualgrid.ptr), "game_gpu_init")
-        self._check(self.lib.game_gpu_set_precision(precision), "set_precision")
-        self._check(self.lib.game_gpu_set_resident(1 if resident else 0), "set_resident")
-        self._check(self.lib.game_gpu_set_graphs(1 if graphs else 0), "set_graphs")
+        try:
+            self._check(self.lib.game_gpu_set_precision(precision), "set_precision")
+            self._check(self.lib.game_gpu_set_resident(1 if resident else 0), "set_resident")
+            self._check(self.lib.game_gpu_set_graphs(1 if graphs else 0), "set_graphs")
+            self._check(self.lib.game_gpu_set_column_solver(column_solver), "set_column_solver")
+        except GpuError:
+            self.lib.game_gpu_finalize()
+            raise
         self.resident = resident
 
     def _check(self, rc, what):

@@ -139,7 +139,7 @@ int run_device_step(Context *c, const StepParams &p, StateMirror *so, StateMirro
         c->temperature_from_step = 1;
         return 0;
     }
-    Context::GraphKey key{p, c->precision, so, sn, st};
+    Context::GraphKey key{p, c->precision, c->column_solver, so, sn, st};
     auto it = c->graphs.find(key);
     if (it == c->graphs.end()) {
         const int before = c->kernel_launches;
@@ -197,6 +197,16 @@ int game_gpu_set_resident(int resident)
 {
     if (check_ready(nullptr)) return -1;
     ctx()->resident = resident ? 1 : 0;
+    return 0;
+}
+
+int game_gpu_set_column_solver(int mode)
+{
+    if (check_ready(nullptr)) return -1;
+    if (mode < 0 || mode > 2)
+        return fail("column solver mode must be 0 (by layer count and precision), 1 (per-thread Thomas sweeps) or 2 "
+                    "(warp cyclic reduction)");
+    ctx()->column_solver = mode;
     return 0;
 }
 

@@ -31,6 +31,7 @@ const char *last_error() { return g_err.c_str(); }
 bool Context::GraphKey::operator<(const GraphKey &o) const
 {
     if (prec != o.prec) return prec < o.prec;
+    if (solver != o.solver) return solver < o.solver;
     if (so != o.so) return so < o.so;
     if (sn != o.sn) return sn < o.sn;
     if (st != o.st) return st < o.st;
@@ -177,7 +178,7 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     c->ncurl = d.n_curl;
     /* State members rho .. temperature_soil, contiguous in the reference struct */
     c->state_len = (long long)(c->n_const + 3) * c->ns + c->nv + (long long)d.n_soil * d.n_cells;
-    if (n_layers > 64) return fail("more than 64 layers are not supported by the column solvers");
+    if (n_layers > 256) return fail("more than 256 layers are not supported by the column solvers");
     const int NC = c->nc, NE = c->ne, NT = c->nt, L = n_layers;
     const long long VPL = (long long)NC + NE, DPL = (long long)NE + NT, NS = c->ns, NV = c->nv;
 

@@ -130,7 +130,7 @@ struct Context {
      * flag), the precision and the three state mirrors */
     struct GraphKey {
         StepParams p;
-        int prec;
+        int prec, solver;
         const void *so, *sn, *st;
         bool operator<(const GraphKey &o) const;
     };
@@ -147,6 +147,7 @@ struct Context {
     /* grid terms of the mixed-path sound-wave rows [6][L-1][Nc] */
     double *wv_geo = nullptr;
     int use_graphs = 1;
+    int column_solver = 0; /* 0 by layer count, 1 per-thread sweeps, 2 warp cyclic reduction */
     int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */
     long long h2d_bytes = 0, d2h_bytes = 0;
 

@@ -17,8 +17,8 @@
  *                       -> horizontal tendency and wind update
  *   k_momentum_v        the same for w at the interfaces
  *   k_scalar_tend       mass / rho*theta_v flux divergences -> tendencies
- *   k_vertical_waves    implicit vertical sound-wave column solve
- *   k_vertical_tracers  implicit vertical tracer advection column solve
+ * The implicit vertical column solves (sound waves, tracer advection and
+ * sedimentation) are in solvers.cuh.
  */
 #pragma once
 
@@ -1087,103 +1087,8 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
     }
 }
 
-/* ------------------------------------------------------- column solvers
- * src/time_stepping/column_solvers.c, one column per thread, FP64 */
+/* per-thread column sweeps of the adjoint hold at most this many layers */
 constexpr int MAX_L = 64;
-
-/* tridiagonal solve (column_solvers.c:641-669); c, e: sub/super diagonal,
- * solution written over r */
-__device__ __forceinline__ void thomas(const double *cv, const double *dv, const double *ev, double *rv, int n)
-{
-    double ep[MAX_L];
-    ep[0] = ev[0] / dv[0];
-    for (int j = 1; j < n - 1; ++j) ep[j] = ev[j] / (dv[j] - ep[j - 1] * cv[j - 1]);
-    rv[0] = rv[0] / dv[0];
-    for (int j = 1; j < n; ++j) rv[j] = (rv[j] - rv[j - 1] * cv[j - 1]) / (dv[j] - ep[j - 1] * cv[j - 1]);
-    for (int j = n - 2; j >= 0; --j) rv[j] = rv[j] - ep[j] * rv[j + 1];
-}
-
-/* vertical advection and sedimentation of every constituent except the main
- * gas (column_solvers.c:385-639); one thread per column, constituents in the
- * reference's order because the sedimentation heat accumulates over them */
-__global__ void k_vertical_tracers(VGrid vg, StepParams p, DState so, DState sn, DState st, const double *temperature,
-                                   double *sed_heat, int rk)
-{
-    const int i = (int)gtid();
-    if (i >= vg.nc) return;
-    const int nl = vg.nl, nc = vg.nc, cond = p.n_cond;
-    const long long ns = (long long)nl * nc;
-    const double dt = p.dt, iw = 0.5, ew = 1.0 - iw;
-    const long long bot = i + ns - nc;
-    const double a_sfc = vg.area_v[(long long)nl * nc + i];
-    for (int k = 0; k < p.n_const; ++k) {
-        if (k == cond) continue;
-        double vsink = 0.0;
-        bool has_sink = false;
-        if (k < cond / 4) { vsink = p.snow_velocity; has_sink = true; }
-        else if (k < cond / 2) { vsink = p.rain_velocity; has_sink = true; }
-        else if (k < cond) { vsink = p.cloud_velocity; has_sink = true; }
-        double cvec[MAX_L], dvec[MAX_L], evec[MAX_L], rvec[MAX_L], fi[MAX_L], fr[MAX_L], fe[MAX_L];
-        const double *ro = so.rho + k * ns;
-        for (int j = 0; j < nl - 1; ++j) {
-            if (rk == 0 && k == 0) sed_heat[(long long)j * nc + i] = 0.0;
-            const long long b = i + (long long)j * nc, lo = b + nc, wi = i + (long long)(j + 1) * nc;
-            double a_ = so.w[wi], b_ = sn.w[wi];
-            if (has_sink) { a_ -= vsink; b_ -= vsink; }
-            const double ar = vg.area_v[wi];
-            a_ = ar * a_;
-            b_ = ar * b_;
-            double dio, tio;
-            if (b_ >= 0.0) { dio = ro[lo]; tio = temperature[lo]; }
-            else { dio = ro[b]; tio = temperature[b]; }
-            fi[j] = a_;
-            fr[j] = dio * b_;
-            fe[j] = c_p_cond(k, tio) * tio * fr[j];
-        }
-        if (rk == 0 && k == 0) sed_heat[(long long)(nl - 1) * nc + i] = 0.0;
-        for (int j = 0; j < nl - 1; ++j) {
-            const long long b = i + (long long)j * nc;
-            if (fi[j] >= 0.0) { cvec[j] = 0.0; evec[j] = -iw * dt / vg.volume[b] * fi[j]; }
-            else { cvec[j] = iw * dt / vg.volume[b + nc] * fi[j]; evec[j] = 0.0; }
-        }
-        for (int j = 0; j < nl; ++j) {
-            const long long b = i + (long long)j * nc;
-            const double vol = vg.volume[b];
-            if (j == 0) {
-                dvec[j] = fi[0] >= 0.0 ? 1.0 : 1.0 - iw * dt / vol * fi[0];
-            } else if (j == nl - 1) {
-                dvec[j] = fi[j - 1] >= 0.0 ? 1.0 + iw * dt / vol * fi[j - 1] : 1.0;
-                if (has_sink) dvec[j] += iw * vsink * dt * a_sfc / vol;
-            } else {
-                dvec[j] = 1.0;
-                if (fi[j - 1] >= 0.0) dvec[j] += iw * dt / vol * fi[j - 1];
-                if (fi[j] < 0.0) dvec[j] -= iw * dt / vol * fi[j];
-            }
-            rvec[j] = ro[b] + dt * st.rho[k * ns + b];
-            if (j == 0) {
-                rvec[j] += ew * dt * fr[j] / vol;
-                if (rk == 0 && k < cond) sed_heat[b] += fe[j] / vol;
-            } else if (j == nl - 1) {
-                rvec[j] += -ew * dt * fr[j - 1] / vol;
-                if (rk == 0 && k < cond) sed_heat[b] += -fe[j - 1] / vol;
-                if (has_sink) {
-                    rvec[j] += -ew * vsink * dt * ro[bot] * a_sfc / vol;
-                    if (rk == 0)
-                        sed_heat[b] += -vsink * temperature[bot] * c_p_cond(k, temperature[bot]) * ro[bot] * a_sfc / vol;
-                }
-            } else {
-                rvec[j] += ew * dt * (-fr[j - 1] + fr[j]) / vol;
-                if (rk == 0 && k < cond) sed_heat[b] += (-fe[j - 1] + fe[j]) / vol;
-            }
-        }
-        thomas(cvec, dvec, evec, rvec, nl);
-        for (int j = 0; j < nl; ++j) {
-            double v = rvec[j];
-            if (v < 0.0) v = 0.0;
-            sn.rho[k * ns + i + (long long)j * nc] = v;
-        }
-    }
-}
 
 }  // namespace
 }  // namespace game

@@ -256,14 +256,15 @@ __global__ void k_waves_thomas(int nc, WavesWork ww)
     }
 }
 
-/* generic layer count: the sweep in local memory */
-template <bool EXACT>
+/* generic layer count (nl - 1 <= CAP): the sweep in local memory, FP64
+ * divisions on both paths */
+template <int CAP, bool EXACT>
 __global__ void k_waves_thomas_any(int nc, int nl, WavesWork ww)
 {
     const int i = (int)gtid();
     if (i >= nc) return;
     const int n = nl - 1;
-    double ep[MAX_L], rp[MAX_L];
+    double ep[CAP], rp[CAP];
     for (int j = 0; j < n; ++j) {
         const long long q = (long long)j * nc + i;
         const double dj = ww.d[q], rj = ww.r[q];
@@ -355,12 +356,15 @@ __device__ __forceinline__ double sink_velocity(const StepParams &p, int k, bool
 }
 
 /* vertical advection + sedimentation of constituent k in one column
- * (column_solvers.c:398-635); thread = (k-slot, column) */
-template <int NL, bool EXACT>
+ * (column_solvers.c:398-635); thread = (k-slot, column).  NL > 0: the layer
+ * count is a compile-time constant and the sweep stays in registers; NL = 0:
+ * the layer count is vg.nl (at most CAP) and the sweep lives in local memory */
+template <int NL, int CAP, bool EXACT>
 __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DState st, TracerWork tw, float *sh_rho)
 {
     const int nc = vg.nc;
-    const long long ns = (long long)NL * nc;
+    const int nl = NL > 0 ? NL : vg.nl;
+    const long long ns = (long long)nl * nc;
     const long long q = gtid();
     const int n_tr = p.n_const - 1;
     if (q >= (long long)n_tr * nc) return;
@@ -372,11 +376,11 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
     const double *ro = so.rho + k * ns;
     const double *tr = st.rho + k * ns;
     const long long bot = i + ns - nc;
-    const double a_sfc = vg.area_v[(long long)NL * nc + i];
-    double ep[NL], rp[NL];
+    const double a_sfc = vg.area_v[(long long)nl * nc + i];
+    double ep[NL > 0 ? NL : CAP], rp[NL > 0 ? NL : CAP];
     double fi_prev = 0.0, fr_prev = 0.0, c_prev = 0.0;
 #pragma unroll
-    for (int j = 0; j < NL; ++j) {
+    for (int j = 0; j < nl; ++j) {
         const long long b = i + (long long)j * nc;
         const double vol = EXACT ? vg.volume[b] : 0.0;
         /* mixed path: implicit and explicit weights are both 1/2, so every
@@ -384,7 +388,7 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
         const double g = EXACT ? 0.0 : half_dt * tw.inv_vol[b];
         /* flux at interface j (below layer j) */
         double fi = 0.0, fr = 0.0, cj = 0.0, ej = 0.0;
-        if (j < NL - 1) {
+        if (j < nl - 1) {
             const long long wi = b + nc;
             double a_ = so.w[wi], b_ = sn.w[wi];
             if (has_sink) {
@@ -411,7 +415,7 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
             if (j == 0) {
                 dj = fi >= 0.0 ? 1.0 : 1.0 - iw * dt / vol * fi;
                 rj += ew * dt * fr / vol;
-            } else if (j == NL - 1) {
+            } else if (j == nl - 1) {
                 dj = fi_prev >= 0.0 ? 1.0 + iw * dt / vol * fi_prev : 1.0;
                 if (has_sink) dj += iw * vsink * dt * a_sfc / vol;
                 rj += -ew * dt * fr_prev / vol;
@@ -426,7 +430,7 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
             if (j == 0) {
                 dj = fi >= 0.0 ? 1.0 : 1.0 - g * fi;
                 rj += g * fr;
-            } else if (j == NL - 1) {
+            } else if (j == nl - 1) {
                 dj = fi_prev >= 0.0 ? 1.0 + g * fi_prev : 1.0;
                 rj -= g * fr_prev;
                 if (has_sink) {
@@ -452,11 +456,11 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
         } else {
             const double den = dj - ep[j - 1] * c_prev;
             if (EXACT) {
-                if (j < NL - 1) ep[j] = ej / den;
+                if (j < nl - 1) ep[j] = ej / den;
                 rp[j] = (rj - rp[j - 1] * c_prev) / den;
             } else {
                 const double inv = rcp_nr<2>(den);
-                if (j < NL - 1) ep[j] = ej * inv;
+                if (j < nl - 1) ep[j] = ej * inv;
                 rp[j] = (rj - rp[j - 1] * c_prev) * inv;
             }
         }
@@ -466,14 +470,14 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
     }
     double *rn = sn.rho + k * ns;
     float *rs = sh_rho ? sh_rho + k * ns : nullptr;
-    double x = rp[NL - 1];
+    double x = rp[nl - 1];
     {
         const double v = x < 0.0 ? 0.0 : x;
-        rn[(long long)(NL - 1) * nc + i] = v;
-        if (rs) rs[(long long)(NL - 1) * nc + i] = float(v);
+        rn[(long long)(nl - 1) * nc + i] = v;
+        if (rs) rs[(long long)(nl - 1) * nc + i] = float(v);
     }
 #pragma unroll
-    for (int j = NL - 2; j >= 0; --j) {
+    for (int j = nl - 2; j >= 0; --j) {
         x = rp[j] - ep[j] * x;
         const double v = x < 0.0 ? 0.0 : x;
         rn[(long long)j * nc + i] = v;
@@ -524,6 +528,220 @@ __global__ void k_tracers_sedheat(VGrid vg, StepParams p, DState so, DState sn, 
         }
     }
     sed_heat[b] = sh;
+}
+
+
+/* ------------------------------------------------ deep columns: warp PCR
+ * One warp solves one tridiagonal system a_j x_{j-1} + b_j x_j + c_j x_{j+1}
+ * = d_j (j < n, a_0 = c_{n-1} = 0) by parallel cyclic reduction (Hockney and
+ * Jesshope): in step s = 1, 2, 4, ... every row eliminates its couplings at
+ * distance s with the rows j - s and j + s, so after ceil(log2 n) steps row j
+ * reads x_j = d_j.  Rows are kept normalised to b_j = 1, one reciprocal per
+ * row and step (an FP64 division on the FP64 path, a Newton-refined
+ * reciprocal on the mixed path).
+ * A block holds PCR_WARPS systems of neighbouring columns.  Its threads load
+ * and store the rows cooperatively, PCR_WARPS consecutive columns of one row
+ * per group of threads, so that the [layer][cell] accesses fill whole
+ * sectors; warp w then reduces system w in shared memory, double-buffered
+ * (one __syncwarp per step), lane l handling rows l, l + 32, ....
+ * Shared memory: 6 n doubles per system, 48 KB per block at n = 256. */
+constexpr int PCR_MAX_ROWS = 256;
+constexpr int PCR_WARPS = 4; /* systems (warps) per block */
+static_assert(PCR_WARPS * 6 * PCR_MAX_ROWS * sizeof(double) <= 48 * 1024, "PCR block exceeds 48 KB");
+
+template <bool EXACT>
+__device__ __forceinline__ double pcr_inv(double b)
+{
+    return EXACT ? 1.0 / b : rcp_nr<2>(b);
+}
+
+/* reduction steps for n rows: ceil(log2 n) */
+__device__ __forceinline__ int pcr_steps(int n)
+{
+    int s = 0;
+    for (int st = 1; st < n; st <<= 1) ++s;
+    return s;
+}
+
+/* s: [a | c | d] of n normalised rows followed by the second buffer; the
+ * solution ends in d of buffer pcr_steps(n) & 1 */
+template <bool EXACT>
+__device__ __forceinline__ void pcr_warp(double *s, int n)
+{
+    const int lane = threadIdx.x & 31;
+    double *cur = s, *nxt = s + 3 * n;
+    for (int st = 1; st < n; st <<= 1) {
+        const double *a = cur, *c = cur + n, *d = cur + 2 * n;
+        for (int j = lane; j < n; j += 32) {
+            double an = 0.0, cn = 0.0, bn = 1.0, dn = d[j];
+            if (j - st >= 0) {
+                const double k = a[j];
+                an = -k * a[j - st];
+                bn -= k * c[j - st];
+                dn -= k * d[j - st];
+            }
+            if (j + st < n) {
+                const double k = c[j];
+                cn = -k * c[j + st];
+                bn -= k * a[j + st];
+                dn -= k * d[j + st];
+            }
+            const double r = pcr_inv<EXACT>(bn);
+            nxt[j] = an * r;
+            nxt[n + j] = cn * r;
+            nxt[2 * n + j] = dn * r;
+        }
+        __syncwarp();
+        double *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+}
+
+__device__ __forceinline__ const double *pcr_solution(const double *s, int n)
+{
+    return s + (pcr_steps(n) & 1) * 3 * n + 2 * n;
+}
+
+/* sound waves: the rows of k_waves_rows(_mixed) of PCR_WARPS neighbouring
+ * columns, solution divided by the damping denominator into r */
+template <bool EXACT>
+__global__ void __launch_bounds__(32 * PCR_WARPS) k_waves_pcr(int nc, int nl, WavesWork ww)
+{
+    extern __shared__ double smem[];
+    const int n = nl - 1;
+    const int t = threadIdx.x, warp = t >> 5, sys = t % PCR_WARPS, row0 = t / PCR_WARPS;
+    const int i0 = blockIdx.x * PCR_WARPS, i = i0 + sys;
+    double *s = smem + (size_t)sys * 6 * n;
+    if (i < nc)
+        for (int j = row0; j < n; j += 32) {
+            const long long q = (long long)j * nc + i;
+            const double r = pcr_inv<EXACT>(ww.d[q]);
+            s[j] = j > 0 ? ww.c[q - nc] * r : 0.0;
+            s[n + j] = j < n - 1 ? ww.e[q] * r : 0.0;
+            s[2 * n + j] = ww.r[q] * r;
+        }
+    __syncthreads();
+    if (i0 + warp < nc) pcr_warp<EXACT>(smem + (size_t)warp * 6 * n, n);
+    __syncthreads();
+    if (i < nc) {
+        const double *x = pcr_solution(s, n);
+        for (int j = row0; j < n; j += 32) {
+            const long long q = (long long)j * nc + i;
+            ww.r[q] = EXACT ? x[j] / ww.dden[q] : x[j] * ww.damp_inv[q];
+        }
+    }
+}
+
+/* tracers: vertical advection and sedimentation of constituent k (the rows of
+ * k_tracers_solve, column_solvers.c:398-635) for PCR_WARPS consecutive
+ * (k-slot, column) systems, clipped at 0; the sedimentation heat comes from
+ * k_tracers_sedheat.  The interface fluxes are staged in the second buffer,
+ * which the reduction overwrites only after the rows are built. */
+template <bool EXACT>
+__global__ void __launch_bounds__(32 * PCR_WARPS)
+    k_tracers_pcr(VGrid vg, StepParams p, DState so, DState sn, DState st, TracerWork tw, float *sh_rho)
+{
+    extern __shared__ double smem[];
+    const int nc = vg.nc, nl = vg.nl, n = nl;
+    const int t = threadIdx.x, warp = t >> 5, sys = t % PCR_WARPS, row0 = t / PCR_WARPS;
+    const int n_tr = p.n_const - 1;
+    const long long nsys = (long long)n_tr * nc, q0 = (long long)blockIdx.x * PCR_WARPS, q = q0 + sys;
+    const bool valid = q < nsys;
+    const int slot = valid ? (int)(q / nc) : 0, i = valid ? (int)(q - (long long)slot * nc) : 0;
+    const int k = slot < p.n_cond ? slot : slot + 1;
+    const long long ns = (long long)nl * nc;
+    bool has_sink;
+    const double vsink = sink_velocity(p, k, has_sink);
+    const double dt = p.dt, iw = 0.5, ew = 1.0 - iw, half_dt = 0.5 * dt;
+    const double *ro = so.rho + k * ns, *tr = st.rho + k * ns;
+    double *s = smem + (size_t)sys * 6 * n;
+    double *fi = s + 3 * n, *fr = s + 4 * n;
+    /* interface fluxes (below layer j) */
+    if (valid)
+        for (int j = row0; j < n; j += 32) {
+            double a_ = 0.0, f_ = 0.0;
+            if (j < nl - 1) {
+                const long long b = i + (long long)j * nc, wi = b + nc;
+                double wo = so.w[wi], wn = sn.w[wi];
+                if (has_sink) {
+                    wo -= vsink;
+                    wn -= vsink;
+                }
+                const double ar = vg.area_v[wi];
+                a_ = ar * wo;
+                const double b_ = ar * wn;
+                f_ = (b_ >= 0.0 ? ro[b + nc] : ro[b]) * b_;
+            }
+            fi[j] = a_;
+            fr[j] = f_;
+        }
+    __syncthreads();
+    if (valid) {
+        const long long bot = i + ns - nc;
+        const double a_sfc = vg.area_v[(long long)nl * nc + i];
+        for (int j = row0; j < n; j += 32) {
+            const long long b = i + (long long)j * nc;
+            const double fij = j < nl - 1 ? fi[j] : 0.0, fip = j > 0 ? fi[j - 1] : 0.0;
+            const double frj = j < nl - 1 ? fr[j] : 0.0, frp = j > 0 ? fr[j - 1] : 0.0;
+            double aj = 0.0, cj = 0.0, dj, rj = ro[b] + dt * tr[b];
+            if (EXACT) {
+                const double vol = vg.volume[b];
+                if (j > 0 && fip < 0.0) aj = iw * dt / vol * fip;
+                if (j < nl - 1 && fij >= 0.0) cj = -iw * dt / vol * fij;
+                if (j == 0) {
+                    dj = fij >= 0.0 ? 1.0 : 1.0 - iw * dt / vol * fij;
+                    rj += ew * dt * frj / vol;
+                } else if (j == nl - 1) {
+                    dj = fip >= 0.0 ? 1.0 + iw * dt / vol * fip : 1.0;
+                    if (has_sink) dj += iw * vsink * dt * a_sfc / vol;
+                    rj += -ew * dt * frp / vol;
+                    if (has_sink) rj += -ew * vsink * dt * ro[bot] * a_sfc / vol;
+                } else {
+                    dj = 1.0;
+                    if (fip >= 0.0) dj += iw * dt / vol * fip;
+                    if (fij < 0.0) dj -= iw * dt / vol * fij;
+                    rj += ew * dt * (-frp + frj) / vol;
+                }
+            } else {
+                const double g = half_dt * tw.inv_vol[b];
+                if (j > 0 && fip < 0.0) aj = g * fip;
+                if (j < nl - 1 && fij >= 0.0) cj = -g * fij;
+                if (j == 0) {
+                    dj = fij >= 0.0 ? 1.0 : 1.0 - g * fij;
+                    rj += g * frj;
+                } else if (j == nl - 1) {
+                    dj = fip >= 0.0 ? 1.0 + g * fip : 1.0;
+                    rj -= g * frp;
+                    if (has_sink) {
+                        const double gs = g * vsink * a_sfc;
+                        dj += gs;
+                        rj -= gs * ro[bot];
+                    }
+                } else {
+                    dj = 1.0 + (fip >= 0.0 ? g * fip : 0.0) - (fij < 0.0 ? g * fij : 0.0);
+                    rj += g * (frj - frp);
+                }
+            }
+            const double r = pcr_inv<EXACT>(dj);
+            s[j] = aj * r;
+            s[n + j] = cj * r;
+            s[2 * n + j] = rj * r;
+        }
+    }
+    __syncthreads();
+    if (q0 + warp < nsys) pcr_warp<EXACT>(smem + (size_t)warp * 6 * n, n);
+    __syncthreads();
+    if (valid) {
+        const double *x = pcr_solution(s, n);
+        double *rn = sn.rho + k * ns;
+        float *rs = sh_rho ? sh_rho + k * ns : nullptr;
+        for (int j = row0; j < n; j += 32) {
+            const double v = x[j] < 0.0 ? 0.0 : x[j];
+            rn[i + (long long)j * nc] = v;
+            if (rs) rs[i + (long long)j * nc] = float(v);
+        }
+    }
 }
 
 }  // namespace

@@ -28,9 +28,29 @@ template <>
 inline Work<float> &work<float>(Context *c) { return c->w32; }
 
 /* the layer count the register-resident column sweeps are compiled for
- * (NO_OF_LAYERS of every GAME configuration); other counts use the generic
- * local-memory sweeps */
+ * (NO_OF_LAYERS of every GAME configuration) */
 constexpr int NL_FIXED = 26;
+/* capacities of the local-memory sweeps for other layer counts */
+constexpr int SWEEP_SMALL = 64, SWEEP_LARGE = 256;
+/* the mixed path solves a batch of fewer systems than this with the warp
+ * cyclic reduction: one thread per system leaves most of the 152 SMs idle
+ * there, while above it the per-thread sweeps, with log2(n) times less FP64
+ * work, are faster (measured on GB300 from 642 to 40962 columns and 64 to 256
+ * layers).  The FP64 path keeps the reference's elimination order at any
+ * depth. */
+constexpr long long PCR_SYSTEMS_BELOW = 6144;
+
+enum { COLUMN_REGISTERS, COLUMN_LOCAL, COLUMN_PCR };
+/* the solver for a batch of n_systems columns (game_gpu_set_column_solver:
+ * 0 chosen by layer count, batch size and precision, 1 per-thread Thomas
+ * sweeps, 2 warp cyclic reduction) */
+inline int column_mode(const Context *c, bool exact, long long n_systems)
+{
+    if (c->column_solver == 2) return COLUMN_PCR;
+    if (c->nl == NL_FIXED) return COLUMN_REGISTERS;
+    if (c->column_solver == 0 && !exact && n_systems < PCR_SYSTEMS_BELOW) return COLUMN_PCR;
+    return COLUMN_LOCAL;
+}
 
 inline WavesWork waves_work(Context *c)
 {
@@ -135,10 +155,16 @@ void launch_waves(Context *c, const StepParams &p, StateMirror *so, StateMirror 
     }
     {
         ProfScope ps(c, "k_waves_thomas");
-        if (c->nl == NL_FIXED)
+        const int mode = column_mode(c, EXACT, c->nc);
+        if (mode == COLUMN_REGISTERS)
             k_waves_thomas<NL_FIXED, EXACT><<<nblocks(c->nc, 64), 64, 0, c->stream>>>(c->nc, ww);
+        else if (mode == COLUMN_LOCAL && c->nl - 1 <= SWEEP_SMALL)
+            k_waves_thomas_any<SWEEP_SMALL, EXACT><<<nblocks(c->nc, 64), 64, 0, c->stream>>>(c->nc, c->nl, ww);
+        else if (mode == COLUMN_LOCAL)
+            k_waves_thomas_any<SWEEP_LARGE, EXACT><<<nblocks(c->nc, 64), 64, 0, c->stream>>>(c->nc, c->nl, ww);
         else
-            k_waves_thomas_any<EXACT><<<nblocks(c->nc, 64), 64, 0, c->stream>>>(c->nc, c->nl, ww);
+            k_waves_pcr<EXACT><<<nblocks(c->nc, PCR_WARPS), 32 * PCR_WARPS,
+                                 (size_t)PCR_WARPS * 6 * (c->nl - 1) * sizeof(double), c->stream>>>(c->nc, c->nl, ww);
     }
     {
         ProfScope ps(c, "k_waves_apply");
@@ -159,21 +185,28 @@ void launch_tracers(Context *c, const StepParams &p, StateMirror *so, StateMirro
     if (!strm) strm = c->stream;
     const long long ns = c->ns;
     TracerWork tw{cp_ice, cp_water, c->inv_vol};
-    if (c->nl == NL_FIXED) {
-        if (rk == 0) {
-            ProfScope ps(c, "k_tracers_sedheat");
-            k_tracers_sedheat<EXACT><<<nblocks(ns, 256), 256, 0, strm>>>(c->vg, p, so->ds, sn->ds, temperature,
-                                                                             tw, sed_heat);
-            c->kernel_launches++;
-        }
-        ProfScope ps(c, "k_tracers_solve");
-        k_tracers_solve<NL_FIXED, EXACT><<<nblocks((long long)(c->n_const - 1) * c->nc, 64), 64, 0, strm>>>(
-            c->vg, p, so->ds, sn->ds, st->ds, tw, sh.rho);
-    } else {
-        ProfScope ps(c, "k_vertical_tracers");
-        k_vertical_tracers<<<nblocks(c->nc, 128), 128, 0, strm>>>(c->vg, p, so->ds, sn->ds, st->ds, temperature,
-                                                                      sed_heat, rk);
+    const long long nsys = (long long)(c->n_const - 1) * c->nc;
+    const int mode = column_mode(c, EXACT, nsys);
+    if (rk == 0) {
+        ProfScope ps(c, "k_tracers_sedheat");
+        k_tracers_sedheat<EXACT><<<nblocks(ns, 256), 256, 0, strm>>>(c->vg, p, so->ds, sn->ds, temperature, tw,
+                                                                         sed_heat);
+        c->kernel_launches++;
     }
+    ProfScope ps(c, "k_tracers_solve");
+    if (mode == COLUMN_REGISTERS)
+        k_tracers_solve<NL_FIXED, NL_FIXED, EXACT><<<nblocks(nsys, 64), 64, 0, strm>>>(c->vg, p, so->ds, sn->ds,
+                                                                                        st->ds, tw, sh.rho);
+    else if (mode == COLUMN_LOCAL && c->nl <= SWEEP_SMALL)
+        k_tracers_solve<0, SWEEP_SMALL, EXACT><<<nblocks(nsys, 64), 64, 0, strm>>>(c->vg, p, so->ds, sn->ds, st->ds,
+                                                                                    tw, sh.rho);
+    else if (mode == COLUMN_LOCAL)
+        k_tracers_solve<0, SWEEP_LARGE, EXACT><<<nblocks(nsys, 64), 64, 0, strm>>>(c->vg, p, so->ds, sn->ds, st->ds,
+                                                                                    tw, sh.rho);
+    else
+        k_tracers_pcr<EXACT><<<nblocks(nsys, PCR_WARPS), 32 * PCR_WARPS,
+                               (size_t)PCR_WARPS * 6 * c->nl * sizeof(double), strm>>>(c->vg, p, so->ds, sn->ds,
+                                                                                       st->ds, tw, sh.rho);
     c->kernel_launches++;
 }
 
@@ -215,9 +248,8 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
      * fields: the tracer solve runs on a second stream (a parallel branch of
      * the captured graph) and joins before substage 1's vertical momentum,
      * whose condensate term reads the tracer densities.  Serial while
-     * profiling, and for the generic layer count (its shadow refresh reads
-     * every density). */
-    const bool fork = c->n_const > 1 && !c->profiling && c->nl == NL_FIXED;
+     * profiling. */
+    const bool fork = c->n_const > 1 && !c->profiling;
     bool join_pending = false;
     for (int rk = 0; rk < 2; ++rk) {
         const bool adv = rk == 1 || p.first_step;
@@ -271,14 +303,6 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             join_pending = true;
         } else {
             launch_tracers<EXACT>(c, p, so, sn, st, rk, v.sh, c->temperature, c->cp_ice, c->cp_water, c->sed_heat);
-        }
-        if (!EXACT && c->nl != NL_FIXED && c->n_const > 1) {
-            /* the generic tracer sweep does not write the shadow: refresh it */
-            const long long n_rho = (long long)c->n_const * ns, nw = (long long)(c->nl + 1) * c->nc,
-                            nu = (long long)c->nl * c->ne;
-            k_make_shadow<<<nblocks(std::max(std::max(n_rho, nw), nu), bs), bs, 0, c->stream>>>(n_rho, ns, nw, nu,
-                                                                                                sn->ds, v.sh);
-            c->kernel_launches++;
         }
     }
 }

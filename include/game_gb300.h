@@ -62,6 +62,16 @@ int game_gpu_finalize(void);
 int game_gpu_set_precision(int precision);
 int game_gpu_set_resident(int resident);
 int game_gpu_set_graphs(int on);
+/* the vertical column solvers (any layer count up to 256): 0 (default) by
+ * layer count, batch size and precision -- per-thread Thomas sweeps (the
+ * reference's elimination order, column_solvers.c:641-669) held in registers
+ * for 26 layers and in local memory otherwise, except that the mixed path
+ * solves a batch of fewer than 6144 columns (the sound-wave solve: one
+ * system per column; the tracer solve: one per constituent and column) of
+ * another layer count with the warp-cooperative parallel cyclic reduction;
+ * 1 per-thread Thomas sweeps; 2 warp cyclic reduction in both precisions (a
+ * different elimination order: the FP64 results move by rounding) */
+int game_gpu_set_column_solver(int mode);
 int game_gpu_sync_to_device(struct state *state);
 int game_gpu_sync_to_host(struct state *state);
 /* writes the library's copies of the lagged step fields back into the host

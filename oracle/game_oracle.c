@@ -24,6 +24,8 @@
 #define R_D 287.057811
 #define R_V 461.524879
 #define N_PENT 12
+/* column arrays of the solvers (the reference sizes them NO_OF_LAYERS) */
+#define ORC_MAX_L 256
 
 #define NC (g->nc)
 #define NE (g->ne)
@@ -840,7 +842,7 @@ int orc_scalar_tendencies_expl(const orc_grid *g, const orc_state *s_old, const 
 static void thomas(const double *cv, const double *dv, const double *ev, const double *rv, double *x, int n)
 {
     /* :641-669 */
-    double ep[64], rp[64];
+    double ep[ORC_MAX_L], rp[ORC_MAX_L];
     ep[0] = ev[0] / dv[0];
     for (int j = 1; j < n - 1; ++j) ep[j] = ev[j] / (dv[j] - ep[j - 1] * cv[j - 1]);
     rp[0] = rv[0] / dv[0];
@@ -854,15 +856,15 @@ int orc_three_band_solver_ver_waves(const orc_grid *g, const orc_state *so, orc_
 {
     /* :19-383 (sensible heat flux and soil off) */
     if (c->sfc_sensible_heat_flux || c->prog_soil_temp) return -1;
-    if (NL > 64) return -2;
+    if (NL > ORC_MAX_L) return -2;
     const double iw = c->impl_thermo_weight;
     const double damp_start = c->damping_start_height_over_toa * g->z_vector[0];
     const double pdw = 0.5;
     const long gp = COND * NS;
     ORC_PAR
     for (long i = 0; i < NC; ++i) {
-        double cvec[64], dvec[64], evec[64], rvec[64], rho_expl[64], rt_expl[64], tp_expl[64], ep_expl[64];
-        double th_int[64], sol[64], rho_io[64], rho_ie[64], alpha[64], beta[64], gam[64];
+        double cvec[ORC_MAX_L], dvec[ORC_MAX_L], evec[ORC_MAX_L], rvec[ORC_MAX_L], rho_expl[ORC_MAX_L], rt_expl[ORC_MAX_L], tp_expl[ORC_MAX_L], ep_expl[ORC_MAX_L];
+        double th_int[ORC_MAX_L], sol[ORC_MAX_L], rho_io[ORC_MAX_L], rho_ie[ORC_MAX_L], alpha[ORC_MAX_L], beta[ORC_MAX_L], gam[ORC_MAX_L];
         for (long j = 0; j < NL; ++j) {
             long b = i + j * NC;
             rho_expl[j] = so->rho[gp + b] + dt * st->rho[gp + b];
@@ -954,7 +956,7 @@ int orc_three_band_solver_gen_densities(const orc_grid *g, const orc_state *so, 
 {
     /* :385-639 */
     const double iw = 0.5, ew = 1.0 - iw;
-    if (NL > 64) return -2;
+    if (NL > ORC_MAX_L) return -2;
     double *sh = ir->condensates_sediment_heat;
     for (int k = 0; k < g->n_const; ++k) {
         if (k == COND) continue;
@@ -966,7 +968,7 @@ int orc_three_band_solver_gen_densities(const orc_grid *g, const orc_state *so, 
         else if (k < COND) { vsink = c->cloud_droplets_velocity; has_sink = 1; }
         ORC_PAR
         for (long i = 0; i < NC; ++i) {
-            double cvec[64], dvec[64], evec[64], rvec[64], fi[64], fr[64], fe[64], sol[64];
+            double cvec[ORC_MAX_L], dvec[ORC_MAX_L], evec[ORC_MAX_L], rvec[ORC_MAX_L], fi[ORC_MAX_L], fr[ORC_MAX_L], fe[ORC_MAX_L], sol[ORC_MAX_L];
             for (long j = 0; j < NL - 1; ++j) {
                 if (rk_step == 0 && k == 0) sh[j * NC + i] = 0.0;
                 long b = i + j * NC, lo = i + (j + 1) * NC, up = b;

@@ -15,13 +15,13 @@ FIELDS = ("rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind")
 
 
 @functools.lru_cache(maxsize=8)
-def grid_tables(res, mountain=False, n_lloyd=200):
-    return tables.GridTables(res, n_lloyd=n_lloyd, mountain=MOUNTAIN if mountain else None)
+def grid_tables(res, mountain=False, n_lloyd=200, n_layers=26):
+    return tables.GridTables(res, n_layers=n_layers, n_lloyd=n_lloyd, mountain=MOUNTAIN if mountain else None)
 
 
-def make_model(res, moist, case, mountain=False, n_lloyd=200):
-    tab = grid_tables(res, mountain, n_lloyd)
-    lay = structs.Layout(res, 26, moist)
+def make_model(res, moist, case, mountain=False, n_lloyd=200, n_layers=26):
+    tab = grid_tables(res, mountain, n_lloyd, n_layers)
+    lay = structs.Layout(res, n_layers, moist)
     m = structs.Model(lay)
     tables.fill_grid(tab, m.grid, m.dualgrid)
     cases.default_config(m)
