@@ -16,6 +16,16 @@ dp = P(ctypes.c_double)
 ip = P(ctypes.c_int)
 
 
+DIAG_FIELDS = ("flux_density", "flux_density_divv", "rel_vort_on_triangles", "rel_vort", "pot_vort", "temperature",
+               "v_squared", "scalar_field_placeholder", "wind_divv", "curl_of_vorticity", "vector_field_placeholder",
+               "n_squared", "dv_hdz")
+IRREV_FIELDS = ("temperature_diffusion_heating", "friction_acc", "heating_diss", "pressure_gradient_decel_factor",
+                "condensates_sediment_heat", "mass_diff_tendency", "phase_trans_rates", "phase_trans_heating_rate",
+                "molecular_diffusion_coeff", "mass_diffusion_coeff_numerical_h", "mass_diffusion_coeff_numerical_v",
+                "temp_diffusion_coeff_numerical_h", "temp_diffusion_coeff_numerical_v", "viscosity", "viscosity_rhombi",
+                "viscosity_triangles", "vert_hor_viscosity", "tke")
+
+
 class OrcGrid(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("nc", "ne", "nt", "nl", "n_oro", "moisture_on", "n_const", "n_cond")] + [
         ("radius", ctypes.c_double)] + [(n, dp) for n in (
@@ -23,7 +33,9 @@ class OrcGrid(ctypes.Structure):
             "exner_bg", "exner_bg_grad", "ipw", "trsk_weights", "rhombi_weights")] + [(n, ip) for n in (
                 "trsk_indices", "trsk_mci", "from_", "to", "adj", "adj_sign", "rhombi_idx", "is_land")] + [
         (n, dp) for n in ("dual_area", "dual_z_vector", "f_vec")] + [
-        (n, ip) for n in ("dual_from", "dual_to", "vort_idx", "vort_sign")] + [("gravity_potential", dp)]
+        (n, ip) for n in ("dual_from", "dual_to", "vort_idx", "vort_sign")] + [("gravity_potential", dp)] + [
+        (n, dp) for n in ("layer_thickness", "dual_normal_distance")] + [
+        (n, ctypes.c_double) for n in ("eff_hor_res", "mean_velocity_area")]
 
 
 class OrcState(ctypes.Structure):
@@ -31,8 +43,7 @@ class OrcState(ctypes.Structure):
 
 
 class OrcDiag(ctypes.Structure):
-    _fields_ = [(n, dp) for n in ("flux_density", "flux_density_divv", "rel_vort_on_triangles", "rel_vort",
-                                  "pot_vort", "temperature", "v_squared", "scalar_field_placeholder")]
+    _fields_ = [(n, dp) for n in DIAG_FIELDS]
 
 
 class OrcForcings(ctypes.Structure):
@@ -41,9 +52,7 @@ class OrcForcings(ctypes.Structure):
 
 
 class OrcIrrev(ctypes.Structure):
-    _fields_ = [(n, dp) for n in ("temperature_diffusion_heating", "friction_acc", "heating_diss",
-                                  "pressure_gradient_decel_factor", "condensates_sediment_heat",
-                                  "mass_diff_tendency", "phase_trans_rates", "phase_trans_heating_rate")]
+    _fields_ = [(n, dp) for n in IRREV_FIELDS]
 
 
 class OrcConfig(ctypes.Structure):
@@ -94,7 +103,8 @@ class Oracle:
                          _i(g["density_to_rhombi_indices"]), _i(g["is_land"]), _d(dg["area"]), _d(dg["z_vector"]),
                          _d(dg["f_vec"]), _i(dg["from_index"]), _i(dg["to_index"]),
                          _i(dg["vorticity_indices_triangles"]), _i(dg["vorticity_signs_triangles"]),
-                         _d(g["gravity_potential"]))
+                         _d(g["gravity_potential"]), _d(g["layer_thickness"]), _d(dg["normal_distance"]),
+                         float(g["eff_hor_res"][0]), float(g["mean_velocity_area"][0]))
         self.lib = lib()
 
     def state(self, s):
@@ -102,8 +112,7 @@ class Oracle:
 
     def diag(self):
         d = self.m.diagnostics
-        return OrcDiag(*[_d(d[n]) for n in ("flux_density", "flux_density_divv", "rel_vort_on_triangles", "rel_vort",
-                                            "pot_vort", "temperature", "v_squared", "scalar_field_placeholder")])
+        return OrcDiag(*[_d(d[n]) for n in DIAG_FIELDS])
 
     def forcings(self):
         f = self.m.forcings
@@ -113,9 +122,7 @@ class Oracle:
 
     def irrev(self):
         r = self.m.irrev
-        return OrcIrrev(*[_d(r[n]) for n in ("temperature_diffusion_heating", "friction_acc", "heating_diss",
-                                             "pressure_gradient_decel_factor", "condensates_sediment_heat",
-                                             "mass_diff_tendency", "phase_trans_rates", "phase_trans_heating_rate")])
+        return OrcIrrev(*[_d(r[n]) for n in IRREV_FIELDS])
 
     def config(self):
         c = self.m.config

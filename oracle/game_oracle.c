@@ -3,8 +3,9 @@
  *
  * CPU restatement of the GAME RKHEVI step with run-time grid sizes.  Every
  * function keeps the reference's order of floating-point operations; build
- * with -ffp-contract=off.  Diffusion, PBL, surface fluxes, soil and radiation
- * are not restated: the step returns -1 if their switches are on.
+ * with -ffp-contract=off.  The diffusion branch (momentum, temperature and
+ * mass diffusion with the TKE scheme) is restated; PBL, surface fluxes, soil
+ * and radiation are not: the step returns -1 if their switches are on.
  */
 #include "game_oracle.h"
 
@@ -754,18 +755,369 @@ int orc_calc_pressure_grad_condensates_v(const orc_grid *g, const orc_state *s, 
     return 0;
 }
 
+/* ------------------------------------------------------ diffusion branch
+ * run at the first RK substep when a diffusion switch is on
+ * (vector_tendencies_expl.c:37-69, scalar_tendencies_expl.c:44-88) */
+#define K_B (1.380649e-23)
+#define EPSILON_SECURITY (1e-10)
+#define ORC_PI 3.14159265358979323846
+#define NDV ((long)(g->nl + 1) * g->ne + (long)g->nl * g->nt)
+
+/* src/spatial_operators/divergences.c:150-185 */
+int orc_add_vertical_divv(const orc_grid *g, const double *in, double *out)
+{
+    ORC_PAR
+    for (long h = 0; h < NC; ++h)
+        for (long l = 0; l < NL; ++l) {
+            long i = l * NC + h;
+            double up, lo;
+            if (l == 0) {
+                up = 0;
+                lo = in[h + (l + 1) * VPL];
+            } else if (l == NL - 1) {
+                up = in[h + l * VPL];
+                lo = 0;
+            } else {
+                up = in[h + l * VPL];
+                lo = in[h + (l + 1) * VPL];
+            }
+            double comp_v = up * g->area[h + l * VPL] - lo * g->area[h + (l + 1) * VPL];
+            out[i] += 1 / g->volume[i] * comp_v;
+        }
+    return 0;
+}
+
+/* molecular diffusion coefficient from kinetic gas theory
+ * (src/constituents/derived_quantities.c:117-134) */
+static double calc_diffusion_coeff(double temperature, double density)
+{
+    double particle_radius = 130e-12;
+    double particle_mass = M_D / N_A;
+    double thermal_velocity = sqrt(8.0 * K_B * temperature / (ORC_PI * particle_mass));
+    double particle_density = density / particle_mass;
+    double cross_section = 4.0 * ORC_PI * pow(particle_radius, 2.0);
+    double mean_free_path = 1.0 / (sqrt(2.0) * particle_density * cross_section);
+    return 1.0 / 3.0 * thermal_velocity * mean_free_path;
+}
+
+/* src/subgrid_scale/effective_diff_coeffs.c:293-303 */
+static double tke2hor_diff_coeff(double tke, double effective_resolution)
+{
+    double mean_velocity = pow(2.0 * tke, 0.5);
+    double mean_free_path = effective_resolution / 6.0;
+    return 1.0 / 6.0 * mean_free_path * mean_velocity;
+}
+
+/* src/subgrid_scale/effective_diff_coeffs.c:305-320 */
+static double tke2vert_diff_coeff(double tke, double n_squared, double layer_thickness)
+{
+    double tke_vert = 3.0 * 1e-3 * tke;
+    double mean_velocity = pow(2.0 * tke_vert, 0.5);
+    double n_used = pow(fmax(n_squared, 1e-4), 0.5);
+    double mean_free_path = pow(2.0 * tke_vert, 0.5) / n_used;
+    mean_free_path = fmin(mean_free_path, layer_thickness);
+    return 1.0 / 6.0 * mean_free_path * mean_velocity;
+}
+
+/* src/subgrid_scale/effective_diff_coeffs.c:233-291.  For the last layer the
+ * reference writes n_squared[NO_OF_SCALARS - NO_OF_SCALARS_H + i] from
+ * vector_field_placeholder[NO_OF_VECTORS - NO_OF_VECTORS_PER_LAYER -
+ * NO_OF_SCALARS_H + i], both past the ends of their arrays: the read lands in
+ * the Diagnostics members after vector_field_placeholder, the write in those
+ * after n_squared, and the last layer of n_squared keeps its value.  The
+ * same accesses are made here on the same struct. */
+int orc_update_n_squared(const orc_grid *g, const orc_state *s, orc_diag *d)
+{
+    double *ph = d->scalar_field_placeholder, *vph = d->vector_field_placeholder;
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) ph[i] = g->theta_v_bg[i] + s->theta_v_pert[i];
+    orc_grad_vert_cov(g, ph, vph);
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) ph[i] = 1.0 / ph[i];
+    orc_scalar_times_vector_v(g, ph, vph, vph);
+    ORC_PAR
+    for (long i = NC; i < (long)(NL + 1) * NC - NC; ++i) {
+        long layer = i / NC, h = i - layer * NC, vi = h + layer * VPL;
+        vph[vi] = g->gravity_m[vi] * vph[vi];
+    }
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) {
+        long layer = i / NC, h = i - layer * NC;
+        if (layer == 0)
+            d->n_squared[i] = vph[VPL + i];
+        else if (layer == NL - 1)
+            d->n_squared[NS - NC + i] = vph[NV - VPL - NC + i];
+        else
+            d->n_squared[i] = g->ipw[8 * i + 6] * vph[h + layer * VPL] + g->ipw[8 * i + 7] * vph[h + (layer + 1) * VPL];
+    }
+    return 0;
+}
+
+/* src/subgrid_scale/tke.c:16-60 */
+int orc_tke_update(const orc_grid *g, orc_irrev *ir, double dt, const orc_state *s, orc_diag *d)
+{
+    orc_grad(g, ir->tke, d->vector_field_placeholder);
+    orc_inner_product(g, d->vector_field_placeholder, s->wind, d->scalar_field_placeholder);
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) {
+        double decay = 8.0 * pow(ORC_PI, 2.0) / g->mean_velocity_area * ir->viscosity[i] / s->rho[COND * NS + i];
+        ir->tke[i] += dt * (-d->scalar_field_placeholder[i] + ir->heating_diss[i] / s->rho[COND * NS + i]
+                            - decay * ir->tke[i]);
+        if (ir->tke[i] < 0.0) ir->tke[i] = 0.0;
+    }
+    return 0;
+}
+
+/* src/subgrid_scale/effective_diff_coeffs.c:19-112: molecular + turbulent
+ * viscosity, averaged to rhombi and triangles and multiplied by the gas
+ * density; the cell values are then replaced by density times the turbulent
+ * part alone */
+int orc_hor_viscosity(const orc_grid *g, const orc_state *s, orc_irrev *ir, const orc_diag *d)
+{
+    const double *rg = &s->rho[COND * NS];
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) {
+        ir->molecular_diffusion_coeff[i] = calc_diffusion_coeff(d->temperature[i], rg[i]);
+        ir->viscosity[i] = ir->molecular_diffusion_coeff[i];
+        ir->viscosity[i] += tke2hor_diff_coeff(ir->tke[i], g->eff_hor_res);
+    }
+    ORC_PAR
+    for (long e = 0; e < NE; ++e)
+        for (long l = 0; l < NL; ++l) {
+            long vi = NC + l * VPL + e, f = l * NC + g->from[e], t = l * NC + g->to[e];
+            ir->viscosity_rhombi[vi] = 0.5 * (ir->viscosity[f] + ir->viscosity[t]);
+            ir->viscosity_rhombi[vi] = 0.5 * (rg[f] + rg[t]) * ir->viscosity_rhombi[vi];
+        }
+    ORC_PAR
+    for (long i = 0; i < (long)NL * NT; ++i) {
+        long layer = i / NT, h = i - layer * NT, sb = layer * NC;
+        const int *vt = &g->vort_idx[3 * h];
+        const double *v = ir->viscosity;
+        ir->viscosity_triangles[i] = 1.0 / 6.0 * (v[sb + g->from[vt[0]]] + v[sb + g->to[vt[0]]] + v[sb + g->from[vt[1]]]
+                                                  + v[sb + g->to[vt[1]]] + v[sb + g->from[vt[2]]] + v[sb + g->to[vt[2]]]);
+        double dens = 1.0 / 6.0 * (rg[sb + g->from[vt[0]]] + rg[sb + g->to[vt[0]]] + rg[sb + g->from[vt[1]]]
+                                   + rg[sb + g->to[vt[1]]] + rg[sb + g->from[vt[2]]] + rg[sb + g->to[vt[2]]]);
+        ir->viscosity_triangles[i] = dens * ir->viscosity_triangles[i];
+    }
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) ir->viscosity[i] = rg[i] * tke2hor_diff_coeff(ir->tke[i], g->eff_hor_res);
+    return 0;
+}
+
+/* src/spatial_operators/momentum_diff_diss.c:207-294 */
+static void hor_calc_curl_of_vorticity(const orc_grid *g, const double *vort, const double *zt, double *out)
+{
+    ORC_PAR
+    for (long i = 0; i < (long)NL * NE; ++i) {
+        long layer = i / NE, h = i - layer * NE, vi = NC + layer * VPL + h;
+        long tt = g->dual_to[h], tf = g->dual_from[h], base = NE + layer * DPL;
+        const double *dn = g->dual_normal_distance;
+        out[vi] = 0.0;
+        double delta_z = 0.0;
+        double zto = zt[layer * NT + tt], zfr = zt[layer * NT + tf];
+        double cdw = fabs(zto - zfr) / (fabs(zto) + fabs(zfr) + EPSILON_SECURITY);
+        for (int j = 0; j < 3; ++j) {
+            out[vi] += +1.0 / 3.0 * (1.0 - cdw)
+                       * (dn[base + tt] * vort[NE + layer * 2 * NE + g->vort_idx[3 * tt + j]]
+                          - dn[base + tf] * vort[NE + layer * 2 * NE + g->vort_idx[3 * tf + j]]);
+            delta_z += 1.0 / 3.0 * (g->z_vector[NC + layer * VPL + g->vort_idx[3 * tt + j]]
+                                    - g->z_vector[NC + layer * VPL + g->vort_idx[3 * tf + j]]);
+        }
+        out[vi] += cdw * (zto * dn[base + tt] - zfr * dn[base + tf]);
+        out[vi] = out[vi] / g->area[vi];
+        if (layer >= NL - g->n_oro) {
+            double delta_x = dn[NDV - NE + h];
+            delta_x = delta_x * (g->radius + g->z_vector[vi]) / g->radius;
+            double tangential_slope = delta_z / delta_x;
+            long uz = NC + (layer - 1) * VPL + h, lz = NC + (layer + 1) * VPL + h;
+            long uzeta = NE + (layer - 1) * 2 * NE + h, lzeta = NE + (layer + 1) * 2 * NE + h;
+            if (layer == 0) {
+                uz = NC + layer * VPL + h;
+                uzeta = NE + layer * 2 * NE + h;
+            }
+            if (layer == NL - 1) {
+                lz = NC + layer * VPL + h;
+                lzeta = NE + layer * 2 * NE + h;
+            }
+            double delta_zeta = vort[uzeta] - vort[lzeta];
+            delta_z = g->z_vector[uz] - g->z_vector[lz];
+            double dzeta_dz = delta_zeta / delta_z;
+            out[vi] -= tangential_slope * dzeta_dz;
+        }
+    }
+}
+
+/* src/spatial_operators/momentum_diff_diss.c:22-80 */
+int orc_hor_momentum_diffusion(const orc_grid *g, const orc_state *s, orc_diag *d, orc_irrev *ir)
+{
+    orc_divv_h(g, s->wind, d->wind_divv);
+    orc_calc_rel_vort(g, s->wind, d);
+    orc_hor_viscosity(g, s, ir, d);
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) d->wind_divv[i] = ir->viscosity[i] * d->wind_divv[i];
+    orc_grad_hor(g, d->wind_divv, d->vector_field_placeholder);
+    ORC_PAR
+    for (long h = 0; h < NE; ++h)
+        for (long l = 0; l < NL; ++l) {
+            long ci = NE + 2 * l * NE + h;
+            d->rel_vort[ci] = ir->viscosity_rhombi[NC + l * VPL + h] * d->rel_vort[ci];
+        }
+    ORC_PAR
+    for (long i = 0; i < (long)NL * NT; ++i)
+        d->rel_vort_on_triangles[i] = ir->viscosity_triangles[i] * d->rel_vort_on_triangles[i];
+    hor_calc_curl_of_vorticity(g, d->rel_vort, d->rel_vort_on_triangles, d->curl_of_vorticity);
+    ORC_PAR
+    for (long h = 0; h < NE; ++h)
+        for (long l = 0; l < NL; ++l) {
+            long vi = NC + l * VPL + h, f = l * NC + g->from[h], t = l * NC + g->to[h];
+            ir->friction_acc[vi] = (d->vector_field_placeholder[vi] - d->curl_of_vorticity[vi])
+                                   / (0.5 * (density_total(g, s, f) + density_total(g, s, t)));
+        }
+    return 0;
+}
+
+/* src/subgrid_scale/effective_diff_coeffs.c:114-168 */
+static void vert_hor_mom_viscosity(const orc_grid *g, const orc_state *s, const orc_diag *d, orc_irrev *ir)
+{
+    const double *rg = &s->rho[COND * NS], *n2 = d->n_squared, *lt = g->layer_thickness, *tke = ir->tke;
+    const double *mol = ir->molecular_diffusion_coeff;
+    ORC_PAR
+    for (long i = 0; i < (long)NL * NE - NE; ++i) {
+        long layer = i / NE, h = i - layer * NE;
+        long f0 = layer * NC + g->from[h], t0 = layer * NC + g->to[h];
+        long f1 = (layer + 1) * NC + g->from[h], t1 = (layer + 1) * NC + g->to[h];
+        double mdc = 0.25 * (tke2vert_diff_coeff(tke[f0], n2[f0], lt[f0]) + tke2vert_diff_coeff(tke[t0], n2[t0], lt[t0])
+                             + tke2vert_diff_coeff(tke[f1], n2[f1], lt[f1]) + tke2vert_diff_coeff(tke[t1], n2[t1], lt[t1]));
+        double molecular_viscosity = 0.25 * (mol[f0] + mol[t0] + mol[f1] + mol[t1]);
+        mdc += molecular_viscosity;
+        ir->vert_hor_viscosity[i + NE] = 0.25 * (rg[f0] + rg[t0] + rg[f1] + rg[t1]) * mdc;
+    }
+    ORC_PAR
+    for (long i = 0; i < NE; ++i) ir->vert_hor_viscosity[i] = ir->vert_hor_viscosity[i + NE];
+    ORC_PAR
+    for (long i = (long)NL * NE; i < (long)NL * NE + NE; ++i) ir->vert_hor_viscosity[i] = ir->vert_hor_viscosity[i - NE];
+}
+
+/* src/subgrid_scale/effective_diff_coeffs.c:170-193 */
+static void vert_vert_mom_viscosity(const orc_grid *g, const orc_state *s, orc_diag *d, const orc_irrev *ir)
+{
+    ORC_PAR
+    for (long h = 0; h < NC; ++h)
+        for (long l = 0; l < NL; ++l) {
+            long i = l * NC + h;
+            double mdc = ir->molecular_diffusion_coeff[i]
+                         + tke2vert_diff_coeff(ir->tke[i], d->n_squared[i], g->layer_thickness[i]);
+            d->scalar_field_placeholder[i] = s->rho[COND * NS + i] * mdc * d->scalar_field_placeholder[i];
+        }
+}
+
+/* src/spatial_operators/momentum_diff_diss.c:82-205.  The TOA row of dv_hdz
+ * is never written (the branch meant for it cannot be reached) and keeps its
+ * values. */
+int orc_vert_momentum_diffusion(const orc_grid *g, const orc_state *s, orc_diag *d, orc_irrev *ir)
+{
+    const double *zv = g->z_vector, *w = s->wind;
+    /* 1. vertical diffusion of horizontal velocity */
+    ORC_PAR
+    for (long i = NE; i < (long)NL * NE + NE; ++i) {
+        long layer = i / NE, h = i - layer * NE, vi = NC + h + (layer - 1) * VPL;
+        if (layer == NL)
+            d->dv_hdz[i] = w[vi] / (zv[vi] - 0.5 * (zv[NV - NC + g->from[h]] + zv[NV - NC + g->to[h]]));
+        else if (layer >= 1)
+            d->dv_hdz[i] = (w[vi] - w[vi + VPL]) / (zv[vi] - zv[vi + VPL]);
+    }
+    vert_hor_mom_viscosity(g, s, d, ir);
+    ORC_PAR
+    for (long i = 0; i < (long)NL * NE; ++i) {
+        long layer = i / NE, h = i - layer * NE, vi = NC + layer * VPL + h;
+        double z_upper = 0.5 * (zv[layer * VPL + g->from[h]] + zv[layer * VPL + g->to[h]]);
+        double z_lower = 0.5 * (zv[(layer + 1) * VPL + g->from[h]] + zv[(layer + 1) * VPL + g->to[h]]);
+        double delta_z = z_upper - z_lower;
+        ir->friction_acc[vi] += (ir->vert_hor_viscosity[i] * d->dv_hdz[i] - ir->vert_hor_viscosity[i + NE] * d->dv_hdz[i + NE])
+                                / delta_z
+                                / (0.5 * (density_total(g, s, layer * NC + g->from[h])
+                                          + density_total(g, s, layer * NC + g->to[h])));
+    }
+    /* 2. vertical diffusion of vertical velocity */
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) d->scalar_field_placeholder[i] = 0.0;
+    orc_add_vertical_divv(g, w, d->scalar_field_placeholder);
+    vert_vert_mom_viscosity(g, s, d, ir);
+    orc_grad_vert_cov(g, d->scalar_field_placeholder, ir->friction_acc);
+    /* 3. horizontal diffusion of vertical velocity */
+    ORC_PAR
+    for (long h = 0; h < NC; ++h)
+        for (long l = 0; l < NL; ++l) {
+            long i = l * NC + h;
+            d->scalar_field_placeholder[i] = g->ipw[8 * i + 6] * w[h + l * VPL] + g->ipw[8 * i + 7] * w[h + (l + 1) * VPL];
+        }
+    orc_grad_hor(g, d->scalar_field_placeholder, d->vector_field_placeholder);
+    ORC_PAR
+    for (long h = 0; h < NE; ++h)
+        for (long l = 0; l < NL; ++l) {
+            long vi = NC + h + l * VPL;
+            d->vector_field_placeholder[vi] = 0.5 * (ir->viscosity[l * NC + g->from[h]] + ir->viscosity[l * NC + g->to[h]])
+                                              * d->vector_field_placeholder[vi];
+        }
+    orc_divv_h(g, d->vector_field_placeholder, d->scalar_field_placeholder);
+    ORC_PAR
+    for (long i = 0; i < (long)(NL + 1) * NC - 2 * NC; ++i) {
+        long layer = i / NC, h = i - layer * NC, vi = h + (layer + 1) * VPL;
+        ir->friction_acc[vi] += 0.5 * (d->scalar_field_placeholder[h + layer * NC]
+                                       + d->scalar_field_placeholder[h + (layer + 1) * NC]);
+        ir->friction_acc[vi] = ir->friction_acc[vi] / (0.5 * (density_total(g, s, h + layer * NC)
+                                                              + density_total(g, s, h + (layer + 1) * NC)));
+    }
+    return 0;
+}
+
+/* src/spatial_operators/momentum_diff_diss.c:296-310 */
+int orc_simple_dissipation_rate(const orc_grid *g, const orc_state *s, orc_irrev *ir)
+{
+    orc_inner_product(g, s->wind, ir->friction_acc, ir->heating_diss);
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) ir->heating_diss[i] = -density_total(g, s, i) * ir->heating_diss[i];
+    return 0;
+}
+
+/* src/subgrid_scale/effective_diff_coeffs.c:195-231 */
+int orc_scalar_diffusion_coeffs(const orc_grid *g, const orc_state *s, const orc_config *c, orc_irrev *ir,
+                                orc_diag *d)
+{
+    if (c->momentum_diff_h == 0) orc_hor_viscosity(g, s, ir, d);
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) {
+        ir->mass_diffusion_coeff_numerical_h[i] = ir->viscosity[i] / s->rho[COND * NS + i];
+        ir->mass_diffusion_coeff_numerical_v[i] = ir->molecular_diffusion_coeff[i]
+                                                  + tke2vert_diff_coeff(ir->tke[i], d->n_squared[i], g->layer_thickness[i]);
+        ir->temp_diffusion_coeff_numerical_h[i] = c_v_mass_weighted_air(g, s, d, i) * ir->mass_diffusion_coeff_numerical_h[i];
+        ir->temp_diffusion_coeff_numerical_v[i] = c_v_mass_weighted_air(g, s, d, i) * ir->mass_diffusion_coeff_numerical_v[i];
+    }
+    return 0;
+}
+
 /* ------------------------------------------------- explicit tendencies
  * src/time_stepping/vector_tendencies_expl.c:18-133 */
 int orc_vector_tendencies_expl(const orc_grid *g, const orc_state *s, orc_state *tend, orc_diag *d,
                                orc_forcings *f, orc_irrev *ir, const orc_config *c, int rk_step, double dt)
 {
-    (void)dt;
     if (rk_step == 1 || c->totally_first_step_bool == 1) {
         orc_scalar_times_vector(g, &s->rho[COND * NS], s->wind, d->flux_density);
         orc_calc_pot_vort(g, s->wind, &s->rho[COND * NS], d);
         orc_vorticity_flux(g, d->flux_density, d->pot_vort, f->pot_vort_tend);
         orc_inner_product(g, s->wind, s->wind, d->v_squared);
         orc_grad(g, d->v_squared, f->v_squared_grad);
+    }
+    /* momentum diffusion and dissipation (:37-69) */
+    if (rk_step == 0) {
+        if (c->momentum_diff_h || c->mass_diff_h || c->temperature_diff_h) {
+            orc_update_n_squared(g, s, d);
+            orc_tke_update(g, ir, dt, s, d);
+        }
+        if (c->momentum_diff_h) orc_hor_momentum_diffusion(g, s, d, ir);
+        if (c->momentum_diff_v) orc_vert_momentum_diffusion(g, s, d, ir);
+        if (c->pbl_scheme > 0) return -1;
+        if (c->momentum_diff_h) orc_simple_dissipation_rate(g, s, ir);
     }
     double new_w = rk_step == 1 ? 0.5 : 1.0, old_w = 1.0 - new_w;
     double cur_hor = 0.5 + c->impl_thermo_weight, old_hor = 1.0 - cur_hor, cur_ver = 1.0 - c->impl_thermo_weight;
@@ -787,7 +1139,7 @@ int orc_vector_tendencies_expl(const orc_grid *g, const orc_state *s, orc_state 
     return 0;
 }
 
-/* src/time_stepping/scalar_tendencies_expl.c:17-181 (diffusion off) */
+/* src/time_stepping/scalar_tendencies_expl.c:17-181 */
 int orc_scalar_tendencies_expl(const orc_grid *g, const orc_state *s_old, const orc_state *s, orc_state *tend,
                                double dt, orc_diag *d, orc_forcings *f, orc_irrev *ir, const orc_config *c,
                                int rk_step)
@@ -799,7 +1151,33 @@ int orc_scalar_tendencies_expl(const orc_grid *g, const orc_state *s_old, const 
         if (rk_step == 1 && k != COND) new_w[k] = 0.5;
         old_w[k] = 1.0 - new_w[k];
     }
-    if (c->mass_diff_h || c->temperature_diff_h) return -1;
+    /* diffusion coefficients, temperature and mass diffusion (:44-88) */
+    if (rk_step == 0 && (c->mass_diff_h || c->temperature_diff_h)) orc_scalar_diffusion_coeffs(g, s, c, ir, d);
+    if (c->temperature_diff_h && rk_step == 0) {
+        orc_grad(g, d->temperature, d->vector_field_placeholder);
+        orc_scalar_times_vector_h(g, ir->temp_diffusion_coeff_numerical_h, d->vector_field_placeholder,
+                                  d->flux_density);
+        orc_divv_h(g, d->flux_density, ir->temperature_diffusion_heating);
+        if (c->temperature_diff_v) {
+            orc_scalar_times_vector_v(g, ir->temp_diffusion_coeff_numerical_v, d->vector_field_placeholder,
+                                      d->flux_density);
+            orc_add_vertical_divv(g, d->flux_density, ir->temperature_diffusion_heating);
+        }
+    }
+    if (c->mass_diff_h && rk_step == 0) {
+        for (int k = 0; k < g->n_const; ++k) {
+            long shift = k * NS;
+            orc_grad(g, &s->rho[shift], d->vector_field_placeholder);
+            orc_scalar_times_vector_h(g, ir->mass_diffusion_coeff_numerical_h, d->vector_field_placeholder,
+                                      d->vector_field_placeholder);
+            orc_divv_h(g, d->vector_field_placeholder, &ir->mass_diff_tendency[shift]);
+            if (c->mass_diff_v) {
+                orc_scalar_times_vector_v(g, ir->mass_diffusion_coeff_numerical_v, d->vector_field_placeholder,
+                                          d->vector_field_placeholder);
+                orc_add_vertical_divv(g, d->vector_field_placeholder, &ir->mass_diff_tendency[shift]);
+            }
+        }
+    }
     for (int k = 0; k < g->n_const; ++k) {
         long shift = k * NS, shift_pt = shift;
         if (g->moisture_on && k == COND + 1) shift_pt = shift - NS;
@@ -1038,8 +1416,7 @@ int orc_manage_rkhevi(const orc_grid *g, const orc_state *so, orc_state *sn, orc
                       orc_forcings *f, orc_irrev *ir, const orc_config *c, double dt, double t)
 {
     (void)t;
-    if (c->sfc_sensible_heat_flux || c->sfc_phase_trans || c->pbl_scheme || c->rad_on || c->momentum_diff_h
-        || c->momentum_diff_v || c->mass_diff_h || c->temperature_diff_h || c->prog_soil_temp)
+    if (c->sfc_sensible_heat_flux || c->sfc_phase_trans || c->pbl_scheme || c->rad_on || c->prog_soil_temp)
         return -1;
     orc_temperature_diagnostics(g, so, d);
     if (g->moisture_on) orc_calc_h2otracers_source_rates(g, so, d, c, ir, dt);

@@ -28,15 +28,23 @@ typedef struct orc_grid {
     const double *dual_area, *dual_z_vector, *f_vec;
     const int *dual_from, *dual_to, *vort_idx, *vort_sign;
     const double *gravity_potential; /* only the output metrics use it */
+    /* diffusion branch */
+    const double *layer_thickness, *dual_normal_distance;
+    double eff_hor_res, mean_velocity_area;
 } orc_grid;
 
 typedef struct orc_state {
     double *rho, *rhotheta_v, *theta_v_pert, *exner_pert, *wind;
 } orc_state;
 
+/* pointers into one Diagnostics struct laid out as the reference's: the
+ * diffusion branch reproduces out-of-range accesses of the reference that land
+ * in the members following n_squared and vector_field_placeholder */
 typedef struct orc_diag {
     double *flux_density, *flux_density_divv, *rel_vort_on_triangles, *rel_vort, *pot_vort;
     double *temperature, *v_squared, *scalar_field_placeholder;
+    /* diffusion branch */
+    double *wind_divv, *curl_of_vorticity, *vector_field_placeholder, *n_squared, *dv_hdz;
 } orc_diag;
 
 typedef struct orc_forcings {
@@ -47,6 +55,10 @@ typedef struct orc_forcings {
 typedef struct orc_irrev {
     double *temperature_diffusion_heating, *friction_acc, *heating_diss, *pressure_gradient_decel_factor;
     double *condensates_sediment_heat, *mass_diff_tendency, *phase_trans_rates, *phase_trans_heating_rate;
+    /* diffusion branch */
+    double *molecular_diffusion_coeff, *mass_diffusion_coeff_numerical_h, *mass_diffusion_coeff_numerical_v;
+    double *temp_diffusion_coeff_numerical_h, *temp_diffusion_coeff_numerical_v, *viscosity, *viscosity_rhombi;
+    double *viscosity_triangles, *vert_hor_viscosity, *tke;
 } orc_irrev;
 
 typedef struct orc_config {
@@ -84,6 +96,16 @@ int orc_calc_h2otracers_source_rates(const orc_grid *g, const orc_state *s, orc_
 int orc_manage_pressure_gradient(const orc_grid *g, const orc_state *s, orc_diag *d, orc_forcings *f,
                                  orc_irrev *ir, const orc_config *c);
 int orc_calc_pressure_grad_condensates_v(const orc_grid *g, const orc_state *s, orc_forcings *f, orc_irrev *ir);
+/* diffusion branch (src/subgrid_scale, src/spatial_operators/momentum_diff_diss.c) */
+int orc_add_vertical_divv(const orc_grid *g, const double *in, double *out);
+int orc_update_n_squared(const orc_grid *g, const orc_state *s, orc_diag *d);
+int orc_tke_update(const orc_grid *g, orc_irrev *ir, double dt, const orc_state *s, orc_diag *d);
+int orc_hor_viscosity(const orc_grid *g, const orc_state *s, orc_irrev *ir, const orc_diag *d);
+int orc_hor_momentum_diffusion(const orc_grid *g, const orc_state *s, orc_diag *d, orc_irrev *ir);
+int orc_vert_momentum_diffusion(const orc_grid *g, const orc_state *s, orc_diag *d, orc_irrev *ir);
+int orc_simple_dissipation_rate(const orc_grid *g, const orc_state *s, orc_irrev *ir);
+int orc_scalar_diffusion_coeffs(const orc_grid *g, const orc_state *s, const orc_config *c, orc_irrev *ir,
+                                orc_diag *d);
 int orc_vector_tendencies_expl(const orc_grid *g, const orc_state *s, orc_state *tend, orc_diag *d,
                                orc_forcings *f, orc_irrev *ir, const orc_config *c, int rk_step, double dt);
 int orc_scalar_tendencies_expl(const orc_grid *g, const orc_state *s_old, const orc_state *s, orc_state *tend,

@@ -71,3 +71,45 @@ def test_reference_operators_equal_oracle():
             lib.divv_h(wind.ctypes.data, a.ctypes.data, m.grid.ptr)
             orc.divv_h(wind, b)
         assert np.array_equal(a, b), name
+
+
+SWITCHES = ("momentum_diff_h", "momentum_diff_v", "temperature_diff_h", "temperature_diff_v", "mass_diff_h",
+            "mass_diff_v")
+DIFFUSION = [
+    # (res, moist, case, mountain, dt, steps, switches on)
+    (3, 1, "tracers", True, 300.0, 3, SWITCHES),
+    (3, 0, "std_wind_tpert", True, 300.0, 3, ("momentum_diff_h",)),
+    (3, 0, "std_wind_tpert", True, 300.0, 3, ("momentum_diff_v",)),
+    (3, 1, "jet_moist", False, 300.0, 2, ("mass_diff_h", "mass_diff_v")),
+    (4, 1, "tracers", True, 200.0, 2, ("momentum_diff_h", "temperature_diff_h", "temperature_diff_v")),
+]
+
+
+def with_diffusion(m, switches, seed=5):
+    """switches on, and a seeded turbulent kinetic energy of 0.5-1 J/kg (the
+    reference reads TKE from its initial-state file)"""
+    for s in SWITCHES:
+        m.config[s][0] = 1 if s in switches else 0
+    rng = np.random.default_rng(seed)
+    m.irrev["tke"][:] = 0.5 + 0.5 * rng.random(m.irrev["tke"].size)
+    return m
+
+
+@pytest.mark.parametrize("cfg", DIFFUSION, ids=lambda c: f"R{c[0]}M{c[1]}-{c[2]}-" + "+".join(
+    s.replace("_diff_", "") for s in c[6]))
+def test_oracle_bitwise_equals_reference_with_diffusion(cfg):
+    res, moist, case, mountain, dt, steps, switches = cfg
+    _, m_ref = make_model(res, moist, case, mountain)
+    with_diffusion(m_ref, switches)
+    m_orc = clone(m_ref)
+    ref = refbind.Reference(m_ref)
+    orc = Oracle(m_orc)
+    driver.start(m_ref, ref.linear_combine_two_states)
+    driver.start(m_orc, orc.linear_combine_two_states)
+    for n in range(steps):
+        driver.step(m_ref, ref.linear_combine_two_states, ref.manage_rkhevi, dt, n * dt)
+        driver.step(m_orc, orc.linear_combine_two_states, orc.manage_rkhevi, dt, n * dt)
+        for k in ("state_old", "state_new", "state_tendency", "diagnostics", "forcings", "irrev"):
+            a, b = getattr(m_ref, k).buf, getattr(m_orc, k).buf
+            assert np.array_equal(a, b), f"step {n}: {k} differs in {np.count_nonzero(a != b)} bytes"
+    assert np.any(m_orc.irrev["friction_acc"] != 0) or "momentum" not in "".join(switches)
