@@ -3,6 +3,7 @@
  */
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include <cmath>
 
@@ -28,6 +29,9 @@ namespace {
 struct Bound {
     const void *grid = nullptr, *dualgrid = nullptr;
     const void *aux_diag = nullptr, *aux_forc = nullptr, *aux_irrev = nullptr;
+    /* structs the diffusion fields were checked / imported from */
+    const void *diff_diag = nullptr, *diff_forc = nullptr, *diff_irrev = nullptr;
+    bool diff_checked = false, diff_imported = false;
 } g_bound;
 
 size_t off(int sid, const char *name) { return game_layout_offset(&ctx()->dims, sid, name); }
@@ -84,14 +88,106 @@ StepParams params_from_config(Context *c, const void *config, double dt)
     return p;
 }
 
-int check_config(const void *config)
+static const char *const DIFF_SWITCHES[6] = {"momentum_diff_h", "momentum_diff_v", "temperature_diff_h",
+                                             "temperature_diff_v", "mass_diff_h", "mass_diff_v"};
+
+/* DIFF_* bits of the config's diffusion switches (same order as DIFF_SWITCHES) */
+int diff_flags(const void *config)
 {
-    static const char *off_switches[] = {"temperature_diff_h", "temperature_diff_v", "momentum_diff_h", "momentum_diff_v",
-                                         "mass_diff_h", "mass_diff_v", "rad_on", "prog_soil_temp", "sfc_phase_trans",
-                                         "sfc_sensible_heat_flux", "pbl_scheme"};
+    int f = 0;
+    for (int k = 0; k < 6; ++k)
+        if (*member<int>(config, GAME_CONFIG, DIFF_SWITCHES[k]) != 0) f |= 1 << k;
+    return f;
+}
+
+/* radiation, PBL, surface fluxes and soil are never part of this library's
+ * step; the diffusion branch is, in manage_rkhevi (allow_diffusion) */
+int check_config(const void *config, bool allow_diffusion = false)
+{
+    static const char *off_switches[] = {"rad_on", "prog_soil_temp", "sfc_phase_trans", "sfc_sensible_heat_flux",
+                                         "pbl_scheme"};
     for (const char *s : off_switches)
         if (*member<int>(config, GAME_CONFIG, s) != 0)
-            return fail(std::string("config switch ") + s + " is on; diffusion, PBL, surface fluxes, soil and radiation are not part of this library's step");
+            return fail(std::string("config switch ") + s + " is on; PBL, surface fluxes, soil and radiation are not part of this library's step");
+    if (!allow_diffusion)
+        for (const char *s : DIFF_SWITCHES)
+            if (*member<int>(config, GAME_CONFIG, s) != 0)
+                return fail(std::string("config switch ") + s + " is on; this entry point has no diffusion branch (manage_rkhevi has)");
+    return 0;
+}
+
+static bool any_nonzero(const double *a, long long n)
+{
+    for (long long i = 0; i < n; ++i)
+        if (a[i] != 0.0) return true;
+    return false;
+}
+
+/* the diffusion branch's fields that persist between steps (the reference
+ * carries them in Diagnostics and Irreversible_quantities): imported from the
+ * caller's structs on the first call that needs them -- a diffusion switch is
+ * on, or one of the irreversible terms the tendencies add is nonzero -- and
+ * kept on the device afterwards, like the other lagged fields */
+int import_diffusion(Context *c, const void *diag, const void *forc, const void *irrev, int diff)
+{
+    const bool same = diag == g_bound.diff_diag && forc == g_bound.diff_forc && irrev == g_bound.diff_irrev;
+    if (!same) {
+        g_bound.diff_diag = diag;
+        g_bound.diff_forc = forc;
+        g_bound.diff_irrev = irrev;
+        g_bound.diff_checked = false;
+        g_bound.diff_imported = false;
+    }
+    if (g_bound.diff_imported) {
+        if (diff) c->irr_active = 1;
+        return 0;
+    }
+    const long long ns = c->ns, nv = c->nv;
+    bool need = diff != 0 || c->irr_active;
+    if (!need && !g_bound.diff_checked) {
+        need = any_nonzero(member<double>(irrev, GAME_IRREV, "friction_acc"), nv)
+               || any_nonzero(member<double>(irrev, GAME_IRREV, "heating_diss"), ns)
+               || any_nonzero(member<double>(irrev, GAME_IRREV, "temperature_diffusion_heating"), ns)
+               || any_nonzero(member<double>(irrev, GAME_IRREV, "mass_diff_tendency"), c->n_const * ns)
+               || any_nonzero(member<double>(forc, GAME_FORCINGS, "radiation_tendency"), ns);
+        g_bound.diff_checked = true;
+    }
+    if (!need) return 0;
+    if (c->nl < 5) return fail("the diffusion branch needs at least 5 layers");
+    if (ensure_diff_buffers(c)) return -1;
+    DiffBufs &b = *c->dbuf;
+    struct {
+        const void *base;
+        int sid;
+        const char *name;
+        double *dev;
+    } scal[] = {
+        {irrev, GAME_IRREV, "tke", b.tke}, {irrev, GAME_IRREV, "viscosity", b.visc},
+        {irrev, GAME_IRREV, "heating_diss", b.hdiss}, {irrev, GAME_IRREV, "molecular_diffusion_coeff", b.mol},
+        {irrev, GAME_IRREV, "temperature_diffusion_heating", b.tdh}, {diag, GAME_DIAGNOSTICS, "n_squared", b.n2},
+        {forc, GAME_FORCINGS, "radiation_tendency", b.rad},
+    };
+    for (auto &f : scal)
+        if (upload_field(member<double>(f.base, f.sid, f.name), f.dev, c->map_s, ns, ns)) return -1;
+    const double *mdt = member<double>(irrev, GAME_IRREV, "mass_diff_tendency");
+    for (int k = 0; k < c->n_const; ++k)
+        if (upload_field(mdt + k * ns, b.mdt + k * ns, c->map_s, ns, ns)) return -1;
+    if (upload_field(member<double>(irrev, GAME_IRREV, "friction_acc"), b.fric, c->map_vec, nv, nv)) return -1;
+    /* TOA and surface vertical entries of vector_field_placeholder */
+    double *t0 = c->dev_tmp[0];
+    if (upload_field(member<double>(diag, GAME_DIAGNOSTICS, "vector_field_placeholder"), t0, c->map_vec, nv, nv))
+        return -1;
+    CK(cudaMemcpyAsync(b.ph_tb, t0, (size_t)c->nc * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(b.ph_tb + c->nc, t0 + (long long)c->nl * c->nc, (size_t)c->nc * sizeof(double),
+                       cudaMemcpyDeviceToDevice, c->stream));
+    /* TOA row of dv_hdz, in device edge order */
+    const double *dv = member<double>(diag, GAME_DIAGNOSTICS, "dv_hdz");
+    std::vector<double> top(c->ne);
+    for (int e = 0; e < c->ne; ++e) top[e] = dv[c->e_n2o[e]];
+    CK(cudaMemcpyAsync(b.dvdz_top, top.data(), (size_t)c->ne * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    g_bound.diff_imported = true;
+    c->irr_active = 1;
     return 0;
 }
 
@@ -276,6 +372,34 @@ int game_gpu_sync_aux_to_host(struct diagnostics *diagnostics, struct forcings *
                                ns, 0, ns)) return -1;
         }
     }
+    /* fields of the diffusion branch that persist between steps */
+    if (c->dbuf && g_bound.diff_imported) {
+        DiffBufs &b = *c->dbuf;
+        struct {
+            const void *base;
+            int sid;
+            const char *name;
+            const double *dev;
+        } scal[] = {
+            {irrev, GAME_IRREV, "tke", b.tke}, {irrev, GAME_IRREV, "viscosity", b.visc},
+            {irrev, GAME_IRREV, "heating_diss", b.hdiss}, {irrev, GAME_IRREV, "molecular_diffusion_coeff", b.mol},
+            {irrev, GAME_IRREV, "temperature_diffusion_heating", b.tdh}, {diagnostics, GAME_DIAGNOSTICS, "n_squared", b.n2},
+        };
+        for (auto &f : scal) {
+            if (!f.base) continue;
+            if (download_field(member<double>(f.base, f.sid, f.name), f.dev, c->map_s, ns, ns, 0, ns)) return -1;
+            CK(cudaStreamSynchronize(c->stream));
+        }
+        if (irrev) {
+            double *mdt = member<double>(irrev, GAME_IRREV, "mass_diff_tendency");
+            for (int k = 0; k < c->n_const; ++k) {
+                if (download_field(mdt + k * ns, b.mdt + k * ns, c->map_s, ns, ns, 0, ns)) return -1;
+                CK(cudaStreamSynchronize(c->stream));
+            }
+            if (download_field(member<double>(irrev, GAME_IRREV, "friction_acc"), b.fric, c->map_vec, nv, nv, 0, nv))
+                return -1;
+        }
+    }
     return finish();
 }
 
@@ -392,17 +516,20 @@ int manage_rkhevi(struct state *state_old, struct state *state_new, struct grid 
     (void)time_coordinate;
     (void)dualgrid;
     if (check_ready(grid)) return -1;
-    if (check_config(config)) return -1;
+    if (check_config(config, true)) return -1;
     Context *c = ctx();
     StateMirror *so = mirror(state_old, 1), *sn = mirror(state_new, 1), *st = mirror(state_tendency, 1);
     if (!so || !sn || !st) return -1;
     if (so == sn || so == st || sn == st) return fail("state_old, state_new and state_tendency must be distinct");
     if (import_aux(diagnostics, forcings, irrev)) return -1;
+    if (import_diffusion(c, diagnostics, forcings, irrev, diff_flags(config))) return -1;
     if (!c->resident) {
         if (upload_state(state_old, so)) return -1;
         if (upload_state(state_new, sn)) return -1;
     }
     StepParams p = params_from_config(c, config, delta_t);
+    p.diff = diff_flags(config);
+    p.irr = c->irr_active;
     if (run_device_step(c, p, so, sn, st)) return -1;
     if (!c->resident) {
         if (download_state(state_new, sn, 1 | 2 | 4 | 8 | 16)) return -1;

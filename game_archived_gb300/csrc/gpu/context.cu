@@ -372,6 +372,20 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
             h_dat[(size_t)l * NT + t] = darea[NE + l * DPL + tn[t]];
             h_dzt[(size_t)l * NT + t] = dz[NE + l * DPL + tn[t]];
         }
+    /* diffusion branch: layer thickness, the dual normal distances of the
+     * triangle prisms and of the surface level's edges */
+    {
+        const double *dnd = DD("normal_distance");
+        std::vector<double> h_lt = cell_field(GD("layer_thickness")), h_dndt((size_t)L * NT), h_dnds(NE);
+        for (int l = 0; l < L; ++l)
+            for (int t = 0; t < NT; ++t) h_dndt[(size_t)l * NT + t] = dnd[NE + l * DPL + tn[t]];
+        for (int e = 0; e < NE; ++e) h_dnds[e] = dnd[(long long)L * DPL + en[e]];
+        c->dg.layer_thickness = dupload(c, h_lt);
+        c->dg.dual_nd_t = dupload(c, h_dndt);
+        c->dg.dual_nd_sfc = dupload(c, h_dnds);
+        c->dg.eff_hor_res = *GD("eff_hor_res");
+        c->dg.mean_velocity_area = *GD("mean_velocity_area");
+    }
 
     /* ---- upload */
     Dual t_vol = dual_upload(c, h_vol), t_ipw = dual_upload(c, h_ipw), t_ndv = dual_upload(c, h_ndv),
@@ -538,6 +552,7 @@ int destroy_context()
     for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
     for (auto &kv : c->states) cudaFree(kv.second.dev);
     for (auto &b : c->owned) cudaFree(b.p);
+    delete c->dbuf;
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
@@ -575,6 +590,28 @@ StateMirror *mirror(const void *host_state, int create)
     set_mirror_views(c, m);
     c->states[host_state] = m;
     return &c->states[host_state];
+}
+
+int ensure_diff_buffers(Context *c)
+{
+    if (c->dbuf) return 0;
+    const size_t S = (size_t)c->ns, C = (size_t)c->n_const, L = (size_t)c->nl;
+    const size_t NC = (size_t)c->nc, NE = (size_t)c->ne, NT = (size_t)c->nt;
+    DiffBufs *b = new DiffBufs();
+    c->dbuf = b;
+    struct Want {
+        double **p;
+        size_t n;
+    } want[] = {
+        {&b->tke, S}, {&b->visc, S}, {&b->hdiss, S}, {&b->fric, (size_t)c->nv}, {&b->mol, S}, {&b->n2, S},
+        {&b->mdt, C * S}, {&b->tdh, S}, {&b->rad, S}, {&b->ph_tb, 2 * NC}, {&b->dvdz_top, NE},
+        {&b->adv, S}, {&b->vint, S}, {&b->wdv, S}, {&b->tri, L * NT}, {&b->zt, L * NT}, {&b->zr, L * NE},
+        {&b->s1, S}, {&b->s2, S}, {&b->s3, S}, {&b->flx, L * NE}, {&b->mch, S}, {&b->mcv, S}, {&b->tch, S},
+        {&b->tcv, S}, {&b->fh, (C + 1) * L * NE}, {&b->fv, (C + 1) * (L + 1) * NC},
+    };
+    for (auto &w : want)
+        if (!(*w.p = dalloc<double>(c, w.n))) return fail("device allocation of the diffusion fields failed");
+    return 0;
 }
 
 int ensure_sub_buffers(Context *c)

@@ -146,6 +146,13 @@ struct Context {
     double damp_key[3] = {-1.0, -1.0, -1.0};
     /* grid terms of the mixed-path sound-wave rows [6][L-1][Nc] */
     double *wv_geo = nullptr;
+    /* diffusion branch: tables, fields (allocated with the lagged fields on
+     * their first import) and whether the tendencies add the irreversible
+     * terms (set once a diffusion switch was on or an imported term was
+     * nonzero) */
+    DiffGrid dg{};
+    DiffBufs *dbuf = nullptr;
+    int irr_active = 0;
     int use_graphs = 1;
     int column_solver = 0; /* 0 by layer count, 1 per-thread sweeps, 2 warp cyclic reduction */
     int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */
@@ -197,6 +204,7 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid, co
 int destroy_context();
 StateMirror *mirror(const void *host_state, int create);
 int ensure_sub_buffers(Context *c);
+int ensure_diff_buffers(Context *c);
 int upload_state(const void *host_state, StateMirror *m);
 int download_state(const void *host_state, StateMirror *m, int which_mask);
 int upload_field(const double *host, double *dev, const int *map, long long n, long long host_len);

@@ -109,6 +109,10 @@ struct Shadow {
 /* run configuration of one step (no padding: compared bytewise as a key) */
 struct StepParams {
     int n_const, n_cond, moist, first_step;
+    /* diffusion switches (DIFF_* bits) and whether the step adds the
+     * irreversible terms (friction, dissipative and diffusive heating,
+     * radiation, mass diffusion) to its tendencies */
+    int diff, irr, pad_i0, pad_i1;
     double dt;
     double impl_thermo_weight, damping_start_height, damping_coeff_max, toa;
     double snow_velocity, rain_velocity, cloud_velocity;
@@ -121,7 +125,35 @@ struct StepParams {
     double cur_hor, old_hor, cur_ver;
     float cur_hor_f, old_hor_f, cur_ver_f, pad_f;
 };
-static_assert(sizeof(StepParams) == 4 * sizeof(int) + 14 * sizeof(double) + 4 * sizeof(float),
+static_assert(sizeof(StepParams) == 8 * sizeof(int) + 14 * sizeof(double) + 4 * sizeof(float),
               "StepParams has padding");
+
+/* config switches of the diffusion branch (StepParams::diff) */
+enum {
+    DIFF_MOM_H = 1, DIFF_MOM_V = 2, DIFF_TEMP_H = 4, DIFF_TEMP_V = 8, DIFF_MASS_H = 16, DIFF_MASS_V = 32
+};
+
+/* tables of the diffusion branch (double) */
+struct DiffGrid {
+    const double *layer_thickness; /* [L][Nc] */
+    const double *dual_nd_t;       /* [L][Nt] vertical extent of the triangle prisms (dual normal distance) */
+    const double *dual_nd_sfc;     /* [Ne] dual normal distance of the surface level's edges */
+    double eff_hor_res, mean_velocity_area;
+};
+
+/* fields of the diffusion branch, device layout.  Persistent between steps
+ * (imported from and exported to the caller's structs): tke, visc (viscosity),
+ * hdiss (heating_diss), fric (friction_acc, vector layout), mol
+ * (molecular_diffusion_coeff), n2 (n_squared), mdt (mass_diff_tendency,
+ * [C][L][Nc]), tdh (temperature_diffusion_heating), rad (radiation_tendency),
+ * ph_tb (TOA and surface vertical entries of vector_field_placeholder,
+ * [2][Nc]) and dvdz_top (TOA row of dv_hdz, [Ne]).  The rest is scratch of
+ * one step. */
+struct DiffBufs {
+    double *tke, *visc, *hdiss, *fric, *mol, *n2, *mdt, *tdh, *rad, *ph_tb, *dvdz_top;
+    double *adv, *vint, *wdv, *tri, *zt, *zr, *s1, *s2, *s3, *flx;
+    double *mch, *mcv, *tch, *tcv; /* mass / temperature diffusion coefficients, h and v */
+    double *fh, *fv;               /* diffusive fluxes of T and the C densities: [C+1][L][Ne], [C+1][L+1][Nc] */
+};
 
 }  // namespace game

@@ -762,7 +762,8 @@ __device__ __forceinline__ R pgrad_v(const HGrid<R> &g, const StepParams &p, con
 template <typename R, bool ADV, bool PG>
 __global__ void k_momentum_h(HGrid<R> g, StepParams p, SView<R> sv, double *u_new, float *u_shadow, const double *u_old,
                              double *tend_u, R *P_h, R *pg_old_h, R *pvt_h, R *v2g_h, const R *flux_h,
-                             const R *flux_v, const R *zh, const R *zv, const R *v2, double new_w, double old_w)
+                             const R *flux_v, const R *zh, const R *zv, const R *v2, double new_w, double old_w,
+                             const double *fric_u)
 {
     const long long n = (long long)g.nl * g.ne;
     const long long i = gtid();
@@ -791,6 +792,8 @@ __global__ void k_momentum_h(HGrid<R> g, StepParams p, SView<R> sv, double *u_ne
     constexpr bool F = sizeof(R) == sizeof(float);
     const R cur_hor = F ? R(p.cur_hor_f) : R(p.cur_hor), old_hor = F ? R(p.old_hor_f) : R(p.old_hor);
     R y = old_hor * pgo - cur_hor * P + pvt - R(0.5) * v2g;
+    /* friction acceleration of the diffusion branch, when it is active */
+    if (fric_u) y = y + R(fric_u[i]);
     /* the pressure gradient is recomputed in substage 0 only, where the new
      * weight is 1 */
     double t = PG ? double(y) : old_w * tend_u[i] + new_w * double(y);
@@ -805,7 +808,8 @@ __global__ void k_momentum_h(HGrid<R> g, StepParams p, SView<R> sv, double *u_ne
  * condensate term (manage_pressure_gradient.c:74-87) */
 template <typename R, bool ADV, bool PG>
 __global__ void k_momentum_v(HGrid<R> g, StepParams p, SView<R> sv, double *tend_w, R *P_v, R *pvt_v, R *v2g_v,
-                             const R *flux_h, const R *zh, const R *v2, double new_w, double old_w)
+                             const R *flux_h, const R *zh, const R *v2, double new_w, double old_w,
+                             const double *fric_w)
 {
     const long long n = (long long)(g.nl + 1) * g.nc;
     const long long i = gtid();
@@ -854,7 +858,9 @@ __global__ void k_momentum_v(HGrid<R> g, StepParams p, SView<R> sv, double *tend
     R d_lo = sv.rho[p.n_cond * ns + lo] / density_total_r(sv.rho, p.n_const, ns, lo) - R(1);
     R pgc = (R(0.5) * (d_up + d_lo)) * g.gravity_m_v[i];
     const R cur_ver = sizeof(R) == sizeof(float) ? R(p.cur_ver_f) : R(p.cur_ver);
-    R y = -cur_ver * P + pvt - R(0.5) * v2g + pgc;
+    R y = -cur_ver * P + pvt - R(0.5) * v2g;
+    if (fric_w) y = y + R(fric_w[i]);
+    y = y + pgc;
     double t = PG ? double(y) : old_w * tend_w[i] + new_w * double(y);
     tend_w[i] = t;
 }
@@ -926,11 +932,18 @@ struct FluxSum<float> {
  * rho*theta_v flux; the terrain correction of the wind is computed once for
  * all tracers.  Edge fluxes are products in R, divergences accumulate in
  * double (FluxSum) and tendencies are formed in double. */
-template <typename R>
+/* irreversible terms of the tendencies (scalar_tendencies_expl.c:125-176):
+ * dissipative and diffusive heating, radiation, mass diffusion [C][L][Nc] */
+struct IrrTerms {
+    const double *heating_diss, *temp_diff_heating, *radiation, *mass_diff;
+};
+
+template <typename R, bool IRR>
 __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, SView<R> sv, DState st,
                                                       const R *theta, const R *cp_ice, const R *cp_water,
                                                       const double *pt_rates, const double *pt_heat,
-                                                      const double *sed_heat, const double *inv_vol_tab, int rk)
+                                                      const double *sed_heat, const double *inv_vol_tab, int rk,
+                                                      IrrTerms irr)
 {
     const long long ns = (long long)g.nl * g.nc;
     const long long i = gtid();
@@ -1009,23 +1022,29 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
         if (lo_corr) layer_pass(l + 1, false, false, true);
         const double div = inv_vol * (hm.value() + comp_v(um, lm));
         double y = -div;
+        if (IRR) y = y + irr.mass_diff[cond * ns + i];
         if (p.moist) y = y + pt_rates[cond * ns + i];
         st.rho[cond * ns + i] = rk == 0 ? y : 0.0 * st.rho[cond * ns + i] + 1.0 * y;
         const double div_t = inv_vol * (ht.value() + comp_v(ut, lt));
         double yt = -div_t;
-        if (p.moist) {
+        if (p.moist || IRR) {
             /* diabatic heating: c_v-weighted, divided by c_p * Pi */
             R cv = R(0);
             for (int kk = 0; kk < cond; ++kk) cv += sv.rho[kk * ns + i] * ((kk % 2 == 0) ? cp_ice[i] : cp_water[i]);
             cv += sv.rho[cond * ns + i] * R(C_D_V);
-            cv += sv.rho[(cond + 1) * ns + i] * R(C_V_V);
+            if (p.moist) cv += sv.rho[(cond + 1) * ns + i] * R(C_V_V);
+            double heat = pt_heat[i] + sed_heat[i], rate = pt_rates[cond * ns + i];
+            if (IRR) {
+                heat = irr.heating_diss[i] + irr.temp_diff_heating[i] + irr.radiation[i] + pt_heat[i] + sed_heat[i];
+                rate = pt_rates[cond * ns + i] + irr.mass_diff[cond * ns + i];
+            }
             if (sizeof(R) == sizeof(double)) {
-                yt = yt + C_D_V * double(sv.rho[cond * ns + i]) / double(cv) * (pt_heat[i] + sed_heat[i])
+                yt = yt + C_D_V * double(sv.rho[cond * ns + i]) / double(cv) * heat
                               / (C_D_P * (double(g.exner_bg[i]) + double(sv.exner_pert[i])))
-                     + pt_rates[cond * ns + i] * double(theta[i]);
+                     + rate * double(theta[i]);
             } else {
                 const R fac = R(C_D_V) * sv.rho[cond * ns + i] / cv / (R(C_D_P) * (g.exner_bg[i] + sv.exner_pert[i]));
-                yt = yt + double(fac) * (pt_heat[i] + sed_heat[i]) + pt_rates[cond * ns + i] * double(theta[i]);
+                yt = yt + double(fac) * heat + rate * double(theta[i]);
             }
         }
         st.rhotheta_v[i] = rk == 0 ? yt : 0.0 * st.rhotheta_v[i] + 1.0 * yt;
@@ -1078,6 +1097,7 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
         }
         const double div = inv_vol * (h.value() + cv);
         double y = -div;
+        if (IRR) y = y + irr.mass_diff[k * ns + i];
         if (p.moist) {
             long long pt = k * ns;
             if (k == cond + 1) pt -= ns;

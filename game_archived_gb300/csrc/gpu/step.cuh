@@ -7,6 +7,7 @@
 #pragma once
 
 #include "context.h"
+#include "diff.h"
 #include "kernels.cuh"
 #include "solvers.cuh"
 
@@ -108,8 +109,9 @@ static void launch_momentum_v(Context *c, const StepParams &p, const Views<R> &v
     HGrid<R> &g = hgrid<R>(c);
     Work<R> &w = work<R>(c);
     ProfScope ps(c, "k_momentum_v");
+    const double *fric_w = p.irr ? c->dbuf->fric : nullptr;
     k_momentum_v<R, ADV, PG><<<nblocks((long long)(c->nl + 1) * c->nc, 256), 256, 0, c->stream>>>(
-        g, p, v.sv, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w);
+        g, p, v.sv, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w, fric_w);
     c->kernel_launches++;
 }
 
@@ -120,9 +122,10 @@ static void launch_momentum_h(Context *c, const StepParams &p, const Views<R> &v
     HGrid<R> &g = hgrid<R>(c);
     Work<R> &w = work<R>(c);
     ProfScope ps(c, "k_momentum_h");
+    const double *fric_u = p.irr ? c->dbuf->fric + (long long)(c->nl + 1) * c->nc : nullptr;
     k_momentum_h<R, ADV, PG><<<nblocks((long long)c->nl * c->ne, 256), 256, 0, c->stream>>>(
         g, p, v.sv, sn->ds.u, v.sh.u, so->ds.u, st->ds.u, w.P_h, w.pg_old_h, w.pvt_h, w.v2g_h, w.flux_h, w.flux_v,
-        w.zh, w.zv, w.v2, new_w, old_w);
+        w.zh, w.zv, w.v2, new_w, old_w, fric_u);
     c->kernel_launches++;
 }
 
@@ -270,6 +273,8 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             }
             c->kernel_launches += 3;
         }
+        /* diffusion branch: momentum part on state_new before the wind update */
+        if (rk == 0 && p.diff) launch_diffusion_momentum(c, p, sn->ds);
         if (rk == 0 && adv) {
             launch_momentum<R, true, true>(c, p, v, so, sn, st, new_w, old_w);
         } else if (rk == 0) {
@@ -283,15 +288,24 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             }
             launch_momentum_v<R, true, false>(c, p, v, st, new_w, old_w);
         }
+        /* diffusion branch: temperature and mass diffusion */
+        if (rk == 0 && p.diff) launch_diffusion_scalar(c, p, sn->ds);
         {
             ProfScope ps(c, "k_theta");
             k_theta<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(c->nl, c->nc, c->n_cond, v.sv, theta);
         }
         {
             ProfScope ps(c, "k_scalar_tend");
-            k_scalar_tend2<R><<<nblocks(ns, 128), 128, 0, c->stream>>>(g, p, v.sv, st->ds, theta, cpi, cpw,
-                                                                        c->pt_rates, c->pt_heat, c->sed_heat,
-                                                                        c->inv_vol, rk);
+            if (p.irr) {
+                const DiffBufs &b = *c->dbuf;
+                k_scalar_tend2<R, true><<<nblocks(ns, 128), 128, 0, c->stream>>>(
+                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol, rk,
+                    IrrTerms{b.hdiss, b.tdh, b.rad, b.mdt});
+            } else {
+                k_scalar_tend2<R, false><<<nblocks(ns, 128), 128, 0, c->stream>>>(
+                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol, rk,
+                    IrrTerms{});
+            }
         }
         c->kernel_launches += 2;
         launch_waves<EXACT>(c, p, so, sn, st, rk, v.sh);
