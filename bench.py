@@ -339,6 +339,33 @@ def time_adjoint(res, n_lloyd, n_steps, dt, device, repeats=3):
                     "hand-written adjoint kernels; window times include the host-in/host-out copy of one State"}
 
 
+DIFF_SWITCHES = ("momentum_diff_h", "momentum_diff_v", "temperature_diff_h", "temperature_diff_v", "mass_diff_h",
+                 "mass_diff_v")
+
+
+def time_diffusion(model0, steps, warmup, dt, device, base_ms):
+    """The headline workload with every diffusion switch on (the reference's
+    ideal and operational run scripts) and a seeded TKE of 0.5-1 J/kg:
+    device-resident steps/s in both precisions, the ratio to the step
+    without diffusion, and the per-step time of the diffusion kernels (kd_*)
+    from the profiled pass."""
+    import numpy as np
+    from game_archived_gb300 import abi
+    m = copy_model(model0, pinned=False)
+    for s in DIFF_SWITCHES:
+        m.config[s][0] = 1
+    m.irrev["tke"][:] = 0.5 + 0.5 * np.random.default_rng(5).random(m.irrev["tke"].size)
+    out = {"config": "as the headline workload, momentum, temperature and mass diffusion on (horizontal and "
+                     "vertical), TKE 0.5-1 J/kg seeded"}
+    for prec, name in ((abi.MIXED, "mixed"), (abi.FP64, "fp64")):
+        ms, launches, _, prof, ok = time_resident(m, prec, steps, warmup, dt, device, profile=True)
+        kd = {k: v[0] / steps for k, v in prof.items() if k.startswith("kd_")}
+        out[name] = {"steps_per_s": 1000.0 / ms, "ms_per_step": ms, "over_no_diffusion": ms / base_ms[name],
+                     "diffusion_kernels_ms_per_step_profiled": sum(kd.values()), "kernels": kd,
+                     "gpu_launches": int(launches), "finite": bool(ok)}
+    return out
+
+
 def cpu_baseline(model0, dt, max_seconds=25.0):
     """oracle on all host threads; bounded number of steps"""
     from game_archived_gb300 import driver
@@ -465,6 +492,9 @@ def run_ours(args):
         "clocks": clocks,
         "finite": bool(ok32 and ok64),
     }
+    if not args.no_diffusion:
+        line["diffusion"] = time_diffusion(model0, max(20, args.steps // 4), args.warmup, dt, local,
+                                           {"mixed": ms32, "fp64": ms64})
     if not args.no_adjoint:
         line["adjoint"] = time_adjoint(args.adjoint_res, args.n_lloyd, 12, 200.0, local)
     if world == 1 and not args.no_cpu_baseline:
@@ -568,6 +598,7 @@ def main():
     ap.add_argument("--n-lloyd", type=int, default=300)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-diffusion", action="store_true")
     ap.add_argument("--adjoint-res", type=int, default=5)
     ap.add_argument("--column-study", action="store_true",
                     help="time the column solvers at 26, 64 and 128 layers instead of the headline line")
