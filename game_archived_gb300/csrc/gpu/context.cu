@@ -380,11 +380,10 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
         for (int l = 0; l < L; ++l)
             for (int t = 0; t < NT; ++t) h_dndt[(size_t)l * NT + t] = dnd[NE + l * DPL + tn[t]];
         for (int e = 0; e < NE; ++e) h_dnds[e] = dnd[(long long)L * DPL + en[e]];
-        c->dg.layer_thickness = dupload(c, h_lt);
-        c->dg.dual_nd_t = dupload(c, h_dndt);
-        c->dg.dual_nd_sfc = dupload(c, h_dnds);
-        c->dg.eff_hor_res = *GD("eff_hor_res");
-        c->dg.mean_velocity_area = *GD("mean_velocity_area");
+        const Dual lt = dual_upload(c, h_lt), dndt = dual_upload(c, h_dndt), dnds = dual_upload(c, h_dnds),
+                   zvi = dual_upload(c, iface_field(zv));
+        c->dg64 = {lt.d, dndt.d, dnds.d, zvi.d, *GD("eff_hor_res"), *GD("mean_velocity_area")};
+        c->dg32 = {lt.f, dndt.f, dnds.f, zvi.f, *GD("eff_hor_res"), *GD("mean_velocity_area")};
     }
 
     /* ---- upload */

@@ -150,7 +150,8 @@ struct Context {
      * their first import) and whether the tendencies add the irreversible
      * terms (set once a diffusion switch was on or an imported term was
      * nonzero) */
-    DiffGrid dg{};
+    DiffGrid<double> dg64{};
+    DiffGrid<float> dg32{};
     DiffBufs *dbuf = nullptr;
     int irr_active = 0;
     int use_graphs = 1;

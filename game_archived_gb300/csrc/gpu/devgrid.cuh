@@ -133,11 +133,13 @@ enum {
     DIFF_MOM_H = 1, DIFF_MOM_V = 2, DIFF_TEMP_H = 4, DIFF_TEMP_V = 8, DIFF_MASS_H = 16, DIFF_MASS_V = 32
 };
 
-/* tables of the diffusion branch (double) */
+/* tables of the diffusion branch in the horizontal precision R */
+template <typename R>
 struct DiffGrid {
-    const double *layer_thickness; /* [L][Nc] */
-    const double *dual_nd_t;       /* [L][Nt] vertical extent of the triangle prisms (dual normal distance) */
-    const double *dual_nd_sfc;     /* [Ne] dual normal distance of the surface level's edges */
+    const R *layer_thickness; /* [L][Nc] */
+    const R *dual_nd_t;       /* [L][Nt] vertical extent of the triangle prisms (dual normal distance) */
+    const R *dual_nd_sfc;     /* [Ne] dual normal distance of the surface level's edges */
+    const R *z_v;             /* [L+1][Nc] height of the interfaces */
     double eff_hor_res, mean_velocity_area;
 };
 
@@ -155,5 +157,18 @@ struct DiffBufs {
     double *mch, *mcv, *tch, *tcv; /* mass / temperature diffusion coefficients, h and v */
     double *fh, *fv;               /* diffusive fluxes of T and the C densities: [C+1][L][Ne], [C+1][L+1][Nc] */
 };
+
+/* the scratch part of DiffBufs in precision R (on the mixed path the double
+ * allocations hold float arrays of the same length) */
+template <typename R>
+struct DiffScratch {
+    R *adv, *vint, *wdv, *tri, *zt, *zr, *s1, *s2, *s3, *flx, *mch, *mcv, *tch, *tcv, *fh, *fv;
+};
+template <typename R>
+inline DiffScratch<R> diff_scratch(const DiffBufs &b)
+{
+    return {(R *)b.adv, (R *)b.vint, (R *)b.wdv, (R *)b.tri, (R *)b.zt, (R *)b.zr, (R *)b.s1, (R *)b.s2,
+            (R *)b.s3, (R *)b.flx, (R *)b.mch, (R *)b.mcv, (R *)b.tch, (R *)b.tcv, (R *)b.fh, (R *)b.fv};
+}
 
 }  // namespace game

@@ -1,6 +1,7 @@
 /*
- * Diffusion branch of the RKHEVI step (diff_f64.cu), run at the first RK
- * substep when a diffusion switch is on.
+ * Diffusion branch of the RKHEVI step (kernels in diff.cuh), run at the
+ * first RK substep when a diffusion switch is on: FP64 instantiation in
+ * diff_f64.cu, FP32 (mixed path) in diff_mixed.cu.
  */
 #pragma once
 
@@ -10,12 +11,15 @@ namespace game {
 
 /* momentum part (vector_tendencies_expl.c:41-69): Brunt-Vaisala frequency and
  * TKE update, horizontal and vertical momentum diffusion into the friction
- * acceleration, dissipation rate.  Reads state_new before the wind update. */
-void launch_diffusion_momentum(Context *c, const StepParams &p, const DState &sn);
+ * acceleration, dissipation rate.  sv: state_new (FP64) or its FP32 shadow,
+ * read before the wind update. */
+void launch_diffusion_momentum(Context *c, const StepParams &p, const SView<double> &sv);
+void launch_diffusion_momentum(Context *c, const StepParams &p, const SView<float> &sv);
 
 /* scalar part (scalar_tendencies_expl.c:44-88): diffusion coefficients,
  * temperature and mass diffusion into temperature_diffusion_heating and
  * mass_diff_tendency */
-void launch_diffusion_scalar(Context *c, const StepParams &p, const DState &sn);
+void launch_diffusion_scalar(Context *c, const StepParams &p, const SView<double> &sv);
+void launch_diffusion_scalar(Context *c, const StepParams &p, const SView<float> &sv);
 
 }  // namespace game

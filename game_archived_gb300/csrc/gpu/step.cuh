@@ -274,7 +274,7 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             c->kernel_launches += 3;
         }
         /* diffusion branch: momentum part on state_new before the wind update */
-        if (rk == 0 && p.diff) launch_diffusion_momentum(c, p, sn->ds);
+        if (rk == 0 && p.diff) launch_diffusion_momentum(c, p, v.sv);
         if (rk == 0 && adv) {
             launch_momentum<R, true, true>(c, p, v, so, sn, st, new_w, old_w);
         } else if (rk == 0) {
@@ -289,7 +289,7 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             launch_momentum_v<R, true, false>(c, p, v, st, new_w, old_w);
         }
         /* diffusion branch: temperature and mass diffusion */
-        if (rk == 0 && p.diff) launch_diffusion_scalar(c, p, sn->ds);
+        if (rk == 0 && p.diff) launch_diffusion_scalar(c, p, v.sv);
         {
             ProfScope ps(c, "k_theta");
             k_theta<R><<<nblocks(ns, bs), bs, 0, c->stream>>>(c->nl, c->nc, c->n_cond, v.sv, theta);
