@@ -606,7 +606,7 @@ int ensure_diff_buffers(Context *c)
         {&b->mdt, C * S}, {&b->tdh, S}, {&b->rad, S}, {&b->ph_tb, 2 * NC}, {&b->dvdz_top, NE},
         {&b->adv, S}, {&b->vint, S}, {&b->wdv, S}, {&b->tri, L * NT}, {&b->zt, L * NT}, {&b->zr, L * NE},
         {&b->s1, S}, {&b->s2, S}, {&b->s3, S}, {&b->flx, L * NE}, {&b->mch, S}, {&b->mcv, S}, {&b->tch, S},
-        {&b->tcv, S}, {&b->fh, (C + 1) * L * NE}, {&b->fv, (C + 1) * (L + 1) * NC},
+        {&b->tcv, S}, {&b->fh, (C + 1) * L * NE}, {&b->fv, (C + 1) * (L + 1) * NC}, {&b->kvt, S},
     };
     for (auto &w : want)
         if (!(*w.p = dalloc<double>(c, w.n))) return fail("device allocation of the diffusion fields failed");

@@ -156,19 +156,21 @@ struct DiffBufs {
     double *adv, *vint, *wdv, *tri, *zt, *zr, *s1, *s2, *s3, *flx;
     double *mch, *mcv, *tch, *tcv; /* mass / temperature diffusion coefficients, h and v */
     double *fh, *fv;               /* diffusive fluxes of T and the C densities: [C+1][L][Ne], [C+1][L+1][Nc] */
+    double *kvt;                   /* turbulent vertical diffusivity of the cells [L][Nc] */
 };
 
 /* the scratch part of DiffBufs in precision R (on the mixed path the double
  * allocations hold float arrays of the same length) */
 template <typename R>
 struct DiffScratch {
-    R *adv, *vint, *wdv, *tri, *zt, *zr, *s1, *s2, *s3, *flx, *mch, *mcv, *tch, *tcv, *fh, *fv;
+    R *adv, *vint, *wdv, *tri, *zt, *zr, *s1, *s2, *s3, *flx, *mch, *mcv, *tch, *tcv, *fh, *fv, *kvt;
 };
 template <typename R>
 inline DiffScratch<R> diff_scratch(const DiffBufs &b)
 {
     return {(R *)b.adv, (R *)b.vint, (R *)b.wdv, (R *)b.tri, (R *)b.zt, (R *)b.zr, (R *)b.s1, (R *)b.s2,
-            (R *)b.s3, (R *)b.flx, (R *)b.mch, (R *)b.mcv, (R *)b.tch, (R *)b.tcv, (R *)b.fh, (R *)b.fv};
+            (R *)b.s3, (R *)b.flx, (R *)b.mch, (R *)b.mcv, (R *)b.tch, (R *)b.tcv, (R *)b.fh, (R *)b.fv,
+            (R *)b.kvt};
 }
 
 }  // namespace game

@@ -267,7 +267,7 @@ __device__ __forceinline__ R curl_of_vorticity(const HGrid<R> &g, const DiffGrid
  * (effective_diff_coeffs.c:114-168); the TOA and surface levels take the
  * values of the levels next to them */
 template <typename R>
-__device__ __forceinline__ R vert_hor_viscosity(const HGrid<R> &g, const DiffGrid<R> &dg, const DiffBufs &b,
+__device__ __forceinline__ R vert_hor_viscosity(const HGrid<R> &g, const DiffBufs &b, const DiffScratch<R> &s,
                                                 const R *rg, int k, int e)
 {
     if (k == 0) k = 1;
@@ -275,9 +275,8 @@ __device__ __forceinline__ R vert_hor_viscosity(const HGrid<R> &g, const DiffGri
     const long long nc = g.nc;
     const long long f0 = (long long)(k - 1) * nc + g.from[e], t0 = (long long)(k - 1) * nc + g.to[e];
     const long long f1 = (long long)k * nc + g.from[e], t1 = (long long)k * nc + g.to[e];
-    const R *lt = dg.layer_thickness;
-    auto t2v = [&](long long q) { return tke2vert(R(b.tke[q]), R(b.n2[q]), lt[q]); };
-    R mdc = R(0.25) * (t2v(f0) + t2v(t0) + t2v(f1) + t2v(t1));
+    const R *kv = s.kvt;
+    R mdc = R(0.25) * (kv[f0] + kv[t0] + kv[f1] + kv[t1]);
     const R molecular_viscosity = R(0.25) * (R(b.mol[f0]) + R(b.mol[t0]) + R(b.mol[f1]) + R(b.mol[t1]));
     mdc += molecular_viscosity;
     return R(0.25) * (rg[f0] + rg[t0] + rg[f1] + rg[t1]) * mdc;
@@ -325,8 +324,8 @@ __global__ void kd_fric_h(HGrid<R> g, DiffGrid<R> dg, int n_const, int gas, SVie
         const R z_upper = R(0.5) * (dg.z_v[(long long)l * nc + fr] + dg.z_v[(long long)l * nc + to]);
         const R z_lower = R(0.5) * (dg.z_v[(long long)(l + 1) * nc + fr] + dg.z_v[(long long)(l + 1) * nc + to]);
         const R delta_z = z_upper - z_lower;
-        fa += (vert_hor_viscosity(g, dg, b, rg, l, e) * dv_hdz(g, dg, b, sv, l, e)
-               - vert_hor_viscosity(g, dg, b, rg, l + 1, e) * dv_hdz(g, dg, b, sv, l + 1, e))
+        fa += (vert_hor_viscosity(g, b, s, rg, l, e) * dv_hdz(g, dg, b, sv, l, e)
+               - vert_hor_viscosity(g, b, s, rg, l + 1, e) * dv_hdz(g, dg, b, sv, l + 1, e))
               / delta_z
               / (R(0.5) * (density_total_r(sv.rho, n_const, ns, f) + density_total_r(sv.rho, n_const, ns, t)));
     }
@@ -334,7 +333,9 @@ __global__ void kd_fric_h(HGrid<R> g, DiffGrid<R> dg, int n_const, int gas, SVie
 }
 
 /* diffusion of w, step a (momentum_diff_diss.c:137-150 and 153-166):
- * s1 = rho * viscosity * dw/dz, s2 = w averaged to the cell */
+ * s1 = rho * viscosity * dw/dz, s2 = w averaged to the cell; also the
+ * turbulent vertical diffusivity of the cell (kvt), which the vertical
+ * diffusion of u averages to its half levels */
 template <typename R>
 __global__ void kd_wdiff_a(HGrid<R> g, DiffGrid<R> dg, int gas, SView<R> sv, DiffBufs b, DiffScratch<R> s)
 {
@@ -346,7 +347,9 @@ __global__ void kd_wdiff_a(HGrid<R> g, DiffGrid<R> dg, int gas, SView<R> sv, Dif
     const R lo = l == nl - 1 ? R(0) : sv.w[(long long)(l + 1) * nc + c];
     const R comp_v = up * g.area_v[(long long)l * nc + c] - lo * g.area_v[(long long)(l + 1) * nc + c];
     const R dwdz = R(0) + R(1) / g.volume[i] * comp_v;
-    const R mdc = R(b.mol[i]) + tke2vert(R(b.tke[i]), R(b.n2[i]), dg.layer_thickness[i]);
+    const R kv = tke2vert(R(b.tke[i]), R(b.n2[i]), dg.layer_thickness[i]);
+    s.kvt[i] = kv;
+    const R mdc = R(b.mol[i]) + kv;
     s.s1[i] = sv.rho[gas * ns + i] * mdc * dwdz;
     s.s2[i] = ipw_at(g, 6, l, c) * sv.w[(long long)l * nc + c] + ipw_at(g, 7, l, c) * sv.w[(long long)(l + 1) * nc + c];
 }
@@ -430,7 +433,7 @@ __global__ void kd_sdiff_coeff(long long ns, int n_cond, int moist, const R *lt,
 }
 
 /* the fields a scalar-diffusion pass treats: temperature (stored in double)
- * and/or every density (read in R) */
+ * and/or every density (read in R); inv_vol (mixed path) is 1 / volume */
 template <typename R>
 struct SFields {
     int nf;
@@ -439,54 +442,152 @@ struct SFields {
     const R *kh[8], *kv[8];
     int vert[8];
     double *out[8];     /* [L][Nc] */
+    const double *inv_vol;
 };
 
-/* diffusive fluxes: horizontal at every edge (grad + scalar_times_vector_h),
- * vertical at the inner interfaces (scalar_times_vector_v), of field q */
+template <typename R>
+__device__ __forceinline__ R sfield(const SFields<R> &sf, int q, long long idx)
+{
+    return sf.f_double[q] ? R(((const double *)sf.f[q])[idx]) : ((const R *)sf.f[q])[idx];
+}
+
+/* diffusive fluxes: one thread per edge of a layer (gradient with the
+ * terrain-following correction, gradient_operators.c:66-74, times the
+ * coefficient averaged to the edge, multiplications.c:45-66) or per inner
+ * interface (vertical gradient times the coefficient averaged to the
+ * interface, multiplications.c:98-117), for every field; the grid terms
+ * are loaded once for all fields.  FP64 path: divisions as the reference;
+ * mixed path: one reciprocal per distance, shared by the fields. */
 template <typename R>
 __global__ void kd_sdiff_flux(HGrid<R> g, SFields<R> sf, DiffScratch<R> s)
 {
-    const long long nh = (long long)g.nl * g.ne, nv = (long long)(g.nl - 1) * g.nc;
-    const long long per = nh + nv, i = gtid();
-    if (i >= (long long)sf.nf * per) return;
-    const int q = (int)(i / per);
-    const long long r = i - (long long)q * per;
+    constexpr bool EXACT = sizeof(R) == sizeof(double);
+    auto quot = [](R x, R d, R rd) { return EXACT ? x / d : x * rd; };
+    const long long nh = (long long)g.nl * g.ne, nv = (long long)(g.nl - 1) * g.nc, i = gtid();
     const long long nc = g.nc;
-    if (r < nh) {
-        const int l = (int)(r / g.ne), e = (int)(r - (long long)l * g.ne);
+    const int nl = g.nl;
+    if (i < nh) {
+        const int l = (int)(i / g.ne), e = (int)(i - (long long)l * g.ne);
+        const int fr = g.from[e], to = g.to[e];
         const long long o = (long long)l * nc;
-        const R sc = R(0.5) * (sf.kh[q][o + g.to[e]] + sf.kh[q][o + g.from[e]]);
-        const R gr = sf.f_double[q] ? grad_h(g, (const double *)sf.f[q], l, e) : grad_h(g, (const R *)sf.f[q], l, e);
-        s.fh[(long long)q * nh + r] = sc * gr;
-    } else if (sf.vert[q]) {
-        const long long rv = r - nh;
+        const R nd = g.nd_h[i];
+        const bool oro = l >= nl - g.n_oro, below = l < nl - 1;
+        R w6f = R(0), w6t = R(0), w7f = R(0), w7t = R(0), d6f = R(1), d6t = R(1), d7f = R(1), d7t = R(1), sl = R(0);
+        if (oro) {
+            w6f = ipw_at(g, 6, l, fr);
+            w6t = ipw_at(g, 6, l, to);
+            d6f = g.nd_v[o + fr];
+            d6t = g.nd_v[o + to];
+            if (below) {
+                w7f = ipw_at(g, 7, l, fr);
+                w7t = ipw_at(g, 7, l, to);
+                d7f = g.nd_v[o + nc + fr];
+                d7t = g.nd_v[o + nc + to];
+            }
+            sl = g.slope_h[i];
+        }
+        const R rnd = EXACT ? R(0) : R(1) / nd, r6f = EXACT ? R(0) : R(1) / d6f, r6t = EXACT ? R(0) : R(1) / d6t;
+        const R r7f = EXACT ? R(0) : R(1) / d7f, r7t = EXACT ? R(0) : R(1) / d7t;
+        for (int q = 0; q < sf.nf; ++q) {
+            R gr = quot(sfield(sf, q, o + to) - sfield(sf, q, o + fr), nd, rnd);
+            if (oro) {
+                R cc = w6f * quot(sfield(sf, q, o - nc + fr) - sfield(sf, q, o + fr), d6f, r6f);
+                cc += w6t * quot(sfield(sf, q, o - nc + to) - sfield(sf, q, o + to), d6t, r6t);
+                if (below) {
+                    cc += w7f * quot(sfield(sf, q, o + fr) - sfield(sf, q, o + nc + fr), d7f, r7f);
+                    cc += w7t * quot(sfield(sf, q, o + to) - sfield(sf, q, o + nc + to), d7t, r7t);
+                }
+                cc = R(0.5) * cc;
+                gr += -sl * cc;
+            }
+            const R sc = R(0.5) * (sf.kh[q][o + to] + sf.kh[q][o + fr]);
+            s.fh[(long long)q * nh + i] = sc * gr;
+        }
+    } else if (i < nh + nv) {
+        const long long rv = i - nh;
         const int k = (int)(rv / nc) + 1, c = (int)(rv - (long long)(k - 1) * nc);
-        const R sc = R(0.5) * (sf.kv[q][(long long)(k - 1) * nc + c] + sf.kv[q][(long long)k * nc + c]);
-        const R gr = sf.f_double[q] ? grad_v(g, (const double *)sf.f[q], k, c) : grad_v(g, (const R *)sf.f[q], k, c);
-        s.fv[(long long)q * (g.nl + 1) * nc + (long long)k * nc + c] = sc * gr;
+        const long long up = (long long)(k - 1) * nc + c, lo = (long long)k * nc + c;
+        const R nd = g.nd_v[lo], rnd = EXACT ? R(0) : R(1) / nd;
+        for (int q = 0; q < sf.nf; ++q) {
+            if (!sf.vert[q]) continue;
+            const R sc = R(0.5) * (sf.kv[q][up] + sf.kv[q][lo]);
+            const R gr = quot(sfield(sf, q, up) - sfield(sf, q, lo), nd, rnd);
+            s.fv[(long long)q * (nl + 1) * nc + lo] = sc * gr;
+        }
     }
 }
 
-/* their divergences: divv_h, then add_vertical_divv (divergences.c:150-185) */
+/* their divergences, one thread per cell for every field: divv_h
+ * (divergences.c:14-64) and add_vertical_divv (:150-185).  The cell's edges,
+ * signs, face areas and terrain-correction weights are loaded once; the
+ * terms are summed in the reference's order (FP64 path) or as double-word
+ * pairs (mixed path), and the mixed path multiplies by 1 / volume */
 template <typename R>
 __global__ void kd_sdiff_div(HGrid<R> g, SFields<R> sf, DiffScratch<R> s)
 {
     const long long ns = (long long)g.nl * g.nc, i = gtid();
-    if (i >= (long long)sf.nf * ns) return;
-    const int q = (int)(i / ns);
-    const long long sidx = i - (long long)q * ns;
-    const int nl = g.nl, l = (int)(sidx / g.nc), c = (int)(sidx - (long long)l * g.nc);
-    const long long nc = g.nc;
-    double out = divv_h_cell(g, s.fh + (long long)q * nl * g.ne, l, c);
-    if (sf.vert[q]) {
-        const R *fv = s.fv + (long long)q * (nl + 1) * nc;
-        const R up = l == 0 ? R(0) : fv[(long long)l * nc + c];
-        const R lo = l == nl - 1 ? R(0) : fv[(long long)(l + 1) * nc + c];
-        const double comp_v = double(up * g.area_v[(long long)l * nc + c])
-                              - double(lo * g.area_v[(long long)(l + 1) * nc + c]);
-        out += 1 / double(g.volume[sidx]) * comp_v;
+    if (i >= ns) return;
+    const int nl = g.nl, n_oro = g.n_oro, l = (int)(i / g.nc), c = (int)(i - (long long)l * g.nc);
+    const long long nc = g.nc, ne = g.ne, nh = (long long)nl * ne;
+    const int n_edges = c < N_PENT ? 5 : 6;
+    int ej[6];
+    R sg[6], ar[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        const bool on = j < n_edges;
+        ej[j] = on ? g.adj[j * nc + c] : 0;
+        sg[j] = on ? R(g.adj_sign[j * nc + c]) : R(0);
+        ar[j] = on ? g.area_h[(long long)l * ne + ej[j]] : R(0);
     }
-    sf.out[q][sidx] = out;
+    /* terrain correction (averaging.c:41-95) at level l (up, from layers l-1
+     * and l) and level l+1 (lo, from layers l and l+1) */
+    const bool oro = l >= nl - n_oro - 1;
+    const bool need_up = oro && l != nl - n_oro - 1, need_lo = oro && l != nl - 1;
+    const bool up_prev = need_up && l > nl - n_oro, lo_prev = need_lo && l + 1 > nl - n_oro;
+    R wu0[6], wu1[6], wl1[6];
+    auto wcorr = [&](int ll, int j) { return R(-0.5) * ipw_at(g, j, ll, c) * g.slope_h[(long long)ll * ne + ej[j]]; };
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        const bool on = j < n_edges;
+        wu0[j] = on && up_prev ? wcorr(l - 1, j) : R(0);
+        wu1[j] = on && (need_up || lo_prev) ? wcorr(l, j) : R(0);
+        wl1[j] = on && need_lo ? wcorr(l + 1, j) : R(0);
+    }
+    const R area_up = g.area_v[(long long)l * nc + c], area_lo = g.area_v[(long long)(l + 1) * nc + c];
+    const bool exact = sizeof(R) == sizeof(double);
+    const double iv = exact ? 0.0 : sf.inv_vol[i];
+    for (int q = 0; q < sf.nf; ++q) {
+        const R *fh = s.fh + (long long)q * nh;
+        FluxSum<R> comp_h;
+        for (int j = 0; j < n_edges; ++j) comp_h.add(fh[(long long)l * ne + ej[j]] * sg[j] * ar[j]);
+        R up = R(0), lo = R(0);
+        if (need_up) {
+            if (up_prev)
+                for (int j = 0; j < n_edges; ++j) up += wu0[j] * fh[(long long)(l - 1) * ne + ej[j]];
+            for (int j = 0; j < n_edges; ++j) up += wu1[j] * fh[(long long)l * ne + ej[j]];
+        }
+        if (need_lo) {
+            if (lo_prev)
+                for (int j = 0; j < n_edges; ++j) lo += wu1[j] * fh[(long long)l * ne + ej[j]];
+            for (int j = 0; j < n_edges; ++j) lo += wl1[j] * fh[(long long)(l + 1) * ne + ej[j]];
+        }
+        R comp_v = R(0);
+        if (oro) {
+            if (l == nl - n_oro - 1) comp_v = -lo * area_lo;
+            else if (l == nl - 1) comp_v = up * area_up;
+            else comp_v = up * area_up - lo * area_lo;
+        }
+        double out = exact ? 1.0 / double(g.volume[i]) * (comp_h.value() + double(comp_v))
+                           : iv * (comp_h.value() + double(comp_v));
+        if (sf.vert[q]) {
+            const R *fv = s.fv + (long long)q * (nl + 1) * nc;
+            const R vu = l == 0 ? R(0) : fv[(long long)l * nc + c];
+            const R vl = l == nl - 1 ? R(0) : fv[(long long)(l + 1) * nc + c];
+            const double cv = double(vu * area_up) - double(vl * area_lo);
+            out += exact ? 1 / double(g.volume[i]) * cv : iv * cv;
+        }
+        sf.out[q][i] = out;
+    }
 }
 
 /* the momentum part of the branch (vector_tendencies_expl.c:41-69) */
@@ -532,6 +633,11 @@ void diffusion_momentum(Context *c, const StepParams &p, const HGrid<R> &g, cons
         }
         c->kernel_launches += 4;
     }
+    if (V) {
+        ProfScope ps(c, "kd_wdiff_a");
+        kd_wdiff_a<R><<<dnb(ns), 256, 0, st>>>(g, dg, gas, sv, b, s);
+        c->kernel_launches++;
+    }
     {
         ProfScope ps(c, "kd_fric_h");
         if (H && V) kd_fric_h<R, true, true><<<dnb(nh), 256, 0, st>>>(g, dg, c->n_const, gas, sv, b, s);
@@ -540,10 +646,6 @@ void diffusion_momentum(Context *c, const StepParams &p, const HGrid<R> &g, cons
         if (H || V) c->kernel_launches++;
     }
     if (V) {
-        {
-            ProfScope ps(c, "kd_wdiff_a");
-            kd_wdiff_a<R><<<dnb(ns), 256, 0, st>>>(g, dg, gas, sv, b, s);
-        }
         {
             ProfScope ps(c, "kd_wdiff_b");
             kd_wdiff_b<R><<<dnb(nh), 256, 0, st>>>(g, b, s);
@@ -556,7 +658,7 @@ void diffusion_momentum(Context *c, const StepParams &p, const HGrid<R> &g, cons
             ProfScope ps(c, "kd_wdiff_d");
             kd_wdiff_d<R><<<dnb((long long)(c->nl - 1) * c->nc), 256, 0, st>>>(g, c->n_const, sv, b, s);
         }
-        c->kernel_launches += 4;
+        c->kernel_launches += 3;
     }
     if (H) {
         ProfScope ps(c, "kd_dissipation");
@@ -611,14 +713,15 @@ void diffusion_scalar(Context *c, const StepParams &p, const HGrid<R> &g, const 
             sf.out[sf.nf] = b.mdt + (long long)k * ns;
             ++sf.nf;
         }
+    sf.inv_vol = c->inv_vol;
     const long long per = (long long)c->nl * c->ne + (long long)(c->nl - 1) * c->nc;
     {
         ProfScope ps(c, "kd_sdiff_flux");
-        kd_sdiff_flux<R><<<dnb(sf.nf * per), 256, 0, st>>>(g, sf, s);
+        kd_sdiff_flux<R><<<dnb(per), 256, 0, st>>>(g, sf, s);
     }
     {
         ProfScope ps(c, "kd_sdiff_div");
-        kd_sdiff_div<R><<<dnb(sf.nf * ns), 256, 0, st>>>(g, sf, s);
+        kd_sdiff_div<R><<<dnb(ns, 128), 128, 0, st>>>(g, sf, s);
     }
     c->kernel_launches += 2;
 }
