@@ -35,7 +35,7 @@ class OrcGrid(ctypes.Structure):
         (n, dp) for n in ("dual_area", "dual_z_vector", "f_vec")] + [
         (n, ip) for n in ("dual_from", "dual_to", "vort_idx", "vort_sign")] + [("gravity_potential", dp)] + [
         (n, dp) for n in ("layer_thickness", "dual_normal_distance")] + [
-        (n, ctypes.c_double) for n in ("eff_hor_res", "mean_velocity_area")]
+        (n, ctypes.c_double) for n in ("eff_hor_res", "mean_velocity_area")] + [("latitude_scalar", dp)]
 
 
 class OrcState(ctypes.Structure):
@@ -48,7 +48,8 @@ class OrcDiag(ctypes.Structure):
 
 class OrcForcings(ctypes.Structure):
     _fields_ = [(n, dp) for n in ("pgrad_acc_old", "pgrad_nl", "pgrad_l", "pgrad_condensates_v",
-                                  "v_squared_grad", "pot_vort_tend", "radiation_tendency")]
+                                  "v_squared_grad", "pot_vort_tend", "radiation_tendency", "sfc_sw_in",
+                                  "sfc_lw_out")]
 
 
 class OrcIrrev(ctypes.Structure):
@@ -104,7 +105,7 @@ class Oracle:
                          _d(dg["f_vec"]), _i(dg["from_index"]), _i(dg["to_index"]),
                          _i(dg["vorticity_indices_triangles"]), _i(dg["vorticity_signs_triangles"]),
                          _d(g["gravity_potential"]), _d(g["layer_thickness"]), _d(dg["normal_distance"]),
-                         float(g["eff_hor_res"][0]), float(g["mean_velocity_area"][0]))
+                         float(g["eff_hor_res"][0]), float(g["mean_velocity_area"][0]), _d(g["latitude_scalar"]))
         self.lib = lib()
 
     def state(self, s):
@@ -118,7 +119,8 @@ class Oracle:
         f = self.m.forcings
         return OrcForcings(*[_d(f[n]) for n in ("pgrad_acc_old", "pressure_gradient_acc_neg_nl",
                                                 "pressure_gradient_acc_neg_l", "pressure_grad_condensates_v",
-                                                "v_squared_grad", "pot_vort_tend", "radiation_tendency")])
+                                                "v_squared_grad", "pot_vort_tend", "radiation_tendency",
+                                                "sfc_sw_in", "sfc_lw_out")])
 
     def irrev(self):
         r = self.m.irrev

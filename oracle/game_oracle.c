@@ -1096,6 +1096,101 @@ int orc_scalar_diffusion_coeffs(const orc_grid *g, const orc_state *s, const orc
     return 0;
 }
 
+/* ------------------------------------------------- Held-Suarez forcing
+ * (rad_on = 2, pbl_scheme = 2) */
+#define P_HS_0 100000.0
+
+/* src/radiation/held_suar.c:34-46 */
+static double hs_t_eq(double latitude, double pressure)
+{
+    double delta_t_y = 60.0, delta_theta_v_z = 10.0, kappa = 2.0 / 7.0, result = 315.0;
+    result = result - delta_t_y * pow(sin(latitude), 2.0);
+    result = result - delta_theta_v_z * log(pressure / P_HS_0) * pow(cos(latitude), 2.0);
+    result = result * pow(pressure / P_HS_0, kappa);
+    result = fmax(200.0, result);
+    return result;
+}
+
+/* src/radiation/held_suar.c:48-56 */
+static double hs_k_T(double latitude, double pressure)
+{
+    double k_a = 1.0 / 40.0 * 1.0 / 86400.0, k_s = 1.0 / 4.0 * 1.0 / 86400.0, sigma_b = 0.7;
+    double sigma = pressure / P_HS_0;
+    return k_a + (k_s - k_a) * fmax(0.0, (sigma - sigma_b) / (1.0 - sigma_b)) * pow(cos(latitude), 4.0);
+}
+
+/* src/radiation/held_suar.c:18-32 through call_radiation
+ * (manage_radiation_calls.c:22-78).  The reference cuts the scalar points
+ * into NO_OF_RAD_BLOCKS = 18 blocks of NO_OF_SCALARS/18 points, reshaped into
+ * (NO_OF_SCALARS/18)/NO_OF_LAYERS columns each; every point's tendency
+ * depends on its own values only, so the blocks just select the points: the
+ * first 18 * columns-per-block cells of every layer.  When NO_OF_SCALARS/18
+ * is not a multiple of the layer count the reference's loops run into a
+ * layer NO_OF_LAYERS and write past the end of radiation_tendency; such grids
+ * are refused (-1).  The blocks' surface fluxes, which Held-Suarez leaves at
+ * zero, are copied back for the covered cells. */
+int orc_held_suarez_radiation(const orc_grid *g, const orc_state *s, const orc_diag *d, orc_forcings *f)
+{
+    const long n_rad = NS / 18, per_layer = n_rad / NL, covered = 18 * per_layer;
+    if (n_rad % NL != 0) return -1;
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) {
+        long layer = i / NC, h = i - layer * NC;
+        if (h >= covered) continue;
+        double rg = s->rho[COND * NS + i], t = d->temperature[i];
+        double pressure = rg * R_D * t;
+        f->radiation_tendency[i] = -hs_k_T(g->latitude_scalar[h], pressure) * (t - hs_t_eq(g->latitude_scalar[h], pressure));
+        f->radiation_tendency[i] = C_D_V * rg * f->radiation_tendency[i];
+    }
+    for (long h = 0; h < covered; ++h) f->sfc_sw_in[h] = f->sfc_lw_out[h] = 0.0;
+    return 0;
+}
+
+/* src/constituents/derived_quantities.c:42-61 */
+static double gas_constant_diagnostics(const orc_grid *g, const orc_state *s, long i)
+{
+    double result = 0.0;
+    if (!g->moisture_on) result = R_D;
+    if (g->moisture_on) {
+        result = (s->rho[COND * NS + i] - s->rho[(COND + 1) * NS + i]) * R_D + s->rho[(COND + 1) * NS + i] * R_V;
+        result = result / s->rho[COND * NS + i];
+    }
+    return result;
+}
+
+/* boundary-layer friction of the Held-Suarez test
+ * (src/subgrid_scale/planetary_boundary_layer.c:141-197), added to the
+ * friction acceleration of every horizontal wind point */
+int orc_pbl_held_suarez(const orc_grid *g, const orc_state *s, const orc_diag *d, orc_irrev *ir)
+{
+    const double bndr_lr_visc_max = 1.0 / 86400.0, sigma_b = 0.7, lapse = 0.0065;
+    ORC_PAR
+    for (long i = 0; i < (long)NL * NE; ++i) {
+        long layer = i / NE, h = i - layer * NE, vi = NC + layer * VPL + h;
+        long f = g->from[h], t = g->to[h];
+        double exner_from = g->exner_bg[layer * NC + f] + s->exner_pert[layer * NC + f];
+        double exner_to = g->exner_bg[layer * NC + t] + s->exner_pert[layer * NC + t];
+        double pressure_from = P_HS_0 * pow(exner_from, C_D_P / R_D);
+        double pressure_to = P_HS_0 * pow(exner_to, C_D_P / R_D);
+        double pressure = 0.5 * (pressure_from + pressure_to);
+        double psfc[2];
+        for (int side = 0; side < 2; ++side) {
+            long c = side == 0 ? f : t, lo = (NL - 1) * NC + c;
+            double temp_lowest_layer = d->temperature[lo];
+            double exner = g->exner_bg[lo] + s->exner_pert[lo];
+            double pressure_value_lowest_layer = P_HS_0 * pow(exner, C_D_P / R_D);
+            double temp_surface = temp_lowest_layer + lapse * (g->z_scalar[c + (NL - 1) * NC] - g->z_vector[NV - NC + c]);
+            double surface_p_factor = pow(1.0 - (temp_surface - temp_lowest_layer) / temp_surface,
+                                          g->gravity_m[(NL - 1) * VPL + c] / (gas_constant_diagnostics(g, s, lo) * lapse));
+            psfc[side] = pressure_value_lowest_layer / surface_p_factor;
+        }
+        double pressure_sfc = 0.5 * (psfc[0] + psfc[1]);
+        double sigma = pressure / pressure_sfc;
+        ir->friction_acc[vi] += -bndr_lr_visc_max * fmax(0.0, (sigma - sigma_b) / (1.0 - sigma_b)) * s->wind[vi];
+    }
+    return 0;
+}
+
 /* ------------------------------------------------- explicit tendencies
  * src/time_stepping/vector_tendencies_expl.c:18-133 */
 int orc_vector_tendencies_expl(const orc_grid *g, const orc_state *s, orc_state *tend, orc_diag *d,
@@ -1116,8 +1211,9 @@ int orc_vector_tendencies_expl(const orc_grid *g, const orc_state *s, orc_state 
         }
         if (c->momentum_diff_h) orc_hor_momentum_diffusion(g, s, d, ir);
         if (c->momentum_diff_v) orc_vert_momentum_diffusion(g, s, d, ir);
-        if (c->pbl_scheme > 0) return -1;
-        if (c->momentum_diff_h) orc_simple_dissipation_rate(g, s, ir);
+        if (c->pbl_scheme == 1) return -1;
+        if (c->pbl_scheme == 2) orc_pbl_held_suarez(g, s, d, ir);
+        if (c->momentum_diff_h || c->pbl_scheme > 0) orc_simple_dissipation_rate(g, s, ir);
     }
     double new_w = rk_step == 1 ? 0.5 : 1.0, old_w = 1.0 - new_w;
     double cur_hor = 0.5 + c->impl_thermo_weight, old_hor = 1.0 - cur_hor, cur_ver = 1.0 - c->impl_thermo_weight;
@@ -1416,7 +1512,8 @@ int orc_manage_rkhevi(const orc_grid *g, const orc_state *so, orc_state *sn, orc
                       orc_forcings *f, orc_irrev *ir, const orc_config *c, double dt, double t)
 {
     (void)t;
-    if (c->sfc_sensible_heat_flux || c->sfc_phase_trans || c->pbl_scheme || c->rad_on || c->prog_soil_temp)
+    if (c->sfc_sensible_heat_flux || c->sfc_phase_trans || c->pbl_scheme == 1 || c->pbl_scheme > 2 || c->rad_on == 1
+        || c->rad_on > 2 || c->prog_soil_temp)
         return -1;
     orc_temperature_diagnostics(g, so, d);
     if (g->moisture_on) orc_calc_h2otracers_source_rates(g, so, d, c, ir, dt);
@@ -1430,6 +1527,9 @@ int orc_manage_rkhevi(const orc_grid *g, const orc_state *so, orc_state *sn, orc
                 long vi = NC + l * VPL + e;
                 sn->wind[vi] = so->wind[vi] + dt * st->wind[vi];
             }
+        /* radiation: the Held-Suarez forcing, on state_old (manage_rkhevi.c:80-84) */
+        if (c->rad_on == 2 && c->rad_update == 1 && rk == 0)
+            if (orc_held_suarez_radiation(g, so, d, f)) return -1;
         if (orc_scalar_tendencies_expl(g, so, sn, st, dt, d, f, ir, c, rk)) return -1;
         if (orc_three_band_solver_ver_waves(g, so, sn, st, c, dt, rk)) return -1;
         if (g->n_const > 1) orc_three_band_solver_gen_densities(g, so, sn, st, d, ir, c, dt, rk);

@@ -31,6 +31,8 @@ typedef struct orc_grid {
     /* diffusion branch */
     const double *layer_thickness, *dual_normal_distance;
     double eff_hor_res, mean_velocity_area;
+    /* Held-Suarez forcing */
+    const double *latitude_scalar;
 } orc_grid;
 
 typedef struct orc_state {
@@ -50,6 +52,7 @@ typedef struct orc_diag {
 typedef struct orc_forcings {
     double *pgrad_acc_old, *pgrad_nl, *pgrad_l, *pgrad_condensates_v, *v_squared_grad, *pot_vort_tend;
     double *radiation_tendency;
+    double *sfc_sw_in, *sfc_lw_out; /* Held-Suarez forcing: written as zero */
 } orc_forcings;
 
 typedef struct orc_irrev {
@@ -106,6 +109,9 @@ int orc_vert_momentum_diffusion(const orc_grid *g, const orc_state *s, orc_diag 
 int orc_simple_dissipation_rate(const orc_grid *g, const orc_state *s, orc_irrev *ir);
 int orc_scalar_diffusion_coeffs(const orc_grid *g, const orc_state *s, const orc_config *c, orc_irrev *ir,
                                 orc_diag *d);
+/* Held-Suarez forcing (src/radiation/held_suar.c, planetary_boundary_layer.c) */
+int orc_held_suarez_radiation(const orc_grid *g, const orc_state *s, const orc_diag *d, orc_forcings *f);
+int orc_pbl_held_suarez(const orc_grid *g, const orc_state *s, const orc_diag *d, orc_irrev *ir);
 int orc_vector_tendencies_expl(const orc_grid *g, const orc_state *s, orc_state *tend, orc_diag *d,
                                orc_forcings *f, orc_irrev *ir, const orc_config *c, int rk_step, double dt);
 int orc_scalar_tendencies_expl(const orc_grid *g, const orc_state *s_old, const orc_state *s, orc_state *tend,

@@ -113,3 +113,32 @@ def test_oracle_bitwise_equals_reference_with_diffusion(cfg):
             a, b = getattr(m_ref, k).buf, getattr(m_orc, k).buf
             assert np.array_equal(a, b), f"step {n}: {k} differs in {np.count_nonzero(a != b)} bytes"
     assert np.any(m_orc.irrev["friction_acc"] != 0) or "momentum" not in "".join(switches)
+
+
+@pytest.mark.parametrize("moist,case,mountain", [(0, "std_wind_tpert", True), (1, "tracers", False)],
+                         ids=["dry-oro", "moist"])
+def test_oracle_bitwise_equals_reference_held_suarez(moist, case, mountain):
+    """the reference's Held-Suarez run configuration (run_scripts/held_suar.sh:
+    rad_on = 2, pbl_scheme = 2, horizontal momentum diffusion), the radiation
+    updated at every other step as the reference's driver does for a longer
+    radiation time step.  RES_ID = 5: its 10242 cells per layer split into the
+    reference's 18 radiation blocks exactly (on RES3/4/6 grids with 26 layers
+    the reference's block loops write past the end of radiation_tendency)."""
+    _, m_ref = make_model(5, moist, case, mountain)
+    with_diffusion(m_ref, ("momentum_diff_h",))
+    m_ref.config["rad_on"][0] = 2
+    m_ref.config["pbl_scheme"][0] = 2
+    m_orc = clone(m_ref)
+    ref = refbind.Reference(m_ref)
+    orc = Oracle(m_orc)
+    driver.start(m_ref, ref.linear_combine_two_states)
+    driver.start(m_orc, orc.linear_combine_two_states)
+    for n in range(4):
+        for m in (m_ref, m_orc):
+            m.config["rad_update"][0] = 1 if n % 2 == 0 else 0
+        driver.step(m_ref, ref.linear_combine_two_states, ref.manage_rkhevi, 300.0, n * 300.0)
+        driver.step(m_orc, orc.linear_combine_two_states, orc.manage_rkhevi, 300.0, n * 300.0)
+        for k in ("state_old", "state_new", "state_tendency", "diagnostics", "forcings", "irrev"):
+            a, b = getattr(m_ref, k).buf, getattr(m_orc, k).buf
+            assert np.array_equal(a, b), f"step {n}: {k} differs in {np.count_nonzero(a != b)} bytes"
+    assert np.any(m_orc.forcings["radiation_tendency"] != 0)
