@@ -97,22 +97,37 @@ int diff_flags(const void *config)
     int f = 0;
     for (int k = 0; k < 6; ++k)
         if (*member<int>(config, GAME_CONFIG, DIFF_SWITCHES[k]) != 0) f |= 1 << k;
+    if (*member<int>(config, GAME_CONFIG, "pbl_scheme") == 2) f |= DIFF_PBL_HS;
+    if (*member<int>(config, GAME_CONFIG, "rad_on") == 2 && *member<int>(config, GAME_CONFIG, "rad_update") == 1)
+        f |= DIFF_RAD_HS;
     return f;
 }
 
-/* radiation, PBL, surface fluxes and soil are never part of this library's
- * step; the diffusion branch is, in manage_rkhevi (allow_diffusion) */
+/* RTE+RRTMGP radiation (rad_on = 1), the NWP boundary layer (pbl_scheme = 1),
+ * surface fluxes and soil are never part of this library's step.  The
+ * diffusion branch and the Held-Suarez forcing (rad_on = 2, pbl_scheme = 2)
+ * are, in manage_rkhevi (allow_diffusion); the other entry points refuse
+ * every one of these switches */
 int check_config(const void *config, bool allow_diffusion = false)
 {
-    static const char *off_switches[] = {"rad_on", "prog_soil_temp", "sfc_phase_trans", "sfc_sensible_heat_flux",
-                                         "pbl_scheme"};
+    static const char *off_switches[] = {"prog_soil_temp", "sfc_phase_trans", "sfc_sensible_heat_flux"};
     for (const char *s : off_switches)
         if (*member<int>(config, GAME_CONFIG, s) != 0)
-            return fail(std::string("config switch ") + s + " is on; PBL, surface fluxes, soil and radiation are not part of this library's step");
+            return fail(std::string("config switch ") + s + " is on; surface fluxes and soil are not part of this library's step");
+    const int rad_on = *member<int>(config, GAME_CONFIG, "rad_on"), pbl = *member<int>(config, GAME_CONFIG, "pbl_scheme");
+    if (rad_on != 0 && !(allow_diffusion && rad_on == 2))
+        return fail(allow_diffusion ? "config switch rad_on is 1: RTE+RRTMGP radiation is not part of this library's step (rad_on = 2, Held-Suarez, is)"
+                                    : "config switch rad_on is on; this entry point has no radiation (manage_rkhevi has the Held-Suarez forcing)");
+    if (pbl != 0 && !(allow_diffusion && pbl == 2))
+        return fail(allow_diffusion ? "config switch pbl_scheme is 1: the NWP boundary layer is not part of this library's step (pbl_scheme = 2, Held-Suarez, is)"
+                                    : "config switch pbl_scheme is on; this entry point has no boundary layer (manage_rkhevi has the Held-Suarez friction)");
     if (!allow_diffusion)
         for (const char *s : DIFF_SWITCHES)
             if (*member<int>(config, GAME_CONFIG, s) != 0)
                 return fail(std::string("config switch ") + s + " is on; this entry point has no diffusion branch (manage_rkhevi has)");
+    if (rad_on == 2 && !ctx()->rad_blocks_ok)
+        return fail("rad_on = 2: the reference's 18 radiation blocks do not tile this grid (NO_OF_SCALARS / 18 is not a "
+                    "multiple of NO_OF_LAYERS; the reference's own block loops write past radiation_tendency here)");
     return 0;
 }
 
@@ -390,6 +405,11 @@ int game_gpu_sync_aux_to_host(struct diagnostics *diagnostics, struct forcings *
             if (download_field(member<double>(f.base, f.sid, f.name), f.dev, c->map_s, ns, ns, 0, ns)) return -1;
             CK(cudaStreamSynchronize(c->stream));
         }
+        if (forcings) {
+            if (download_field(member<double>(forcings, GAME_FORCINGS, "radiation_tendency"), b.rad, c->map_s, ns, ns, 0,
+                               ns)) return -1;
+            CK(cudaStreamSynchronize(c->stream));
+        }
         if (irrev) {
             double *mdt = member<double>(irrev, GAME_IRREV, "mass_diff_tendency");
             for (int k = 0; k < c->n_const; ++k) {
@@ -530,6 +550,12 @@ int manage_rkhevi(struct state *state_old, struct state *state_new, struct grid 
     StepParams p = params_from_config(c, config, delta_t);
     p.diff = diff_flags(config);
     p.irr = c->irr_active;
+    if (p.diff & DIFF_RAD_HS) {
+        /* the Held-Suarez radiation blocks hand back zero surface fluxes
+         * (manage_radiation_calls.c:71-72) */
+        std::memset(member<double>(forcings, GAME_FORCINGS, "sfc_sw_in"), 0, (size_t)c->rad_covered * sizeof(double));
+        std::memset(member<double>(forcings, GAME_FORCINGS, "sfc_lw_out"), 0, (size_t)c->rad_covered * sizeof(double));
+    }
     if (run_device_step(c, p, so, sn, st)) return -1;
     if (!c->resident) {
         if (download_state(state_new, sn, 1 | 2 | 4 | 8 | 16)) return -1;

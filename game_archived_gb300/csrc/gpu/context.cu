@@ -382,8 +382,22 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
         for (int e = 0; e < NE; ++e) h_dnds[e] = dnd[(long long)L * DPL + en[e]];
         const Dual lt = dual_upload(c, h_lt), dndt = dual_upload(c, h_dndt), dnds = dual_upload(c, h_dnds),
                    zvi = dual_upload(c, iface_field(zv));
-        c->dg64 = {lt.d, dndt.d, dnds.d, zvi.d, *GD("eff_hor_res"), *GD("mean_velocity_area")};
-        c->dg32 = {lt.f, dndt.f, dnds.f, zvi.f, *GD("eff_hor_res"), *GD("mean_velocity_area")};
+        /* Held-Suarez radiation: the reference's 18 radiation blocks take
+         * (NS / 18) / L columns each, the first 18 * that cells of every layer
+         * in its numbering (manage_radiation_calls.c:86-100) */
+        const long long n_rad = NS / 18, per_block = n_rad / L;
+        c->rad_blocks_ok = n_rad % L == 0;
+        std::vector<double> h_lat(NC);
+        std::vector<int> h_cov(NC);
+        for (int i = 0; i < NC; ++i) {
+            h_lat[i] = lat[cn[i]];
+            h_cov[i] = cn[i] < 18 * per_block ? 1 : 0;
+        }
+        const Dual zsc = dual_upload(c, h_zs), lat_d = dual_upload(c, h_lat);
+        const int *cov = dupload(c, h_cov);
+        c->rad_covered = (int)(18 * per_block);
+        c->dg64 = {lt.d, dndt.d, dnds.d, zvi.d, zsc.d, lat_d.d, cov, *GD("eff_hor_res"), *GD("mean_velocity_area")};
+        c->dg32 = {lt.f, dndt.f, dnds.f, zvi.f, zsc.f, lat_d.f, cov, *GD("eff_hor_res"), *GD("mean_velocity_area")};
     }
 
     /* ---- upload */
@@ -607,6 +621,7 @@ int ensure_diff_buffers(Context *c)
         {&b->adv, S}, {&b->vint, S}, {&b->wdv, S}, {&b->tri, L * NT}, {&b->zt, L * NT}, {&b->zr, L * NE},
         {&b->s1, S}, {&b->s2, S}, {&b->s3, S}, {&b->flx, L * NE}, {&b->mch, S}, {&b->mcv, S}, {&b->tch, S},
         {&b->tcv, S}, {&b->fh, (C + 1) * L * NE}, {&b->fv, (C + 1) * (L + 1) * NC}, {&b->kvt, S},
+        {&b->hs_p, S}, {&b->hs_ps, NC},
     };
     for (auto &w : want)
         if (!(*w.p = dalloc<double>(c, w.n))) return fail("device allocation of the diffusion fields failed");

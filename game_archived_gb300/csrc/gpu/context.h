@@ -154,6 +154,10 @@ struct Context {
     DiffGrid<float> dg32{};
     DiffBufs *dbuf = nullptr;
     int irr_active = 0;
+    /* Held-Suarez radiation: whether the reference's radiation blocks tile
+     * the grid without overrunning radiation_tendency, and how many cells of
+     * a layer (in reference numbering) they cover */
+    int rad_blocks_ok = 0, rad_covered = 0;
     int use_graphs = 1;
     int column_solver = 0; /* 0 by layer count, 1 per-thread sweeps, 2 warp cyclic reduction */
     int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */

@@ -130,7 +130,10 @@ static_assert(sizeof(StepParams) == 8 * sizeof(int) + 14 * sizeof(double) + 4 * 
 
 /* config switches of the diffusion branch (StepParams::diff) */
 enum {
-    DIFF_MOM_H = 1, DIFF_MOM_V = 2, DIFF_TEMP_H = 4, DIFF_TEMP_V = 8, DIFF_MASS_H = 16, DIFF_MASS_V = 32
+    DIFF_MOM_H = 1, DIFF_MOM_V = 2, DIFF_TEMP_H = 4, DIFF_TEMP_V = 8, DIFF_MASS_H = 16, DIFF_MASS_V = 32,
+    /* Held-Suarez forcing: boundary-layer friction (pbl_scheme = 2) and the
+     * radiation relaxation updated in this step (rad_on = 2, rad_update = 1) */
+    DIFF_PBL_HS = 64, DIFF_RAD_HS = 128
 };
 
 /* tables of the diffusion branch in the horizontal precision R */
@@ -140,6 +143,9 @@ struct DiffGrid {
     const R *dual_nd_t;       /* [L][Nt] vertical extent of the triangle prisms (dual normal distance) */
     const R *dual_nd_sfc;     /* [Ne] dual normal distance of the surface level's edges */
     const R *z_v;             /* [L+1][Nc] height of the interfaces */
+    const R *z_scalar;        /* [L][Nc] height of the cell centres */
+    const R *lat;             /* [Nc] latitude */
+    const int *rad_cov;       /* [Nc] 1 where the reference's radiation blocks reach the cell */
     double eff_hor_res, mean_velocity_area;
 };
 
@@ -157,20 +163,21 @@ struct DiffBufs {
     double *mch, *mcv, *tch, *tcv; /* mass / temperature diffusion coefficients, h and v */
     double *fh, *fv;               /* diffusive fluxes of T and the C densities: [C+1][L][Ne], [C+1][L+1][Nc] */
     double *kvt;                   /* turbulent vertical diffusivity of the cells [L][Nc] */
+    double *hs_p, *hs_ps;          /* Held-Suarez boundary layer: pressure [L][Nc], surface pressure [Nc] */
 };
 
 /* the scratch part of DiffBufs in precision R (on the mixed path the double
  * allocations hold float arrays of the same length) */
 template <typename R>
 struct DiffScratch {
-    R *adv, *vint, *wdv, *tri, *zt, *zr, *s1, *s2, *s3, *flx, *mch, *mcv, *tch, *tcv, *fh, *fv, *kvt;
+    R *adv, *vint, *wdv, *tri, *zt, *zr, *s1, *s2, *s3, *flx, *mch, *mcv, *tch, *tcv, *fh, *fv, *kvt, *hs_p, *hs_ps;
 };
 template <typename R>
 inline DiffScratch<R> diff_scratch(const DiffBufs &b)
 {
     return {(R *)b.adv, (R *)b.vint, (R *)b.wdv, (R *)b.tri, (R *)b.zt, (R *)b.zr, (R *)b.s1, (R *)b.s2,
             (R *)b.s3, (R *)b.flx, (R *)b.mch, (R *)b.mcv, (R *)b.tch, (R *)b.tcv, (R *)b.fh, (R *)b.fv,
-            (R *)b.kvt};
+            (R *)b.kvt, (R *)b.hs_p, (R *)b.hs_ps};
 }
 
 }  // namespace game

@@ -410,6 +410,89 @@ __global__ void kd_dissipation(HGrid<R> g, int n_const, SView<R> sv, DiffBufs b)
     b.hdiss[i] = double(-density_total_r(sv.rho, n_const, ns, i) * r);
 }
 
+/* ------------------------------------------------- Held-Suarez forcing */
+
+/* boundary-layer friction of the Held-Suarez test
+ * (src/subgrid_scale/planetary_boundary_layer.c:141-197), step a per cell:
+ * the layer's pressure and, in the lowest layer, the surface pressure
+ * extrapolated with the standard lapse rate; the reference evaluates both at
+ * each edge's two cells, the same values */
+template <typename R>
+__global__ void kd_pbl_hs_cell(HGrid<R> g, DiffGrid<R> dg, int gas, int moist, const double *temperature, SView<R> sv,
+                               DiffScratch<R> s)
+{
+    const long long ns = (long long)g.nl * g.nc, i = gtid();
+    if (i >= ns) return;
+    const int nl = g.nl, l = (int)(i / g.nc), c = (int)(i - (long long)l * g.nc);
+    const R exner = g.exner_bg[i] + sv.exner_pert[i];
+    const R p = R(P_0) * pow(exner, R(C_D_P / R_D));
+    s.hs_p[i] = p;
+    if (l == nl - 1) {
+        const R lapse = R(0.0065);
+        const R temp_lowest_layer = R(temperature[i]);
+        const R temp_surface = temp_lowest_layer + lapse * (dg.z_scalar[i] - dg.z_v[(long long)nl * g.nc + c]);
+        R gas_constant = R(R_D);
+        if (moist) {
+            const R rg = sv.rho[gas * ns + i], rv = sv.rho[(gas + 1) * ns + i];
+            gas_constant = (rg - rv) * R(R_D) + rv * R(R_V);
+            gas_constant = gas_constant / rg;
+        }
+        const R surface_p_factor = pow(R(1) - (temp_surface - temp_lowest_layer) / temp_surface,
+                                       g.gravity_m_v[(long long)(nl - 1) * g.nc + c] / (gas_constant * lapse));
+        s.hs_ps[c] = p / surface_p_factor;
+    }
+}
+
+/* step b per edge: Rayleigh friction below sigma = 0.7, added to the
+ * friction acceleration */
+template <typename R>
+__global__ void kd_pbl_hs(HGrid<R> g, SView<R> sv, DiffBufs b, DiffScratch<R> s)
+{
+    const long long n = (long long)g.nl * g.ne, i = gtid();
+    if (i >= n) return;
+    const long long nw = (long long)(g.nl + 1) * g.nc;
+    const int l = (int)(i / g.ne), e = (int)(i - (long long)l * g.ne);
+    const long long o = (long long)l * g.nc;
+    const R pressure = R(0.5) * (s.hs_p[o + g.from[e]] + s.hs_p[o + g.to[e]]);
+    const R pressure_sfc = R(0.5) * (s.hs_ps[g.from[e]] + s.hs_ps[g.to[e]]);
+    const R sigma = pressure / pressure_sfc, sigma_b = R(0.7);
+    const R fa = R(b.fric[nw + i]) + -R(1.0 / 86400.0) * fmax(R(0), (sigma - sigma_b) / (R(1) - sigma_b)) * sv.u[i];
+    b.fric[nw + i] = double(fa);
+}
+
+/* Held-Suarez radiative forcing (src/radiation/held_suar.c:18-56), FP64 on
+ * both paths (it is updated only every radiation time step), at the cells the
+ * reference's radiation blocks reach */
+__device__ __forceinline__ double hs_t_eq(double latitude, double pressure)
+{
+    const double delta_t_y = 60.0, delta_theta_v_z = 10.0, kappa = 2.0 / 7.0;
+    double result = 315.0;
+    result = result - delta_t_y * pow(sin(latitude), 2.0);
+    result = result - delta_theta_v_z * log(pressure / P_0) * pow(cos(latitude), 2.0);
+    result = result * pow(pressure / P_0, kappa);
+    return fmax(200.0, result);
+}
+
+__device__ __forceinline__ double hs_k_t(double latitude, double pressure)
+{
+    const double k_a = 1.0 / 40.0 * 1.0 / 86400.0, k_s = 1.0 / 4.0 * 1.0 / 86400.0, sigma_b = 0.7;
+    const double sigma = pressure / P_0;
+    return k_a + (k_s - k_a) * fmax(0.0, (sigma - sigma_b) / (1.0 - sigma_b)) * pow(cos(latitude), 4.0);
+}
+
+__global__ void kd_hs_rad(long long ns, int nc, int gas, const double *lat, const int *cov, const double *temperature,
+                          DState so, double *rad)
+{
+    const long long i = gtid();
+    if (i >= ns) return;
+    const int c = (int)(i % nc);
+    if (!cov[c]) return;
+    const double rg = so.rho[gas * ns + i], t = temperature[i];
+    const double pressure = rg * R_D * t;
+    double r = -hs_k_t(lat[c], pressure) * (t - hs_t_eq(lat[c], pressure));
+    rad[i] = C_D_V * rg * r;
+}
+
 /* -------------------------------------------------------------- scalars */
 
 /* scalar_diffusion_coeffs (effective_diff_coeffs.c:203-229); c_v as
@@ -596,8 +679,8 @@ void diffusion_momentum(Context *c, const StepParams &p, const HGrid<R> &g, cons
                         const SView<R> &sv)
 {
     const bool any_h = p.diff & (DIFF_MOM_H | DIFF_TEMP_H | DIFF_MASS_H);
-    const bool H = p.diff & DIFF_MOM_H, V = p.diff & DIFF_MOM_V;
-    if (!any_h && !V) return;
+    const bool H = p.diff & DIFF_MOM_H, V = p.diff & DIFF_MOM_V, PBL = p.diff & DIFF_PBL_HS;
+    if (!any_h && !V && !PBL) return;
     DiffBufs &b = *c->dbuf;
     const DiffScratch<R> s = diff_scratch<R>(b);
     const long long ns = c->ns, nh = (long long)c->nl * c->ne;
@@ -660,7 +743,18 @@ void diffusion_momentum(Context *c, const StepParams &p, const HGrid<R> &g, cons
         }
         c->kernel_launches += 3;
     }
-    if (H) {
+    if (PBL) {
+        {
+            ProfScope ps(c, "kd_pbl_hs_cell");
+            kd_pbl_hs_cell<R><<<dnb(ns), 256, 0, st>>>(g, dg, gas, c->moist, c->temperature, sv, s);
+        }
+        {
+            ProfScope ps(c, "kd_pbl_hs");
+            kd_pbl_hs<R><<<dnb(nh), 256, 0, st>>>(g, sv, b, s);
+        }
+        c->kernel_launches += 2;
+    }
+    if (H || PBL) {
         ProfScope ps(c, "kd_dissipation");
         kd_dissipation<R><<<dnb(ns), 256, 0, st>>>(g, c->n_const, sv, b);
         c->kernel_launches++;

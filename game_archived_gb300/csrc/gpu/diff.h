@@ -22,4 +22,9 @@ void launch_diffusion_momentum(Context *c, const StepParams &p, const SView<floa
 void launch_diffusion_scalar(Context *c, const StepParams &p, const SView<double> &sv);
 void launch_diffusion_scalar(Context *c, const StepParams &p, const SView<float> &sv);
 
+/* Held-Suarez radiative forcing (rad_on = 2) into radiation_tendency, from
+ * state_old and its temperature, at the first RK substep of a step with
+ * rad_update = 1 (manage_rkhevi.c:80-84); FP64 on both paths */
+void launch_held_suarez_radiation(Context *c, const DState &so);
+
 }  // namespace game

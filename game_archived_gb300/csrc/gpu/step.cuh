@@ -289,6 +289,7 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             launch_momentum_v<R, true, false>(c, p, v, st, new_w, old_w);
         }
         /* diffusion branch: temperature and mass diffusion */
+        if (rk == 0 && (p.diff & DIFF_RAD_HS)) launch_held_suarez_radiation(c, so->ds);
         if (rk == 0 && p.diff) launch_diffusion_scalar(c, p, v.sv);
         {
             ProfScope ps(c, "k_theta");

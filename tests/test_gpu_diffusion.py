@@ -11,8 +11,12 @@ switch combinations and a seeded turbulent kinetic energy:
 * device-resident steps with CUDA graphs give the same bits as host-in/host-out
   steps;
 * the mixed path stays as close to FP64 as without diffusion;
-* radiation and the sub-step entry points without a diffusion branch are
-  refused on the host.
+* the Held-Suarez configuration (radiation relaxation and boundary-layer
+  friction with horizontal momentum diffusion) within 1e-12 of the oracle at
+  RES_ID = 5, where the reference's radiation blocks tile the grid, and
+  refused where they would overrun radiation_tendency;
+* RTE+RRTMGP radiation and the sub-step entry points without a diffusion
+  branch are refused on the host.
 """
 import numpy as np
 import pytest
@@ -129,5 +133,84 @@ def test_out_of_scope_switches_refused():
         m.config["rad_on"][0] = 0
         with pytest.raises(abi.GpuError, match="diffusion branch"):
             g.three_band_solver_ver_waves(m.state_old, m.state_new, m.state_tendency, 300.0, 0)
+    finally:
+        g.close()
+
+
+def held_suarez(m):
+    """the reference's Held-Suarez run configuration (run_scripts/held_suar.sh):
+    Held-Suarez radiation and boundary-layer friction, horizontal momentum
+    diffusion"""
+    with_diffusion(m, ("momentum_diff_h",))
+    m.config["rad_on"][0] = 2
+    m.config["pbl_scheme"][0] = 2
+    return m
+
+
+@pytest.mark.parametrize("moist,case,mountain", [(0, "std_wind_tpert", True), (1, "tracers", False)],
+                         ids=["dry-oro", "moist"])
+def test_held_suarez_fp64_matches_oracle(moist, case, mountain):
+    """RES_ID = 5 (the reference's 18 radiation blocks tile its 10242 cells);
+    the radiation is updated at every other step, as the reference's driver
+    does for a radiation time step of two model steps"""
+    _, m_orc = make_model(5, moist, case, mountain)
+    held_suarez(m_orc)
+    m_gpu = clone(m_orc)
+    orc = Oracle(m_orc)
+    g = abi.GpuModel(m_gpu, abi.FP64)
+    worst = 0.0
+    try:
+        driver.start(m_orc, orc.linear_combine_two_states)
+        driver.start(m_gpu, g.linear_combine_two_states)
+        for n in range(4):
+            for m in (m_orc, m_gpu):
+                m.config["rad_update"][0] = 1 if n % 2 == 0 else 0
+            driver.step(m_orc, orc.linear_combine_two_states, orc.manage_rkhevi, 200.0, n * 200.0)
+            driver.step(m_gpu, g.linear_combine_two_states, g.manage_rkhevi, 200.0, n * 200.0)
+            e = state_errors(m_gpu.state_new, m_orc.state_new, m_gpu.layout)
+            worst = max(worst, max(e.values()))
+            assert max(e.values()) <= 1e-12, f"step {n}: {e}"
+        g.sync_aux_to_host()
+    finally:
+        g.close()
+    rad = rel_err(m_gpu.forcings["radiation_tendency"], m_orc.forcings["radiation_tendency"])
+    fric = rel_err(m_gpu.irrev["friction_acc"], m_orc.irrev["friction_acc"])
+    print(f"Held-Suarez, {case}: worst state error {worst:.3g}, radiation_tendency {rad:.3g}, friction {fric:.3g}")
+    assert rad <= 1e-11 and fric <= 1e-11
+    assert np.all(m_gpu.forcings["sfc_sw_in"] == 0.0)
+
+
+def test_held_suarez_mixed_close_to_fp64():
+    _, m64 = make_model(5, 0, "std_wind_tpert", True)
+    held_suarez(m64)
+    m64.config["rad_update"][0] = 1
+    m32 = clone(m64)
+    for m, prec in ((m64, abi.FP64), (m32, abi.MIXED)):
+        g = abi.GpuModel(m, prec)
+        try:
+            driver.run(m, 4, 200.0, g.linear_combine_two_states, g.manage_rkhevi)
+        finally:
+            g.close()
+    e = state_errors(m32.state_new, m64.state_new, m64.layout)
+    print(f"Held-Suarez, mixed vs FP64 after 4 steps: {e}")
+    assert e["rho[0]"] < 1e-5 and e["rhotheta_v"] < 1e-5 and e["exner_pert"] < 1e-3 and e["wind_h"] < 1e-3, e
+
+
+def test_held_suarez_refused_where_the_reference_overruns():
+    """RES_ID = 3 with 26 layers: NO_OF_SCALARS / 18 = 927 is not a multiple of
+    26, so the reference's radiation-block loops write past the end of
+    radiation_tendency; the library refuses instead.  rad_on = 1 (RTE+RRTMGP)
+    is refused on every grid."""
+    _, m = make_model(3, 0, "std_wind")
+    held_suarez(m)
+    m.config["rad_update"][0] = 1
+    g = abi.GpuModel(m, abi.FP64)
+    try:
+        driver.start(m, g.linear_combine_two_states)
+        with pytest.raises(abi.GpuError, match="radiation blocks"):
+            g.manage_rkhevi(200.0)
+        m.config["rad_on"][0] = 1
+        with pytest.raises(abi.GpuError, match="RTE"):
+            g.manage_rkhevi(200.0)
     finally:
         g.close()
