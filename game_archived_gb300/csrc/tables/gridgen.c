@@ -276,6 +276,174 @@ static void hor_cov_to_con_h(const grad_ctx *g, double *f)
 }
 
 /* ------------------------------------------------------------------ build */
+/* ------------------------------------------------ lat-lon output tables
+ * Interpolation of the cell fields to the regular lat-lon output grid
+ * (grid_generator/src/interpolate_ll.c:16-85): for every lat-lon point the
+ * five cells nearest by the reference's geodetic distance
+ * (geodesy.c:calculate_distance_h), weights 1 / (d^(2 + eps) + eps)
+ * normalised to sum one.  The reference scans every cell for every point; here
+ * the cells are bucketed on a 3-D grid and each point scans the buckets inside
+ * a chord radius that grows until it provably holds the five nearest, then
+ * applies the reference's selection rule to those candidates, so the
+ * indices and weights are the ones the reference's scan gives.  That rule
+ * (index_helpers.c:find_min_index_exclude) starts every search from cell 0,
+ * chosen or not, and takes a later cell only if it is strictly nearer and
+ * not chosen yet: cell 0 is therefore always a candidate, ties go to the
+ * lowest index, and near cell 0 the same index can be chosen more than
+ * once. */
+#define LL_EPS 1e-10
+
+static double ll_distance(double lat_a, double lon_a, double lat_b, double lon_b)
+{
+    return 2.0 * 1.0 * asin(sqrt(0.5 - 0.5 * (cos(lat_a) * cos(lat_b) * cos(lon_b - lon_a) + sin(lat_a) * sin(lat_b))));
+}
+
+static int cmp_int(const void *a, const void *b)
+{
+    const int x = *(const int *)a, y = *(const int *)b;
+    return (x > y) - (x < y);
+}
+
+static int latlon_tables(game_tables *T, int res_id, const double *lat_c, const double *lon_c, int Nc)
+{
+    const int n_lat = (int)(2 * pow(2, res_id)), n_lon = (int)(4 * pow(2, res_id));
+    const long n_ll = (long)n_lat * n_lon;
+    int *idx = add_array(T, "latlon_interpol_indices", GT_INT, 5 * n_ll);
+    double *wts = add_array(T, "latlon_interpol_weights", GT_DOUBLE, 5 * n_ll);
+    if (!idx || !wts) return -1;
+    /* buckets: a B^3 grid over [-1, 1]^3 with about one cell spacing per edge */
+    int B = (int)ceil(2.0 / sqrt(4.0 * M_PI / Nc));
+    if (B < 1) B = 1;
+    const double h = 2.0 / B;
+    const long nb = (long)B * B * B;
+    int *start = calloc((size_t)nb + 1, sizeof(int)), *fill = malloc((size_t)nb * sizeof(int));
+    int *order = malloc((size_t)Nc * sizeof(int)), *bucket = malloc((size_t)Nc * sizeof(int));
+    v3 *P = malloc((size_t)Nc * sizeof(v3));
+    int err = !start || !fill || !order || !bucket || !P;
+    if (!err) {
+        for (int c = 0; c < Nc; ++c) {
+            P[c] = v3_from_geo(lat_c[c], lon_c[c]);
+            int ix = (int)((P[c].x + 1.0) / h), iy = (int)((P[c].y + 1.0) / h), iz = (int)((P[c].z + 1.0) / h);
+            ix = ix < 0 ? 0 : (ix >= B ? B - 1 : ix);
+            iy = iy < 0 ? 0 : (iy >= B ? B - 1 : iy);
+            iz = iz < 0 ? 0 : (iz >= B ? B - 1 : iz);
+            bucket[c] = (ix * B + iy) * B + iz;
+            start[bucket[c] + 1]++;
+        }
+        for (long b = 0; b < nb; ++b) start[b + 1] += start[b];
+        for (long b = 0; b < nb; ++b) fill[b] = start[b];
+        for (int c = 0; c < Nc; ++c) order[fill[bucket[c]]++] = c;
+    }
+    const double d_lat = M_PI / n_lat, d_lon = 2 * M_PI / n_lon;
+    const long n_run = err ? 0 : n_ll;
+    #pragma omp parallel for schedule(dynamic, 64) reduction(|:err)
+    for (long i = 0; i < n_run; ++i) {
+        const int lat_index = (int)(i / n_lon), lon_index = (int)(i - (long)lat_index * n_lon);
+        const double lat_value = M_PI / 2 - 0.5 * d_lat - lat_index * d_lat, lon_value = lon_index * d_lon;
+        const v3 q = v3_from_geo(lat_value, lon_value);
+        int *cand = NULL, n_cand = 0, cap = 0, oom = 0;
+        /* grow a chord radius until the fifth-nearest cell inside it lies
+         * well within it: then no cell outside can be among the five nearest
+         * whatever the rounding of either distance formula */
+        for (double r = 2.0 * h;; r *= 2.0) {
+            const int whole = r >= 2.0;
+            n_cand = 0;
+            int lo[3], hi[3];
+            const double qc[3] = {q.x, q.y, q.z};
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = whole ? 0 : (int)floor((qc[a] - r + 1.0) / h);
+                hi[a] = whole ? B - 1 : (int)floor((qc[a] + r + 1.0) / h);
+                if (lo[a] < 0) lo[a] = 0;
+                if (hi[a] > B - 1) hi[a] = B - 1;
+            }
+            for (int ix = lo[0]; ix <= hi[0]; ++ix)
+                for (int iy = lo[1]; iy <= hi[1]; ++iy)
+                    for (int iz = lo[2]; iz <= hi[2]; ++iz) {
+                        const long b = ((long)ix * B + iy) * B + iz;
+                        for (int k = start[b]; k < start[b + 1]; ++k) {
+                            const int c = order[k];
+                            const v3 dv = v3_sub(P[c], q);
+                            if (!whole && v3_dot(dv, dv) > r * r) continue;
+                            if (n_cand == cap) {
+                                /* one slot more than cap stays free for cell 0 */
+                                int *grown = oom ? NULL : realloc(cand, (size_t)(2 * cap + 65) * sizeof(int));
+                                if (!grown) {
+                                    oom = 1;
+                                    continue;
+                                }
+                                cand = grown;
+                                cap = 2 * cap + 64;
+                            }
+                            cand[n_cand++] = c;
+                        }
+                    }
+            if (oom || whole) break;
+            if (n_cand >= 5) {
+                double best[5] = {1e300, 1e300, 1e300, 1e300, 1e300};
+                for (int k = 0; k < n_cand; ++k) {
+                    const v3 dv = v3_sub(P[cand[k]], q);
+                    double d2 = v3_dot(dv, dv);
+                    for (int m = 0; m < 5; ++m)
+                        if (d2 < best[m]) {
+                            const double t = best[m];
+                            best[m] = d2;
+                            d2 = t;
+                        }
+                }
+                if (sqrt(best[4]) < 0.8 * r) break;
+            }
+        }
+        if (oom || n_cand < 5) {
+            free(cand);
+            err = 1;
+            continue;
+        }
+        /* cell 0 takes part in every search (the scan starts from it) */
+        int has0 = 0;
+        for (int k = 0; k < n_cand; ++k) has0 |= cand[k] == 0;
+        if (!has0) cand[n_cand++] = 0; /* room for one more is always kept */
+        qsort(cand, (size_t)n_cand, sizeof(int), cmp_int);
+        double *dist = malloc((size_t)n_cand * sizeof(double));
+        if (!dist) {
+            free(cand);
+            err = 1;
+            continue;
+        }
+        for (int k = 0; k < n_cand; ++k) dist[k] = ll_distance(lat_value, lon_value, lat_c[cand[k]], lon_c[cand[k]]);
+        int chosen[5] = {-1, -1, -1, -1, -1};
+        double w[5], w_sum = 0;
+        for (int j = 0; j < 5; ++j) {
+            int result = 0;
+            double current = dist[0]; /* cand[0] == 0 */
+            for (int k = 1; k < n_cand; ++k) {
+                if (dist[k] < current) {
+                    int excluded = 0;
+                    for (int m = 0; m < 5; ++m) excluded |= chosen[m] == cand[k];
+                    if (!excluded) {
+                        current = dist[k];
+                        result = cand[k];
+                    }
+                }
+            }
+            chosen[j] = result;
+            w[j] = 1 / (pow(ll_distance(lat_value, lon_value, lat_c[result], lon_c[result]), 2 + LL_EPS) + LL_EPS);
+            w_sum += w[j];
+        }
+        for (int j = 0; j < 5; ++j) {
+            idx[5 * i + j] = chosen[j];
+            wts[5 * i + j] = w[j] / w_sum;
+        }
+        free(cand);
+        free(dist);
+    }
+    free(start);
+    free(fill);
+    free(order);
+    free(bucket);
+    free(P);
+    return err ? -1 : 0;
+}
+
 game_tables *gt_build(int res_id, int n_layers, int n_oro_layers, double toa,
                       double stretching, double radius_rescale, int n_lloyd,
                       int oro_kind, const double *oro_params, int n_threads)
@@ -518,6 +686,7 @@ game_tables *gt_build(int res_id, int n_layers, int n_oro_layers, double toa,
     if (!lat_c || !lon_c || !lat_e || !lon_e || !lat_t || !lon_t || !direction || !direction_dual || !f_vec
         || !cell_unit || !tri_unit || !oro || !mid) FAIL("out of memory");
     for (int c = 0; c < Nc; ++c) v3_to_geo(X[c], &lat_c[c], &lon_c[c]);
+    if (latlon_tables(T, res_id, lat_c, lon_c, Nc)) FAIL("lat-lon interpolation tables: out of memory");
     for (int t = 0; t < Nt; ++t) v3_to_geo(circ[t], &lat_t[t], &lon_t[t]);
     int orth_bad = 0;
     for (int e = 0; e < Ne; ++e) {

@@ -63,7 +63,8 @@ GRID_MEMBERS = ["normal_distance", "volume", "area", "z_scalar", "z_vector", "gr
                 "slope", "theta_v_bg", "exner_bg", "exner_bg_grad", "layer_thickness", "trsk_indices",
                 "trsk_modified_curl_indices", "from_index", "to_index", "adjacent_vector_indices_h",
                 "adjacent_signs_h", "density_to_rhombi_indices", "latitude_scalar", "longitude_scalar",
-                "inner_product_weights", "direction", "density_to_rhombi_weights", "trsk_weights"]
+                "inner_product_weights", "direction", "density_to_rhombi_weights", "trsk_weights",
+                "latlon_interpol_indices", "latlon_interpol_weights"]
 
 
 def fill_grid(tables, grid, dualgrid):

@@ -13,12 +13,17 @@ compiles it with gcc:
   src/subgrid_scale, src/radiation/{held_suar,manage_radiation_calls}.c;
 * grid_generator/src/{geodesy,index_helpers}.c stand in for the un-vendored
   geos95 library (they define passive_turn, find_min_index and rad2deg);
+* grid_generator/src/interpolate_ll.c (the lat-lon interpolation tables);
+* src/io/{write_output,spatial_ops_for_output}.c, the output diagnostics,
+  against stand-ins for the netCDF and ecCodes headers (oracle/ref_stubs/)
+  whose definitions (oracle/ref_io_stubs.c) write no file but record the
+  arrays handed to the writers;
 * the Fortran radiation coupler is replaced by a stub that aborts if called
   (radiation is off in every configuration used here);
 * oracle/ref_harness.c (ours) exports sizeof/offsetof of the reference structs
   so the run-time layout can be checked against the compiler's.
 
-Output: oracle/_ref/libgame_ref_R<res>_M<moist>.so.  Nothing is copied into the
+Output: oracle/_ref/libgame_ref_v<version>_R<res>_M<moist>.so.  Nothing is copied into the
 repository; oracle/_ref/ is git-ignored.  Runs only where the reference tree
 exists (this build container), never on the GPU host.
 """
@@ -34,6 +39,13 @@ OUT = os.path.join(HERE, "_ref")
 SRC_DIRS = ["time_stepping", "spatial_operators", "constituents", "subgrid_scale"]
 RAD_FILES = ["held_suar.c", "manage_radiation_calls.c"]
 GEOS_FILES = ["geodesy.c", "index_helpers.c"]
+# the grid generator's lat-lon interpolation table builder
+GRIDGEN_FILES = ["interpolate_ll.c"]
+# the output diagnostics (write_out) and the operators only output uses
+IO_FILES = ["write_output.c", "spatial_ops_for_output.c"]
+# bumped whenever the set of compiled sources changes, so that stale
+# libraries are not reused
+BUILD_VERSION = 2
 
 GEOS95_H = """/* declarations of the geos95 functions the model uses; their definitions
    come from grid_generator/src/geodesy.c and index_helpers.c */
@@ -61,7 +73,7 @@ def available():
 
 
 def lib_path(res_id, moisture_on):
-    return os.path.join(OUT, f"libgame_ref_R{res_id}_M{moisture_on}.so")
+    return os.path.join(OUT, f"libgame_ref_v{BUILD_VERSION}_R{res_id}_M{moisture_on}.so")
 
 
 def _link(src, dst):
@@ -96,16 +108,16 @@ def build(res_id, moisture_on, n_layers=26, force=False):
     for d in SRC_DIRS + ["radiation", "io"]:
         os.makedirs(os.path.join(src, d), exist_ok=True)
         for name in os.listdir(os.path.join(REF_ROOT, "src", d)):
-            if name.endswith(".h") or (name.endswith(".c") and (d in SRC_DIRS or name in RAD_FILES)):
+            if name.endswith(".h") or (name.endswith(".c") and (d in SRC_DIRS or name in RAD_FILES or name in IO_FILES)):
                 _link(os.path.join(REF_ROOT, "src", d, name), os.path.join(src, d, name))
                 if name.endswith(".c"):
                     sources.append(os.path.join(src, d, name))
     gg = os.path.join(bdir, "grid_generator", "src")
     os.makedirs(gg, exist_ok=True)
     for name in os.listdir(os.path.join(REF_ROOT, "grid_generator", "src")):
-        if name.endswith(".h") or name in GEOS_FILES:
+        if name.endswith(".h") or name in GEOS_FILES + GRIDGEN_FILES:
             _link(os.path.join(REF_ROOT, "grid_generator", "src", name), os.path.join(gg, name))
-            if name in GEOS_FILES:
+            if name in GEOS_FILES + GRIDGEN_FILES:
                 sources.append(os.path.join(gg, name))
     inc = os.path.join(bdir, "include")
     os.makedirs(inc, exist_ok=True)
@@ -114,9 +126,9 @@ def build(res_id, moisture_on, n_layers=26, force=False):
     stub = os.path.join(bdir, "radiation_stub.c")
     with open(stub, "w") as f:
         f.write(RAD_STUB_C)
-    harness = os.path.join(HERE, "ref_harness.c")
+    harness = [os.path.join(HERE, "ref_harness.c"), os.path.join(HERE, "ref_io_stubs.c")]
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-w",
-           "-I", inc, "-I", src, "-o", out] + sources + [stub, harness, "-lm"]
+           "-I", inc, "-I", os.path.join(HERE, "ref_stubs"), "-I", src, "-o", out] + sources + [stub] + harness + ["-lm"]
     subprocess.run(cmd, check=True)
     return out
 
