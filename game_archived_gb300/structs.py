@@ -28,6 +28,7 @@ class Layout:
         self.n_scalars, self.n_vectors, self.n_dual_vectors = d.n_scalars, d.n_vectors, d.n_dual_vectors
         self.vpl, self.dpl, self.n_curl = d.vpl, d.dpl, d.n_curl
         self.n_const, self.n_cond = d.n_constituents, d.n_condensed
+        self.n_latlon = d.n_latlon
         self.members = {}
         self.sizes = {}
         for name, sid in STRUCT_IDS.items():

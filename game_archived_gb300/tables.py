@@ -76,8 +76,15 @@ def fill_grid(tables, grid, dualgrid):
     grid["radius"] = tables.radius
     grid["stretching_parameter"] = tables.stretching
     grid["oro_id"] = 0 if tables.mountain is None else 1
-    # surface properties: sea everywhere (set_grid_properties.c:224-252 soil grid)
+    # surface properties: sea everywhere, the values the reference's grid
+    # generator gives sea cells (grid_generator/src/phys_sfc_properties.c:155-
+    # 199: albedo of water, rho*c_p of water, sea roughness length, thermal
+    # conductivity of water) and the soil grid (set_grid_properties.c:224-252)
     grid["is_land"] = 0
+    grid["sfc_albedo"] = 0.06
+    grid["sfc_rho_c"] = 1024.0 * 4184.0
+    grid["roughness_length"] = max(0.0001, 0.08)
+    grid["t_conduc_soil"] = 1.4e-7
     grid["z_t_const"] = -10.0
     grid["t_const_soil"] = 273.15 + 25.0 * np.cos(2.0 * tables["latitude_scalar"])
     sigma_soil = 0.352

@@ -18,7 +18,8 @@ ip = P(ctypes.c_int)
 
 DIAG_FIELDS = ("flux_density", "flux_density_divv", "rel_vort_on_triangles", "rel_vort", "pot_vort", "temperature",
                "v_squared", "scalar_field_placeholder", "wind_divv", "curl_of_vorticity", "vector_field_placeholder",
-               "n_squared", "dv_hdz")
+               "n_squared", "dv_hdz", "u_at_edge", "v_at_edge", "u_at_cell", "v_at_cell", "monin_obukhov_length",
+               "roughness_velocity")
 IRREV_FIELDS = ("temperature_diffusion_heating", "friction_acc", "heating_diss", "pressure_gradient_decel_factor",
                 "condensates_sediment_heat", "mass_diff_tendency", "phase_trans_rates", "phase_trans_heating_rate",
                 "molecular_diffusion_coeff", "mass_diffusion_coeff_numerical_h", "mass_diffusion_coeff_numerical_v",
@@ -35,7 +36,20 @@ class OrcGrid(ctypes.Structure):
         (n, dp) for n in ("dual_area", "dual_z_vector", "f_vec")] + [
         (n, ip) for n in ("dual_from", "dual_to", "vort_idx", "vort_sign")] + [("gravity_potential", dp)] + [
         (n, dp) for n in ("layer_thickness", "dual_normal_distance")] + [
-        (n, ctypes.c_double) for n in ("eff_hor_res", "mean_velocity_area")] + [("latitude_scalar", dp)]
+        (n, ctypes.c_double) for n in ("eff_hor_res", "mean_velocity_area")] + [("latitude_scalar", dp)] + [
+        (n, dp) for n in ("direction", "roughness_length", "sfc_albedo", "latlon_weights")] + [
+        ("latlon_indices", ip), ("n_latlon", ctypes.c_long)]
+
+# the fields of orc_output, in its order: surface [Nc], model layers [S],
+# pressure levels [Nc][6]
+OUTPUT_SURFACE = ("mslp", "surface_p", "t2", "tcdc", "rprate", "sprate", "cape", "sfc_sw_down", "u10", "v10", "gusts")
+OUTPUT_LAYERS = ("pressure", "rh", "rel_vort", "divv_h", "epv")
+OUTPUT_PLEVELS = ("geopotential_height", "t_pl", "rh_pl", "epv_pl", "u_pl", "v_pl", "rel_vort_pl")
+N_PRESSURE_LEVELS = 6
+
+
+class OrcOutput(ctypes.Structure):
+    _fields_ = [(n, dp) for n in OUTPUT_SURFACE + OUTPUT_LAYERS + OUTPUT_PLEVELS]
 
 
 class OrcState(ctypes.Structure):
@@ -105,7 +119,9 @@ class Oracle:
                          _d(dg["f_vec"]), _i(dg["from_index"]), _i(dg["to_index"]),
                          _i(dg["vorticity_indices_triangles"]), _i(dg["vorticity_signs_triangles"]),
                          _d(g["gravity_potential"]), _d(g["layer_thickness"]), _d(dg["normal_distance"]),
-                         float(g["eff_hor_res"][0]), float(g["mean_velocity_area"][0]), _d(g["latitude_scalar"]))
+                         float(g["eff_hor_res"][0]), float(g["mean_velocity_area"][0]), _d(g["latitude_scalar"]),
+                         _d(g["direction"]), _d(g["roughness_length"]), _d(g["sfc_albedo"]),
+                         _d(g["latlon_interpol_weights"]), _i(g["latlon_interpol_indices"]), lay.n_latlon)
         self.lib = lib()
 
     def state(self, s):
@@ -256,3 +272,39 @@ class Oracle:
         pot = rho_g * self.m.grid["gravity_potential"]
         internal = rho_g * temperature
         return np.array([0.5 * self.integral(ekin), self.integral(pot), 717.942189 * self.integral(internal)])
+
+
+def _output_arrays(lay):
+    out = {n: np.zeros(lay.nc) for n in OUTPUT_SURFACE}
+    out.update({n: np.zeros(lay.n_scalars) for n in OUTPUT_LAYERS})
+    out.update({n: np.zeros(lay.nc * N_PRESSURE_LEVELS) for n in OUTPUT_PLEVELS})
+    return out
+
+
+def write_out_fields(orc, state, wind_lowest, n_wind_steps):
+    """the fields write_out (src/io/write_output.c:51-1513) computes from
+    state, as a dict of arrays (surface [Nc], model layers [S], pressure
+    levels [Nc][6]); also writes the Diagnostics members write_out writes
+    and rounds the top layer of state's theta_v_pert as the reference does"""
+    m = orc.m
+    lay = m.layout
+    out = _output_arrays(lay)
+    o = OrcOutput(*[_d(out[n]) for n, _ in OrcOutput._fields_])
+    s = orc.state(state)
+    d = orc.diag()
+    c = orc.config()
+    wl = np.ascontiguousarray(wind_lowest, dtype=np.float64)
+    rc = orc.lib.orc_write_out_fields(ctypes.byref(orc.g), ctypes.byref(s), _d(state["temperature_soil"]), _d(wl),
+                                      ctypes.c_int(n_wind_steps), ctypes.byref(d), _d(m.forcings["sfc_sw_in"]),
+                                      ctypes.byref(c), ctypes.byref(o))
+    if rc != 0:
+        raise RuntimeError("oracle write_out_fields failed")
+    return out
+
+
+def interpolate_to_ll(orc, field):
+    """interpolate_to_ll (src/io/spatial_ops_for_output.c:168-197)"""
+    f = np.ascontiguousarray(field, dtype=np.float64)
+    out = np.zeros(orc.m.layout.n_latlon)
+    orc.lib.orc_interpolate_to_ll(ctypes.byref(orc.g), _d(f), _d(out))
+    return out

@@ -1573,3 +1573,396 @@ int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *te
     }
     return 0;
 }
+
+/* ------------------------------------------------------------ output
+ * The operators only output uses and the fields write_out computes
+ * (src/io/write_output.c:51-1513, src/io/spatial_ops_for_output.c,
+ * src/spatial_operators/averaging.c:135-234), without the writers. */
+#define G_MEAN_SFC_ABS 9.80616
+
+static double tangential_wind(const orc_grid *g, const double *in, long layer, long h)
+{
+    /* averaging.c:135-150 */
+    double component = 0;
+    for (int i = 0; i < 10; ++i)
+        component += g->trsk_weights[10 * h + i] * in[NC + layer * VPL + g->trsk_indices[10 * h + i]];
+    return component;
+}
+
+static void passive_turn(double u_in, double v_in, double turn_angle, double *u_out, double *v_out)
+{
+    /* geodesy.c:206-223: the active turn by -turn_angle */
+    const double a = -turn_angle;
+    *u_out = cos(a) * u_in - sin(a) * v_in;
+    *v_out = sin(a) * u_in + cos(a) * v_in;
+}
+
+static int find_min_index(const double *v, int n)
+{
+    /* index_helpers.c:13-28: first index of the minimum */
+    int r = 0;
+    double cur = v[0];
+    for (int i = 1; i < n; ++i)
+        if (v[i] < cur) {
+            cur = v[i];
+            r = i;
+        }
+    return r;
+}
+
+int orc_calc_uv_at_edge(const orc_grid *g, const double *in, double *u, double *v)
+{
+    /* averaging.c:152-174 */
+    ORC_PAR
+    for (long i = 0; i < (long)NL * NE; ++i) {
+        long layer = i / NE, h = i - layer * NE;
+        double w0 = in[NC + layer * VPL + h];
+        double w1 = tangential_wind(g, in, layer, h);
+        passive_turn(w0, w1, -g->direction[h], &u[NC + layer * VPL + h], &v[NC + layer * VPL + h]);
+    }
+    return 0;
+}
+
+int orc_curl_field_to_cells(const orc_grid *g, const double *in, double *out)
+{
+    /* averaging.c:176-204 */
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) {
+        long layer = i / NC, h = i - layer * NC;
+        out[i] = 0;
+        int n_edges = h < N_PENT ? 5 : 6;
+        for (int j = 0; j < n_edges; ++j)
+            out[i] += 0.5 * g->ipw[8 * i + j] * in[NE + layer * 2 * NE + g->adj[6 * h + j]];
+    }
+    return 0;
+}
+
+int orc_edges_to_cells(const orc_grid *g, const double *in, double *out)
+{
+    /* averaging.c:206-234 */
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) {
+        long layer = i / NC, h = i - layer * NC;
+        out[i] = 0;
+        int n_edges = h < N_PENT ? 5 : 6;
+        for (int j = 0; j < n_edges; ++j)
+            out[i] += 0.5 * g->ipw[8 * i + j] * in[NC + layer * VPL + g->adj[6 * h + j]];
+    }
+    return 0;
+}
+
+int orc_edges_to_cells_lowest_layer(const orc_grid *g, const double *in, double *out)
+{
+    /* spatial_ops_for_output.c:199-225 */
+    ORC_PAR
+    for (long i = 0; i < NC; ++i) {
+        out[i] = 0;
+        int n_edges = i < N_PENT ? 5 : 6;
+        for (int j = 0; j < n_edges; ++j)
+            out[i] += 0.5 * g->ipw[8 * (NS - NC + i) + j] * in[g->adj[6 * i + j]];
+    }
+    return 0;
+}
+
+int orc_inner_product_tangential(const orc_grid *g, const double *in0, const double *in1, double *out)
+{
+    /* spatial_ops_for_output.c:137-166: all six edge slots, also for
+     * pentagons (whose sixth slot has weight 0) */
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) {
+        long layer = i / NC, h = i - layer * NC;
+        out[i] = 0;
+        for (int j = 0; j < 6; ++j) {
+            double tw = tangential_wind(g, in1, layer, g->adj[6 * h + j]);
+            out[i] += g->ipw[8 * i + j] * in0[NC + layer * VPL + g->adj[6 * h + j]] * tw;
+        }
+        out[i] += g->ipw[8 * i + 6] * in0[h + layer * VPL] * in1[h + layer * VPL];
+        out[i] += g->ipw[8 * i + 7] * in0[h + (layer + 1) * VPL] * in1[h + (layer + 1) * VPL];
+    }
+    return 0;
+}
+
+int orc_epv_diagnostics(const orc_grid *g, const double *pot_vort, orc_state *s, double *epv)
+{
+    /* spatial_ops_for_output.c:17-135 */
+    /* zero-initialised like the reference's calloc: the gradient leaves the
+     * surface and top levels of its output untouched */
+    double *pv = calloc((size_t)NV, sizeof(double)), *grad_pt = calloc((size_t)NV, sizeof(double));
+    if (!pv || !grad_pt) {
+        free(pv);
+        free(grad_pt);
+        return -1;
+    }
+    const double *zv = g->z_vector;
+    ORC_PAR
+    for (long i = 0; i < NV; ++i) {
+        long layer = i / VPL, h = i - layer * VPL;
+        if (h >= NC) {
+            long e = h - NC, f = g->from[e], t = g->to[e];
+            double lt = 0.5 * (zv[layer * VPL + f] + zv[layer * VPL + t])
+                        - 0.5 * (zv[(layer + 1) * VPL + f] + zv[(layer + 1) * VPL + t]);
+            double upper, lower;
+            if (layer == 0) upper = (0.5 * (zv[layer * VPL + f] + zv[layer * VPL + t]) - zv[i]) / lt;
+            else upper = 0.5 * (zv[i - VPL] - zv[i]) / lt;
+            if (layer == NL - 1) lower = (zv[i] - 0.5 * (zv[(layer + 1) * VPL + f] + zv[(layer + 1) * VPL + t])) / lt;
+            else lower = 0.5 * (zv[i] - zv[i + VPL]) / lt;
+            pv[i] = upper * pot_vort[layer * 2 * NE + e] + lower * pot_vort[(layer + 1) * 2 * NE + e];
+        } else {
+            pv[i] = 0;
+            if (layer == 0) {
+                for (int j = 0; j < 6; ++j)
+                    pv[i] += 0.5 * g->ipw[8 * h + j] * pot_vort[NE + layer * 2 * NE + g->adj[6 * h + j]];
+            } else if (layer == NL) {
+                long si = (long)(NL - 1) * NC + h;
+                for (int j = 0; j < 6; ++j)
+                    pv[i] += 0.5 * g->ipw[8 * si + j] * pot_vort[NE + (layer - 1) * 2 * NE + g->adj[6 * h + j]];
+            } else {
+                long su = (layer - 1) * NC + h, sl = layer * NC + h;
+                for (int j = 0; j < 6; ++j)
+                    pv[i] += 0.25 * g->ipw[8 * su + j] * pot_vort[NE + (layer - 1) * 2 * NE + g->adj[6 * h + j]];
+                for (int j = 0; j < 6; ++j)
+                    pv[i] += 0.25 * g->ipw[8 * sl + j] * pot_vort[NE + layer * 2 * NE + g->adj[6 * h + j]];
+            }
+        }
+    }
+    /* the gradient of theta_v' with the background added in the top layer
+     * only (:113-122) */
+    for (long i = 0; i < NC; ++i) s->theta_v_pert[i] += g->theta_v_bg[i];
+    orc_grad(g, s->theta_v_pert, grad_pt);
+    for (long i = 0; i < NC; ++i) s->theta_v_pert[i] -= g->theta_v_bg[i];
+    orc_inner_product_tangential(g, pv, grad_pt, epv);
+    free(pv);
+    free(grad_pt);
+    return 0;
+}
+
+int orc_interpolate_to_ll(const orc_grid *g, const double *in, double *out)
+{
+    /* spatial_ops_for_output.c:168-197 */
+    ORC_PAR
+    for (long i = 0; i < g->n_latlon; ++i) {
+        out[i] = 0;
+        for (int j = 0; j < 5; ++j) {
+            double v = in[g->latlon_indices[5 * i + j]];
+            if (v != 9999) {
+                out[i] += g->latlon_weights[5 * i + j] * v;
+            } else {
+                out[i] = 9999;
+                break;
+            }
+        }
+    }
+    return 0;
+}
+
+static double rel_humidity(double abs_humidity, double temperature)
+{
+    /* derived_quantities.c:63-81 */
+    double vapour_pressure = abs_humidity * R_V * temperature;
+    double saturation_pressure = 0.0;
+    if (temperature > T_0) saturation_pressure = saturation_pressure_over_water(temperature);
+    if (temperature <= T_0) saturation_pressure = saturation_pressure_over_ice(temperature);
+    return vapour_pressure / saturation_pressure;
+}
+
+static double pseudopotential_temperature(const orc_grid *g, const orc_state *s, const orc_diag *d, long i)
+{
+    /* write_output.c:1680-1736 (Bolton 1980 in the moist case) */
+    if (!g->moisture_on) return g->theta_v_bg[i] + s->theta_v_pert[i];
+    const double T = d->temperature[i];
+    double r = s->rho[(COND + 1) * NS + i] / (s->rho[COND * NS + i] - s->rho[(COND + 1) * NS + i]);
+    double alpha_1 = 0.2854 * (1.0 - 0.28e-3 * r);
+    double alpha_3 = r * (1.0 + 0.81e-3 * r);
+    double pressure = P_0 * pow(g->exner_bg[i] + s->exner_pert[i], C_D_P / R_D);
+    double saturation_pressure;
+    if (T >= T_0) saturation_pressure = saturation_pressure_over_water(T);
+    else saturation_pressure = saturation_pressure_over_ice(T);
+    double vapour_pressure = s->rho[(COND + 1) * NS + i] * R_V * T;
+    double rel_hum = vapour_pressure / saturation_pressure;
+    double t_lcl = 1.0 / (1.0 / (T - 55.0) - log(rel_hum) / 2840.0) + 55.0;
+    double alpha_2 = 3.376 / t_lcl - 0.00254;
+    return T * pow(P_0 / pressure, alpha_1) * exp(alpha_2 * alpha_3);
+}
+
+/* wind speed at a height above the surface by linear inter-/extrapolation of
+ * sqrt(v_squared) between the two layers nearest to it (write_output.c:310-340) */
+static double speed_at_height(const orc_grid *g, const double *v_squared, long i, double height)
+{
+    const double *zs = g->z_scalar, *zv = g->z_vector;
+    double vtm[ORC_MAX_L];
+    for (int j = 0; j < NL; ++j) vtm[j] = fabs(zs[j * NC + i] - (zv[NV - NC + i] + height));
+    int closest = find_min_index(vtm, NL);
+    int second = closest - 1;
+    if (closest < NL - 1 && zs[closest * NC + i] - zv[NV - NC + i] > height) second = closest + 1;
+    return pow(v_squared[i + closest * NC], 0.5)
+           + (pow(v_squared[i + closest * NC], 0.5) - pow(v_squared[i + second * NC], 0.5))
+                 / (zs[i + closest * NC] - zs[i + second * NC]) * (zv[NV - NC + i] + height - zs[i + closest * NC]);
+}
+
+int orc_write_out_fields(const orc_grid *g, orc_state *s, const double *temperature_soil, const double *wind_lowest,
+                         int n_wind_steps, orc_diag *d, const double *sfc_sw_in, const orc_config *c, orc_output *o)
+{
+    const double *zs = g->z_scalar, *zv = g->z_vector;
+    orc_temperature_diagnostics(g, s, d);
+    /* surface fields (:90-211) */
+    const double lapse = 0.0065, z_tropopause = 12e3;
+    const double min_precip_rate = 0.01 / (1000.0 * 3600.0 / 1024.0);
+    ORC_PAR
+    for (long i = 0; i < NC; ++i) {
+        const long lo = (long)(NL - 1) * NC + i;
+        double t_low = d->temperature[lo];
+        double rgas = gas_constant_diagnostics(g, s, lo);
+        double p = s->rho[COND * NS + lo] * rgas * t_low;
+        double gm = g->gravity_m[(NL - 1) * VPL + i];
+        double t_mslp = t_low + lapse * zs[lo];
+        o->mslp[i] = p / pow(1 - (t_mslp - t_low) / t_mslp, gm / (rgas * lapse));
+        double t_sfc = t_low + lapse * (zs[lo] - zv[NV - NC + i]);
+        o->surface_p[i] = p / pow(1.0 - (t_sfc - t_low) / t_sfc, gm / (rgas * lapse));
+        /* 2 m temperature */
+        double vtm[ORC_MAX_L];
+        for (int j = 0; j < NL; ++j) vtm[j] = fabs(zv[(long)NL * VPL + i] + 2 - zs[i + j * NC]);
+        int closest = find_min_index(vtm, NL);
+        double temp_closest = d->temperature[closest * NC + i];
+        double delta_z_temp = zv[(long)NL * VPL + i] + 2 - zs[i + closest * NC];
+        double gradient;
+        if (c->prog_soil_temp == 1) {
+            gradient = (temp_closest - temperature_soil[i]) / (zs[i + closest * NC] - zv[(long)NL * VPL + i]);
+        } else {
+            int second = closest - 1;
+            if (zs[i + closest * NC] > zv[(long)NL * VPL + i] + 2 && closest < NL - 1) second = closest + 1;
+            gradient = (temp_closest - d->temperature[second * NC + i]) / (zs[i + closest * NC] - zs[i + second * NC]);
+        }
+        o->t2[i] = temp_closest + delta_z_temp * gradient;
+        /* CAPE; stops at the top layer where the reference would read above
+         * the model top (a model top below the tropopause) */
+        o->cape[i] = 0.0;
+        int layer = NL - 1;
+        double z_height = zs[layer * NC + i];
+        double theta_e = pseudopotential_temperature(g, s, d, layer * NC + i);
+        while (z_height < z_tropopause) {
+            double theta_v = g->theta_v_bg[layer * NC + i] + s->theta_v_pert[layer * NC + i];
+            double delta_z = g->layer_thickness[layer * NC + i];
+            double integrand = g->gravity_m[layer * VPL + i] * (theta_e - theta_v) / theta_v;
+            if (integrand > 0.0) o->cape[i] += integrand * delta_z;
+            --layer;
+            if (layer < 0) break;
+            z_height = zs[layer * NC + i];
+        }
+        o->sfc_sw_down[i] = sfc_sw_in[i] / (1.0 - g->sfc_albedo[i] + EPSILON_SECURITY);
+        if (COND == 4) {
+            double cwc = 0.0;
+            for (int k = 0; k < NL; ++k)
+                if (zs[k * NC + i] < z_tropopause)
+                    cwc += (s->rho[2 * NS + k * NC + i] + s->rho[3 * NS + k * NC + i])
+                           * (zv[i + k * VPL] - zv[i + (k + 1) * VPL]);
+            o->tcdc[i] = fmin(10.0 * cwc, 1.0);
+            o->tcdc[i] = 100.0 * o->tcdc[i];
+            if (o->tcdc[i] < 0.5) o->tcdc[i] = 0.0;
+        } else {
+            o->tcdc[i] = 0.0;
+        }
+        o->sprate[i] = 0.0;
+        if (COND == 4) o->sprate[i] = c->snow_velocity * s->rho[lo];
+        o->rprate[i] = 0.0;
+        if (COND == 4) o->rprate[i] = c->rain_velocity * s->rho[NS + lo];
+        if (o->rprate[i] < min_precip_rate) o->rprate[i] = 0.0;
+        if (o->sprate[i] < min_precip_rate) o->sprate[i] = 0.0;
+    }
+    /* 10 m wind (:213-292) */
+    double *u = malloc((size_t)NE * sizeof(double)), *v = malloc((size_t)NE * sizeof(double));
+    if (!u || !v) {
+        free(u);
+        free(v);
+        return -1;
+    }
+    ORC_PAR
+    for (long h = 0; h < NE; ++h) {
+        double mu = 0.0, mv = 0.0;
+        for (int t = 0; t < n_wind_steps; ++t) {
+            double wt = 0.0;
+            for (int k = 0; k < 10; ++k)
+                wt += g->trsk_weights[10 * h + k] * wind_lowest[(long)t * NE + g->trsk_indices[10 * h + k]];
+            mu += 1.0 / n_wind_steps * wind_lowest[(long)t * NE + h];
+            mv += 1.0 / n_wind_steps * wt;
+        }
+        passive_turn(mu, mv, -g->direction[h], &u[h], &v[h]);
+        long f = g->from[h], to = g->to[h];
+        double actual = 0.5 * (g->roughness_length[f] + g->roughness_length[to]);
+        double extrapolation = 0.02;
+        if (g->is_land[f] == 0) extrapolation = actual;
+        double z_sfc = 0.5 * (zv[NV - NC + f] + zv[NV - NC + to]);
+        double z_agl = zv[NV - VPL + h] - z_sfc;
+        double rescale = log(10.0 / extrapolation) / log(z_agl / actual);
+        u[h] = rescale * u[h];
+        v[h] = rescale * v[h];
+    }
+    orc_edges_to_cells_lowest_layer(g, u, o->u10);
+    orc_edges_to_cells_lowest_layer(g, v, o->v10);
+    free(u);
+    free(v);
+    /* gusts (:294-350).  The reference's loop shares its work array
+     * vector_to_minimize between OpenMP threads, so with several threads its
+     * result depends on the schedule; this is its one-thread result. */
+    const double h850 = 8000.0 * log(1000.0 / 850.0), h950 = 8000.0 * log(1000.0 / 950.0);
+    ORC_PAR
+    for (long i = 0; i < NC; ++i) {
+        double speed = pow(pow(o->u10[i], 2) + pow(o->v10[i], 2), 0.5);
+        if ((c->sfc_sensible_heat_flux == 1 || c->sfc_phase_trans == 1 || c->pbl_scheme == 1)
+            && fabs(d->monin_obukhov_length[i]) > EPSILON_SECURITY) {
+            o->gusts[i] = speed + 7.71 * d->roughness_velocity[i]
+                                      * pow(fmax(1.0 - 0.5 / 12.0 * 1000.0 / d->monin_obukhov_length[i], 0.0), 1.0 / 3.0);
+            double u850 = speed_at_height(g, d->v_squared, i, h850);
+            double u950 = speed_at_height(g, d->v_squared, i, h950);
+            o->gusts[i] += 0.6 * fmax(0.0, u850 - u950);
+            o->gusts[i] = fmin(o->gusts[i], 3.0 * speed);
+        } else {
+            o->gusts[i] = 1.67 * speed;
+        }
+    }
+    /* model-layer fields (:718-749) */
+    orc_divv_h(g, s->wind, o->divv_h);
+    orc_calc_rel_vort(g, s->wind, d);
+    orc_curl_field_to_cells(g, d->rel_vort, o->rel_vort);
+    orc_calc_uv_at_edge(g, s->wind, d->u_at_edge, d->v_at_edge);
+    orc_edges_to_cells(g, d->u_at_edge, d->u_at_cell);
+    orc_edges_to_cells(g, d->v_at_edge, d->v_at_cell);
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) {
+        if (g->n_const >= 4) o->rh[i] = 100.0 * rel_humidity(s->rho[(COND + 1) * NS + i], d->temperature[i]);
+        else o->rh[i] = 0.0;
+        o->pressure[i] = s->rho[COND * NS + i] * gas_constant_diagnostics(g, s, i) * d->temperature[i];
+    }
+    ORC_PAR
+    for (long i = 0; i < NS; ++i) d->scalar_field_placeholder[i] = s->rho[COND * NS + i];
+    orc_calc_pot_vort(g, s->wind, d->scalar_field_placeholder, d);
+    if (orc_epv_diagnostics(g, d->pot_vort, s, o->epv)) return -1;
+    /* pressure levels (:751-826) */
+    static const double levels[ORC_N_PRESSURE_LEVELS] = {20000, 30000, 50000, 70000, 85000, 92500};
+    ORC_PAR
+    for (long i = 0; i < NC; ++i) {
+        double vtm[ORC_MAX_L];
+        for (int j = 0; j < ORC_N_PRESSURE_LEVELS; ++j) {
+            for (int k = 0; k < NL; ++k) vtm[k] = fabs(log(levels[j] / o->pressure[k * NC + i]));
+            int closest = find_min_index(vtm, NL);
+            int second = closest + 1;
+            if (levels[j] < o->pressure[closest * NC + i]) second = closest - 1;
+            long k = i * ORC_N_PRESSURE_LEVELS + j;
+            if ((closest == NL - 1 && second == NL) || (closest < 0 || second < 0)) {
+                o->geopotential_height[k] = o->t_pl[k] = o->rh_pl[k] = o->epv_pl[k] = 9999;
+                o->rel_vort_pl[k] = o->u_pl[k] = o->v_pl[k] = 9999;
+            } else {
+                long a = closest * NC + i, b = second * NC + i;
+                double w = 1 - vtm[closest] / (fabs(log(o->pressure[a] / o->pressure[b])) + EPSILON_SECURITY);
+                o->geopotential_height[k] = w * g->gravity_potential[a] + (1 - w) * g->gravity_potential[b];
+                o->geopotential_height[k] = o->geopotential_height[k] / G_MEAN_SFC_ABS;
+                o->t_pl[k] = w * d->temperature[a] + (1 - w) * d->temperature[b];
+                o->rh_pl[k] = w * o->rh[a] + (1 - w) * o->rh[b];
+                o->epv_pl[k] = w * o->epv[a] + (1 - w) * o->epv[b];
+                o->rel_vort_pl[k] = w * o->rel_vort[a] + (1 - w) * o->rel_vort[b];
+                o->u_pl[k] = w * d->u_at_cell[a] + (1 - w) * d->u_at_cell[b];
+                o->v_pl[k] = w * d->v_at_cell[a] + (1 - w) * d->v_at_cell[b];
+            }
+        }
+    }
+    return 0;
+}

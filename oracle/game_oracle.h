@@ -33,6 +33,10 @@ typedef struct orc_grid {
     double eff_hor_res, mean_velocity_area;
     /* Held-Suarez forcing */
     const double *latitude_scalar;
+    /* output diagnostics (src/io/write_output.c, src/io/spatial_ops_for_output.c) */
+    const double *direction, *roughness_length, *sfc_albedo, *latlon_weights;
+    const int *latlon_indices;
+    long n_latlon;
 } orc_grid;
 
 typedef struct orc_state {
@@ -47,6 +51,8 @@ typedef struct orc_diag {
     double *temperature, *v_squared, *scalar_field_placeholder;
     /* diffusion branch */
     double *wind_divv, *curl_of_vorticity, *vector_field_placeholder, *n_squared, *dv_hdz;
+    /* output diagnostics */
+    double *u_at_edge, *v_at_edge, *u_at_cell, *v_at_cell, *monin_obukhov_length, *roughness_velocity;
 } orc_diag;
 
 typedef struct orc_forcings {
@@ -130,5 +136,31 @@ double orc_global_scalar_integrator(const orc_grid *g, const double *field);
 /* mslp may be NULL */
 int orc_surface_pressure(const orc_grid *g, const orc_state *s, const double *temperature, double *p_sfc,
                          double *mslp);
+
+/* output diagnostics: the operators only output uses (src/io/io.h:14-16,
+ * src/spatial_operators/spatial_operators.h:27-30) */
+int orc_calc_uv_at_edge(const orc_grid *g, const double *in, double *u, double *v);
+int orc_curl_field_to_cells(const orc_grid *g, const double *in, double *out);
+int orc_edges_to_cells(const orc_grid *g, const double *in, double *out);
+int orc_edges_to_cells_lowest_layer(const orc_grid *g, const double *in, double *out);
+int orc_inner_product_tangential(const orc_grid *g, const double *in0, const double *in1, double *out);
+/* writes state->theta_v_pert of the top layer back as (x + bg) - bg, as the
+ * reference does */
+int orc_epv_diagnostics(const orc_grid *g, const double *pot_vort, orc_state *s, double *epv);
+int orc_interpolate_to_ll(const orc_grid *g, const double *in, double *out);
+
+/* the fields write_out computes (src/io/write_output.c:51-1513), without the
+ * writers */
+#define ORC_N_PRESSURE_LEVELS 6
+typedef struct orc_output {
+    /* surface, [Nc] each (write_output.c:90-351) */
+    double *mslp, *surface_p, *t2, *tcdc, *rprate, *sprate, *cape, *sfc_sw_down, *u10, *v10, *gusts;
+    /* model layers, [S] each (:718-749) */
+    double *pressure, *rh, *rel_vort, *divv_h, *epv;
+    /* pressure levels, [Nc][6] each (:751-826) */
+    double *geopotential_height, *t_pl, *rh_pl, *epv_pl, *u_pl, *v_pl, *rel_vort_pl;
+} orc_output;
+int orc_write_out_fields(const orc_grid *g, orc_state *s, const double *temperature_soil, const double *wind_lowest,
+                         int n_wind_steps, orc_diag *d, const double *sfc_sw_in, const orc_config *c, orc_output *o);
 
 #endif

@@ -84,3 +84,11 @@ void ref_dims(long out[8])
     out[0] = RES_ID; out[1] = NO_OF_LAYERS; out[2] = MOISTURE_ON; out[3] = NO_OF_SCALARS_H;
     out[4] = NO_OF_VECTORS_H; out[5] = NO_OF_DUAL_SCALARS_H; out[6] = NO_OF_CONSTITUENTS; out[7] = NO_OF_VECTORS;
 }
+
+/* OpenMP thread count of the reference's parallel loops.  The gust loop of
+ * write_out (src/io/write_output.c:298-346) shares its work array
+ * vector_to_minimize between threads, so its result depends on the thread
+ * schedule unless it runs on one thread. */
+#include <omp.h>
+void ref_set_num_threads(int n) { omp_set_num_threads(n); }
+int ref_get_max_threads(void) { return omp_get_max_threads(); }

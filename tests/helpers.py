@@ -63,3 +63,40 @@ def wind_parts(wind, lay):
     w = np.stack([wind[k * vpl:k * vpl + nc] for k in range(lay.nl + 1)])
     u = np.stack([wind[k * vpl + nc:(k + 1) * vpl] for k in range(lay.nl)])
     return w, u
+
+
+def output_scenario(res, moist, case, mountain=False, steps=2, dt=300.0, gust_scheme=False, seed=11):
+    """A model after a few oracle steps, prepared for the output diagnostics:
+    seeded cloud condensates and rain/snow (so that cloud cover and
+    precipitation rates take values on both sides of their thresholds), a
+    seeded short-wave flux, and the lowest-layer winds of the last n output
+    steps as the reference's driver collects them (src/coordinator.c:350-358).
+    gust_scheme: the boundary-layer switch on and Monin-Obukhov lengths,
+    roughness velocities and v_squared set, so that the gust diagnostics take
+    their turbulence branch.  Returns (model, wind_lowest, n_wind_steps)."""
+    from game_archived_gb300 import driver
+    _, m = make_model(res, moist, case, mountain)
+    orc = Oracle(m)
+    driver.run(m, steps, dt, orc.linear_combine_two_states, orc.manage_rkhevi)
+    lay = m.layout
+    rng = np.random.default_rng(seed)
+    ns, nc, ne = lay.n_scalars, lay.nc, lay.ne
+    s = m.state_new
+    if lay.n_cond == 4:
+        s["rho"][0:ns] = 2e-6 * rng.random(ns) ** 2
+        s["rho"][ns:2 * ns] = 2e-6 * rng.random(ns) ** 2
+        cloudy = np.tile(rng.random(nc) < 0.6, lay.nl)
+        s["rho"][2 * ns:3 * ns] = 1e-5 * rng.random(ns) ** 3 * cloudy
+        s["rho"][3 * ns:4 * ns] = 1e-5 * rng.random(ns) ** 3 * cloudy
+    m.forcings["sfc_sw_in"][:] = 400.0 * rng.random(nc)
+    n_wind = 3
+    lo = lay.n_vectors - lay.vpl + nc
+    wind_lowest = np.concatenate([s["wind"][lo:lo + ne] * (1.0 + 0.1 * rng.standard_normal(ne))
+                                  for _ in range(n_wind)])
+    if gust_scheme:
+        m.config["pbl_scheme"][0] = 1
+        m.diagnostics["monin_obukhov_length"][:] = rng.choice([-1.0, 1.0], nc) * (10.0 + 500.0 * rng.random(nc))
+        m.diagnostics["monin_obukhov_length"][:5] = 0.0
+        m.diagnostics["roughness_velocity"][:] = 0.5 * rng.random(nc)
+        m.diagnostics["v_squared"][:] = 400.0 * rng.random(ns)
+    return m, wind_lowest, n_wind

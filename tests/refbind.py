@@ -38,3 +38,75 @@ class Reference:
 
     def linear_combine_two_states(self, s0, s1, out, c0, c1):
         self.lib.linear_combine_two_states(s0.ptr, s1.ptr, out.ptr, c0, c1, self.m.grid.ptr)
+
+
+class ConfigIo(ctypes.Structure):
+    """the reference's Config_io (src/game_types.h:240-258)"""
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "grib_output_switch", "netcdf_output_switch", "pressure_level_output_switch", "model_level_output_switch",
+        "surface_output_switch", "write_out_interval", "write_out_integrals", "year", "month", "day", "hour")] + [
+        ("run_id", ctypes.c_char * 100), ("month_string", ctypes.c_char * 3), ("day_string", ctypes.c_char * 3),
+        ("hour_string", ctypes.c_char * 3), ("ideal_input_id", ctypes.c_int)]
+
+
+def write_out(ref, state, wind_lowest, n_wind_steps, workdir, t_init=0.0, t_write=3600.0):
+    """Runs the reference's write_out (src/io/write_output.c:51) with every
+    output switch on, in workdir (it opens its GRIB template at
+    ../../src/io/grib_template.grb2 relative to the working directory), and
+    returns what it handed to the netCDF and GRIB writers, recorded by the
+    harness's stand-ins: {"surface": {var: array}, "pressure_levels": {...},
+    "model_levels": {...}, "grib_surface": [arrays in message order],
+    "grib_pressure_levels": [...], "grib_model_levels": [...]}."""
+    lib = ref.lib
+    m = ref.m
+    cio = ConfigIo(1, 1, 1, 1, 1, 3600, 0, 2000, 1, 1, 0, b"ref", b"01", b"01", b"00", 0)
+    tmpl = os.path.join(workdir, "src", "io")
+    os.makedirs(tmpl, exist_ok=True)
+    open(os.path.join(tmpl, "grib_template.grb2"), "wb").close()
+    run_dir = os.path.join(workdir, "a", "b")
+    os.makedirs(run_dir, exist_ok=True)
+    vp, dbl = ctypes.c_void_p, ctypes.c_double
+    lib.write_out.argtypes = [vp, vp, ctypes.c_int, dbl, dbl, vp, vp, vp, vp, vp, vp, vp]
+    lib.ref_io_record.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_char_p),
+                                  ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long),
+                                  ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]
+    import numpy as np
+    wl = np.ascontiguousarray(wind_lowest, dtype=np.float64)
+    lib.ref_io_reset()
+    cwd = os.getcwd()
+    os.chdir(run_dir)
+    # one thread: the reference's gust loop shares a work array between
+    # threads (write_output.c:298, vector_to_minimize is not private)
+    n_threads = lib.ref_get_max_threads()
+    lib.ref_set_num_threads(1)
+    try:
+        rc = lib.write_out(state.ptr, wl.ctypes.data, n_wind_steps, t_init, t_write, m.diagnostics.ptr,
+                           m.forcings.ptr, m.grid.ptr, m.dualgrid.ptr, ctypes.byref(cio), m.config.ptr, m.irrev.ptr)
+    finally:
+        os.chdir(cwd)
+        lib.ref_set_num_threads(n_threads)
+    assert rc == 0
+    out = {"surface": {}, "pressure_levels": {}, "model_levels": {}, "grib_surface": [], "grib_pressure_levels": [],
+           "grib_model_levels": []}
+    f, nm = ctypes.c_char_p(), ctypes.c_char_p()
+    meta = (ctypes.c_long * 4)()
+    n = ctypes.c_long()
+    data = ctypes.POINTER(ctypes.c_double)()
+    for k in range(lib.ref_io_count()):
+        lib.ref_io_record(k, ctypes.byref(f), ctypes.byref(nm), meta, ctypes.byref(n), ctypes.byref(data))
+        arr = np.ctypeslib.as_array(data, shape=(n.value,)).copy()
+        fname, vname = f.value.decode(), nm.value.decode()
+        if fname.endswith("_surface.nc"):
+            out["surface"][vname] = arr
+        elif fname.endswith("_pressure_levels.nc"):
+            out["pressure_levels"][vname] = arr
+        elif fname.endswith(".nc"):
+            out["model_levels"][vname] = arr
+        elif fname.endswith("_surface.grb2"):
+            out["grib_surface"].append(arr)
+        elif fname.endswith("_pressure_levels.grb2"):
+            out["grib_pressure_levels"].append(arr)
+        else:
+            out["grib_model_levels"].append(arr)
+    lib.ref_io_reset()
+    return out
