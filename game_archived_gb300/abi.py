@@ -74,7 +74,30 @@ SIGNATURES = {
     "rkhevi_window_tl": ([vp, vp], cint),
     "rkhevi_window_backward": ([vp, vp], cint),
     "game_gpu_sfc_pressure_objective": ([vp, vp, ctypes.POINTER(ctypes.c_double), vp], cint),
+    "interpolate_to_ll": ([vp] * 3, cint),
+    "edges_to_cells_lowest_layer": ([vp] * 3, cint),
+    "epv_diagnostics": ([vp] * 5, cint),
+    "inner_product_tangential": ([vp] * 5, cint),
+    "calc_uv_at_edge": ([vp] * 4, cint),
+    "curl_field_to_cells": ([vp] * 3, cint),
+    "edges_to_cells": ([vp] * 3, cint),
+    "game_gpu_write_out_fields": ([vp, vp, cint, vp, vp, vp, vp, vp, vp], cint),
+    "game_gpu_record_wind_lowest": ([vp, cint], cint),
 }
+
+# struct game_gpu_output_fields (include/game_gb300.h), in declaration order,
+# with each field's kind: 0 surface, 1 model layers, 2 pressure levels,
+# 3 vertical wind at the levels (lat-lon only)
+OUTPUT_FIELDS = (("mslp", 0), ("surface_p", 0), ("t2", 0), ("tcdc", 0), ("rprate", 0), ("sprate", 0), ("cape", 0),
+                 ("sfc_sw_down", 0), ("u10", 0), ("v10", 0), ("gusts", 0), ("temperature", 1), ("pressure", 1),
+                 ("rh", 1), ("u", 1), ("v", 1), ("rel_vort", 1), ("divv_h", 1), ("epv", 1),
+                 ("geopotential_height", 2), ("t_pl", 2), ("rh_pl", 2), ("epv_pl", 2), ("u_pl", 2), ("v_pl", 2),
+                 ("rel_vort_pl", 2), ("w", 3))
+N_PRESSURE_LEVELS = 6
+
+
+class OutputFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.POINTER(dbl)) for n, _ in OUTPUT_FIELDS]
 
 FP64, MIXED = 0, 1
 
@@ -319,6 +342,91 @@ class GpuModel:
         self._check(self.lib.game_gpu_surface_pressure(state.ptr, _p(ps), _p(ms) if with_mslp else None),
                     "surface_pressure")
         return (ps, ms) if with_mslp else ps
+
+
+    # -- output diagnostics
+    def output_fields(self, state, wind_lowest, n_wind_steps, native=True, latlon=False, names=None):
+        """the fields write_out computes (game_gpu_write_out_fields): a dict
+        {"native": {name: array}, "latlon": {name: array}}; wind_lowest None
+        takes the recorded device slots"""
+        import numpy as np
+        lay = self.m.layout
+        nc, nl, nll = lay.nc, lay.nl, lay.n_latlon
+        want = [n for n, _ in OUTPUT_FIELDS] if names is None else list(names)
+        out = {}
+        structs_ = []
+        for grid_kind, on in (("native", native), ("latlon", latlon)):
+            if not on:
+                structs_.append(None)
+                continue
+            arrs = {}
+            fs = OutputFields()
+            for n, kind in OUTPUT_FIELDS:
+                if n not in want or (grid_kind == "native" and kind == 3):
+                    continue
+                if grid_kind == "native":
+                    size = {0: nc, 1: nl * nc, 2: nc * N_PRESSURE_LEVELS}[kind]
+                else:
+                    size = {0: 1, 1: nl, 2: N_PRESSURE_LEVELS, 3: nl + 1}[kind] * nll
+                a = np.zeros(size)
+                arrs[n] = a
+                setattr(fs, n, a.ctypes.data_as(ctypes.POINTER(dbl)))
+            out[grid_kind] = arrs
+            structs_.append(fs)
+        wl = None if wind_lowest is None else np.ascontiguousarray(wind_lowest, dtype=np.float64)
+        m = self.m
+        rc = self.lib.game_gpu_write_out_fields(state.ptr, _p(wl) if wl is not None else None, n_wind_steps,
+                                                m.diagnostics.ptr, m.forcings.ptr, m.grid.ptr, m.config.ptr,
+                                                ctypes.byref(structs_[0]) if structs_[0] is not None else None,
+                                                ctypes.byref(structs_[1]) if structs_[1] is not None else None)
+        self._check(rc, "write_out_fields")
+        return out
+
+    def record_wind_lowest(self, state, slot):
+        self._check(self.lib.game_gpu_record_wind_lowest(state.ptr, slot), "record_wind_lowest")
+
+    def interpolate_to_ll(self, field):
+        import numpy as np
+        out = np.zeros(self.m.layout.n_latlon)
+        self._check(self.lib.interpolate_to_ll(_p(np.ascontiguousarray(field)), _p(out), self.m.grid.ptr),
+                    "interpolate_to_ll")
+        return out
+
+    def edges_to_cells_lowest_layer(self, field):
+        import numpy as np
+        out = np.zeros(self.m.layout.nc)
+        self._check(self.lib.edges_to_cells_lowest_layer(_p(np.ascontiguousarray(field)), _p(out), self.m.grid.ptr),
+                    "edges_to_cells_lowest_layer")
+        return out
+
+    def epv_diagnostics(self, pot_vort, state):
+        import numpy as np
+        out = np.zeros(self.m.layout.n_scalars)
+        self._check(self.lib.epv_diagnostics(_p(pot_vort), state.ptr, _p(out), self.m.grid.ptr,
+                                             self.m.dualgrid.ptr), "epv_diagnostics")
+        return out
+
+    def inner_product_tangential(self, a, b):
+        import numpy as np
+        out = np.zeros(self.m.layout.n_scalars)
+        self._check(self.lib.inner_product_tangential(_p(a), _p(b), _p(out), self.m.grid.ptr, self.m.dualgrid.ptr),
+                    "inner_product_tangential")
+        return out
+
+    def calc_uv_at_edge(self, wind, u, v):
+        self._check(self.lib.calc_uv_at_edge(_p(wind), _p(u), _p(v), self.m.grid.ptr), "calc_uv_at_edge")
+
+    def curl_field_to_cells(self, curl):
+        import numpy as np
+        out = np.zeros(self.m.layout.n_scalars)
+        self._check(self.lib.curl_field_to_cells(_p(curl), _p(out), self.m.grid.ptr), "curl_field_to_cells")
+        return out
+
+    def edges_to_cells(self, vec):
+        import numpy as np
+        out = np.zeros(self.m.layout.n_scalars)
+        self._check(self.lib.edges_to_cells(_p(vec), _p(out), self.m.grid.ptr), "edges_to_cells")
+        return out
 
 
 def pinned_model(layout):

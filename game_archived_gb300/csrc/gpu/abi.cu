@@ -14,6 +14,7 @@
 #include "substeps.h"
 #include "adj.h"
 #include "adj_ops.h"
+#include "output.h"
 
 using namespace game;
 
@@ -1267,6 +1268,151 @@ int three_band_solver_ver_waves_adj(struct state *state_old, struct state *state
     if (download_state(state_old_bar, &b.bso, 31) || download_state(state_new_bar, &b.bsn, 31)
         || download_state(state_tendency_bar, &b.bst, 31))
         return -1;
+    return finish();
+}
+
+/* ------------------------------------------------------ output diagnostics
+ * The operators only output uses (host-in/host-out) and the fields of
+ * write_out (output_f64.cu). */
+int interpolate_to_ll(double in_field[], double out_field[], struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *f = c->dev_tmp[0];
+    if (upload_field(in_field, f, c->map_s, c->nc, c->nc)) return -1;
+    if (output_latlon_host(c, f, out_field)) return -1;
+    return finish();
+}
+
+int edges_to_cells_lowest_layer(double in_field[], double out_field[], struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *e = c->dev_tmp[1], *o = c->dev_tmp[0];
+    if (output_upload_edges(c, in_field, 1, e)) return -1;
+    op_edges_to_cells_lowest(c, e, o);
+    if (download_field(out_field, o, c->map_s, c->nc, c->nc, 0, c->nc)) return -1;
+    return finish();
+}
+
+int epv_diagnostics(double *pot_vort, struct state *state, double *epv, struct grid *grid, struct dualgrid *dualgrid)
+{
+    if (check_ready(grid)) return -1;
+    if (dualgrid != g_bound.dualgrid) return fail("dualgrid pointer differs from the one given to game_gpu_init");
+    Context *c = ctx();
+    double *pv = c->dev_tmp[1], *tvp = c->dev_tmp[2], *o = c->dev_tmp[0];
+    double *host_tvp = member<double>(state, GAME_STATE, "theta_v_pert");
+    if (upload_field(pot_vort, pv, c->map_curl, c->ncurl, c->ncurl)) return -1;
+    if (upload_field(host_tvp, tvp, c->map_s, c->ns, c->ns)) return -1;
+    DState s{};
+    s.theta_v_pert = tvp;
+    if (op_epv(c, pv, s, o)) return -1;
+    if (download_field(epv, o, c->map_s, c->ns, c->ns, 0, c->ns)) return -1;
+    /* the top layer of theta_v_pert as the reference leaves it */
+    if (download_field(host_tvp, tvp, c->map_s, c->ns, c->ns, 0, c->nc)) return -1;
+    return finish();
+}
+
+int inner_product_tangential(double *in_field_0, double *in_field_1, double *out_field, struct grid *grid,
+                             struct dualgrid *dualgrid)
+{
+    if (check_ready(grid)) return -1;
+    if (dualgrid != g_bound.dualgrid) return fail("dualgrid pointer differs from the one given to game_gpu_init");
+    Context *c = ctx();
+    double *a = c->dev_tmp[1], *b = c->dev_tmp[2], *o = c->dev_tmp[0];
+    if (upload_field(in_field_0, a, c->map_vec, c->nv, c->nv)) return -1;
+    if (upload_field(in_field_1, b, c->map_vec, c->nv, c->nv)) return -1;
+    op_inner_product_tangential(c, a, b, o);
+    if (download_field(out_field, o, c->map_s, c->ns, c->ns, 0, c->ns)) return -1;
+    return finish();
+}
+
+int calc_uv_at_edge(double *in_field, double *out_field_u, double *out_field_v, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    const long long off = (long long)(c->nl + 1) * c->nc;
+    double *in = c->dev_tmp[1], *u = c->dev_tmp[2], *v = c->dev_tmp[3];
+    if (upload_field(in_field, in, c->map_vec, c->nv, c->nv)) return -1;
+    if (vec_op_prologue(out_field_u, u) || vec_op_prologue(out_field_v, v)) return -1;
+    op_uv_at_edge(c, in + off, u + off, v + off);
+    if (download_field(out_field_u, u, c->map_vec, c->nv, c->nv, 0, c->nv)) return -1;
+    if (download_field(out_field_v, v, c->map_vec, c->nv, c->nv, 0, c->nv)) return -1;
+    return finish();
+}
+
+int curl_field_to_cells(double *in_field, double *out_field, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *in = c->dev_tmp[1], *o = c->dev_tmp[0];
+    if (upload_field(in_field, in, c->map_curl, c->ncurl, c->ncurl)) return -1;
+    op_curl_to_cells(c, in + (long long)(c->nl + 1) * c->ne, o);
+    if (download_field(out_field, o, c->map_s, c->ns, c->ns, 0, c->ns)) return -1;
+    return finish();
+}
+
+int edges_to_cells(double *in_field, double *out_field, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *in = c->dev_tmp[1], *o = c->dev_tmp[0];
+    if (upload_field(in_field, in, c->map_vec, c->nv, c->nv)) return -1;
+    op_edges_to_cells(c, in + (long long)(c->nl + 1) * c->nc, o);
+    if (download_field(out_field, o, c->map_s, c->ns, c->ns, 0, c->ns)) return -1;
+    return finish();
+}
+
+int game_gpu_write_out_fields(struct state *state_write_out, double wind_h_lowest_layer_array[],
+                              int min_no_of_output_steps, struct diagnostics *diagnostics,
+                              struct forcings *forcings, struct grid *grid, struct config *config,
+                              struct game_gpu_output_fields *native, struct game_gpu_output_fields *latlon)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (latlon && !c->og.ll_ok) return fail("lat-lon output: the grid's latlon_interpol_indices are out of range");
+    StateMirror *m = diag_mirror(state_write_out);
+    if (!m) return -1;
+    OutParams p{};
+    p.n_cond = c->n_cond;
+    p.moist = c->moist;
+    p.n_const = c->n_const;
+    p.prog_soil_temp = *member<int>(config, GAME_CONFIG, "prog_soil_temp");
+    p.gust_turbulence = *member<int>(config, GAME_CONFIG, "sfc_sensible_heat_flux") == 1
+                        || *member<int>(config, GAME_CONFIG, "sfc_phase_trans") == 1
+                        || *member<int>(config, GAME_CONFIG, "pbl_scheme") == 1;
+    p.n_wind_steps = min_no_of_output_steps;
+    p.snow_velocity = *member<double>(config, GAME_CONFIG, "snow_velocity");
+    p.rain_velocity = *member<double>(config, GAME_CONFIG, "rain_velocity");
+    OutHost h{};
+    h.sfc_sw_in = member<double>(forcings, GAME_FORCINGS, "sfc_sw_in");
+    h.temperature_soil = member<double>(state_write_out, GAME_STATE, "temperature_soil");
+    h.monin_obukhov_length = member<double>(diagnostics, GAME_DIAGNOSTICS, "monin_obukhov_length");
+    h.roughness_velocity = member<double>(diagnostics, GAME_DIAGNOSTICS, "roughness_velocity");
+    h.v_squared = member<double>(diagnostics, GAME_DIAGNOSTICS, "v_squared");
+    h.wind_lowest = wind_h_lowest_layer_array;
+    if (output_run(c, m, p, h, native, latlon)) return -1;
+    if (finish()) return -1;
+    if (!c->resident) {
+        /* write_out leaves the top layer of theta_v_pert rounded as
+         * (x + theta_v_bg) - theta_v_bg (spatial_ops_for_output.c:113-122) */
+        double *tvp = member<double>(state_write_out, GAME_STATE, "theta_v_pert");
+        const double *bg = member<double>(grid, GAME_GRID, "theta_v_bg");
+        for (int i = 0; i < c->nc; ++i) {
+            const double x = tvp[i] + bg[i];
+            tvp[i] = x - bg[i];
+        }
+    }
+    return 0;
+}
+
+int game_gpu_record_wind_lowest(struct state *state, int slot)
+{
+    if (check_ready(nullptr)) return -1;
+    Context *c = ctx();
+    StateMirror *m = diag_mirror(state);
+    if (!m) return -1;
+    if (output_record_wind(c, m, slot)) return -1;
     return finish();
 }
 

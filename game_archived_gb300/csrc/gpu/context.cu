@@ -399,6 +399,42 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
         c->dg64 = {lt.d, dndt.d, dnds.d, zvi.d, zsc.d, lat_d.d, cov, *GD("eff_hor_res"), *GD("mean_velocity_area")};
         c->dg32 = {lt.f, dndt.f, dnds.f, zvi.f, zsc.f, lat_d.f, cov, *GD("eff_hor_res"), *GD("mean_velocity_area")};
     }
+    /* output diagnostics: edge directions, surface properties, the
+     * permutations and the lat-lon interpolation tables ([5][N_ll], cells in
+     * device numbering; an index outside the grid disables the lat-lon
+     * output instead of failing the initialisation) */
+    {
+        const double *dir = GD("direction"), *rl = GD("roughness_length"), *alb = GD("sfc_albedo");
+        const int *land = GI("is_land"), *lli = GI("latlon_interpol_indices");
+        const double *llw = GD("latlon_interpol_weights");
+        const long long NLL = c->dims.n_latlon;
+        std::vector<double> h_dir(NE), h_rl(NC), h_alb(NC), h_llw((size_t)5 * NLL);
+        std::vector<int> h_land(NC), h_lli((size_t)5 * NLL);
+        for (int e = 0; e < NE; ++e) h_dir[e] = dir[en[e]];
+        for (int i = 0; i < NC; ++i) {
+            h_rl[i] = rl[cn[i]];
+            h_alb[i] = alb[cn[i]];
+            h_land[i] = land[cn[i]];
+        }
+        int ll_ok = 1;
+        for (long long p = 0; p < NLL; ++p)
+            for (int j = 0; j < 5; ++j) {
+                const int ref = lli[5 * p + j];
+                if (ref < 0 || ref >= NC) ll_ok = 0;
+                h_lli[(size_t)j * NLL + p] = (ref >= 0 && ref < NC) ? co[ref] : 0;
+                h_llw[(size_t)j * NLL + p] = llw[5 * p + j];
+            }
+        c->og.direction = dupload(c, h_dir);
+        c->og.roughness_length = dupload(c, h_rl);
+        c->og.sfc_albedo = dupload(c, h_alb);
+        c->og.is_land = dupload(c, h_land);
+        c->og.c_n2o = dupload(c, cn);
+        c->og.e_n2o = dupload(c, en);
+        c->og.ll_idx = dupload(c, h_lli);
+        c->og.ll_w = dupload(c, h_llw);
+        c->og.n_ll = NLL;
+        c->og.ll_ok = ll_ok;
+    }
 
     /* ---- upload */
     Dual t_vol = dual_upload(c, h_vol), t_ipw = dual_upload(c, h_ipw), t_ndv = dual_upload(c, h_ndv),
@@ -562,6 +598,7 @@ int destroy_context()
     profile_flush(c);
     for (auto e : c->user_events) cudaEventDestroy(e);
     if (c->adj_release) c->adj_release(c);
+    if (c->obuf_release) c->obuf_release(c);
     for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
     for (auto &kv : c->states) cudaFree(kv.second.dev);
     for (auto &b : c->owned) cudaFree(b.p);

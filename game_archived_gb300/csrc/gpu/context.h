@@ -158,6 +158,10 @@ struct Context {
      * the grid without overrunning radiation_tendency, and how many cells of
      * a layer (in reference numbering) they cover */
     int rad_blocks_ok = 0, rad_covered = 0;
+    /* output diagnostics: tables, and work arrays allocated on first use */
+    OutGrid og{};
+    struct OutBufs *obuf = nullptr;
+    void (*obuf_release)(Context *) = nullptr;
     int use_graphs = 1;
     int column_solver = 0; /* 0 by layer count, 1 per-thread sweeps, 2 warp cyclic reduction */
     int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */

@@ -76,6 +76,21 @@ struct HGrid {
     const R *dual_z_t;      /* [L][Nt] */
 };
 
+/* device tables of the output pass, built at initialisation (device order
+ * unless stated) */
+struct OutGrid {
+    const double *direction;        /* [Ne] */
+    const double *roughness_length; /* [Nc] */
+    const double *sfc_albedo;       /* [Nc] */
+    const int *is_land;             /* [Nc] */
+    const int *c_n2o;               /* [Nc] device cell -> reference cell */
+    const int *e_n2o;               /* [Ne] device edge -> reference edge */
+    const int *ll_idx;              /* [5][N_ll] device cells of each lat-lon point (lat-lon order) */
+    const double *ll_w;             /* [5][N_ll] */
+    long long n_ll;
+    int ll_ok;                      /* the caller's lat-lon indices were all in range */
+};
+
 /* vertical-solver tables (always double) */
 struct VGrid {
     int nc, nl;

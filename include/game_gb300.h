@@ -300,6 +300,90 @@ int game_gpu_sfc_pressure_objective(struct state *state, const double *weights, 
 int game_gpu_weighted_sums_noalloc(const double *fields, int n_fields, long long n, const double *weights,
                                    double *sums, void *stream);
 
+/* ---- 6. output diagnostics ----
+ *
+ * The operators only the reference's output code uses, with its signatures
+ * (host-in/host-out, like section 2's operators): */
+/* src/io/io.h:15 -> src/io/spatial_ops_for_output.c:168: one [NO_OF_SCALARS_H]
+ * field to the [NO_OF_LATLON_IO_POINTS] lat-lon grid with the grid's
+ * latlon_interpol_indices / _weights */
+int interpolate_to_ll(double in_field[], double out_field[], struct grid *grid);
+/* io.h:16 -> spatial_ops_for_output.c:199: [NO_OF_VECTORS_H] -> [NO_OF_SCALARS_H] */
+int edges_to_cells_lowest_layer(double in_field[], double out_field[], struct grid *grid);
+/* io.h:14 -> spatial_ops_for_output.c:17: Ertel's potential vorticity from
+ * the Curl_field pot_vort (as calc_pot_vort leaves it); also writes state's
+ * theta_v_pert of the top layer back as (x + theta_v_bg) - theta_v_bg, as the
+ * reference does */
+int epv_diagnostics(double *pot_vort, struct state *state, double *epv, struct grid *grid,
+                    struct dualgrid *dualgrid);
+/* spatial_ops_for_output.c:137 (declared in that file) */
+int inner_product_tangential(double *in_field_0, double *in_field_1, double *out_field, struct grid *grid,
+                             struct dualgrid *dualgrid);
+/* src/spatial_operators/spatial_operators.h:27-30 -> averaging.c:152,176,206:
+ * calc_uv_at_edge writes the horizontal entries of out_field_u/_v only */
+int calc_uv_at_edge(double *in_field, double *out_field_u, double *out_field_v, struct grid *grid);
+int curl_field_to_cells(double *in_field, double *out_field, struct grid *grid);
+int edges_to_cells(double *in_field, double *out_field, struct grid *grid);
+
+/* The fields write_out (src/io/write_output.c:51-1513) computes for its
+ * surface, pressure-level and model-level files, without the writers: the
+ * caller passes them to its netCDF / GRIB code.  Every pointer may be NULL
+ * (field not wanted).  Native-grid layout (argument native):
+ *   surface fields            [NO_OF_SCALARS_H]
+ *   model layers              [NO_OF_SCALARS] (Scalar_field order)
+ *   pressure levels           [NO_OF_SCALARS_H][6], levels 200, 300, 500,
+ *                             700, 850, 925 hPa (the reference's arrays)
+ *   w                         unused
+ * Lat-lon layout (argument latlon), interpolate_to_ll of every horizontal
+ * slice, as the GRIB path writes them:
+ *   surface fields            [NO_OF_LATLON_IO_POINTS]
+ *   model layers              [NO_OF_LAYERS][NO_OF_LATLON_IO_POINTS]
+ *   pressure levels           [6][NO_OF_LATLON_IO_POINTS]
+ *   w                         [NO_OF_LEVELS][NO_OF_LATLON_IO_POINTS],
+ *                             the vertical wind at the levels
+ * Missing values (pressure levels below the lowest layer) are 9999, and so
+ * is every lat-lon point next to one. */
+struct game_gpu_output_fields {
+    /* surface: write_output.c:100-350 */
+    double *mslp, *surface_p, *t2, *tcdc, *rprate, *sprate, *cape, *sfc_sw_down, *u10, *v10, *gusts;
+    /* model layers: temperature, pressure, relative humidity (%), eastward
+     * and northward wind, relative vorticity, horizontal divergence, Ertel's
+     * potential vorticity (:718-749) */
+    double *temperature, *pressure, *rh, *u, *v, *rel_vort, *divv_h, *epv;
+    /* pressure levels (:751-826) */
+    double *geopotential_height, *t_pl, *rh_pl, *epv_pl, *u_pl, *v_pl, *rel_vort_pl;
+    double *w;
+};
+
+/* Computes the fields from state_write_out: its device mirror in resident
+ * mode, else the host struct, uploaded.  wind_h_lowest_layer_array holds the
+ * lowest layer's horizontal wind at min_no_of_output_steps time steps,
+ * [min_no_of_output_steps][NO_OF_VECTORS_H] as the reference's driver fills
+ * it (src/coordinator.c:350-358); NULL takes the slots recorded on the device
+ * by game_gpu_record_wind_lowest instead.  Reads diagnostics'
+ * monin_obukhov_length, roughness_velocity and v_squared only when the
+ * config switches the gusts' boundary-layer branch on (sfc_sensible_heat_flux,
+ * sfc_phase_trans or pbl_scheme == 1), forcings' sfc_sw_in, and
+ * state_write_out's temperature_soil only with prog_soil_temp == 1.
+ * Like write_out it rounds the top layer of state_write_out's theta_v_pert as
+ * (x + theta_v_bg) - theta_v_bg (on the mirror in resident mode, else on the
+ * host struct); unlike write_out it leaves the Diagnostics work arrays
+ * (temperature, rel_vort, pot_vort, u/v_at_edge, u/v_at_cell,
+ * scalar_field_placeholder) alone.  The gust diagnostics follow write_out run
+ * on one thread: the reference's loop shares a work array between its
+ * OpenMP threads.  No counterpart function in the reference (the loops are
+ * inside write_out). */
+int game_gpu_write_out_fields(struct state *state_write_out, double wind_h_lowest_layer_array[],
+                              int min_no_of_output_steps, struct diagnostics *diagnostics,
+                              struct forcings *forcings, struct grid *grid, struct config *config,
+                              struct game_gpu_output_fields *native, struct game_gpu_output_fields *latlon);
+
+/* Copies the lowest layer's horizontal wind of state (its device mirror in
+ * resident mode, else the host struct) into device slot `slot`
+ * (0 <= slot < 4096), the device-side counterpart of the driver's
+ * wind_h_lowest_layer bookkeeping (src/coordinator.c:350-358). */
+int game_gpu_record_wind_lowest(struct state *state, int slot);
+
 #ifdef __cplusplus
 }
 #endif

@@ -308,3 +308,24 @@ def interpolate_to_ll(orc, field):
     out = np.zeros(orc.m.layout.n_latlon)
     orc.lib.orc_interpolate_to_ll(ctypes.byref(orc.g), _d(f), _d(out))
     return out
+
+
+def output_op(orc, name, *arrays, out_len=None, extra_out=None):
+    """calls one of the oracle's output operators (orc_calc_uv_at_edge,
+    orc_curl_field_to_cells, orc_edges_to_cells, orc_edges_to_cells_lowest_layer,
+    orc_inner_product_tangential) on host arrays; returns the output array"""
+    lay = orc.m.layout
+    out = np.zeros(out_len if out_len is not None else lay.n_scalars)
+    args = [_d(np.ascontiguousarray(a, dtype=np.float64)) for a in arrays] + [_d(out)]
+    getattr(orc.lib, "orc_" + name)(ctypes.byref(orc.g), *args)
+    return out
+
+
+def epv_diagnostics(orc, pot_vort, state):
+    """orc_epv_diagnostics; rounds state's theta_v_pert top layer in place"""
+    out = np.zeros(orc.m.layout.n_scalars)
+    s = orc.state(state)
+    rc = orc.lib.orc_epv_diagnostics(ctypes.byref(orc.g), _d(np.ascontiguousarray(pot_vort)), ctypes.byref(s), _d(out))
+    if rc != 0:
+        raise RuntimeError("oracle epv_diagnostics failed")
+    return out

@@ -90,7 +90,7 @@ def output_scenario(res, moist, case, mountain=False, steps=2, dt=300.0, gust_sc
         s["rho"][3 * ns:4 * ns] = 1e-5 * rng.random(ns) ** 3 * cloudy
     m.forcings["sfc_sw_in"][:] = 400.0 * rng.random(nc)
     n_wind = 3
-    lo = lay.n_vectors - lay.vpl + nc
+    lo = lay.n_vectors - lay.vpl  # the lowest layer's horizontal wind (coordinator.c:356)
     wind_lowest = np.concatenate([s["wind"][lo:lo + ne] * (1.0 + 0.1 * rng.standard_normal(ne))
                                   for _ in range(n_wind)])
     if gust_scheme:
