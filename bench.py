@@ -366,6 +366,83 @@ def time_diffusion(model0, steps, warmup, dt, device, base_ms):
     return out
 
 
+def time_output(model0, device, n_wind=4, repeats=10):
+    """The output diagnostics of write_out (game_gpu_write_out_fields) on the
+    headline workload's state, device-resident, with the lowest-layer wind of
+    n_wind steps recorded on the device: the device-only pass (every field
+    computed, nothing copied to the host), and the full call with every field
+    on the native grid and on the lat-lon grid written to host memory.  The
+    CPU side is the oracle's restatement of write_out (the reference's
+    algorithm, OpenMP on all host threads) plus its interpolate_to_ll of
+    every horizontal slice, on the same state."""
+    import numpy as np
+    from game_archived_gb300 import abi
+    from oracle import bind
+    m = copy_model(model0, pinned=False)
+    lay = m.layout
+    out = {"config": f"write_out's fields of the headline state: 11 surface, 8 model-layer, 7 pressure-level "
+                     f"fields on {lay.nc} cells and on the {lay.n_latlon}-point lat-lon grid (every slice, as "
+                     f"the GRIB path), 10 m wind over {n_wind} recorded steps"}
+    g = abi.GpuModel(m, abi.FP64, resident=True, device=device)
+    try:
+        g.sync_to_device(m.state_new)
+        for t in range(n_wind):
+            g.record_wind_lowest(m.state_new, t)
+        for _ in range(3):
+            g.output_fields(m.state_new, None, n_wind, native=False, latlon=False)
+        g.synchronize()
+        g.kernel_launches(reset=True)
+        g.event_record(0)
+        for _ in range(repeats):
+            g.output_fields(m.state_new, None, n_wind, native=False, latlon=False)
+        g.event_record(1)
+        g.synchronize()
+        dev_ms = g.event_elapsed_ms(0, 1) / repeats
+        launches = g.kernel_launches(reset=True) / repeats
+        bufs = g.output_fields(m.state_new, None, n_wind, native=True, latlon=True)
+        g.transfer_bytes(reset=True)
+        t0 = time.perf_counter()
+        for _ in range(repeats):
+            g.output_fields(m.state_new, None, n_wind, native=True, latlon=True, buffers=bufs)
+        full_ms = (time.perf_counter() - t0) * 1000.0 / repeats
+        h2d, d2h = g.transfer_bytes(reset=True)
+    finally:
+        g.close()
+    out["gpu"] = {"device_ms": dev_ms, "call_ms_with_host_copies": full_ms, "d2h_bytes_per_call": int(d2h / repeats),
+                  "h2d_bytes_per_call": int(h2d / repeats), "gpu_launches_per_call": launches}
+    # the oracle on the host cores: one untimed call, then timed calls
+    mo = copy_model(model0, pinned=False)
+    orc = bind.Oracle(mo)
+    lo = lay.n_vectors - lay.vpl
+    wl = np.concatenate([mo.state_new["wind"][lo:lo + lay.ne]] * n_wind)
+    nc, nl = lay.nc, lay.nl
+
+    def cpu_call():
+        f = bind.write_out_fields(orc, mo.state_new, wl, n_wind)
+        fields = [f[k] for k in bind.OUTPUT_SURFACE] + [mo.diagnostics["temperature"], mo.diagnostics["u_at_cell"],
+                                                        mo.diagnostics["v_at_cell"]]
+        fields += [f[k] for k in bind.OUTPUT_LAYERS]
+        for a in fields:
+            for k in range(len(a) // nc):
+                bind.interpolate_to_ll(orc, a[k * nc:(k + 1) * nc])
+        for k in bind.OUTPUT_PLEVELS:
+            a = f[k].reshape(nc, 6)
+            for j in range(6):
+                bind.interpolate_to_ll(orc, np.ascontiguousarray(a[:, j]))
+        for k in range(nl + 1):
+            bind.interpolate_to_ll(orc, mo.state_new["wind"][k * lay.vpl:k * lay.vpl + nc])
+    cpu_call()
+    times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        cpu_call()
+        times.append(time.perf_counter() - t0)
+    cpu_ms = 1000.0 * min(times)
+    out["cpu_oracle"] = {"call_ms": cpu_ms, "cores": os.cpu_count(), "kind": "port"}
+    out["speedup_call_with_host_copies"] = cpu_ms / full_ms
+    return out
+
+
 def cpu_baseline(model0, dt, max_seconds=25.0):
     """oracle on all host threads; bounded number of steps"""
     from game_archived_gb300 import driver
@@ -495,6 +572,8 @@ def run_ours(args):
     if not args.no_diffusion:
         line["diffusion"] = time_diffusion(model0, max(20, args.steps // 4), args.warmup, dt, local,
                                            {"mixed": ms32, "fp64": ms64})
+    if not args.no_output:
+        line["output"] = time_output(model0, local)
     if not args.no_adjoint:
         line["adjoint"] = time_adjoint(args.adjoint_res, args.n_lloyd, 12, 200.0, local)
     if world == 1 and not args.no_cpu_baseline:
@@ -599,6 +678,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-diffusion", action="store_true")
+    ap.add_argument("--no-output", action="store_true")
     ap.add_argument("--adjoint-res", type=int, default=5)
     ap.add_argument("--column-study", action="store_true",
                     help="time the column solvers at 26, 64 and 128 layers instead of the headline line")

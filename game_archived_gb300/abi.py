@@ -345,10 +345,11 @@ class GpuModel:
 
 
     # -- output diagnostics
-    def output_fields(self, state, wind_lowest, n_wind_steps, native=True, latlon=False, names=None):
+    def output_fields(self, state, wind_lowest, n_wind_steps, native=True, latlon=False, names=None, buffers=None):
         """the fields write_out computes (game_gpu_write_out_fields): a dict
         {"native": {name: array}, "latlon": {name: array}}; wind_lowest None
-        takes the recorded device slots"""
+        takes the recorded device slots; buffers: a dict of that shape from an
+        earlier call, reused instead of new arrays"""
         import numpy as np
         lay = self.m.layout
         nc, nl, nll = lay.nc, lay.nl, lay.n_latlon
@@ -368,7 +369,7 @@ class GpuModel:
                     size = {0: nc, 1: nl * nc, 2: nc * N_PRESSURE_LEVELS}[kind]
                 else:
                     size = {0: 1, 1: nl, 2: N_PRESSURE_LEVELS, 3: nl + 1}[kind] * nll
-                a = np.zeros(size)
+                a = buffers[grid_kind][n] if buffers is not None else np.zeros(size)
                 arrs[n] = a
                 setattr(fs, n, a.ctypes.data_as(ctypes.POINTER(dbl)))
             out[grid_kind] = arrs
