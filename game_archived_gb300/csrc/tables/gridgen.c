@@ -89,6 +89,83 @@ static double turn_angle(double a0, double a1)
     return r;
 }
 
+/* ------------------------------------------- dual-vector directions
+ * The reference's generator gives a dual vector the direction of the great
+ * circle through its two dual points, evaluated at the point of that circle
+ * nearest to the primal vector point, where "nearest" is the first minimum
+ * of the chord distance over the 1001 sample parameters t_i = i / 1002
+ * (horizontal_generation.c:519-576 with geodesy.c:15-92 and 369-387).  The
+ * samples, distances and directions below are computed from geographical
+ * coordinates with the same formulas, so the sampled parameter and the
+ * direction are the reference's.  Only the window of samples searched
+ * differs: the distance along the circle has a single minimum, at the
+ * angle t* = atan2(p.q, p.a) / theta (a, q an orthonormal pair spanning the
+ * circle's plane, a the first point), so the first minimum over all samples
+ * lies within a sample of t* and a window of +-DUAL_WINDOW samples around it
+ * holds it. */
+#define DUAL_SAMPLES 1001
+#define DUAL_WINDOW 4
+
+static double chord_geo(double lat_1, double lon_1, double lat_2, double lon_2)
+{
+    if (lat_1 == lat_2 && lon_1 == lon_2) return 0;
+    const double x_1 = cos(lat_1) * cos(lon_1), y_1 = cos(lat_1) * sin(lon_1), z_1 = sin(lat_1);
+    const double x_2 = cos(lat_2) * cos(lon_2), y_2 = cos(lat_2) * sin(lon_2), z_2 = sin(lat_2);
+    return sqrt(pow(x_2 - x_1, 2) + pow(y_2 - y_1, 2) + pow(z_2 - z_1, 2));
+}
+
+/* the point at parameter t of the great circle from 1 to 2, uniform in angle */
+static void geodetic_point(double lat_1, double lon_1, double lat_2, double lon_2, double t, double *lat,
+                           double *lon)
+{
+    const double d = chord_geo(lat_1, lon_1, lat_2, lon_2);
+    const double theta = 2.0 * asin(d / 2.0);
+    const double tau = 0.5 + sqrt(1.0 / pow(d, 2) - 0.25) * tan(theta * (t - 0.5));
+    const double z = tau * sin(lat_2) + (1.0 - tau) * sin(lat_1);
+    const double x = tau * cos(lat_2) * cos(lon_2) + (1.0 - tau) * cos(lat_1) * cos(lon_1);
+    const double y = tau * cos(lat_2) * sin(lon_2) + (1.0 - tau) * cos(lat_1) * sin(lon_1);
+    *lat = asin(z / sqrt(pow(x, 2) + pow(y, 2) + pow(z, 2)));
+    *lon = atan2(y, x);
+}
+
+/* direction (counter-clockwise from east) of the chord 1 -> 2 in the local
+ * frame of the circle's point at parameter t */
+static double geodetic_direction(double lat_1, double lon_1, double lat_2, double lon_2, double t)
+{
+    const double rx = cos(lat_2) * cos(lon_2) - cos(lat_1) * cos(lon_1);
+    const double ry = cos(lat_2) * sin(lon_2) - cos(lat_1) * sin(lon_1);
+    const double rz = sin(lat_2) - sin(lat_1);
+    double lat, lon;
+    geodetic_point(lat_1, lon_1, lat_2, lon_2, t, &lat, &lon);
+    const double x_comp = -sin(lon) * rx + cos(lon) * ry + 0 * rz;
+    const double y_comp = -sin(lat) * cos(lon) * rx + -sin(lat) * sin(lon) * ry + cos(lat) * rz;
+    return atan2(y_comp, x_comp);
+}
+
+/* the sampled parameter of the point of the circle 1 -> 2 nearest to p */
+static double nearest_sample(double lat_1, double lon_1, double lat_2, double lon_2, double lat_p, double lon_p)
+{
+    const v3 a = v3_from_geo(lat_1, lon_1), b = v3_from_geo(lat_2, lon_2), p = v3_from_geo(lat_p, lon_p);
+    const v3 q = v3_unit(v3_sub(b, v3_scale(a, v3_dot(a, b))));
+    const double theta = atan2(v3_dot(b, q), v3_dot(b, a));
+    const double t_star = atan2(v3_dot(p, q), v3_dot(p, a)) / theta;
+    int i_0 = (int)floor(t_star * (DUAL_SAMPLES + 1.0)) - DUAL_WINDOW, i_1 = i_0 + 2 * DUAL_WINDOW + 1;
+    if (i_0 < 0) i_0 = 0;
+    if (i_1 > DUAL_SAMPLES - 1) i_1 = DUAL_SAMPLES - 1;
+    int best = -1;
+    double best_d = 0;
+    for (int i = i_0; i <= i_1; ++i) {
+        double lat, lon;
+        geodetic_point(lat_1, lon_1, lat_2, lon_2, (i + 0.0) / (DUAL_SAMPLES + 1.0), &lat, &lon);
+        const double d = chord_geo(lat_p, lon_p, lat, lon);
+        if (best < 0 || d < best_d) {
+            best = i;
+            best_d = d;
+        }
+    }
+    return (best + 0.0) / (DUAL_SAMPLES + 1.0);
+}
+
 /* ----------------------------------------------------------- pair hashing */
 typedef struct { int64_t *keys; int *vals; long cap; } pairmap;
 
@@ -698,10 +775,12 @@ game_tables *gt_build(int res_id, int n_layers, int n_oro_layers, double toa,
         /* dual orientation so that the dual direction is the normal turned
          * counter-clockwise by 90 degrees (direct_tangential_unity) */
         int ta = e_tri[2 * e], tb = e_tri[2 * e + 1];
-        double dd = chord_direction(circ[ta], circ[tb], mid[e]);
+        double rel = nearest_sample(lat_t[ta], lon_t[ta], lat_t[tb], lon_t[tb], lat_e[e], lon_e[e]);
+        double dd = geodetic_direction(lat_t[ta], lon_t[ta], lat_t[tb], lon_t[tb], rel);
         if (turn_angle(direction[e], dd) * 180.0 / M_PI < -ORTH_CRITERION_DEG) {
             int s = ta; ta = tb; tb = s;
-            dd = chord_direction(circ[ta], circ[tb], mid[e]);
+            rel = 1 - rel;
+            dd = geodetic_direction(lat_t[ta], lon_t[ta], lat_t[tb], lon_t[tb], rel);
         }
         double ang = fabs(turn_angle(direction[e], dd) * 180.0 / M_PI);
         if (ang < ORTH_CRITERION_DEG || ang > 90 + (90 - ORTH_CRITERION_DEG)) orth_bad++;

@@ -19,10 +19,20 @@ DEFAULT_STRETCHING = 1.3
 DEFAULT_ORO_LAYERS = 23
 
 
+def as_float32(x):
+    """the value the reference's generator sees for a command-line argument
+    it parses with strtof (grid_generator/src/coordinator.c:51-56): x rounded
+    to single precision"""
+    return float(np.float32(x))
+
+
 class GridTables:
     def __init__(self, res_id, n_layers=26, n_oro_layers=DEFAULT_ORO_LAYERS, toa=DEFAULT_TOA,
                  stretching=DEFAULT_STRETCHING, radius_rescale=1.0, n_lloyd=None, mountain=None, n_threads=0):
-        """mountain: None (flat) or (height_m, half_width_m, lat_deg, lon_deg)."""
+        """mountain: None (flat) or (height_m, half_width_m, lat_deg, lon_deg).
+        toa, stretching and radius_rescale are rounded to single precision
+        first, as the reference's generator reads them."""
+        toa, stretching, radius_rescale = as_float32(toa), as_float32(stretching), as_float32(radius_rescale)
         if n_lloyd is None:
             n_lloyd = 2000 if res_id <= 6 else 500
         lib = native.tables()

@@ -23,7 +23,13 @@ compiles it with gcc:
 * oracle/ref_harness.c (ours) exports sizeof/offsetof of the reference structs
   so the run-time layout can be checked against the compiler's.
 
-Output: oracle/_ref/libgame_ref_v<version>_R<res>_M<moist>.so.  Nothing is copied into the
+Output: oracle/_ref/libgame_ref_v<version>_R<res>_M<moist>.so.
+
+build_gridgen compiles the reference's grid generator program
+(grid_generator/src/*.c) the same way into
+oracle/_ref/libgame_refgrid_v<version>_R<res>_L<layers>.so; its main runs
+in-process and the tables it would write to its netCDF grid file are
+recorded by the stand-in.  Nothing is copied into the
 repository; oracle/_ref/ is git-ignored.  Runs only where the reference tree
 exists (this build container), never on the GPU host.
 """
@@ -129,6 +135,53 @@ def build(res_id, moisture_on, n_layers=26, force=False):
     harness = [os.path.join(HERE, "ref_harness.c"), os.path.join(HERE, "ref_io_stubs.c")]
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-w",
            "-I", inc, "-I", os.path.join(HERE, "ref_stubs"), "-I", src, "-o", out] + sources + [stub] + harness + ["-lm"]
+    subprocess.run(cmd, check=True)
+    return out
+
+
+def gridgen_path(res_id, n_layers=26):
+    return os.path.join(OUT, f"libgame_refgrid_v{BUILD_VERSION}_R{res_id}_L{n_layers}.so")
+
+
+def build_gridgen(res_id, n_layers=26, force=False):
+    """Builds (or reuses) the reference's grid generator (every source of
+    grid_generator/src, its main renamed ref_gridgen_main) with the netCDF
+    stand-in, which records every table the generator writes to its grid
+    file instead of writing it."""
+    if not available():
+        raise RuntimeError("reference sources not present")
+    out = gridgen_path(res_id, n_layers)
+    if os.path.exists(out) and not force:
+        return out
+    bdir = os.path.join(OUT, f"build_grid_R{res_id}_L{n_layers}")
+    src = os.path.join(bdir, "src")
+    os.makedirs(src, exist_ok=True)
+    with open(os.path.join(REF_ROOT, "src", "game_types.h")) as f:
+        hdr = f.read()
+    hdr = re.sub(r"RES_ID = \d+", f"RES_ID = {res_id}", hdr)
+    hdr = re.sub(r"NO_OF_LAYERS = \d+", f"NO_OF_LAYERS = {n_layers}", hdr)
+    gen = os.path.join(src, "game_types.h")
+    if os.path.lexists(gen):
+        os.remove(gen)
+    with open(gen, "w") as f:
+        f.write(hdr)
+    _link(os.path.join(REF_ROOT, "src", "game_constants.h"), os.path.join(src, "game_constants.h"))
+    # vertical_grid.c includes the model's constituents header (declarations only)
+    os.makedirs(os.path.join(src, "constituents"), exist_ok=True)
+    for name in os.listdir(os.path.join(REF_ROOT, "src", "constituents")):
+        if name.endswith(".h"):
+            _link(os.path.join(REF_ROOT, "src", "constituents", name), os.path.join(src, "constituents", name))
+    gg = os.path.join(bdir, "grid_generator", "src")
+    os.makedirs(gg, exist_ok=True)
+    sources = []
+    for name in sorted(os.listdir(os.path.join(REF_ROOT, "grid_generator", "src"))):
+        if name.endswith(".h") or name.endswith(".c"):
+            _link(os.path.join(REF_ROOT, "grid_generator", "src", name), os.path.join(gg, name))
+            if name.endswith(".c"):
+                sources.append(os.path.join(gg, name))
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-w", "-Dmain=ref_gridgen_main",
+           "-I", os.path.join(HERE, "ref_stubs"), "-I", src, "-o", out] + sources + [
+        os.path.join(HERE, "ref_io_stubs.c"), os.path.join(HERE, "ref_harness_grid.c"), "-lm"]
     subprocess.run(cmd, check=True)
     return out
 

@@ -110,3 +110,39 @@ def write_out(ref, state, wind_lowest, n_wind_steps, workdir, t_init=0.0, t_writ
             out["grib_model_levels"].append(arr)
     lib.ref_io_reset()
     return out
+
+
+def run_gridgen(res_id, n_iterations, workdir, n_layers=26, stretching=1.3, n_oro_layers=23, toa=41152.0,
+                radius_rescale=1.0):
+    """Runs the reference's grid generator program (grid_generator/src/
+    coordinator.c main, flat orography) in-process in workdir and returns the
+    tables it writes to its grid file, recorded by the netCDF stand-in:
+    {variable name: array} (integer tables as float arrays)."""
+    import numpy as np
+    lib = ctypes.CDLL(build_ref.build_gridgen(res_id, n_layers))
+    os.makedirs(os.path.join(workdir, "statistics"), exist_ok=True)
+    os.makedirs(os.path.join(workdir, "grids"), exist_ok=True)
+    args = [b"grid_generator", b"0", str(n_iterations).encode(), b"0", b"none", repr(stretching).encode(),
+            str(n_oro_layers).encode(), repr(toa).encode(), repr(radius_rescale).encode(), b"7"]
+    argv = (ctypes.c_char_p * len(args))(*args)
+    lib.ref_run_gridgen.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p)]
+    lib.ref_io_record.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_char_p),
+                                  ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long),
+                                  ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]
+    lib.ref_io_reset()
+    cwd = os.getcwd()
+    try:
+        rc = lib.ref_run_gridgen(workdir.encode(), len(args), argv)
+    finally:
+        os.chdir(cwd)
+    assert rc == 0
+    out = {}
+    f, nm = ctypes.c_char_p(), ctypes.c_char_p()
+    meta = (ctypes.c_long * 4)()
+    n = ctypes.c_long()
+    data = ctypes.POINTER(ctypes.c_double)()
+    for k in range(lib.ref_io_count()):
+        lib.ref_io_record(k, ctypes.byref(f), ctypes.byref(nm), meta, ctypes.byref(n), ctypes.byref(data))
+        out[nm.value.decode()] = np.ctypeslib.as_array(data, shape=(n.value,)).copy()
+    lib.ref_io_reset()
+    return out
