@@ -399,6 +399,14 @@ def time_output(model0, device, n_wind=4, repeats=10):
         g.synchronize()
         dev_ms = g.event_elapsed_ms(0, 1) / repeats
         launches = g.kernel_launches(reset=True) / repeats
+        # per-kernel-group times (events around each launch group, a separate
+        # pass: the events serialise the launches)
+        g.profile(True)
+        for _ in range(repeats):
+            g.output_fields(m.state_new, None, n_wind, native=False, latlon=True)
+        g.synchronize()
+        g.profile(False)
+        prof = {k: v[0] / repeats for k, v in g.profile_results().items() if k.startswith("out_")}
         bufs = g.output_fields(m.state_new, None, n_wind, native=True, latlon=True)
         g.transfer_bytes(reset=True)
         t0 = time.perf_counter()
@@ -409,7 +417,8 @@ def time_output(model0, device, n_wind=4, repeats=10):
     finally:
         g.close()
     out["gpu"] = {"device_ms": dev_ms, "call_ms_with_host_copies": full_ms, "d2h_bytes_per_call": int(d2h / repeats),
-                  "h2d_bytes_per_call": int(h2d / repeats), "gpu_launches_per_call": launches}
+                  "h2d_bytes_per_call": int(h2d / repeats), "gpu_launches_per_call": launches,
+                  "kernel_groups_ms_profiled_with_latlon": prof}
     # the oracle on the host cores: one untimed call, then timed calls
     mo = copy_model(model0, pinned=False)
     orc = bind.Oracle(mo)

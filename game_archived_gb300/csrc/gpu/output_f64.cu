@@ -625,29 +625,50 @@ int output_fields(Context *c, StateMirror *sm, const OutParams &p, const OutInpu
     const long long S = c->ns;
     cudaStream_t st = c->stream;
     double *T = f.temperature, *P = f.pressure, *RH = f.rh;
-    k_out_cells<<<nb(S), 256, 0, st>>>(c->vg, s, p, T, P, RH);
+    {
+        ProfScope ps(c, "out_cells");
+        k_out_cells<<<nb(S), 256, 0, st>>>(c->vg, s, p, T, P, RH);
+    }
     SurfOut so{f.mslp, f.surface_p, f.t2, f.tcdc, f.rprate, f.sprate, f.cape, f.sfc_sw_down};
-    k_out_surface<<<nb(c->nc, 128), 128, 0, st>>>(c->hg64, c->vg, c->og, c->dg64.layer_thickness, s, p, T,
-                                                   in.sfc_sw_in, in.temperature_soil, so);
-    k_out_wind10_e<<<nb(c->ne), 256, 0, st>>>(c->hg64, c->vg, c->og, in.wind_lowest, p.n_wind_steps, b->u10e,
-                                              b->v10e);
-    k_out_wind10_c<<<nb(c->nc, 128), 128, 0, st>>>(c->hg64, c->vg, p, b->u10e, b->v10e, in.monin_obukhov_length,
-                                                    in.roughness_velocity, in.v_squared, f.u10, f.v10, f.gusts);
+    {
+        ProfScope ps(c, "out_surface");
+        k_out_surface<<<nb(c->nc, 128), 128, 0, st>>>(c->hg64, c->vg, c->og, c->dg64.layer_thickness, s, p, T,
+                                                       in.sfc_sw_in, in.temperature_soil, so);
+    }
+    {
+        ProfScope ps(c, "out_wind10");
+        k_out_wind10_e<<<nb(c->ne), 256, 0, st>>>(c->hg64, c->vg, c->og, in.wind_lowest, p.n_wind_steps, b->u10e,
+                                                  b->v10e);
+        k_out_wind10_c<<<nb(c->nc, 128), 128, 0, st>>>(c->hg64, c->vg, p, b->u10e, b->v10e, in.monin_obukhov_length,
+                                                        in.roughness_velocity, in.v_squared, f.u10, f.v10, f.gusts);
+    }
     c->kernel_launches += 4;
     /* model layers: divergence, relative vorticity, winds at the cells */
-    op_divv(c, s.w, nullptr, nullptr, f.divv_h, 0);
-    op_rel_vort(c, s.w, b->tri, b->rel);
-    op_curl_to_cells(c, b->rel + (long long)(c->nl + 1) * c->ne, f.rel_vort);
-    op_uv_at_edge(c, s.u, b->ue, b->ve);
-    op_edges_to_cells(c, b->ue, f.u);
-    op_edges_to_cells(c, b->ve, f.v);
+    {
+        ProfScope ps(c, "out_divv_vort");
+        op_divv(c, s.w, nullptr, nullptr, f.divv_h, 0);
+        op_rel_vort(c, s.w, b->tri, b->rel);
+        op_curl_to_cells(c, b->rel + (long long)(c->nl + 1) * c->ne, f.rel_vort);
+    }
+    {
+        ProfScope ps(c, "out_uv");
+        op_uv_at_edge(c, s.u, b->ue, b->ve);
+        op_edges_to_cells(c, b->ue, f.u);
+        op_edges_to_cells(c, b->ve, f.v);
+    }
     /* Ertel's potential vorticity from the potential vorticity of the dry
      * air density */
-    op_pot_vort(c, b->rel, s.rho + (long long)p.n_cond * S, b->pv);
-    if (op_epv(c, b->pv, s, f.epv)) return -1;
+    {
+        ProfScope ps(c, "out_epv");
+        op_pot_vort(c, b->rel, s.rho + (long long)p.n_cond * S, b->pv);
+        if (op_epv(c, b->pv, s, f.epv)) return -1;
+    }
     PlIn pi{P, c->gravity_potential, T, RH, f.epv, f.u, f.v, f.rel_vort};
     PlOut po{f.geopotential_height, f.t_pl, f.rh_pl, f.epv_pl, f.u_pl, f.v_pl, f.rel_vort_pl};
-    k_out_plevels<<<nb(c->nc, 128), 128, 0, st>>>(c->nc, c->nl, pi, po);
+    {
+        ProfScope ps(c, "out_plevels");
+        k_out_plevels<<<nb(c->nc, 128), 128, 0, st>>>(c->nc, c->nl, pi, po);
+    }
     c->kernel_launches++;
     CK(cudaGetLastError());
     return 0;
@@ -658,6 +679,7 @@ int output_latlon(Context *c, const double *const *src, int n_fields, double *ds
     if (!c->og.ll_ok) return fail("lat-lon output: the grid's latlon_interpol_indices are out of range");
     if (n_fields < 1 || n_fields > 65535) return fail("lat-lon output: field count out of range");
     dim3 grid(nb(c->og.n_ll), (unsigned)n_fields);
+    ProfScope ps(c, "out_latlon");
     k_latlon<<<grid, 256, 0, c->stream>>>(c->og, src, dst);
     c->kernel_launches++;
     CK(cudaGetLastError());
