@@ -434,14 +434,20 @@ const char *game_gpu_last_error(void) { return last_error(); }
 
 int game_gpu_host_alloc(void **ptr, size_t bytes)
 {
-    cudaError_t e = cudaMallocHost(ptr, bytes);
-    if (e != cudaSuccess) return fail(std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocPortable | cudaHostAllocMapped);
+    if (e != cudaSuccess) return fail(std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
     memset(*ptr, 0, bytes);
+    /* States inside this allocation are copied by kernels that access it
+     * directly; without a device address they take the staged copies */
+    void *dev = nullptr;
+    if (cudaHostGetDevicePointer(&dev, *ptr, 0) == cudaSuccess && dev) pinned_register(*ptr, dev, bytes);
+    else cudaGetLastError();
     return 0;
 }
 
 int game_gpu_host_free(void *ptr)
 {
+    pinned_unregister(ptr);
     cudaError_t e = cudaFreeHost(ptr);
     if (e != cudaSuccess) return fail(std::string("cudaFreeHost: ") + cudaGetErrorString(e));
     return 0;

@@ -50,6 +50,56 @@ __global__ void k_scatter(double *dst, const double *src, const int *map, long l
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dst[map[i]] = src[i];
 }
+
+/* State copies straight between the caller's pinned host struct and the
+ * device mirror, without the staging array: host positions [lo, lo + n) are
+ * read (upload) or written (download) in order, so the NVLink-C2C traffic is
+ * sequential; the device side is addressed through the reference -> device
+ * map of the state block. */
+__global__ void k_state_from_host(double *dev, const double *host, const int *imap, long long lo, long long n)
+{
+    const long long j = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < lo + n) dev[imap[j]] = host[j];
+}
+__global__ void k_state_to_host(double *host, const double *dev, const int *imap, long long lo, long long n)
+{
+    const long long j = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < lo + n) host[j] = dev[imap[j]];
+}
+
+/* ------------------------------------------------- pinned host allocations
+ * Allocations made through game_gpu_host_alloc, with the device address of
+ * each: a State that lies entirely inside one of them is copied by the
+ * kernels above. */
+namespace {
+struct PinnedAlloc {
+    const char *host;
+    char *dev;
+    size_t bytes;
+};
+std::vector<PinnedAlloc> g_pinned;
+}  // namespace
+
+void pinned_register(void *host, void *dev, size_t bytes) { g_pinned.push_back({(const char *)host, (char *)dev, bytes}); }
+
+void pinned_unregister(void *host)
+{
+    for (size_t i = 0; i < g_pinned.size(); ++i)
+        if (g_pinned[i].host == host) {
+            g_pinned.erase(g_pinned.begin() + (long)i);
+            return;
+        }
+}
+
+/* the device address of [host, host + bytes) if that range lies inside one
+ * registered pinned allocation, else null */
+static char *pinned_device_range(const void *host, size_t bytes)
+{
+    const char *h = (const char *)host;
+    for (const PinnedAlloc &a : g_pinned)
+        if (h >= a.host && h + bytes <= a.host + a.bytes) return a.dev + (h - a.host);
+    return nullptr;
+}
 void launch_gather(double *dst, const double *src, const int *map, long long n, cudaStream_t s)
 {
     if (n <= 0) return;
@@ -501,6 +551,11 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     c->map_curl = dupload(c, m_curl);
     c->map_tri = dupload(c, m_tri);
     c->map_state = dupload(c, m_state);
+    {
+        std::vector<int> inv(m_state.size());
+        for (size_t q = 0; q < m_state.size(); ++q) inv[(size_t)m_state[q]] = (int)q;
+        c->imap_state = dupload(c, inv);
+    }
     c->staging_len = (size_t)std::max<long long>(std::max<long long>(c->state_len, c->ncurl), 8 * NS);
     c->staging = dalloc<double>(c, c->staging_len);
     for (int k = 0; k < 4; ++k) c->dev_tmp[k] = dalloc<double>(c, (size_t)std::max<long long>(NV, c->ncurl));
@@ -692,6 +747,14 @@ int upload_state(const void *host_state, StateMirror *m)
 {
     Context *c = g_ctx;
     const double *h = (const double *)((const char *)host_state + c->off_state_rho);
+    if (const char *hd = pinned_device_range(h, (size_t)c->state_len * sizeof(double))) {
+        k_state_from_host<<<(unsigned)((c->state_len + 255) / 256), 256, 0, c->stream>>>(
+            m->dev, (const double *)hd, c->imap_state, 0, c->state_len);
+        c->kernel_launches++;
+        c->h2d_bytes += (long long)c->state_len * (long long)sizeof(double);
+        CK(cudaGetLastError());
+        return 0;
+    }
     CK(cudaMemcpyAsync(c->staging, h, (size_t)c->state_len * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     c->h2d_bytes += (long long)c->state_len * (long long)sizeof(double);
     launch_gather(m->dev, c->staging, c->map_state, c->state_len, c->stream);
@@ -702,13 +765,24 @@ int upload_state(const void *host_state, StateMirror *m)
 int download_state(const void *host_state, StateMirror *m, int which_mask)
 {
     Context *c = g_ctx;
-    launch_scatter(c->staging, m->dev, c->map_state, c->state_len, c->stream);
     double *h = (double *)((char *)host_state + c->off_state_rho);
     const long long ns = c->ns;
     const long long soil0 = (c->n_const + 3) * ns + c->nv;
     struct Part { int bit; long long lo, n; } parts[6] = {
         {1, 0, c->n_const * ns}, {2, c->n_const * ns, ns}, {4, (c->n_const + 1) * ns, ns},
         {8, (c->n_const + 2) * ns, ns}, {16, (c->n_const + 3) * ns, c->nv}, {32, soil0, c->state_len - soil0}};
+    if (char *hd = pinned_device_range(h, (size_t)c->state_len * sizeof(double))) {
+        for (auto &p : parts)
+            if ((which_mask & p.bit) && p.n > 0) {
+                k_state_to_host<<<(unsigned)((p.n + 255) / 256), 256, 0, c->stream>>>((double *)hd, m->dev,
+                                                                                     c->imap_state, p.lo, p.n);
+                c->kernel_launches++;
+                c->d2h_bytes += p.n * (long long)sizeof(double);
+            }
+        CK(cudaGetLastError());
+        return 0;
+    }
+    launch_scatter(c->staging, m->dev, c->map_state, c->state_len, c->stream);
     if (which_mask == 63) {
         CK(cudaMemcpyAsync(h, c->staging, (size_t)c->state_len * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         c->d2h_bytes += (long long)c->state_len * (long long)sizeof(double);

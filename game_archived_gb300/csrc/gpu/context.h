@@ -72,6 +72,7 @@ struct Context {
 
     /* index maps device position -> reference position */
     int *map_state = nullptr;   /* state block, length state_len */
+    int *imap_state = nullptr;  /* its inverse: reference position -> device position */
     int *map_s = nullptr;       /* scalar field, length S */
     int *map_vec = nullptr;     /* vector field: [w (L+1)*Nc][u L*Ne], length Vt */
     int *map_curl = nullptr;    /* curl field: [zh (L+1)*Ne][zv L*Ne], length NCURL */
@@ -214,6 +215,11 @@ int destroy_context();
 StateMirror *mirror(const void *host_state, int create);
 int ensure_sub_buffers(Context *c);
 int ensure_diff_buffers(Context *c);
+/* the library's own pinned host allocations (game_gpu_host_alloc) and
+ * their device addresses: States inside them are copied by kernels that read
+ * and write host memory directly over NVLink-C2C */
+void pinned_register(void *host, void *dev, size_t bytes);
+void pinned_unregister(void *host);
 int upload_state(const void *host_state, StateMirror *m);
 int download_state(const void *host_state, StateMirror *m, int which_mask);
 int upload_field(const double *host, double *dev, const int *map, long long n, long long host_len);
