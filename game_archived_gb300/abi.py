@@ -83,6 +83,9 @@ SIGNATURES = {
     "edges_to_cells": ([vp] * 3, cint),
     "game_gpu_write_out_fields": ([vp, vp, cint, vp, vp, vp, vp, vp, vp], cint),
     "game_gpu_record_wind_lowest": ([vp, cint], cint),
+    "write_out": ([vp, vp, cint, dbl, dbl, vp, vp, vp, vp, vp, vp, vp], cint),
+    "write_out_integral": ([vp, dbl, vp, vp, vp, cint], cint),
+    "interpolation_t": ([vp, vp, vp, dbl, dbl, dbl, vp], cint),
 }
 
 # struct game_gpu_output_fields (include/game_gb300.h), in declaration order,

@@ -40,7 +40,8 @@ def _run(cmd):
 
 
 def tables_sources():
-    return [os.path.join(CSRC, "tables", "gridgen.c"), os.path.join(CSRC, "common", "layout.c")]
+    return [os.path.join(CSRC, "tables", "gridgen.c"), os.path.join(CSRC, "common", "layout.c"),
+            os.path.join(CSRC, "common", "ncwrite.c")]
 
 
 def build_tables(force=False):
@@ -76,7 +77,7 @@ def build_gpu(force=False, jobs=None):
     srcs = gpu_sources()
     hdrs = glob.glob(os.path.join(CSRC, "gpu", "*.h")) + glob.glob(os.path.join(CSRC, "gpu", "*.cuh")) \
         + glob.glob(os.path.join(CSRC, "common", "*.h")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
-    common_c = [os.path.join(CSRC, "common", "layout.c")]
+    common_c = [os.path.join(CSRC, "common", "layout.c"), os.path.join(CSRC, "common", "ncwrite.c")]
     if not force and not _newer(GPU_LIB, srcs + hdrs + common_c):
         return GPU_LIB
     os.makedirs(BUILD, exist_ok=True)

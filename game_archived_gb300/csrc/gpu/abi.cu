@@ -1,6 +1,7 @@
 /*
  * extern "C" entry points of include/game_gb300.h.
  */
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -15,6 +16,7 @@
 #include "adj.h"
 #include "adj_ops.h"
 #include "output.h"
+#include "ncwrite.h"
 
 using namespace game;
 
@@ -1420,6 +1422,142 @@ int game_gpu_record_wind_lowest(struct state *state, int slot)
     if (!m) return -1;
     if (output_record_wind(c, m, slot)) return -1;
     return finish();
+}
+
+/* ------------------------------------------------ write_out, write_out_integral
+ * The reference's output entry points (src/io/io.h:10-11): the fields on the
+ * GPU, the files on the host.  Config_io (src/game_types.h:240-258) has no
+ * size that depends on the grid, so its layout is fixed. */
+struct ConfigIoLayout {
+    int grib_output_switch, netcdf_output_switch, pressure_level_output_switch, model_level_output_switch,
+        surface_output_switch, write_out_interval, write_out_integrals, year, month, day, hour;
+    char run_id[100], month_string[3], day_string[3], hour_string[3];
+    int ideal_input_id;
+};
+
+int write_out(struct state *state_write_out, double wind_h_lowest_layer_array[], int min_no_of_output_steps,
+              double t_init, double t_write, struct diagnostics *diagnostics, struct forcings *forcings,
+              struct grid *grid, struct dualgrid *dualgrid, struct config_io *config_io, struct config *config,
+              struct irreversible_quantities *irrev)
+{
+    if (check_ready(grid)) return -1;
+    if (dualgrid != g_bound.dualgrid) return fail("dualgrid pointer differs from the one given to game_gpu_init");
+    const ConfigIoLayout *io = (const ConfigIoLayout *)config_io;
+    if (io->grib_output_switch == 1)
+        return fail("write_out: GRIB output is not available in this library (set grib_output_switch = 0; the "
+                    "lat-lon fields the GRIB path writes come from game_gpu_write_out_fields)");
+    Context *c = ctx();
+    const long long nc = c->nc, ns = c->ns, nv = c->nv;
+    const int t_rel = (int)(t_write - t_init);
+    const bool netcdf = io->netcdf_output_switch == 1;
+    const bool surface = netcdf && io->surface_output_switch == 1;
+    const bool plevels = netcdf && io->pressure_level_output_switch == 1;
+    const bool model = (io->model_level_output_switch == 1 && netcdf)
+                       || (io->ideal_input_id == -1 && t_rel == *member<int>(config, GAME_CONFIG, "time_to_next_analysis"));
+    /* the fields, reference order */
+    std::vector<double> sf(11 * nc), ml(6 * ns), pl(7 * 6 * nc);
+    game_gpu_output_fields nat{};
+    double *sp[11];
+    for (int k = 0; k < 11; ++k) sp[k] = sf.data() + k * nc;
+    nat.mslp = sp[0]; nat.surface_p = sp[1]; nat.t2 = sp[2]; nat.tcdc = sp[3]; nat.rprate = sp[4];
+    nat.sprate = sp[5]; nat.cape = sp[6]; nat.sfc_sw_down = sp[7]; nat.u10 = sp[8]; nat.v10 = sp[9];
+    nat.gusts = sp[10];
+    nat.temperature = ml.data(); nat.rh = ml.data() + ns; nat.rel_vort = ml.data() + 2 * ns;
+    nat.divv_h = ml.data() + 3 * ns; nat.u = ml.data() + 4 * ns; nat.v = ml.data() + 5 * ns;
+    std::vector<double> epv(ns), pressure(ns);
+    nat.epv = epv.data(); nat.pressure = pressure.data();
+    double *pp[7];
+    for (int k = 0; k < 7; ++k) pp[k] = pl.data() + k * 6 * nc;
+    nat.geopotential_height = pp[0]; nat.t_pl = pp[1]; nat.rh_pl = pp[2]; nat.epv_pl = pp[3]; nat.u_pl = pp[4];
+    nat.v_pl = pp[5]; nat.rel_vort_pl = pp[6];
+    if (game_gpu_write_out_fields(state_write_out, wind_h_lowest_layer_array, min_no_of_output_steps, diagnostics,
+                                  forcings, grid, config, &nat, nullptr))
+        return -1;
+    static const double levels[6] = {20000, 30000, 50000, 70000, 85000, 92500};
+    ncw_output o{};
+    o.n_cells = nc; o.n_scalars = ns; o.n_vectors = nv; o.n_densities = (long long)c->n_const * ns;
+    o.n_h_vectors = (long long)c->nl * c->ne; o.n_v_vectors = (long long)(c->nl + 1) * nc; o.n_curl = c->ncurl;
+    o.n_soil = (long long)c->dims.n_soil * nc;
+    o.mslp = nat.mslp; o.surface_p = nat.surface_p; o.t2 = nat.t2; o.tcdc = nat.tcdc; o.rprate = nat.rprate;
+    o.sprate = nat.sprate; o.cape = nat.cape; o.sfc_sw_down = nat.sfc_sw_down; o.u10 = nat.u10; o.v10 = nat.v10;
+    o.gusts = nat.gusts; o.pressure_levels = levels;
+    o.geopotential_height = nat.geopotential_height; o.t_pl = nat.t_pl; o.rh_pl = nat.rh_pl; o.epv_pl = nat.epv_pl;
+    o.u_pl = nat.u_pl; o.v_pl = nat.v_pl; o.rel_vort_pl = nat.rel_vort_pl;
+    o.temperature = nat.temperature; o.rh = nat.rh; o.rel_vort = nat.rel_vort; o.divv_h = nat.divv_h;
+    /* the prognostic state, the soil temperature and the TKE as they are at
+     * this point: the device copies where the library holds them */
+    std::vector<double> state_copy, tke_copy;
+    const double *rho = member<double>(state_write_out, GAME_STATE, "rho");
+    const double *wind = member<double>(state_write_out, GAME_STATE, "wind");
+    const double *t_soil = member<double>(state_write_out, GAME_STATE, "temperature_soil");
+    const double *tke = member<double>(irrev, GAME_IRREV, "tke");
+    if (model && c->resident) {
+        StateMirror *m = mirror(state_write_out, 0);
+        if (!m) return fail("resident mode: this State has no device mirror (game_gpu_sync_to_device it first)");
+        /* a host image of the State block, filled from the mirror */
+        state_copy.resize((size_t)c->state_len);
+        const size_t off = c->off_state_rho;
+        std::vector<char> img(off + state_copy.size() * sizeof(double));
+        if (download_state(img.data(), m, 1 | 16 | 32) || finish()) return -1;
+        std::memcpy(state_copy.data(), img.data() + off, state_copy.size() * sizeof(double));
+        rho = state_copy.data();
+        wind = state_copy.data() + (c->n_const + 3) * ns;
+        t_soil = state_copy.data() + (c->n_const + 3) * ns + nv;
+    }
+    if (model && g_bound.diff_imported && c->dbuf) {
+        tke_copy.resize((size_t)ns);
+        if (download_field(tke_copy.data(), c->dbuf->tke, c->map_s, ns, ns, 0, ns) || finish()) return -1;
+        tke = tke_copy.data();
+    }
+    o.densities = rho; o.wind = wind; o.t_soil = t_soil; o.tke = tke;
+    char path[320];
+    if (surface) {
+        snprintf(path, sizeof path, "%s+%ds_surface.nc", io->run_id, t_rel);
+        if (ncw_write_surface(path, &o)) return fail(std::string("write_out: ") + ncw_last_error());
+    }
+    if (plevels) {
+        snprintf(path, sizeof path, "%s+%ds_pressure_levels.nc", io->run_id, t_rel);
+        if (ncw_write_pressure_levels(path, &o)) return fail(std::string("write_out: ") + ncw_last_error());
+    }
+    if (model) {
+        snprintf(path, sizeof path, "%s+%ds.nc", io->run_id, t_rel);
+        if (ncw_write_model_levels(path, &o)) return fail(std::string("write_out: ") + ncw_last_error());
+    }
+    return 0;
+}
+
+int write_out_integral(struct state *state_write_out, double time_since_init, struct grid *grid,
+                       struct dualgrid *dualgrid, struct diagnostics *diagnostics, int integral_id)
+{
+    (void)diagnostics;
+    if (check_ready(grid)) return -1;
+    if (dualgrid != g_bound.dualgrid) return fail("dualgrid pointer differs from the one given to game_gpu_init");
+    double r[INTEGRAL_MAX_FIELDS];
+    if (game_gpu_write_out_integral(state_write_out, integral_id, r)) return -1;
+    static const char *names[3] = {"masses", "potential_temperature_density", "energy"};
+    FILE *f = std::fopen(names[integral_id], "a");
+    if (!f) return fail(std::string("write_out_integral: cannot open ") + names[integral_id]);
+    /* write_output.c:1539-1592: "%lf" fields, tab-separated */
+    if (integral_id == 0) {
+        std::fprintf(f, "%lf\t", time_since_init);
+        for (int k = 0; k < ctx()->n_const; ++k) std::fprintf(f, k == ctx()->n_const - 1 ? "%lf\n" : "%lf\t", r[k]);
+    } else if (integral_id == 1) {
+        std::fprintf(f, "%lf\t%lf\n", time_since_init, r[0]);
+    } else {
+        std::fprintf(f, "%lf\t%lf\t%lf\t%lf\n", time_since_init, r[0], r[1], r[2]);
+    }
+    std::fclose(f);
+    return 0;
+}
+
+/* io.h:12 -> write_output.c:1670-1677: the State at t_write by linear
+ * interpolation in time between state_0 at t_0 and state_p1 at t_p1 */
+int interpolation_t(struct state *state_0, struct state *state_p1, struct state *state_write, double t_0,
+                    double t_p1, double t_write, struct grid *grid)
+{
+    const double weight_p1 = (t_write - t_0) / (t_p1 - t_0);
+    const double weight_0 = 1.0 - weight_p1;
+    return linear_combine_two_states(state_0, state_p1, state_write, weight_0, weight_p1, grid);
 }
 
 }  // extern "C"

@@ -104,3 +104,13 @@ class Model:
 
     def pointers(self):
         return {k: getattr(self, k).ptr for k in self.KINDS}
+
+
+class ConfigIo(ctypes.Structure):
+    """the reference's Config_io (src/game_types.h:240-258): output switches
+    and the run id of write_out; its layout does not depend on the grid"""
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "grib_output_switch", "netcdf_output_switch", "pressure_level_output_switch", "model_level_output_switch",
+        "surface_output_switch", "write_out_interval", "write_out_integrals", "year", "month", "day", "hour")] + [
+        ("run_id", ctypes.c_char * 100), ("month_string", ctypes.c_char * 3), ("day_string", ctypes.c_char * 3),
+        ("hour_string", ctypes.c_char * 3), ("ideal_input_id", ctypes.c_int)]

@@ -44,6 +44,7 @@ struct diagnostics;
 struct forcings;
 struct irreversible_quantities;
 struct config;
+struct config_io;
 
 /* ------------------------------------------------------------------------
  * 1. library control (no counterpart in the reference)
@@ -377,6 +378,28 @@ int game_gpu_write_out_fields(struct state *state_write_out, double wind_h_lowes
                               int min_no_of_output_steps, struct diagnostics *diagnostics,
                               struct forcings *forcings, struct grid *grid, struct config *config,
                               struct game_gpu_output_fields *native, struct game_gpu_output_fields *latlon);
+
+/* src/io/io.h:10 -> src/io/write_output.c:51: the fields computed on the GPU
+ * (as game_gpu_write_out_fields does) and the reference's netCDF files
+ * written in the working directory: <run_id>+<t>s_surface.nc,
+ * <run_id>+<t>s_pressure_levels.nc and <run_id>+<t>s.nc, t = (int)(t_write -
+ * t_init), with the reference's dimensions, variables, units and order, under
+ * the reference's switches.  GRIB output (grib_output_switch = 1) is not
+ * available and returns an error.  config_io is the reference's Config_io. */
+int write_out(struct state *state_write_out, double wind_h_lowest_layer_array[], int min_no_of_output_steps,
+              double t_init, double t_write, struct diagnostics *diagnostics, struct forcings *forcings,
+              struct grid *grid, struct dualgrid *dualgrid, struct config_io *config_io, struct config *config,
+              struct irreversible_quantities *irrev);
+/* io.h:12 -> write_output.c:1670: linear_combine_two_states with the
+ * weights of t_write between t_0 and t_p1 */
+int interpolation_t(struct state *state_0, struct state *state_p1, struct state *state_write, double t_0,
+                    double t_p1, double t_write, struct grid *grid);
+/* io.h:11 -> write_output.c:1515: the integral of integral_id (as
+ * game_gpu_write_out_integral computes it) appended to the reference's text
+ * file in the working directory ("masses", "potential_temperature_density"
+ * or "energy") in its format */
+int write_out_integral(struct state *state_write_out, double time_since_init, struct grid *grid,
+                       struct dualgrid *dualgrid, struct diagnostics *diagnostics, int integral_id);
 
 /* Copies the lowest layer's horizontal wind of state (its device mirror in
  * resident mode, else the host struct) into device slot `slot`

@@ -51,7 +51,7 @@ GRIDGEN_FILES = ["interpolate_ll.c"]
 IO_FILES = ["write_output.c", "spatial_ops_for_output.c"]
 # bumped whenever the set of compiled sources changes, so that stale
 # libraries are not reused
-BUILD_VERSION = 3
+BUILD_VERSION = 5
 
 GEOS95_H = """/* declarations of the geos95 functions the model uses; their definitions
    come from grid_generator/src/geodesy.c and index_helpers.c */

@@ -92,3 +92,16 @@ void ref_dims(long out[8])
 #include <omp.h>
 void ref_set_num_threads(int n) { omp_set_num_threads(n); }
 int ref_get_max_threads(void) { return omp_get_max_threads(); }
+
+/* offsets of the members of the reference's Config_io */
+#define CONFIG_IO_MEMBERS(X) X(grib_output_switch) X(netcdf_output_switch) X(pressure_level_output_switch) \
+    X(model_level_output_switch) X(surface_output_switch) X(write_out_interval) X(write_out_integrals) X(year) \
+    X(month) X(day) X(hour) X(run_id) X(month_string) X(day_string) X(hour_string) X(ideal_input_id)
+long ref_config_io_offsetof(const char *name)
+{
+#define CIO(m) if (strcmp(name, #m) == 0) return (long)offsetof(Config_io, m);
+    CONFIG_IO_MEMBERS(CIO)
+#undef CIO
+    return -1;
+}
+long ref_config_io_sizeof(void) { return (long)sizeof(Config_io); }

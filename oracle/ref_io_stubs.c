@@ -73,6 +73,52 @@ int ref_io_record(int k, const char **file, const char **name, long *meta, long 
     return 0;
 }
 
+/* ------------------------------------------------- netCDF file structure
+ * Every dimension and variable definition, in call order: kind 'D' with the
+ * dimension's length, or 'V' with its dimensions' names joined by commas and
+ * the "units" attribute given to it. */
+typedef struct {
+    char file[320];
+    char kind;
+    char name[64];
+    char dims[256];
+    char units[64];
+    long long len;
+} nc_def_record;
+
+static nc_def_record *g_def;
+static int g_n_def, g_cap_def;
+
+static nc_def_record *new_def(void)
+{
+    if (g_n_def == g_cap_def) {
+        int cap = g_cap_def ? 2 * g_cap_def : 64;
+        nc_def_record *grown = realloc(g_def, (size_t)cap * sizeof(nc_def_record));
+        if (!grown) abort();
+        g_def = grown;
+        g_cap_def = cap;
+    }
+    nc_def_record *r = &g_def[g_n_def++];
+    memset(r, 0, sizeof *r);
+    return r;
+}
+
+int ref_nc_def_count(void) { return g_n_def; }
+void ref_nc_def_reset(void) { g_n_def = 0; }
+
+int ref_nc_def_get(int k, const char **file, char *kind, const char **name, const char **dims, const char **units,
+                   long long *len)
+{
+    if (k < 0 || k >= g_n_def) return 1;
+    *file = g_def[k].file;
+    *kind = g_def[k].kind;
+    *name = g_def[k].name;
+    *dims = g_def[k].dims;
+    *units = g_def[k].units;
+    *len = g_def[k].len;
+    return 0;
+}
+
 /* ------------------------------------------------------------------ netCDF */
 #define NC_MAX_FILES 8
 #define NC_MAX_DIMS 32
@@ -83,6 +129,8 @@ static struct {
     char path[320];
     int n_dims, n_vars;
     size_t dim_len[NC_MAX_DIMS];
+    char dim_name[NC_MAX_DIMS][64];
+    int var_def[NC_MAX_VARS]; /* index of the variable's definition record */
     char var_name[NC_MAX_VARS][64];
     long var_len[NC_MAX_VARS];
 } g_nc[NC_MAX_FILES];
@@ -103,9 +151,14 @@ int nc_create(const char *path, int cmode, int *ncidp)
 
 int nc_def_dim(int ncid, const char *name, size_t len, int *idp)
 {
-    (void)name;
     if (ncid < 0 || ncid >= NC_MAX_FILES || g_nc[ncid].n_dims == NC_MAX_DIMS) return 1;
     g_nc[ncid].dim_len[g_nc[ncid].n_dims] = len;
+    strncpy(g_nc[ncid].dim_name[g_nc[ncid].n_dims], name, 63);
+    nc_def_record *r = new_def();
+    strncpy(r->file, g_nc[ncid].path, sizeof r->file - 1);
+    r->kind = 'D';
+    strncpy(r->name, name, sizeof r->name - 1);
+    r->len = (long long)len;
     *idp = g_nc[ncid].n_dims++;
     return 0;
 }
@@ -117,7 +170,17 @@ int nc_def_var(int ncid, const char *name, nc_type xtype, int ndims, const int *
     int v = g_nc[ncid].n_vars++;
     strncpy(g_nc[ncid].var_name[v], name, 63);
     long len = 1;
-    for (int d = 0; d < ndims; ++d) len *= (long)g_nc[ncid].dim_len[dimidsp[d]];
+    nc_def_record *r = new_def();
+    strncpy(r->file, g_nc[ncid].path, sizeof r->file - 1);
+    r->kind = 'V';
+    strncpy(r->name, name, sizeof r->name - 1);
+    for (int d = 0; d < ndims; ++d) {
+        len *= (long)g_nc[ncid].dim_len[dimidsp[d]];
+        if (d) strncat(r->dims, ",", sizeof r->dims - strlen(r->dims) - 1);
+        strncat(r->dims, g_nc[ncid].dim_name[dimidsp[d]], sizeof r->dims - strlen(r->dims) - 1);
+    }
+    r->len = len;
+    g_nc[ncid].var_def[v] = g_n_def - 1;
     g_nc[ncid].var_len[v] = len;
     *varidp = v;
     return 0;
@@ -125,7 +188,13 @@ int nc_def_var(int ncid, const char *name, nc_type xtype, int ndims, const int *
 
 int nc_put_att_text(int ncid, int varid, const char *name, size_t len, const char *op)
 {
-    (void)ncid; (void)varid; (void)name; (void)len; (void)op;
+    if (ncid < 0 || ncid >= NC_MAX_FILES || varid < 0 || varid >= g_nc[ncid].n_vars) return 1;
+    if (!strcmp(name, "units")) {
+        nc_def_record *r = &g_def[g_nc[ncid].var_def[varid]];
+        const size_t n = len < sizeof r->units - 1 ? len : sizeof r->units - 1;
+        memcpy(r->units, op, n);
+        r->units[n] = 0;
+    }
     return 0;
 }
 

@@ -40,13 +40,7 @@ class Reference:
         self.lib.linear_combine_two_states(s0.ptr, s1.ptr, out.ptr, c0, c1, self.m.grid.ptr)
 
 
-class ConfigIo(ctypes.Structure):
-    """the reference's Config_io (src/game_types.h:240-258)"""
-    _fields_ = [(n, ctypes.c_int) for n in (
-        "grib_output_switch", "netcdf_output_switch", "pressure_level_output_switch", "model_level_output_switch",
-        "surface_output_switch", "write_out_interval", "write_out_integrals", "year", "month", "day", "hour")] + [
-        ("run_id", ctypes.c_char * 100), ("month_string", ctypes.c_char * 3), ("day_string", ctypes.c_char * 3),
-        ("hour_string", ctypes.c_char * 3), ("ideal_input_id", ctypes.c_int)]
+from game_archived_gb300.structs import ConfigIo  # noqa: E402
 
 
 def write_out(ref, state, wind_lowest, n_wind_steps, workdir, t_init=0.0, t_write=3600.0):
@@ -73,6 +67,7 @@ def write_out(ref, state, wind_lowest, n_wind_steps, workdir, t_init=0.0, t_writ
     import numpy as np
     wl = np.ascontiguousarray(wind_lowest, dtype=np.float64)
     lib.ref_io_reset()
+    lib.ref_nc_def_reset()
     cwd = os.getcwd()
     os.chdir(run_dir)
     # one thread: the reference's gust loop shares a work array between
@@ -109,6 +104,22 @@ def write_out(ref, state, wind_lowest, n_wind_steps, workdir, t_init=0.0, t_writ
         else:
             out["grib_model_levels"].append(arr)
     lib.ref_io_reset()
+    # the netCDF file structure: (file kind, 'D' or 'V', name, dimension
+    # names, units, length) in definition order
+    lib.ref_nc_def_get.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_char),
+                                   ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_char_p),
+                                   ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_longlong)]
+    kind, dims, units, ln = ctypes.c_char(), ctypes.c_char_p(), ctypes.c_char_p(), ctypes.c_longlong()
+    out["defs"] = []
+    for k in range(lib.ref_nc_def_count()):
+        lib.ref_nc_def_get(k, ctypes.byref(f), ctypes.byref(kind), ctypes.byref(nm), ctypes.byref(dims),
+                           ctypes.byref(units), ctypes.byref(ln))
+        fname = f.value.decode()
+        fk = "surface" if fname.endswith("_surface.nc") else \
+            "pressure_levels" if fname.endswith("_pressure_levels.nc") else "model_levels"
+        out["defs"].append((fk, kind.value.decode(), nm.value.decode(), dims.value.decode(), units.value.decode(),
+                            ln.value))
+    lib.ref_nc_def_reset()
     return out
 
 

@@ -38,3 +38,20 @@ def test_layout_matches_reference_compiler(res, moist):
         assert lay.sizes[kind] == lib.ref_sizeof(sid), kind
         for name, (_, _, off) in lay.members[kind].items():
             assert lib.ref_offsetof(sid, name.encode()) == off, (kind, name)
+
+
+def test_config_io_layout_matches_reference():
+    """structs.ConfigIo against the reference compiler's offsetof/sizeof"""
+    import ctypes
+    from oracle import build_ref
+    from game_archived_gb300.structs import ConfigIo
+    if not build_ref.available():
+        import pytest
+        pytest.skip("reference sources not present")
+    lib = ctypes.CDLL(build_ref.build(3, 0))
+    lib.ref_config_io_offsetof.restype = ctypes.c_long
+    lib.ref_config_io_offsetof.argtypes = [ctypes.c_char_p]
+    lib.ref_config_io_sizeof.restype = ctypes.c_long
+    for name, _ in ConfigIo._fields_:
+        assert getattr(ConfigIo, name).offset == lib.ref_config_io_offsetof(name.encode()), name
+    assert ctypes.sizeof(ConfigIo) == lib.ref_config_io_sizeof()
