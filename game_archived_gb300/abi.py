@@ -59,6 +59,9 @@ SIGNATURES = {
     "scalar_times_vector_h_upstream": ([vp] * 4, cint),
     "scalar_times_vector_v": ([vp] * 4, cint),
     "inner_product": ([vp] * 4, cint),
+    "scalar_times_scalar": ([vp] * 3, cint),
+    "vector_times_vector": ([vp] * 3, cint),
+    "add_vertical_divv": ([vp] * 3, cint),
     "global_scalar_integrator": ([vp, vp], dbl),
     "game_gpu_write_out_integral": ([vp, cint, vp], cint),
     "game_gpu_surface_pressure": ([vp, vp, vp], cint),

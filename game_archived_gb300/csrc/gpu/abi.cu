@@ -590,6 +590,44 @@ int linear_combine_two_states(struct state *state_0, struct state *state_1, stru
 }
 
 /* --------------------------------------------------------- single operators */
+/* pointwise product of two host fields of n values (no layout change) */
+static int pointwise_product(const double *a, const double *b, double *out, long long n)
+{
+    Context *c = ctx();
+    double *da = c->dev_tmp[0], *db = c->dev_tmp[1], *dout = c->dev_tmp[2];
+    CK(cudaMemcpyAsync(da, a, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(db, b, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    c->h2d_bytes += 2 * n * (long long)sizeof(double);
+    op_mul(c, n, da, db, dout);
+    CK(cudaMemcpyAsync(out, dout, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    c->d2h_bytes += n * (long long)sizeof(double);
+    return finish();
+}
+
+int scalar_times_scalar(double *in_field_0, double *in_field_1, double *out_field)
+{
+    if (check_ready(nullptr)) return -1;
+    return pointwise_product(in_field_0, in_field_1, out_field, ctx()->ns);
+}
+
+int vector_times_vector(double *in_field_0, double *in_field_1, double *out_field)
+{
+    if (check_ready(nullptr)) return -1;
+    return pointwise_product(in_field_0, in_field_1, out_field, ctx()->nv);
+}
+
+int add_vertical_divv(double *in_field, double *out_field, struct grid *grid)
+{
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    double *v = c->dev_tmp[1], *o = c->dev_tmp[0];
+    if (upload_field(in_field, v, c->map_vec, c->nv, c->nv)) return -1;
+    if (upload_field(out_field, o, c->map_s, c->ns, c->ns)) return -1;
+    op_add_vertical_divv(c, v, o);
+    if (download_field(out_field, o, c->map_s, c->ns, c->ns, 0, c->ns)) return -1;
+    return finish();
+}
+
 static int vec_op_prologue(double *out_field, double *dev_out)
 {
     /* the output keeps the entries the operator does not write */

@@ -16,6 +16,8 @@ void op_inner_product(Context *c, const double *a, const double *b, double *out)
 void op_rel_vort(Context *c, const double *wind, double *tri, double *curl);
 void op_pot_vort(Context *c, const double *rel, const double *rho, double *pv);
 void op_vorticity_flux(Context *c, const double *flux, const double *pv, double *out);
+void op_mul(Context *c, long long n, const double *a, const double *b, double *out);
+void op_add_vertical_divv(Context *c, const double *vec, double *out);
 void op_linear_combine(Context *c, StateMirror *a, StateMirror *b, StateMirror *o, double c0, double c1);
 
 int launch_step_f64(Context *c, const StepParams &p, StateMirror *so, StateMirror *sn, StateMirror *st);

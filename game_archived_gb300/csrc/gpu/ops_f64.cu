@@ -239,9 +239,44 @@ __global__ void k_op_lincomb_theta(VGrid vg, int n_cond, DState o)
     if (i < ns) o.theta_v_pert[i] = o.rhotheta_v[i] / o.rho[n_cond * ns + i] - vg.theta_v_bg[i];
 }
 
+/* scalar_times_scalar, vector_times_vector (multiplications.c:15-33):
+ * pointwise products, in any element order */
+__global__ void k_op_mul(long long n, const double *a, const double *b, double *out)
+{
+    const long long i = gtid();
+    if (i < n) out[i] = a[i] * b[i];
+}
+
+/* add_vertical_divv (divergences.c:150-185): out += 1 / V * the divergence of
+ * the vertical part w [L+1][Nc] of a vector field, zero flux at the top and
+ * bottom of the column */
+__global__ void k_op_add_vertical_divv(G g, const double *w, double *out)
+{
+    const long long ns = (long long)g.nl * g.nc, i = gtid();
+    if (i >= ns) return;
+    const int l = (int)(i / g.nc), c = (int)(i - (long long)l * g.nc);
+    const long long up = (long long)l * g.nc + c, lo = (long long)(l + 1) * g.nc + c;
+    const double contra_upper = l == 0 ? 0.0 : w[up];
+    const double contra_lower = l == g.nl - 1 ? 0.0 : w[lo];
+    const double comp_v = contra_upper * g.area_v[up] - contra_lower * g.area_v[lo];
+    out[i] += 1 / g.volume[i] * comp_v;
+}
+
 }  // namespace
 
 static unsigned nb(long long n) { return (unsigned)((n + 255) / 256); }
+
+void op_mul(Context *c, long long n, const double *a, const double *b, double *out)
+{
+    k_op_mul<<<nb(n), 256, 0, c->stream>>>(n, a, b, out);
+    c->kernel_launches++;
+}
+
+void op_add_vertical_divv(Context *c, const double *vec, double *out)
+{
+    k_op_add_vertical_divv<<<nb(c->ns), 256, 0, c->stream>>>(c->hg64, vec, out);
+    c->kernel_launches++;
+}
 
 void op_grad(Context *c, const double *f, double *vec, int parts)
 {

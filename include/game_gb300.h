@@ -171,6 +171,19 @@ int scalar_times_vector_h_upstream(double *in_field_h, double *vector_field, dou
 int scalar_times_vector_v(double *in_field_v, double *vector_field, double *out_field, struct grid *grid);
 /* spatial_operators.h:25 -> inner_product.c:13 */
 int inner_product(double *in_field_0, double *in_field_1, double *out_field, struct grid *grid);
+/* spatial_operators.h:19,24 -> multiplications.c:15,25: pointwise products of
+ * two Scalar_fields / Vector_fields */
+int scalar_times_scalar(double *in_field_0, double *in_field_1, double *out_field);
+int vector_times_vector(double *in_field_0, double *in_field_1, double *out_field);
+/* spatial_operators.h:18 -> divergences.c:150: adds the divergence of the
+ * vertical part of in_field to out_field */
+int add_vertical_divv(double *in_field, double *out_field, struct grid *grid);
+/* Not exported: the per-point helpers tangential_wind,
+ * vertical_contravariant_corr, remap_verpri2horpri_vector and
+ * horizontal_covariant (spatial_operators.h:27-31), which only the operators
+ * this library replaces call, and the diffusion sub-steps
+ * hor_momentum_diffusion, vert_momentum_diffusion and simple_dissipation_rate
+ * (:34-36), which run inside manage_rkhevi. */
 
 /* ---- 3. integrals and surface pressure (the model's monitoring output) ---- */
 

@@ -102,3 +102,22 @@ def test_linear_combine(setup):
     Oracle(m2).linear_combine_two_states(m2.state_old, m2.state_new, m2.state_tendency, 0.3, 0.7)
     for f in ("rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind"):
         assert rel_err(m.state_tendency[f], m2.state_tendency[f]) <= TOL, f
+
+
+def test_pointwise_products_and_vertical_divergence(setup):
+    """scalar_times_scalar and vector_times_vector give numpy's products bit
+    for bit; add_vertical_divv adds to its output as the oracle does"""
+    import ctypes
+    m, g, o = setup
+    rho, wind, scal = _fields(m)
+    out = np.zeros(m.layout.n_scalars)
+    assert g.lib.scalar_times_scalar(abi._p(rho), abi._p(scal), abi._p(out)) == 0
+    assert np.array_equal(out, rho * scal)
+    outv = np.zeros(m.layout.n_vectors)
+    assert g.lib.vector_times_vector(abi._p(wind), abi._p(wind), abi._p(outv)) == 0
+    assert np.array_equal(outv, wind * wind)
+    a, b = scal.copy(), scal.copy()
+    assert g.lib.add_vertical_divv(abi._p(wind), abi._p(a), m.grid.ptr) == 0
+    o.lib.orc_add_vertical_divv(ctypes.byref(o.g), wind.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                b.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rel_err(a, b) <= TOL
