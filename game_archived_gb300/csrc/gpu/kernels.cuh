@@ -521,7 +521,7 @@ __global__ void k_make_shadow(long long n_rho, long long ns, long long nw, long 
 /* ------------------------------------------------------- k_tri_vort
  * vertical relative vorticity on triangles (vorticities.c:167-222) */
 template <typename R>
-__global__ void k_tri_vort(HGrid<R> g, const R *u, R *tri_vort)
+__global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_tri_vort(HGrid<R> g, const R *u, R *tri_vort)
 {
     const long long n = (long long)g.nl * g.nt;
     const long long i = gtid();
@@ -574,7 +574,7 @@ __device__ __forceinline__ R rel_vort_tangential(const HGrid<R> &g, const R *u, 
  * potential vorticity (vorticities.c:18-85) and the horizontal mass flux
  * density (multiplications.c:45-66), one thread per (edge, level 0..L) */
 template <typename R>
-__global__ void k_edge_vort(HGrid<R> g, const R *u, const R *w, const R *rho_gas, const R *tri_vort, R *zh, R *zv,
+__global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_edge_vort(HGrid<R> g, const R *u, const R *w, const R *rho_gas, const R *tri_vort, R *zh, R *zv,
                             R *flux_h)
 {
     const long long n = (long long)(g.nl + 1) * g.ne;
@@ -760,7 +760,7 @@ __device__ __forceinline__ R pgrad_v(const HGrid<R> &g, const StepParams &p, con
  * recomputed in this substage; PG: the pressure gradient is recomputed.
  * The wind update is FP64; u_shadow (mixed path) receives its FP32 copy. */
 template <typename R, bool ADV, bool PG>
-__global__ void k_momentum_h(HGrid<R> g, StepParams p, SView<R> sv, double *u_new, float *u_shadow, const double *u_old,
+__global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_momentum_h(HGrid<R> g, StepParams p, SView<R> sv, double *u_new, float *u_shadow, const double *u_old,
                              double *tend_u, R *P_h, R *pg_old_h, R *pvt_h, R *v2g_h, const R *flux_h,
                              const R *flux_v, const R *zh, const R *zv, const R *v2, double new_w, double old_w,
                              const double *fric_u)
@@ -807,7 +807,7 @@ __global__ void k_momentum_h(HGrid<R> g, StepParams p, SView<R> sv, double *u_ne
  * vertical momentum at interface k of cell c: tendency including the
  * condensate term (manage_pressure_gradient.c:74-87) */
 template <typename R, bool ADV, bool PG>
-__global__ void k_momentum_v(HGrid<R> g, StepParams p, SView<R> sv, double *tend_w, R *P_v, R *pvt_v, R *v2g_v,
+__global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_momentum_v(HGrid<R> g, StepParams p, SView<R> sv, double *tend_w, R *P_v, R *pvt_v, R *v2g_v,
                              const R *flux_h, const R *zh, const R *v2, double new_w, double old_w,
                              const double *fric_w)
 {
