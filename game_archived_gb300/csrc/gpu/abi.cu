@@ -567,8 +567,14 @@ int manage_rkhevi(struct state *state_old, struct state *state_new, struct grid 
     }
     if (run_device_step(c, p, so, sn, st)) return -1;
     if (!c->resident) {
+        /* a pinned tendency is copied out on the second stream as soon as the
+         * step has finished it, while the vertical solves still run */
+        CK(cudaStreamWaitEvent(c->stream2, c->ev_tend, 0));
+        const int tend_async = download_state_pinned(state_tendency, st, 1 | 2 | 16, c->stream2);
+        if (tend_async) CK(cudaEventRecord(c->ev_tend_copied, c->stream2));
         if (download_state(state_new, sn, 1 | 2 | 4 | 8 | 16)) return -1;
-        if (download_state(state_tendency, st, 1 | 2 | 16)) return -1;
+        if (tend_async) CK(cudaStreamWaitEvent(c->stream, c->ev_tend_copied, 0));
+        else if (download_state(state_tendency, st, 1 | 2 | 16)) return -1;
     }
     return finish();
 }

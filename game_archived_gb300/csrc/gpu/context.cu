@@ -620,6 +620,8 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_tend, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_tend_copied, cudaEventDisableTiming));
     CK(cudaDeviceSynchronize());
     CK(cudaGetLastError());
     return 0;
@@ -662,6 +664,8 @@ int destroy_context()
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_tend) cudaEventDestroy(c->ev_tend);
+    if (c->ev_tend_copied) cudaEventDestroy(c->ev_tend_copied);
     delete c;
     g_ctx = nullptr;
     return 0;
@@ -762,6 +766,27 @@ int upload_state(const void *host_state, StateMirror *m)
 }
 
 /* which_mask bits: 1 rho, 2 rhotheta_v, 4 theta_v_pert, 8 exner_pert, 16 wind, 32 temperature_soil */
+int download_state_pinned(const void *host_state, StateMirror *m, int which_mask, cudaStream_t s)
+{
+    Context *c = g_ctx;
+    double *h = (double *)((char *)host_state + c->off_state_rho);
+    char *hd = pinned_device_range(h, (size_t)c->state_len * sizeof(double));
+    if (!hd) return 0;
+    const long long ns = c->ns;
+    const long long soil0 = (c->n_const + 3) * ns + c->nv;
+    struct Part { int bit; long long lo, n; } parts[6] = {
+        {1, 0, c->n_const * ns}, {2, c->n_const * ns, ns}, {4, (c->n_const + 1) * ns, ns},
+        {8, (c->n_const + 2) * ns, ns}, {16, (c->n_const + 3) * ns, c->nv}, {32, soil0, c->state_len - soil0}};
+    for (auto &p : parts)
+        if ((which_mask & p.bit) && p.n > 0) {
+            k_state_to_host<<<(unsigned)((p.n + 255) / 256), 256, 0, s>>>((double *)hd, m->dev, c->imap_state, p.lo,
+                                                                       p.n);
+            c->kernel_launches++;
+            c->d2h_bytes += p.n * (long long)sizeof(double);
+        }
+    return 1;
+}
+
 int download_state(const void *host_state, StateMirror *m, int which_mask)
 {
     Context *c = g_ctx;
@@ -771,17 +796,7 @@ int download_state(const void *host_state, StateMirror *m, int which_mask)
     struct Part { int bit; long long lo, n; } parts[6] = {
         {1, 0, c->n_const * ns}, {2, c->n_const * ns, ns}, {4, (c->n_const + 1) * ns, ns},
         {8, (c->n_const + 2) * ns, ns}, {16, (c->n_const + 3) * ns, c->nv}, {32, soil0, c->state_len - soil0}};
-    if (char *hd = pinned_device_range(h, (size_t)c->state_len * sizeof(double))) {
-        for (auto &p : parts)
-            if ((which_mask & p.bit) && p.n > 0) {
-                k_state_to_host<<<(unsigned)((p.n + 255) / 256), 256, 0, c->stream>>>((double *)hd, m->dev,
-                                                                                     c->imap_state, p.lo, p.n);
-                c->kernel_launches++;
-                c->d2h_bytes += p.n * (long long)sizeof(double);
-            }
-        CK(cudaGetLastError());
-        return 0;
-    }
+    if (download_state_pinned(host_state, m, which_mask, c->stream)) return 0;
     launch_scatter(c->staging, m->dev, c->map_state, c->state_len, c->stream);
     if (which_mask == 63) {
         CK(cudaMemcpyAsync(h, c->staging, (size_t)c->state_len * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -56,6 +56,9 @@ struct Context {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;                   /* second branch of the step */
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr; /* fork / join of the branches */
+    /* recorded by the step once the tendency is final (after substage 1's
+     * scalar tendencies), and after its copy to a pinned host State */
+    cudaEvent_t ev_tend = nullptr, ev_tend_copied = nullptr;
 
     /* host struct offsets (bytes) */
     size_t off_grid_z_vector = 0;
@@ -222,6 +225,9 @@ void pinned_register(void *host, void *dev, size_t bytes);
 void pinned_unregister(void *host);
 int upload_state(const void *host_state, StateMirror *m);
 int download_state(const void *host_state, StateMirror *m, int which_mask);
+/* download_state on stream s for a State inside a pinned allocation of the
+ * library (no staging array involved); 0 when the State is not in one */
+int download_state_pinned(const void *host_state, StateMirror *m, int which_mask, cudaStream_t s);
 int upload_field(const double *host, double *dev, const int *map, long long n, long long host_len);
 int download_field(double *host, const double *dev, const int *map, long long n, long long host_len,
                    long long host_lo, long long host_hi);

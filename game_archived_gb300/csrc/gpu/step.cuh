@@ -309,6 +309,18 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             }
         }
         c->kernel_launches += 2;
+        /* the tendency is final from here on: a host-in/host-out call copies
+         * it out while the solvers run */
+        if (rk == 1) {
+            /* inside a graph capture: an external event node, which streams
+             * outside the graph can wait on */
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            cudaStreamIsCapturing(c->stream, &cs);
+            if (cs == cudaStreamCaptureStatusActive)
+                cudaEventRecordWithFlags(c->ev_tend, c->stream, cudaEventRecordExternal);
+            else
+                cudaEventRecord(c->ev_tend, c->stream);
+        }
         launch_waves<EXACT>(c, p, so, sn, st, rk, v.sh);
         if (rk == 0 && fork) {
             cudaEventRecord(c->ev_fork, c->stream);
