@@ -212,7 +212,15 @@ def measured_peak():
 
 
 # ------------------------------------------------------------------ GPU arm
-def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, profile=False, column_solver=0):
+def device_used_bytes(device):
+    """bytes in use on the device (cudaMemGetInfo: total - free)"""
+    import torch
+    free, total = torch.cuda.mem_get_info(device)
+    return total - free
+
+
+def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, profile=False, column_solver=0,
+                  mem_used=None):
     from game_archived_gb300 import abi, driver
     m = copy_model(model0, pinned=False)
     g = abi.GpuModel(m, precision, resident=True, graphs=True, device=device, column_solver=column_solver)
@@ -246,6 +254,8 @@ def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, pr
             g.profile(False)
             prof = g.profile_results()
         g.sync_to_host(m.state_new)
+        if mem_used is not None:
+            mem_used.append(device_used_bytes(device))
         import numpy as np
         finite = bool(np.isfinite(m.state_new["rho"]).all() and np.isfinite(m.state_new["wind"]).all())
         return ms / steps, launches, clocks, prof, finite
@@ -337,6 +347,69 @@ def time_adjoint(res, n_lloyd, n_steps, dt, device, repeats=3):
             "objective": J,
             "note": "backward recomputes each step from its checkpoint (both RK stage states kept) and runs the "
                     "hand-written adjoint kernels; window times include the host-in/host-out copy of one State"}
+
+
+def time_large_run(res, n_lloyd, steps, dt, device, window=24):
+    """The large configuration: RES_ID=7 (163842 cells, 491520 edges), 26
+    layers, the 2 km Gaussian mountain, moist build with its five non-main
+    constituents advected as seeded log-normal (sigma 0.5) x exp(-z / 3 km)
+    fields, dt = 50 s, `steps` mixed-precision steps (1728 = 24 h),
+    device-resident with CUDA graphs.  The adjoint window runs on the dry
+    build of the same grid (the adjoint covers the dry step): `window` steps
+    of dt with both RK stage states checkpointed, FP64.  Device memory is read
+    with cudaMemGetInfo after each part, less what was in use before the
+    library's first allocation."""
+    from game_archived_gb300 import abi, cases, structs, tables
+    from game_archived_gb300.ops import CAbiOps
+    import numpy as np
+    base = device_used_bytes(device)
+    tab, m = build_model(res, 1, n_lloyd, pinned=False, mountain=MOUNTAIN)
+    g = abi.GpuModel(m, abi.FP64, device=device)
+    try:
+        cases.build_initial_state(m, tab, "tracers", CAbiOps(g.lib, m))
+    finally:
+        g.close()
+    lay = m.layout
+    mem = []
+    t0 = time.perf_counter()
+    ms, launches, _, _, finite = time_resident(m, abi.MIXED, steps, 3, dt, device, mem_used=mem)
+    wall = time.perf_counter() - t0
+    fwd = {"steps": steps, "dt_s": dt, "steps_per_s": 1000.0 / ms, "ms_per_step": ms,
+           "simulated_hours": steps * dt / 3600.0, "wall_s_incl_setup": wall,
+           "device_bytes_in_use": int(mem[0] - base), "gpu_launches": int(launches), "finite": finite,
+           "state_struct_bytes": int(lay.sizes["state"])}
+    # adjoint window on the dry build of the same grid
+    lay_d = structs.Layout(res, L, 0)
+    md = structs.Model(lay_d)
+    tables.fill_grid(tab, md.grid, md.dualgrid)
+    cases.default_config(md)
+    g = abi.GpuModel(md, abi.FP64, device=device)
+    try:
+        cases.build_initial_state(md, tab, "std_wind_tpert", CAbiOps(g.lib, md))
+        md.config["totally_first_step_bool"][0] = 1
+        out, bar, grad = (structs.HostStruct(lay_d, "state") for _ in range(3))
+        w = cap_weights(md)
+        g.event_record(0)
+        g.window_forward(md.state_old, out, dt, window)
+        g.event_record(1)
+        J = g.sfc_pressure_objective(out, w, bar)
+        g.event_record(2)
+        g.window_backward(bar, grad)
+        g.event_record(3)
+        g.synchronize()
+        used = device_used_bytes(device) - base
+        tf, tb = g.event_elapsed_ms(0, 1), g.event_elapsed_ms(2, 3)
+        ok = bool(np.isfinite(grad["rho"]).all() and np.isfinite(grad["wind"]).all())
+    finally:
+        g.close()
+    adj = {"build": "dry (the adjoint covers the dry step)", "window_steps": window, "dt_s": dt,
+           "window_forward_ms_per_step": tf / window, "window_backward_ms_per_step": tb / window,
+           "steps_per_s_backward": 1000.0 * window / tb, "device_bytes_in_use": int(used),
+           "objective": J, "finite": ok}
+    return {"config": f"RES_ID={res} ({grid_sizes(res)['nc']} cells, {grid_sizes(res)['ne']} edges), 26 layers, "
+                      f"2 km Gaussian mountain, moist build, 5 advected constituents log-normal(0.5) x exp(-z/3 km), "
+                      f"mixed precision, dt={dt:g} s",
+            "forward": fwd, "adjoint": adj}
 
 
 DIFF_SWITCHES = ("momentum_diff_h", "momentum_diff_v", "temperature_diff_h", "temperature_diff_v", "mass_diff_h",
@@ -585,6 +658,8 @@ def run_ours(args):
         line["output"] = time_output(model0, local)
     if not args.no_adjoint:
         line["adjoint"] = time_adjoint(args.adjoint_res, args.n_lloyd, 12, 200.0, local)
+    if not args.no_large:
+        line["large_run"] = time_large_run(7, args.n_lloyd, args.large_steps, 50.0, local)
     if world == 1 and not args.no_cpu_baseline:
         sec, n = cpu_baseline(model0, dt)
         line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
@@ -689,6 +764,8 @@ def main():
     ap.add_argument("--no-diffusion", action="store_true")
     ap.add_argument("--no-output", action="store_true")
     ap.add_argument("--adjoint-res", type=int, default=5)
+    ap.add_argument("--no-large", action="store_true", help="skip the RES_ID=7 run with five constituents")
+    ap.add_argument("--large-steps", type=int, default=1728)
     ap.add_argument("--column-study", action="store_true",
                     help="time the column solvers at 26, 64 and 128 layers instead of the headline line")
     args = ap.parse_args()

@@ -68,6 +68,8 @@ SIGNATURES = {
     "game_gpu_weighted_sums_noalloc": ([vp, cint, ctypes.c_longlong, vp, vp, vp], cint),
     "grad_adj": ([vp] * 3, cint),
     "divv_h_adj": ([vp] * 3, cint),
+    "divv_h_tracer_adj": ([vp] * 8, cint),
+    "three_band_solver_gen_densities_adj": ([vp] * 6 + [dbl, cint] + [vp] * 6, cint),
     "scalar_times_vector_adj": ([vp] * 6, cint),
     "inner_product_adj": ([vp] * 6, cint),
     "calc_pot_vort_adj": ([vp] * 7, cint),
@@ -273,6 +275,10 @@ class GpuModel:
     def divv_h_adj(self, out_bar, in_bar):
         self._check(self.lib.divv_h_adj(_p(out_bar), _p(in_bar), self.m.grid.ptr), "divv_h_adj")
 
+    def divv_h_tracer_adj(self, v, dens, wind, out_bar, v_bar, dens_bar, wind_bar):
+        self._check(self.lib.divv_h_tracer_adj(_p(v), _p(dens), _p(wind), _p(out_bar), _p(v_bar), _p(dens_bar),
+                                               _p(wind_bar), self.m.grid.ptr), "divv_h_tracer_adj")
+
     def scalar_times_vector_adj(self, s, v, out_bar, s_bar, v_bar):
         self._check(self.lib.scalar_times_vector_adj(_p(s), _p(v), _p(out_bar), _p(s_bar), _p(v_bar),
                                                      self.m.grid.ptr), "scalar_times_vector_adj")
@@ -297,6 +303,15 @@ class GpuModel:
                                                              m.forcings.ptr, m.config.ptr, dt, m.grid.ptr, rk,
                                                              so_bar.ptr, sn_bar.ptr, st_bar.ptr),
                     "three_band_solver_ver_waves_adj")
+
+    def three_band_solver_gen_densities_adj(self, s_old, s_new, tend, dt, rk, so_bar, sn_bar, st_bar, diag_bar,
+                                            irrev_bar):
+        m = self.m
+        self._check(self.lib.three_band_solver_gen_densities_adj(s_old.ptr, s_new.ptr, tend.ptr, m.diagnostics.ptr,
+                                                                 m.irrev.ptr, m.config.ptr, dt, rk, m.grid.ptr,
+                                                                 so_bar.ptr, sn_bar.ptr, st_bar.ptr, diag_bar.ptr,
+                                                                 irrev_bar.ptr),
+                    "three_band_solver_gen_densities_adj")
 
     # -- adjoint / tangent-linear windows (dry build)
     def window_forward(self, s_init, s_final, dt, n_steps):

@@ -1323,6 +1323,60 @@ int three_band_solver_ver_waves_adj(struct state *state_old, struct state *state
     return finish();
 }
 
+int divv_h_tracer_adj(double *in_field, double *density_field, double *wind_field, double *out_field_bar,
+                      double *in_field_bar, double *density_field_bar, double *wind_field_bar, struct grid *grid)
+{
+    (void)in_field; /* the operator is linear in it */
+    if (check_ready(grid)) return -1;
+    Context *c = ctx();
+    if (ensure_sub_buffers(c)) return -1;
+    double **v = c->sub.vec;
+    if (up(density_field, v[0], c->map_s, c->ns) || up(wind_field, v[1], c->map_vec, c->nv)
+        || up(out_field_bar, v[2], c->map_s, c->ns) || up(in_field_bar, v[3], c->map_vec, c->nv)
+        || up(density_field_bar, v[4], c->map_s, c->ns) || up(wind_field_bar, v[5], c->map_vec, c->nv))
+        return -1;
+    op_divv_tracer_adj(c, v[0], v[1], v[2], v[3], v[4], v[5]);
+    if (down(in_field_bar, v[3], c->map_vec, c->nv) || down(density_field_bar, v[4], c->map_s, c->ns)
+        || down(wind_field_bar, v[5], c->map_vec, c->nv))
+        return -1;
+    return finish();
+}
+
+int three_band_solver_gen_densities_adj(struct state *state_old, struct state *state_new,
+                                        struct state *state_tendency, struct diagnostics *diagnostics,
+                                        struct irreversible_quantities *irrev, struct config *config, double delta_t,
+                                        int rk_step, struct grid *grid, struct state *state_old_bar,
+                                        struct state *state_new_bar, struct state *state_tendency_bar,
+                                        struct diagnostics *diagnostics_bar,
+                                        struct irreversible_quantities *irrev_bar)
+{
+    (void)irrev;
+    if (check_ready(grid)) return -1;
+    if (check_config(config)) return -1;
+    Context *c = ctx();
+    if (c->n_const <= 1) return finish();
+    if (ensure_sub_buffers(c)) return -1;
+    Context::SubBuffers &b = c->sub;
+    double *t_b = b.vec[0], *sed_b = b.vec[1];
+    if (upload_state(state_old, &b.so) || upload_state(state_new, &b.sn) || upload_state(state_tendency, &b.st))
+        return -1;
+    if (upload_state(state_old_bar, &b.bso) || upload_state(state_new_bar, &b.bsn)
+        || upload_state(state_tendency_bar, &b.bst))
+        return -1;
+    if (up_scal(diagnostics, GAME_DIAGNOSTICS, "temperature", b.temperature)) return -1;
+    if (up_scal(diagnostics_bar, GAME_DIAGNOSTICS, "temperature", t_b)) return -1;
+    if (rk_step == 0 && up_scal(irrev_bar, GAME_IRREV, "condensates_sediment_heat", sed_b)) return -1;
+    StepParams p = params_from_config(c, config, delta_t);
+    if (adj_gen_densities(c, p, &b.so, &b.sn, &b.st, b.temperature, rk_step, sed_b, &b.bso, &b.bsn, &b.bst, t_b))
+        return fail("three_band_solver_gen_densities_adj: more than 256 layers or a launch error");
+    if (download_state(state_old_bar, &b.bso, 1 | 16) || download_state(state_new_bar, &b.bsn, 1 | 16)
+        || download_state(state_tendency_bar, &b.bst, 1))
+        return -1;
+    if (down_scal(diagnostics_bar, GAME_DIAGNOSTICS, "temperature", t_b)) return -1;
+    if (rk_step == 0 && down_scal(irrev_bar, GAME_IRREV, "condensates_sediment_heat", sed_b)) return -1;
+    return finish();
+}
+
 /* ------------------------------------------------------ output diagnostics
  * The operators only output uses (host-in/host-out) and the fields of
  * write_out (output_f64.cu). */

@@ -256,6 +256,12 @@ int game_gpu_surface_pressure(struct state *state, double *surface_p, double *ms
 int grad_adj(double *out_field_bar, double *in_field_bar, struct grid *grid);
 /* divergences.c:14 (divv_h) */
 int divv_h_adj(double *out_field_bar, double *in_field_bar, struct grid *grid);
+/* divergences.c:66 (divv_h_tracer): bars of the flux field (its horizontal
+ * part), of the density and of the wind (its horizontal part, which enters
+ * through the terrain-following correction in the orography layers); the
+ * upstream density pick is held fixed */
+int divv_h_tracer_adj(double *in_field, double *density_field, double *wind_field, double *out_field_bar,
+                      double *in_field_bar, double *density_field_bar, double *wind_field_bar, struct grid *grid);
 /* multiplications.c:35 (scalar_times_vector) */
 int scalar_times_vector_adj(double *scalar_field, double *vector_field, double *out_field_bar,
                             double *scalar_field_bar, double *vector_field_bar, struct grid *grid);
@@ -279,6 +285,24 @@ int three_band_solver_ver_waves_adj(struct state *state_old, struct state *state
                                     struct diagnostics *diagnostics, struct forcings *forcings, struct config *config,
                                     double delta_t, struct grid *grid, int rk_step, struct state *state_old_bar,
                                     struct state *state_new_bar, struct state *state_tendency_bar);
+/* column_solvers.c:385 (three_band_solver_gen_densities, moist build): the
+ * adjoint of the tracers' implicit vertical advection and sedimentation with
+ * its tridiagonal elimination.  state_new_bar holds on entry the bar of the
+ * new tracer densities the forward writes (zero on return: the forward
+ * overwrites them) and accumulates the bar of the new vertical wind;
+ * state_old_bar (tracer densities, vertical wind), state_tendency_bar
+ * (tracer densities) and diagnostics_bar->temperature are accumulated.  At
+ * rk_step 0 irrev_bar->condensates_sediment_heat is read as the bar of the
+ * sedimentation heat the forward writes and zeroed.  Upwind picks and
+ * flux-sign branches are held fixed; clipped (negative) solutions carry no
+ * derivative.  Up to 256 layers. */
+int three_band_solver_gen_densities_adj(struct state *state_old, struct state *state_new,
+                                        struct state *state_tendency, struct diagnostics *diagnostics,
+                                        struct irreversible_quantities *irrev, struct config *config, double delta_t,
+                                        int rk_step, struct grid *grid, struct state *state_old_bar,
+                                        struct state *state_new_bar, struct state *state_tendency_bar,
+                                        struct diagnostics *diagnostics_bar,
+                                        struct irreversible_quantities *irrev_bar);
 
 int rkhevi_window_forward(struct state *state_init, struct state *state_final, struct grid *grid,
                           struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,

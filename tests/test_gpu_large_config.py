@@ -1,0 +1,101 @@
+"""The large configuration on the GPU: RES_ID=7 (163842 cells, 491520 edges),
+26 layers, the 2 km Gaussian mountain, moist build with its five non-main
+constituents seeded as log-normal (sigma 0.5) x exp(-z / 3 km) fields,
+dt = 50 s.
+
+* FP64 against the oracle for two steps, each from the oracle's state:
+  every prognostic field within 1e-12 relative.
+* The mixed path against the FP64 path over 24 steps from the same state.
+  The reference's microphysics switches at the freezing point
+  (src/constituents/phase_trans.c:236-262: below T_0 all rain turns to snow
+  within one step, at or above it all snow to rain), so in a column whose
+  temperature hovers at T_0 a rounding difference of the order of FP32's
+  shifts the conversion by a step and the two runs differ there by a finite
+  amount (about 2e-4 kg/m^3 of snow and its latent heat of fusion), while
+  in the same case at RES_ID=5 two FP64 runs whose states differ by 1e-9
+  did not flip within 24 steps.  So the test
+  bounds the root-mean-square error of every field (relative to the field's
+  largest magnitude) by 2e-3 and the share of points that differ by more
+  than 1e-4 of it by 1e-2, not the pointwise maximum; the maxima are
+  printed.  Measured on GB300: rms 8e-4 (rain) and 6e-4 (snow), at most 3e-5
+  for every other field; share 3.2e-3 (Exner pressure, which carries the
+  sound and gravity waves the flips send out), below 2e-4 elsewhere.  The dry-air
+  mass (the main constituent: no sources, no flux through the surface or the
+  top) is conserved on both paths to 1e-13 relative, and no constituent
+  density goes negative.
+"""
+import numpy as np
+import pytest
+
+from game_archived_gb300 import abi, driver
+from helpers import clone, make_model, state_errors
+from oracle.bind import Oracle
+
+pytestmark = pytest.mark.gpu
+
+RES, DT = 7, 50.0
+
+
+@pytest.fixture(scope="module")
+def model():
+    return make_model(RES, 1, "tracers", True)[1]
+
+
+def test_fp64_matches_oracle_res7(model):
+    m_orc, m_gpu = clone(model), clone(model)
+    orc = Oracle(m_orc)
+    gpu = abi.GpuModel(m_gpu, abi.FP64)
+    try:
+        driver.start(m_orc, orc.linear_combine_two_states)
+        driver.start(m_gpu, gpu.linear_combine_two_states)
+        for n in range(2):
+            driver.step(m_orc, orc.linear_combine_two_states, orc.manage_rkhevi, DT, n * DT)
+            driver.step(m_gpu, gpu.linear_combine_two_states, gpu.manage_rkhevi, DT, n * DT)
+            e = state_errors(m_gpu.state_new, m_orc.state_new, m_gpu.layout)
+            assert max(e.values()) <= 1e-12, f"step {n}: {e}"
+            m_gpu.state_new.copy_from(m_orc.state_new)
+    finally:
+        gpu.close()
+
+
+def _run(m, precision, steps):
+    g = abi.GpuModel(m, precision, resident=True, graphs=True)
+    try:
+        for s in (m.state_old, m.state_new, m.state_tendency):
+            g.sync_to_device(s)
+        driver.run(m, steps, DT, g.linear_combine_two_states, g.manage_rkhevi)
+        g.sync_to_host(m.state_new)
+    finally:
+        g.close()
+
+
+def _rms_and_share(a, b):
+    scale = np.max(np.abs(b))
+    d = np.abs(a - b) / scale
+    return float(np.sqrt(np.mean(d * d))), float(np.mean(d > 1e-4))
+
+
+def test_mixed_vs_fp64_res7_24_steps(model):
+    steps = 24
+    m64, m32 = clone(model), clone(model)
+    _run(m64, abi.FP64, steps)
+    _run(m32, abi.MIXED, steps)
+    lay = model.layout
+    ns = lay.n_scalars
+    print("max error, mixed vs FP64 after 24 steps:", state_errors(m32.state_new, m64.state_new, lay))
+    a, b = m32.state_new, m64.state_new
+    pairs = {f"rho[{k}]": (a["rho"][k * ns:(k + 1) * ns], b["rho"][k * ns:(k + 1) * ns]) for k in range(lay.n_const)}
+    for f in ("rhotheta_v", "theta_v_pert", "exner_pert", "wind"):
+        pairs[f] = (a[f], b[f])
+    stats = {k: _rms_and_share(x, y) for k, (x, y) in pairs.items()}
+    print("rms error, share of points above 1e-4:", stats)
+    for k, (rms, share) in stats.items():
+        assert rms <= 2e-3 and share <= 1e-2, (k, stats)
+    vol = model.grid["volume"][:ns]
+    main = lay.n_cond
+    mass = lambda s: float(np.dot(s["rho"][main * ns:(main + 1) * ns], vol))
+    m0 = mass(model.state_old)
+    for m in (m64, m32):
+        assert abs(mass(m.state_new) - m0) <= 1e-13 * m0
+        assert np.isfinite(m.state_new["rho"]).all() and np.isfinite(m.state_new["wind"]).all()
+        assert m.state_new["rho"].min() >= 0.0

@@ -176,3 +176,92 @@ def test_three_band_solver_ver_waves_adj(model, rk):
     rhs = sum(float(dso[f] @ sob[f] + dsn[f] @ snb[f] + dst[f] @ stb[f]) for f in FIELDS)
     print(f"column solver adjoint, rk {rk}: FD tangent {lhs:.15g}, adjoint {rhs:.15g}")
     _close(lhs, rhs, 1e-6)
+
+
+def test_divv_h_tracer_adj(model, gpu):
+    """bilinear in (density, wind) with the upstream pick held: central
+    differences at a small step are exact up to rounding"""
+    lay = model.layout
+    rng = np.random.default_rng(7)
+    v = rng.standard_normal(lay.n_vectors)
+    dens, wind = model.state_old["rho"][:lay.n_scalars].copy(), model.state_old["wind"].copy()
+    dv, dd, dw = rng.standard_normal(v.size), dens * rng.standard_normal(dens.size), rng.standard_normal(wind.size)
+    h = 1e-6
+    op, om = np.zeros(lay.n_scalars), np.zeros(lay.n_scalars)
+    gpu.divv_h_tracer(v + h * dv, dens + h * dd, wind + h * dw, op)
+    gpu.divv_h_tracer(v - h * dv, dens - h * dd, wind - h * dw, om)
+    tl = (op - om) / (2 * h)
+    yb = rng.standard_normal(lay.n_scalars)
+    vb, db, wb = np.zeros(v.size), np.zeros(dens.size), np.zeros(wind.size)
+    gpu.divv_h_tracer_adj(v, dens, wind, yb, vb, db, wb)
+    _close(tl @ yb, dv @ vb + dd @ db + dw @ wb, 1e-8)
+    # the terrain term alone (flux field unperturbed) is exercised too
+    assert np.abs(db).max() > 0 and np.abs(wb).max() > 0
+
+
+@pytest.fixture(scope="module")
+def moist_model():
+    """RES_ID=3, moist build, seeded tracers, 2 km mountain, after two oracle
+    steps (tendencies, temperature and vertical wind of a running model)"""
+    _, m = make_model(3, 1, "tracers", mountain=True)
+    orc = Oracle(m)
+    driver.start(m, orc.linear_combine_two_states)
+    for n in range(2):
+        driver.step(m, orc.linear_combine_two_states, orc.manage_rkhevi, 300.0, n * 300.0)
+    return m
+
+
+@pytest.mark.parametrize("rk", [0, 1])
+def test_three_band_solver_gen_densities_adj(moist_model, rk):
+    """central differences of the tracer column solver (densities and, at rk
+    0, sedimentation heat) along random directions in the old and new
+    vertical wind, the old densities, the tendencies and the temperature"""
+    m = moist_model
+    lay = m.layout
+    ns, n_const, cond = lay.n_scalars, lay.n_const, lay.n_cond
+    tracer = np.ones(n_const * ns, dtype=bool)
+    tracer[cond * ns:(cond + 1) * ns] = False
+    rng = np.random.default_rng(20 + rk)
+    dt, h = 300.0, 1e-6
+    dso, dsn, dst = (structs.HostStruct(lay, "state") for _ in range(3))
+    dso["rho"][:] = np.where(tracer, m.state_old["rho"] * rng.standard_normal(n_const * ns), 0.0)
+    # scaled by the local density so that no perturbed solution crosses the clip at zero
+    dst["rho"][:] = np.where(tracer, m.state_old["rho"] / dt * rng.standard_normal(n_const * ns), 0.0)
+    for d in (dso, dsn):
+        d["wind"][:(lay.nl + 1) * lay.nc] = 0.1 * rng.standard_normal((lay.nl + 1) * lay.nc)
+    t0 = m.diagnostics["temperature"].copy()
+    dT = rng.standard_normal(t0.size)
+    g = abi.GpuModel(clone(m), abi.FP64)
+    mm = g.m
+    try:
+        outs = []
+        for sgn in (1.0, -1.0):
+            so, sn, st = (structs.HostStruct(lay, "state") for _ in range(3))
+            for s, base, d in ((so, m.state_old, dso), (sn, m.state_new, dsn), (st, m.state_tendency, dst)):
+                for f in FIELDS:
+                    s[f][:] = base[f] + sgn * h * d[f]
+            mm.diagnostics["temperature"][:] = t0 + sgn * h * dT
+            mm.irrev["condensates_sediment_heat"][:] = 0.0
+            g.three_band_solver_gen_densities(so, sn, st, dt, rk)
+            outs.append((sn["rho"].copy(), mm.irrev["condensates_sediment_heat"].copy()))
+        yb = np.where(tracer, rng.standard_normal(n_const * ns) / np.std(m.state_new["rho"][tracer]), 0.0)
+        hb = rng.standard_normal(ns) / (np.std(outs[0][1]) + 1e-30) if rk == 0 else np.zeros(ns)
+        lhs = float((outs[0][0] - outs[1][0]) @ yb) / (2 * h)
+        if rk == 0:
+            lhs += float((outs[0][1] - outs[1][1]) @ hb) / (2 * h)
+        mm.diagnostics["temperature"][:] = t0
+        sob, snb, stb = (structs.HostStruct(lay, "state") for _ in range(3))
+        snb["rho"][:] = yb
+        db, ib = structs.HostStruct(lay, "diagnostics"), structs.HostStruct(lay, "irrev")
+        ib["condensates_sediment_heat"][:] = hb
+        g.three_band_solver_gen_densities_adj(m.state_old, m.state_new, m.state_tendency, dt, rk, sob, snb, stb, db,
+                                              ib)
+    finally:
+        g.close()
+    assert np.all(snb["rho"][tracer] == 0.0)
+    if rk == 0:
+        assert np.all(ib["condensates_sediment_heat"] == 0.0)
+    rhs = sum(float(dso[f] @ sob[f] + dsn[f] @ snb[f] + dst[f] @ stb[f]) for f in FIELDS)
+    rhs += float(dT @ db["temperature"])
+    print(f"tracer solver adjoint, rk {rk}: FD tangent {lhs:.15g}, adjoint {rhs:.15g}")
+    _close(lhs, rhs, 1e-6)
