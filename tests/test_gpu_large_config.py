@@ -20,9 +20,11 @@ dt = 50 s.
   printed.  Measured on GB300: rms 8e-4 (rain) and 6e-4 (snow), at most 3e-5
   for every other field; share 3.2e-3 (Exner pressure, which carries the
   sound and gravity waves the flips send out), below 2e-4 elsewhere.  The dry-air
-  mass (the main constituent: no sources, no flux through the surface or the
-  top) is conserved on both paths to 1e-13 relative, and no constituent
-  density goes negative.
+  mass is conserved on both paths to 1e-13 relative: the main constituent
+  is moist air, which gains the vapour's phase-transition source
+  (src/time_stepping/scalar_tendencies_expl.c:97-132), so the dry air is the
+  main constituent less the vapour, and neither has a flux through the
+  surface or the top.  No constituent density goes negative.
 """
 import numpy as np
 import pytest
@@ -93,7 +95,7 @@ def test_mixed_vs_fp64_res7_24_steps(model):
         assert rms <= 2e-3 and share <= 1e-2, (k, stats)
     vol = model.grid["volume"][:ns]
     main = lay.n_cond
-    mass = lambda s: float(np.dot(s["rho"][main * ns:(main + 1) * ns], vol))
+    mass = lambda s: float(np.dot(s["rho"][main * ns:(main + 1) * ns] - s["rho"][(main + 1) * ns:(main + 2) * ns], vol))
     m0 = mass(model.state_old)
     for m in (m64, m32):
         assert abs(mass(m.state_new) - m0) <= 1e-13 * m0
