@@ -69,6 +69,7 @@ SIGNATURES = {
     "grad_adj": ([vp] * 3, cint),
     "divv_h_adj": ([vp] * 3, cint),
     "divv_h_tracer_adj": ([vp] * 8, cint),
+    "manage_rkhevi_adj": ([vp] * 9 + [dbl, dbl, vp, vp], cint),
     "three_band_solver_gen_densities_adj": ([vp] * 6 + [dbl, cint] + [vp] * 6, cint),
     "scalar_times_vector_adj": ([vp] * 6, cint),
     "inner_product_adj": ([vp] * 6, cint),
@@ -312,6 +313,13 @@ class GpuModel:
                                                                  so_bar.ptr, sn_bar.ptr, st_bar.ptr, diag_bar.ptr,
                                                                  irrev_bar.ptr),
                     "three_band_solver_gen_densities_adj")
+
+    def manage_rkhevi_adj(self, dt, t, s_new_bar, s_old_bar):
+        m = self.m
+        self._check(self.lib.manage_rkhevi_adj(m.state_old.ptr, m.state_new.ptr, m.grid.ptr, m.dualgrid.ptr,
+                                               m.state_tendency.ptr, m.diagnostics.ptr, m.forcings.ptr, m.irrev.ptr,
+                                               m.config.ptr, dt, t, s_new_bar.ptr, s_old_bar.ptr),
+                    "manage_rkhevi_adj")
 
     # -- adjoint / tangent-linear windows (dry build)
     def window_forward(self, s_init, s_final, dt, n_steps):

@@ -1126,16 +1126,16 @@ static int adj_download(struct state *host, StateMirror *m, const double *blk)
     return finish();
 }
 
-int rkhevi_window_forward(struct state *state_init, struct state *state_final, struct grid *grid,
-                          struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,
-                          struct irreversible_quantities *irrev, struct config *config, double delta_t, int n_steps)
+/* the window forward on the device: result in the sub-step mirror sn */
+static int window_forward_dev(const char *who, struct state *state_init, struct grid *grid,
+                              struct diagnostics *diagnostics, struct forcings *forcings, struct config *config,
+                              double delta_t, int n_steps)
 {
-    (void)dualgrid;
-    (void)irrev;
     if (check_ready(grid)) return -1;
     if (check_config(config)) return -1;
     Context *c = ctx();
-    if (c->n_const != 1) return fail("rkhevi_window_forward: the adjoint model covers the dry build (MOISTURE_ON = 0)");
+    if (c->n_const != 1)
+        return fail(std::string(who) + ": the adjoint model covers the dry build (MOISTURE_ON = 0)");
     if (ensure_sub_buffers(c)) return -1;
     Context::SubBuffers &b = c->sub;
     if (upload_state(state_init, &b.so)) return -1;
@@ -1149,8 +1149,39 @@ int rkhevi_window_forward(struct state *state_init, struct state *state_final, s
         if (up_vec(forcings, GAME_FORCINGS, "v_squared_grad", auxG)) return -1;
         adj_add_into(c, auxP, b.vec[4], c->nv); /* the step reads nl + l */
     }
-    if (adj_window_forward(c, &b.so, p, n_steps, auxP, auxV, auxG, fl, &b.sn)) return -1;
-    return adj_download(state_final, &b.sn, b.sn.dev);
+    return adj_window_forward(c, &b.so, p, n_steps, auxP, auxV, auxG, fl, &b.sn);
+}
+
+int rkhevi_window_forward(struct state *state_init, struct state *state_final, struct grid *grid,
+                          struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,
+                          struct irreversible_quantities *irrev, struct config *config, double delta_t, int n_steps)
+{
+    (void)dualgrid;
+    (void)irrev;
+    if (window_forward_dev("rkhevi_window_forward", state_init, grid, diagnostics, forcings, config, delta_t,
+                           n_steps))
+        return -1;
+    Context *c = ctx();
+    return adj_download(state_final, &c->sub.sn, c->sub.sn.dev);
+}
+
+int manage_rkhevi_adj(struct state *state_old, struct state *state_new, struct grid *grid, struct dualgrid *dualgrid,
+                      struct state *state_tendency, struct diagnostics *diagnostics, struct forcings *forcings,
+                      struct irreversible_quantities *irrev, struct config *config, double delta_t,
+                      double time_coordinate, struct state *state_new_bar, struct state *state_old_bar)
+{
+    (void)state_new;
+    (void)dualgrid;
+    (void)state_tendency;
+    (void)irrev;
+    (void)time_coordinate;
+    if (window_forward_dev("manage_rkhevi_adj", state_old, grid, diagnostics, forcings, config, delta_t, 1))
+        return -1;
+    Context *c = ctx();
+    Context::SubBuffers &b = c->sub;
+    if (upload_state(state_new_bar, &b.st)) return -1;
+    if (adj_window_backward(c, b.st.dev, b.sn.dev)) return -1;
+    return adj_download(state_old_bar, &b.sn, b.sn.dev);
 }
 
 int rkhevi_window_tl(struct state *state_init_dot, struct state *state_final_dot)

@@ -304,6 +304,21 @@ int three_band_solver_gen_densities_adj(struct state *state_old, struct state *s
                                         struct diagnostics *diagnostics_bar,
                                         struct irreversible_quantities *irrev_bar);
 
+/* time_stepping.h:6 (manage_rkhevi, dry build): the adjoint of one step,
+ * the reference's arguments followed by the bars.  state_new_bar is the bar
+ * of the state_new the step returns; state_old_bar receives the bar of
+ * state_old (written, not accumulated).  As in the reference's time loop
+ * (src/coordinator.c:305), state_new equals state_old on entry, so the step
+ * is a function of state_old alone; the lagged fields of forcings (the
+ * previous step's pressure gradient, vorticity flux and kinetic-energy
+ * gradient) are constants of the call unless config->totally_first_step_bool
+ * is set.  Equal to a one-step window (rkhevi_window_forward with n_steps =
+ * 1, then rkhevi_window_backward), which it replaces for a caller that
+ * differentiates one step at a time. */
+int manage_rkhevi_adj(struct state *state_old, struct state *state_new, struct grid *grid, struct dualgrid *dualgrid,
+                      struct state *state_tendency, struct diagnostics *diagnostics, struct forcings *forcings,
+                      struct irreversible_quantities *irrev, struct config *config, double delta_t,
+                      double time_coordinate, struct state *state_new_bar, struct state *state_old_bar);
 int rkhevi_window_forward(struct state *state_init, struct state *state_final, struct grid *grid,
                           struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,
                           struct irreversible_quantities *irrev, struct config *config, double delta_t, int n_steps);

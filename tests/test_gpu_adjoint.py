@@ -222,3 +222,39 @@ def test_adjoint_matches_the_torch_cpu_adjoint():
     errs = {f: rel_err(grad[f], ref[f]) for f in ("rho", "rhotheta_v", "exner_pert", "wind")}
     print(f"GPU adjoint vs CPU (torch) adjoint, max |diff| / max |ref| per field: {errs}")
     assert max(errs.values()) <= 1e-9, errs
+
+
+def test_manage_rkhevi_adj_is_the_one_step_window(dry4):
+    """the single-step adjoint equals a one-step window (to 1e-12 of each
+    field's largest bar: the adjoint scatters with atomic additions, whose
+    order varies from run to run) and passes the dot-product test against
+    the one-step tangent-linear model; mid-run, so the lagged fields of
+    forcings are constants of the call"""
+    _, m0 = dry4
+    m = clone(m0)
+    orc = Oracle(m)
+    driver.start(m, orc.linear_combine_two_states)
+    for n in range(2):
+        driver.step(m, orc.linear_combine_two_states, orc.manage_rkhevi, 200.0, n * 200.0)
+    orc.linear_combine_two_states(m.state_new, m.state_old, m.state_old, 1.0, 0.0)
+    orc.linear_combine_two_states(m.state_old, m.state_old, m.state_new, 1.0, 0.0)
+    rng = np.random.default_rng(11)
+    g = abi.GpuModel(m, abi.FP64)
+    try:
+        m.config["totally_first_step_bool"][0] = 0
+        yb = _random_bar(m, rng)
+        xb_step = _state_like(m.layout)
+        g.manage_rkhevi_adj(200.0, 400.0, yb, xb_step)
+        out = _state_like(m.layout)
+        g.window_forward(m.state_old, out, 200.0, 1)
+        dx = _random_dx(m, rng)
+        dy = _state_like(m.layout)
+        g.window_tl(dx, dy)
+        xb_win = _state_like(m.layout)
+        g.window_backward(yb, xb_win)
+    finally:
+        g.close()
+    for f in FIELDS:
+        assert np.max(np.abs(xb_step[f] - xb_win[f])) <= 1e-12 * max(np.max(np.abs(xb_win[f])), 1e-300), f
+    lhs, rhs = _dot(dy, yb), _dot(dx, xb_step)
+    assert abs(lhs - rhs) <= 1e-10 * max(abs(lhs), abs(rhs)), (lhs, rhs)
