@@ -23,6 +23,12 @@ CONFIGS = [
     (4, 0, "std_wind_tpert", True, 200.0, 5),
     (4, 1, "jet_moist", False, 300.0, 5),
     (3, 1, "tracers", True, 300.0, 4),
+    # the benchmark configurations at their own sizes: RES_ID=4 standard
+    # atmosphere with wind noise (400 s, 10 steps), RES_ID=5 with the
+    # mountain and 1 K noise (200 s), RES_ID=6 moist jet (100 s)
+    (4, 0, "std_wind", False, 400.0, 10),
+    (5, 0, "std_wind_tpert", True, 200.0, 3),
+    (6, 1, "jet_moist", False, 100.0, 2),
 ]
 
 
