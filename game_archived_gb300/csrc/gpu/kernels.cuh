@@ -53,6 +53,17 @@ __device__ __forceinline__ double rcp_nr(double x)
     return r;
 }
 
+/* x >= 0 for the solvers' branch and clip tests.  The FP64 path compares as
+ * the reference does; the mixed path reads the sign bit on the integer pipe
+ * instead of issuing an FP64 comparison (FP64 issues at 1/64 of the FP32
+ * rate on this GPU).  The two differ only at -0, where every branch they
+ * select between yields the same values up to the sign of a zero term. */
+template <bool EXACT>
+__device__ __forceinline__ bool nonneg(double x)
+{
+    return EXACT ? x >= 0.0 : __double2hiint(x) >= 0;
+}
+
 template <typename R>
 __device__ __forceinline__ R ipw_at(const HGrid<R> &g, int j, int l, int c)
 {

@@ -398,18 +398,18 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
             const double ar = vg.area_v[wi];
             a_ = ar * a_;
             b_ = ar * b_;
-            const double dio = b_ >= 0.0 ? ro[b + nc] : ro[b];
+            const double dio = nonneg<EXACT>(b_) ? ro[b + nc] : ro[b];
             fi = a_;
             fr = dio * b_;
             if (EXACT) {
                 if (fi >= 0.0) ej = -iw * dt / vol * fi;
                 else cj = iw * dt / vg.volume[b + nc] * fi;
-            } else if (fi >= 0.0) {
+            } else if (nonneg<EXACT>(fi)) {
                 ej = -g * fi;
             }
         }
         if (!EXACT) /* sub-diagonal of row j - 1, formed with row j's factor */
-            c_prev = fi_prev < 0.0 ? g * fi_prev : 0.0;
+            c_prev = nonneg<EXACT>(fi_prev) ? 0.0 : g * fi_prev;
         double dj, rj = ro[b] + dt * tr[b];
         if (EXACT) {
             if (j == 0) {
@@ -428,10 +428,10 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
             }
         } else {
             if (j == 0) {
-                dj = fi >= 0.0 ? 1.0 : 1.0 - g * fi;
+                dj = nonneg<EXACT>(fi) ? 1.0 : 1.0 - g * fi;
                 rj += g * fr;
             } else if (j == nl - 1) {
-                dj = fi_prev >= 0.0 ? 1.0 + g * fi_prev : 1.0;
+                dj = nonneg<EXACT>(fi_prev) ? 1.0 + g * fi_prev : 1.0;
                 rj -= g * fr_prev;
                 if (has_sink) {
                     const double gs = g * vsink * a_sfc;
@@ -439,7 +439,7 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
                     rj -= gs * ro[bot];
                 }
             } else {
-                dj = 1.0 + (fi_prev >= 0.0 ? g * fi_prev : 0.0) - (fi < 0.0 ? g * fi : 0.0);
+                dj = 1.0 + (nonneg<EXACT>(fi_prev) ? g * fi_prev : 0.0) - (nonneg<EXACT>(fi) ? 0.0 : g * fi);
                 rj += g * (fr - fr_prev);
             }
         }
@@ -472,14 +472,14 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
     float *rs = sh_rho ? sh_rho + k * ns : nullptr;
     double x = rp[nl - 1];
     {
-        const double v = x < 0.0 ? 0.0 : x;
+        const double v = EXACT ? (x < 0.0 ? 0.0 : x) : (nonneg<false>(x) ? x : 0.0);
         rn[(long long)(nl - 1) * nc + i] = v;
         if (rs) rs[(long long)(nl - 1) * nc + i] = float(v);
     }
 #pragma unroll
     for (int j = nl - 2; j >= 0; --j) {
         x = rp[j] - ep[j] * x;
-        const double v = x < 0.0 ? 0.0 : x;
+        const double v = EXACT ? (x < 0.0 ? 0.0 : x) : (nonneg<false>(x) ? x : 0.0);
         rn[(long long)j * nc + i] = v;
         if (rs) rs[(long long)j * nc + i] = float(v);
     }
@@ -505,7 +505,7 @@ __global__ void k_tracers_sedheat(VGrid vg, StepParams p, DState so, DState sn, 
         double b_ = sn.w[wi];
         if (has) b_ -= vsink;
         b_ = vg.area_v[wi] * b_;
-        const long long up = b_ >= 0.0 ? bb + nc : bb;
+        const long long up = nonneg<EXACT>(b_) ? bb + nc : bb;
         const double dio = so.rho[k * ns + up], tio = temperature[up];
         const double fr = dio * b_;
         const double cp = (k % 2 == 0) ? tw.cp_ice[up] : tw.cp_water[up];
@@ -671,7 +671,7 @@ __global__ void __launch_bounds__(32 * PCR_WARPS)
                 const double ar = vg.area_v[wi];
                 a_ = ar * wo;
                 const double b_ = ar * wn;
-                f_ = (b_ >= 0.0 ? ro[b + nc] : ro[b]) * b_;
+                f_ = (nonneg<EXACT>(b_) ? ro[b + nc] : ro[b]) * b_;
             }
             fi[j] = a_;
             fr[j] = f_;
@@ -705,13 +705,13 @@ __global__ void __launch_bounds__(32 * PCR_WARPS)
                 }
             } else {
                 const double g = half_dt * tw.inv_vol[b];
-                if (j > 0 && fip < 0.0) aj = g * fip;
-                if (j < nl - 1 && fij >= 0.0) cj = -g * fij;
+                if (j > 0 && !nonneg<false>(fip)) aj = g * fip;
+                if (j < nl - 1 && nonneg<false>(fij)) cj = -g * fij;
                 if (j == 0) {
-                    dj = fij >= 0.0 ? 1.0 : 1.0 - g * fij;
+                    dj = nonneg<false>(fij) ? 1.0 : 1.0 - g * fij;
                     rj += g * frj;
                 } else if (j == nl - 1) {
-                    dj = fip >= 0.0 ? 1.0 + g * fip : 1.0;
+                    dj = nonneg<false>(fip) ? 1.0 + g * fip : 1.0;
                     rj -= g * frp;
                     if (has_sink) {
                         const double gs = g * vsink * a_sfc;
@@ -719,7 +719,7 @@ __global__ void __launch_bounds__(32 * PCR_WARPS)
                         rj -= gs * ro[bot];
                     }
                 } else {
-                    dj = 1.0 + (fip >= 0.0 ? g * fip : 0.0) - (fij < 0.0 ? g * fij : 0.0);
+                    dj = 1.0 + (nonneg<false>(fip) ? g * fip : 0.0) - (nonneg<false>(fij) ? 0.0 : g * fij);
                     rj += g * (frj - frp);
                 }
             }
@@ -737,7 +737,7 @@ __global__ void __launch_bounds__(32 * PCR_WARPS)
         double *rn = sn.rho + k * ns;
         float *rs = sh_rho ? sh_rho + k * ns : nullptr;
         for (int j = row0; j < n; j += 32) {
-            const double v = x[j] < 0.0 ? 0.0 : x[j];
+            const double v = EXACT ? (x[j] < 0.0 ? 0.0 : x[j]) : (nonneg<false>(x[j]) ? x[j] : 0.0);
             rn[i + (long long)j * nc] = v;
             if (rs) rs[i + (long long)j * nc] = float(v);
         }
