@@ -64,6 +64,26 @@ __device__ __forceinline__ bool nonneg(double x)
     return EXACT ? x >= 0.0 : __double2hiint(x) >= 0;
 }
 
+/* double -> float rounded to nearest even, by integer operations for values
+ * whose float is a normal number (or overflows to infinity by rounding);
+ * zeros, subnormals, infinities and NaNs go through the conversion
+ * instruction.  The same bits as float(x); used by the mixed path where it
+ * writes its FP32 shadow from FP64 results, to keep the conversion off the
+ * FP64 pipe. */
+__device__ __forceinline__ float to_float(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    if (e - 897u <= 253u) { /* float exponent field e - 896 in [1, 254] */
+        const unsigned long long m = b & 0xfffffffffffffULL;
+        unsigned r = ((unsigned)(b >> 63) << 31) | ((e - 896u) << 23) | (unsigned)(m >> 29);
+        const unsigned rem = (unsigned)(m & 0x1fffffffULL), half = 0x10000000u;
+        r += (rem > half || (rem == half && (r & 1u))) ? 1u : 0u;
+        return __uint_as_float(r);
+    }
+    return __double2float_rn(x);
+}
+
 template <typename R>
 __device__ __forceinline__ R ipw_at(const HGrid<R> &g, int j, int l, int c)
 {

@@ -319,10 +319,10 @@ __global__ void k_waves_apply(VGrid vg, StepParams p, DState so, DState sn, Wave
     sn.theta_v_pert[b] = tp_new;
     sn.exner_pert[b] = ep_new;
     if (sh.rho) {
-        sh.rho[gp + b] = float(r_new);
-        sh.rhotheta_v[b] = float(rt_new);
-        sh.theta_v_pert[b] = float(tp_new);
-        sh.exner_pert[b] = float(ep_new);
+        sh.rho[gp + b] = to_float(r_new);
+        sh.rhotheta_v[b] = to_float(rt_new);
+        sh.theta_v_pert[b] = to_float(tp_new);
+        sh.exner_pert[b] = to_float(ep_new);
     }
     if (j < nl - 1) {
         const long long wi = b + nc;
@@ -334,7 +334,7 @@ __global__ void k_waves_apply(VGrid vg, StepParams p, DState so, DState sn, Wave
         else /* rho_io holds 1 / rho at the interface on the mixed path */
             wn = (2.0 * sol[b] * ww.inv_area_v[wi] - dint * so.w[wi]) * ww.rho_io[b];
         sn.w[wi] = wn;
-        if (sh.w) sh.w[wi] = float(wn);
+        if (sh.w) sh.w[wi] = to_float(wn);
     }
 }
 
@@ -474,14 +474,14 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
     {
         const double v = EXACT ? (x < 0.0 ? 0.0 : x) : (nonneg<false>(x) ? x : 0.0);
         rn[(long long)(nl - 1) * nc + i] = v;
-        if (rs) rs[(long long)(nl - 1) * nc + i] = float(v);
+        if (rs) rs[(long long)(nl - 1) * nc + i] = to_float(v);
     }
 #pragma unroll
     for (int j = nl - 2; j >= 0; --j) {
         x = rp[j] - ep[j] * x;
         const double v = EXACT ? (x < 0.0 ? 0.0 : x) : (nonneg<false>(x) ? x : 0.0);
         rn[(long long)j * nc + i] = v;
-        if (rs) rs[(long long)j * nc + i] = float(v);
+        if (rs) rs[(long long)j * nc + i] = to_float(v);
     }
 }
 
@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(32 * PCR_WARPS)
         for (int j = row0; j < n; j += 32) {
             const double v = EXACT ? (x[j] < 0.0 ? 0.0 : x[j]) : (nonneg<false>(x[j]) ? x[j] : 0.0);
             rn[i + (long long)j * nc] = v;
-            if (rs) rs[i + (long long)j * nc] = float(v);
+            if (rs) rs[i + (long long)j * nc] = to_float(v);
         }
     }
 }
