@@ -84,6 +84,24 @@ __device__ __forceinline__ float to_float(double x)
     return __double2float_rn(x);
 }
 
+/* float -> double (exact) by integer operations for normal numbers and
+ * zeros; subnormals, infinities and NaNs through the conversion instruction.
+ * The same bits as double(x); the mixed path widens its FP32 sums and
+ * products with it before the FP64 accumulation, keeping the conversion off
+ * the FP64 pipe.  wide() is the identity on double. */
+__device__ __forceinline__ double to_double(float x)
+{
+    const unsigned u = __float_as_uint(x);
+    const unsigned fe = (u >> 23) & 0xffu;
+    if (fe - 1u <= 253u) /* normal */
+        return __hiloint2double((int)((u & 0x80000000u) | ((fe + 896u) << 20) | ((u >> 3) & 0xfffffu)),
+                                (int)(u << 29));
+    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)x;
+}
+__device__ __forceinline__ double wide(float x) { return to_double(x); }
+__device__ __forceinline__ double wide(double x) { return x; }
+
 template <typename R>
 __device__ __forceinline__ R ipw_at(const HGrid<R> &g, int j, int l, int c)
 {
@@ -827,11 +845,11 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_mom
     if (fric_u) y = y + R(fric_u[i]);
     /* the pressure gradient is recomputed in substage 0 only, where the new
      * weight is 1 */
-    double t = PG ? double(y) : old_w * tend_u[i] + new_w * double(y);
+    double t = PG ? wide(y) : old_w * tend_u[i] + new_w * wide(y);
     tend_u[i] = t;
     const double un = u_old[i] + p.dt * t;
     u_new[i] = un;
-    if (u_shadow) u_shadow[i] = float(un);
+    if (u_shadow) u_shadow[i] = to_float(un);
 }
 
 /* ------------------------------------------------------- k_momentum_v
@@ -892,7 +910,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_mom
     R y = -cur_ver * P + pvt - R(0.5) * v2g;
     if (fric_w) y = y + R(fric_w[i]);
     y = y + pgc;
-    double t = PG ? double(y) : old_w * tend_w[i] + new_w * double(y);
+    double t = PG ? wide(y) : old_w * tend_w[i] + new_w * wide(y);
     tend_w[i] = t;
 }
 
@@ -951,7 +969,7 @@ struct FluxSum<float> {
         hi = t;
         lo += err;
     }
-    __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
+    __device__ __forceinline__ double value() const { return to_double(hi) + to_double(lo); }
 };
 
 /* Explicit mass and rho*theta_v tendencies (scalar_tendencies_expl.c:90-178)
@@ -998,9 +1016,9 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
     auto uval = [&](int ll, int j) { return sv.u[(long long)ll * ne + edge(j)]; };
     auto comp_v = [&](R up, R lo) -> double {
         if (!oro) return 0.0;
-        if (l == nl - n_oro - 1) return double(-lo * area_lo);
-        if (l == nl - 1) return double(up * area_up);
-        return double(up * area_up - lo * area_lo);
+        if (l == nl - n_oro - 1) return wide(-lo * area_lo);
+        if (l == nl - 1) return wide(up * area_up);
+        return wide(up * area_up - lo * area_lo);
     };
     /* terrain correction of the wind at levels l and l+1 (shared by the tracers) */
     R w_up = R(0), w_lo = R(0);
@@ -1075,7 +1093,7 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
                      + rate * double(theta[i]);
             } else {
                 const R fac = R(C_D_V) * sv.rho[cond * ns + i] / cv / (R(C_D_P) * (g.exner_bg[i] + sv.exner_pert[i]));
-                yt = yt + double(fac) * heat + rate * double(theta[i]);
+                yt = yt + wide(fac) * heat + rate * wide(theta[i]);
             }
         }
         st.rhotheta_v[i] = rk == 0 ? yt : 0.0 * st.rhotheta_v[i] + 1.0 * yt;
@@ -1116,14 +1134,14 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
             const R d_here = f[i];
             if (l == nl - n_oro - 1) {
                 const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
-                cv = double(-d_lo * w_lo * area_lo);
+                cv = wide(-d_lo * w_lo * area_lo);
             } else if (l == nl - 1) {
                 const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
-                cv = double(d_up * w_up * area_up);
+                cv = wide(d_up * w_up * area_up);
             } else {
                 const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
                 const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
-                cv = double(d_up * w_up * area_up - d_lo * w_lo * area_lo);
+                cv = wide(d_up * w_up * area_up - d_lo * w_lo * area_lo);
             }
         }
         const double div = inv_vol * (h.value() + cv);
