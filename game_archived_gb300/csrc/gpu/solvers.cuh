@@ -15,7 +15,7 @@
  * tracers (column_solvers.c:385-639)
  *   k_tracers_solve per (constituent, column): rows built on the fly, Thomas
  *                   sweep in registers, clipping
- *   k_tracers_sedheat per (layer, column): sedimentation enthalpy flux
+ *   k_tracers_sedheat per column: sedimentation enthalpy flux
  *                   divergence, accumulated over the condensates in the
  *                   reference's order
  *
@@ -485,18 +485,21 @@ __global__ void k_tracers_solve(VGrid vg, StepParams p, DState so, DState sn, DS
     }
 }
 
-/* sedimentation heating (rk 0 only): per (layer, column), the condensates'
- * contributions added in the reference's constituent order */
+/* sedimentation heating (rk 0 only): thread = column, walking down the
+ * layers so that each interface's enthalpy fluxes are formed once and reused
+ * by the layer below; the condensates' contributions are added in the
+ * reference's constituent order, with the same operations as the per-layer
+ * form (column_solvers.c:455-462, 551-623) */
+constexpr int SEDHEAT_MAX_COND = 4;
 template <bool EXACT>
 __global__ void k_tracers_sedheat(VGrid vg, StepParams p, DState so, DState sn, const double *temperature,
                                   TracerWork tw, double *sed_heat)
 {
     const int nc = vg.nc, nl = vg.nl;
-    const long long ns = (long long)nl * nc, b = gtid();
-    if (b >= ns) return;
-    const int j = (int)(b / nc), i = (int)(b - (long long)j * nc);
-    const double vol = vg.volume[b];
-    const double ivol = EXACT ? 0.0 : tw.inv_vol[b];
+    const long long ns = (long long)nl * nc;
+    const long long ii = gtid();
+    if (ii >= nc) return;
+    const int i = (int)ii, n_cond = p.n_cond;
     const long long bot = i + ns - nc;
     const double a_sfc = vg.area_v[(long long)nl * nc + i];
     /* enthalpy flux of constituent k at interface jj (below layer jj) */
@@ -511,23 +514,34 @@ __global__ void k_tracers_sedheat(VGrid vg, StepParams p, DState so, DState sn, 
         const double cp = (k % 2 == 0) ? tw.cp_ice[up] : tw.cp_water[up];
         return cp * tio * fr;
     };
-    auto per_vol = [&](double x) { return EXACT ? x / vol : x * ivol; };
-    double sh = 0.0;
-    for (int k = 0; k < p.n_cond; ++k) {
-        bool has;
-        const double vs = sink_velocity(p, k, has);
-        if (j == 0) {
-            sh += per_vol(fe(k, j, vs, has));
-        } else if (j == nl - 1) {
-            sh += per_vol(-fe(k, j - 1, vs, has));
-            const double tb = temperature[bot];
-            const double cp = (k % 2 == 0) ? tw.cp_ice[bot] : tw.cp_water[bot];
-            sh += per_vol(-vs * tb * cp * so.rho[k * ns + bot] * a_sfc);
-        } else {
-            sh += per_vol(-fe(k, j - 1, vs, has) + fe(k, j, vs, has));
+    double h_up[SEDHEAT_MAX_COND];
+    for (int j = 0; j < nl; ++j) {
+        const long long b = i + (long long)j * nc;
+        const double vol = vg.volume[b];
+        const double ivol = EXACT ? 0.0 : tw.inv_vol[b];
+        auto per_vol = [&](double x) { return EXACT ? x / vol : x * ivol; };
+        double sh = 0.0;
+#pragma unroll
+        for (int k = 0; k < SEDHEAT_MAX_COND; ++k) {
+            if (k >= n_cond) break;
+            bool has;
+            const double vs = sink_velocity(p, k, has);
+            if (j == 0) {
+                h_up[k] = fe(k, j, vs, has);
+                sh += per_vol(h_up[k]);
+            } else if (j == nl - 1) {
+                sh += per_vol(-h_up[k]);
+                const double tb = temperature[bot];
+                const double cp = (k % 2 == 0) ? tw.cp_ice[bot] : tw.cp_water[bot];
+                sh += per_vol(-vs * tb * cp * so.rho[k * ns + bot] * a_sfc);
+            } else {
+                const double h = fe(k, j, vs, has);
+                sh += per_vol(-h_up[k] + h);
+                h_up[k] = h;
+            }
         }
+        sed_heat[b] = sh;
     }
-    sed_heat[b] = sh;
 }
 
 
