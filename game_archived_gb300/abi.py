@@ -66,6 +66,7 @@ SIGNATURES = {
     "game_gpu_write_out_integral": ([vp, cint, vp], cint),
     "game_gpu_surface_pressure": ([vp, vp, vp], cint),
     "game_gpu_weighted_sums_noalloc": ([vp, cint, ctypes.c_longlong, vp, vp, vp], cint),
+    "game_gpu_numerics": ([cint, vp, vp, ctypes.c_longlong], cint),
     "grad_adj": ([vp] * 3, cint),
     "divv_h_adj": ([vp] * 3, cint),
     "divv_h_tracer_adj": ([vp] * 8, cint),

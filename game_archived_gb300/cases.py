@@ -20,6 +20,13 @@ Cases (inputs are synthetic; seeds are fixed per case):
                   gradient-wind balance with the surface pressure, standard
                   temperature profile, N(0, 0.5 m/s) wind noise, water vapour at
                   70 % relative humidity below 8 km and none above, condensates 0.
+* ``baroclinic_moist``  the baroclinic jet u = 35 m/s cos^(3/2)(eta_v) sin^2(2 lat)
+                  with its thermal-wind-balanced temperature, the steady state
+                  of Jablonowski and Williamson (2006, QJRMS 132, 2943-2975,
+                  their eqs. 2-10), evaluated at each grid point's height by
+                  solving their geopotential for the pressure; N(0, 0.5 m/s)
+                  wind noise; water vapour at 70 % relative humidity below
+                  8 km and none above, condensates 0.
 * ``tracers``     as ``std_wind_tpert`` with every non-main constituent set to a
                   log-normal (sigma 0.5) field times exp(-z / 3 km).
 """
@@ -37,7 +44,8 @@ M_V = N_A * 0.002991e-23
 OMEGA = 7.292115e-5
 G_MEAN_SFC_ABS = 9.80616
 
-CASE_SEEDS = {"std_wind": 1001, "std_wind_tpert": 1002, "jet_moist": 1003, "tracers": 1005}
+CASE_SEEDS = {"std_wind": 1001, "std_wind_tpert": 1002, "jet_moist": 1003, "tracers": 1005,
+              "baroclinic_moist": 1003}
 
 
 def standard_temp(z):
@@ -68,6 +76,64 @@ def saturation_pressure(t):
     ti = np.clip(tc, -80.0, 0.0)
     ice = np.exp(43.494 - 6545.8 / (ti + 278.0)) / (ti + 868.0) ** 2
     return np.where(t > T_0, water, ice)
+
+
+# Jablonowski and Williamson (2006): parameters of their baroclinic steady state
+JW_U0, JW_T0, JW_GAMMA, JW_DT, JW_ETA_T, JW_ETA_0, JW_P0 = 35.0, 288.0, 0.005, 4.8e5, 0.2, 0.252, 1.0e5
+
+
+def _jw_terms(eta, lat, a):
+    """the latitude-dependent brackets shared by their temperature and
+    geopotential (eqs. 6 and 9)"""
+    s, c = np.sin(lat), np.cos(lat)
+    eta_v = (eta - JW_ETA_0) * np.pi / 2
+    cv = np.cos(eta_v)
+    b1 = -2.0 * s ** 6 * (c ** 2 + 1.0 / 3.0) + 10.0 / 63.0
+    b2 = (8.0 / 5.0 * c ** 3 * (s ** 2 + 2.0 / 3.0) - np.pi / 4.0) * a * OMEGA
+    return eta_v, cv, b1, b2
+
+
+def jw_temperature(eta, lat, a):
+    """eqs. 4-6: horizontal-mean profile plus the balanced perturbation"""
+    expo = R_D * JW_GAMMA / G_MEAN_SFC_ABS
+    t_mean = JW_T0 * eta ** expo + np.where(eta < JW_ETA_T, JW_DT * np.clip(JW_ETA_T - eta, 0.0, None) ** 5, 0.0)
+    eta_v, cv, b1, b2 = _jw_terms(eta, lat, a)
+    return t_mean + 0.75 * eta * np.pi * JW_U0 / R_D * np.sin(eta_v) * np.sqrt(cv) * (
+        b1 * 2.0 * JW_U0 * cv ** 1.5 + b2)
+
+
+def jw_geopotential(eta, lat, a):
+    """eqs. 7-9"""
+    expo = R_D * JW_GAMMA / G_MEAN_SFC_ABS
+    phi_mean = JW_T0 * G_MEAN_SFC_ABS / JW_GAMMA * (1.0 - eta ** expo)
+    et = JW_ETA_T
+    strat = R_D * JW_DT * ((np.log(np.minimum(eta, et) / et) + 137.0 / 60.0) * et ** 5 - 5.0 * et ** 4 * eta
+                           + 5.0 * et ** 3 * eta ** 2 - 10.0 / 3.0 * et ** 2 * eta ** 3 + 1.25 * et * eta ** 4
+                           - 0.2 * eta ** 5)
+    phi_mean = phi_mean - np.where(eta < et, strat, 0.0)
+    eta_v, cv, b1, b2 = _jw_terms(eta, lat, a)
+    return phi_mean + JW_U0 * cv ** 1.5 * (b1 * JW_U0 * cv ** 1.5 + b2)
+
+
+def jw_eta(z, lat, a, iterations=60):
+    """the pressure coordinate eta = p / p0 at height z: Newton iterations on
+    Phi(eta) = g z with dPhi / d ln(eta) = -R_d T (their hydrostatic
+    relation)"""
+    eta = np.full(np.shape(z), 1.0)
+    target = G_MEAN_SFC_ABS * np.asarray(z)
+    for _ in range(iterations):
+        f = jw_geopotential(eta, lat, a) - target
+        eta_new = eta * np.exp(f / (R_D * jw_temperature(eta, lat, a)))
+        if np.max(np.abs(eta_new / eta - 1.0)) < 1e-15:
+            eta = eta_new
+            break
+        eta = eta_new
+    return eta
+
+
+def jw_wind(eta, lat):
+    """eq. 2"""
+    return JW_U0 * np.cos((eta - JW_ETA_0) * np.pi / 2) ** 1.5 * np.sin(2.0 * lat) ** 2
 
 
 def _wind_field(layout, tables, u_of):
@@ -114,6 +180,15 @@ def build_initial_state(model, tables, case, ops, seed=None):
         pressure = pressure * np.exp(np.interp(lat_c, lat_grid, lnp))
         wind = _wind_field(lay, tables, lambda lat, z: 35.0 * np.sin(2 * lat) ** 2 * standard_temp(z) / t_sfc)
         noise = 0.5
+    elif case == "baroclinic_moist":
+        if not lay.moisture_on:
+            raise ValueError("baroclinic_moist needs the moist build")
+        a = tables.radius
+        eta = jw_eta(zs, lat_c, a)
+        pressure = JW_P0 * eta
+        temperature = jw_temperature(eta, lat_c, a)
+        wind = _wind_field(lay, tables, lambda lat, z: jw_wind(jw_eta(z, lat, a), lat))
+        noise = 0.5
     else:
         raise ValueError(f"unknown case {case}")
     # seeded noise on the edge-normal winds
@@ -122,7 +197,7 @@ def build_initial_state(model, tables, case, ops, seed=None):
     if case in ("std_wind_tpert", "tracers"):
         temperature = temperature + rng.standard_normal(ns)
     temperature_v = temperature.copy()
-    if case == "jet_moist":
+    if case in ("jet_moist", "baroclinic_moist"):
         rh = np.where(zs < 8000.0, 0.7, 0.0)
         vapour = rh * saturation_pressure(temperature) / (R_V * temperature)
         rho_moist = pressure / (R_D * temperature)

@@ -15,17 +15,22 @@
  * block and one counter.  They live in the file-scope array below, fixed at
  * INTEGRAL_MAX_FIELDS fields x INTEGRAL_MAX_BLOCKS blocks: 77,824 bytes of
  * partial sums plus 8 counters (77,856 bytes, 256-byte aligned).  The
- * counters must be zero when a launch starts; they are zero when the module
- * is loaded, the first call on each device sets them to zero once more, and
- * every launch leaves them at zero (the last block of each field resets its
- * counter).  The partial sums need no initial value.
+ * counters must be zero when a launch starts.  A __device__ variable is
+ * zero-initialised when the device code is loaded, and every launch leaves
+ * the counters at zero again (the last block of each field resets its
+ * counter), so no call ever writes them from the host: a host-side clear
+ * would be ordered only on the stream it was issued on, not before a kernel
+ * on the caller's non-blocking stream.  The partial sums need no initial
+ * value.
  *
  * First call per device.  The first call with a given device current looks
  * up the device address of the scratch array (cudaGetSymbolAddress, which
- * may load this library's device code) and zeroes the counters with a
- * synchronous cudaMemset.  Make that first call before any stream capture
- * begins, e.g. once right after selecting the device.  Later calls only
- * launch the kernel.
+ * may load this library's device code) and keeps it for that device.  Make
+ * that first call before any stream capture begins, e.g. once right after
+ * selecting the device.  Later calls only launch the kernel.  The address is
+ * kept for the life of the process: after cudaDeviceReset the device code is
+ * loaded anew at another address, so do not call this entry point on a
+ * device that has been reset since its first call.
  *
  * Concurrency.  All calls on one device share the one scratch array.  Two
  * calls whose kernels can run at the same time (different streams without an
@@ -76,11 +81,6 @@ NoallocScratch *scratch_for_current_device()
         return nullptr;
     }
     NoallocScratch *s = (NoallocScratch *)p;
-    e = cudaMemset(s->counters, 0, sizeof(s->counters));
-    if (e != cudaSuccess) {
-        fail(std::string("weighted_sums_noalloc: zeroing the counters: ") + cudaGetErrorString(e));
-        return nullptr;
-    }
     g_scratch_ptr[dev] = s;
     return s;
 }

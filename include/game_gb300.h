@@ -98,6 +98,15 @@ int game_gpu_event_elapsed(int a, int b, float *ms);
 int game_gpu_profile(int on);
 int game_gpu_profile_count(void);
 int game_gpu_profile_get(int i, const char **name, double *ms, long long *launches);
+/* the mixed path's numeric primitives beside the CUDA operations they stand
+ * for, over n host values (for tests; no context needed): op 0 / 1 the
+ * Newton-refined FP64 reciprocal with 1 / 2 steps, 2 IEEE 1.0 / x, 3 / 4
+ * double -> float by integer operations / by the conversion instruction,
+ * 5 / 6 float -> double likewise, 7 the double-float split and join of x,
+ * 8 the double-float reciprocal, 9 / 10 double-float product / sum of in[i]
+ * and in[n + i]; in and out are double arrays except the float side of ops
+ * 3 to 6 */
+int game_gpu_numerics(int op, const void *in, void *out, long long n);
 /* bytes copied host->device and device->host by the library */
 int game_gpu_transfer_bytes(long long *h2d, long long *d2h, int reset);
 
@@ -344,8 +353,11 @@ int game_gpu_sfc_pressure_objective(struct state *state, const double *weights, 
  * given all device memory to their own pool.
  *
  * The first call on each device (with that device current) looks up the
- * scratch array and zeroes its counters, synchronously; make it before any
- * stream capture begins.  Calls on one device share the scratch: calls whose
+ * scratch array's device address and keeps it; make it before any stream
+ * capture begins, and do not call this entry point on a device reset
+ * (cudaDeviceReset) since its first call.  The scratch's counters start at
+ * zero when the device code loads and every call leaves them at zero, so the
+ * host never clears them.  Calls on one device share the scratch: calls whose
  * kernels may overlap (different streams without ordering, several host
  * threads) race and return wrong sums; keep them in one stream.
  *

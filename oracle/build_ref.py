@@ -39,7 +39,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("GAME_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: $GAME_REFERENCE_ROOT, else a directory named
+# "reference" beside the repository's root
+REF_ROOT = os.environ.get("GAME_REFERENCE_ROOT",
+                          os.path.normpath(os.path.join(HERE, os.pardir, os.pardir, "reference")))
 OUT = os.path.join(HERE, "_ref")
 
 SRC_DIRS = ["time_stepping", "spatial_operators", "constituents", "subgrid_scale"]

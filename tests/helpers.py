@@ -58,6 +58,29 @@ def state_errors(s_a, s_b, lay):
     return out
 
 
+def rel_err_pointwise(a, b, floor=1e-6):
+    """max |a - b| / |b| over the entries with |b| >= floor * max |b|"""
+    scale = np.max(np.abs(b))
+    if scale == 0:
+        return float(np.max(np.abs(a - b)))
+    mask = np.abs(b) >= floor * scale
+    return float(np.max(np.abs(a[mask] - b[mask]) / np.abs(b[mask])))
+
+
+def state_errors_pointwise(s_a, s_b, lay, floor=1e-6):
+    """rel_err_pointwise per prognostic field, split as state_errors"""
+    out = {}
+    ns = lay.n_scalars
+    for k in range(lay.n_const):
+        out[f"rho[{k}]"] = rel_err_pointwise(s_a["rho"][k * ns:(k + 1) * ns], s_b["rho"][k * ns:(k + 1) * ns], floor)
+    for f in ("rhotheta_v", "theta_v_pert", "exner_pert"):
+        out[f] = rel_err_pointwise(s_a[f], s_b[f], floor)
+    w_a, w_b = wind_parts(s_a["wind"], lay), wind_parts(s_b["wind"], lay)
+    out["wind_h"] = rel_err_pointwise(w_a[1], w_b[1], floor)
+    out["wind_v"] = rel_err_pointwise(w_a[0], w_b[0], floor)
+    return out
+
+
 def wind_parts(wind, lay):
     nc, ne, vpl = lay.nc, lay.ne, lay.vpl
     w = np.stack([wind[k * vpl:k * vpl + nc] for k in range(lay.nl + 1)])

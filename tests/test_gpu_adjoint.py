@@ -131,6 +131,32 @@ def test_dot_product_mid_run_window(dry4):
     assert abs(lhs - rhs) <= 1e-10 * max(abs(lhs), abs(rhs)), (lhs, rhs)
 
 
+def test_dot_product_config4_window():
+    """the dot-product test on the adjoint configuration's own window: RES_ID=5
+    with the 2 km mountain and the 1 K temperature noise, 12 steps at
+    dt = 200 s from the first step"""
+    _, m0 = make_model(5, 0, "std_wind_tpert", mountain=True)
+    m = clone(m0)
+    rng = np.random.default_rng(412)
+    g = abi.GpuModel(m, abi.FP64)
+    try:
+        m.config["totally_first_step_bool"][0] = 1
+        out = _state_like(m.layout)
+        g.window_forward(m.state_old, out, 200.0, 12)
+        dx = _random_dx(m, rng)
+        dy = _state_like(m.layout)
+        g.window_tl(dx, dy)
+        yb = _random_bar(m, rng)
+        xb = _state_like(m.layout)
+        g.window_backward(yb, xb)
+    finally:
+        g.close()
+    lhs, rhs = _dot(dy, yb), _dot(dx, xb)
+    print(f"dot product, RES_ID=5 12-step window at dt = 200 s: <TL dx, ybar> = {lhs:.17g}, "
+          f"<dx, AD ybar> = {rhs:.17g}, relative difference {abs(lhs - rhs) / abs(lhs):.3g}")
+    assert abs(lhs - rhs) <= 1e-10 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
 def cap_weights(m, lat0=45.0, lon0=0.0, radius_deg=20.0):
     """area_sfc of the columns within radius_deg of (lat0, lon0), else 0"""
     lay = m.layout

@@ -121,3 +121,114 @@ def test_pointwise_products_and_vertical_divergence(setup):
     o.lib.orc_add_vertical_divv(ctypes.byref(o.g), wind.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                 b.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     assert rel_err(a, b) <= TOL
+
+
+# ---------------------------------------------------------------------------
+# The exported operator variants the step does not call itself but the
+# reference's initialisation, output and subgrid code call on host arrays
+# (src/io/set_grid_properties.c:217-221, src/subgrid_scale/*.c): each through
+# the C ABI against the oracle's restatement, on host arrays in the
+# reference's layout.  Outputs start from a sentinel so that the entries the
+# reference leaves untouched are compared too (they must come back as the
+# sentinel on both sides).
+
+def _orc(o, name, *arrays):
+    import ctypes
+    fn = getattr(o.lib, "orc_" + name)
+    args = [ctypes.byref(o.g)] + [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in arrays]
+    assert fn(*args) == 0, name
+
+
+def _pointwise(a, b, floor=1e-300):
+    """max |a - b| / |b| over the entries where b is not (near) zero"""
+    scale = np.max(np.abs(b))
+    mask = np.abs(b) > max(floor, 1e-9 * scale)
+    if not np.any(mask):
+        return 0.0
+    return float(np.max(np.abs(a[mask] - b[mask]) / np.abs(b[mask])))
+
+
+@pytest.mark.parametrize("name", ["grad_hor_cov", "grad_vert_cov", "grad_cov", "grad_hor"])
+def test_gradient_variants(setup, name):
+    """gradient_operators.c:14-91: covariant horizontal and vertical parts,
+    their sum, and the horizontal part made contravariant"""
+    m, g, o = setup
+    _, _, f = _fields(m)
+    a = np.full(m.layout.n_vectors, 7.0)
+    b = a.copy()
+    assert getattr(g.lib, name)(abi._p(f), abi._p(a), m.grid.ptr) == 0, g.lib.game_gpu_last_error()
+    _orc(o, name, f, b)
+    assert rel_err(a, b) <= TOL, name
+    assert _pointwise(a, b) <= 1e-10, name
+    assert np.array_equal(a == 7.0, b == 7.0), name  # the same entries untouched
+
+
+def test_vector_field_hor_cov_to_con(setup):
+    """averaging.c:113-133: in place, the terrain correction of the
+    horizontal components in the orography layers"""
+    m, g, o = setup
+    rng = np.random.default_rng(17)
+    v = m.state_old["wind"] + rng.standard_normal(m.layout.n_vectors)
+    a, b = v.copy(), v.copy()
+    assert g.lib.vector_field_hor_cov_to_con(abi._p(a), m.grid.ptr) == 0, g.lib.game_gpu_last_error()
+    _orc(o, "vector_field_hor_cov_to_con", b)
+    assert rel_err(a, b) <= TOL
+    assert _pointwise(a, b) <= 1e-10
+
+
+@pytest.mark.parametrize("name", ["scalar_times_vector_h", "scalar_times_vector_h_upstream",
+                                  "scalar_times_vector_v"])
+def test_scalar_times_vector_variants(setup, name):
+    """multiplications.c:45-117: edge average (or the upstream cell's value)
+    times the horizontal components, interface average times the vertical
+    ones; the other components are left as they were"""
+    m, g, o = setup
+    rho, wind, _ = _fields(m)
+    a = np.full(m.layout.n_vectors, -3.0)
+    b = a.copy()
+    assert getattr(g.lib, name)(abi._p(rho), abi._p(wind), abi._p(a), m.grid.ptr) == 0, g.lib.game_gpu_last_error()
+    _orc(o, name, rho, wind, b)
+    assert rel_err(a, b) <= TOL, name
+    assert _pointwise(a, b) <= 1e-12, name
+    assert np.array_equal(a == -3.0, b == -3.0), name
+
+
+def test_divv_h_tracer(setup):
+    """divergences.c:66-148: the flux divergence of a tracer, with the
+    upstream densities in the terrain vertical term"""
+    m, g, o = setup
+    lay = m.layout
+    rho, wind, _ = _fields(m)
+    rng = np.random.default_rng(19)
+    dens = rho * (1.0 + 0.1 * rng.standard_normal(lay.n_scalars))
+    flux = np.zeros(lay.n_vectors)
+    _orc(o, "scalar_times_vector", dens, wind, flux)
+    a, b = np.zeros(lay.n_scalars), np.zeros(lay.n_scalars)
+    assert g.lib.divv_h_tracer(abi._p(flux), abi._p(dens), abi._p(wind), abi._p(a), m.grid.ptr) == 0, \
+        g.lib.game_gpu_last_error()
+    _orc(o, "divv_h_tracer", flux, dens, wind, b)
+    assert rel_err(a, b) <= TOL
+
+
+def test_calc_rel_vort_and_add_f_to_rel_vort(setup):
+    """vorticities.c:87-165: relative vorticity (rhombi and the tangential
+    components) and the Coriolis parameter added to a curl field"""
+    import ctypes
+    m, g, o = setup
+    lay = m.layout
+    _, wind, _ = _fields(m)
+    d = m.diagnostics
+    assert g.lib.calc_rel_vort(abi._p(wind), d.ptr, m.grid.ptr, m.dualgrid.ptr) == 0, g.lib.game_gpu_last_error()
+    rel_gpu, tri_gpu = d["rel_vort"].copy(), d["rel_vort_on_triangles"].copy()
+    od = o.diag()
+    assert o.lib.orc_calc_rel_vort(ctypes.byref(o.g), wind.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                   ctypes.byref(od)) == 0
+    assert rel_err(rel_gpu, d["rel_vort"]) <= TOL
+    assert rel_err(tri_gpu, d["rel_vort_on_triangles"]) <= TOL
+    rel = d["rel_vort"].copy()
+    a = np.full(rel.size, 5.0)
+    b = a.copy()
+    assert g.lib.add_f_to_rel_vort(abi._p(rel), abi._p(a), m.dualgrid.ptr) == 0, g.lib.game_gpu_last_error()
+    _orc(o, "add_f_to_rel_vort", rel, b)
+    assert rel_err(a, b) <= TOL
+    assert _pointwise(a, b) <= 1e-12

@@ -10,12 +10,17 @@ import numpy as np
 import pytest
 
 from game_archived_gb300 import abi, driver
-from helpers import clone, make_model, state_errors
+from helpers import clone, make_model, state_errors, state_errors_pointwise
 from oracle.bind import Oracle
 
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
+# pointwise relative error |gpu - oracle| / |oracle| over the entries whose
+# magnitude is at least 1e-6 of the field's largest (the perturbation fields
+# theta_v' and Pi' and the vertical wind pass through zero, where a relative
+# error has no meaning)
+POINTWISE_TOL = 1e-9
 
 CONFIGS = [
     # (res, moist, case, mountain, dt, steps)
@@ -27,7 +32,7 @@ CONFIGS = [
     # atmosphere with wind noise (400 s, 10 steps), RES_ID=5 with the
     # mountain and 1 K noise (200 s), RES_ID=6 moist jet (100 s)
     (4, 0, "std_wind", False, 400.0, 10),
-    (5, 0, "std_wind_tpert", True, 200.0, 3),
+    (5, 0, "std_wind_tpert", True, 200.0, 72),
     (6, 1, "jet_moist", False, 100.0, 2),
 ]
 
@@ -49,7 +54,8 @@ def _run_pair(res, moist, case, mountain, dt, steps, resident=False, graphs=True
             driver.step(m_gpu, gpu.linear_combine_two_states, gpu.manage_rkhevi, dt, n * dt)
             if resident:
                 gpu.sync_to_host(m_gpu.state_new)
-            errs.append(state_errors(m_gpu.state_new, m_orc.state_new, m_gpu.layout))
+            errs.append({"norm": state_errors(m_gpu.state_new, m_orc.state_new, m_gpu.layout),
+                         "pointwise": state_errors_pointwise(m_gpu.state_new, m_orc.state_new, m_gpu.layout)})
             # continue both from the oracle's state so that every step is compared from identical inputs
             m_gpu.state_new.copy_from(m_orc.state_new)
             if resident:
@@ -59,12 +65,18 @@ def _run_pair(res, moist, case, mountain, dt, steps, resident=False, graphs=True
         gpu.close()
 
 
-@pytest.mark.parametrize("cfg", CONFIGS, ids=lambda c: f"R{c[0]}M{c[1]}-{c[2]}{'-oro' if c[3] else ''}")
+@pytest.mark.parametrize("cfg", CONFIGS, ids=lambda c: f"R{c[0]}M{c[1]}-{c[2]}{'-oro' if c[3] else ''}-{c[5]}")
 def test_step_fp64_matches_oracle(cfg):
     errs, *_ = _run_pair(*cfg)
     for n, e in enumerate(errs):
-        worst = max(e.values())
-        assert worst <= TOL, f"step {n}: {e}"
+        worst = max(e["norm"].values())
+        assert worst <= TOL, f"step {n}: {e['norm']}"
+        worst_pw = max(e["pointwise"].values())
+        assert worst_pw <= POINTWISE_TOL, f"step {n}: {e['pointwise']}"
+    norm = {k: max(e["norm"][k] for e in errs) for k in errs[0]["norm"]}
+    pw = {k: max(e["pointwise"][k] for e in errs) for k in errs[0]["pointwise"]}
+    print(f"\n{cfg}: worst over {len(errs)} steps, norm-relative {max(norm.values()):.3g} {norm}; "
+          f"pointwise {max(pw.values()):.3g} {pw}")
 
 
 def test_resident_graph_equals_sync():

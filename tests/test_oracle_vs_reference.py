@@ -142,3 +142,68 @@ def test_oracle_bitwise_equals_reference_held_suarez(moist, case, mountain):
             a, b = getattr(m_ref, k).buf, getattr(m_orc, k).buf
             assert np.array_equal(a, b), f"step {n}: {k} differs in {np.count_nonzero(a != b)} bytes"
     assert np.any(m_orc.forcings["radiation_tendency"] != 0)
+
+
+def test_reference_operator_variants_equal_oracle():
+    """the exported operator variants the reference's initialisation, output
+    and subgrid code call on host arrays (gradient_operators.c:14-91,
+    averaging.c:113-133, multiplications.c:45-117, divergences.c:66-148,
+    vorticities.c:87-165), bit for bit, including the entries each leaves
+    untouched"""
+    import ctypes
+    _, m = make_model(3, 1, "tracers", True)
+    ref = refbind.Reference(m)
+    lib = ref.lib
+    lay = m.layout
+    orc = Oracle(m)
+    vp = ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    rng = np.random.default_rng(13)
+    s = m.state_old["exner_pert"] + 1e-3 * rng.standard_normal(lay.n_scalars)
+    rho = m.state_old["rho"][lay.n_cond * lay.n_scalars:(lay.n_cond + 1) * lay.n_scalars].copy()
+    dens = rho * (1.0 + 0.1 * rng.standard_normal(lay.n_scalars))
+    wind = m.state_old["wind"] + rng.standard_normal(lay.n_vectors)
+
+    def orc_call(name, *arrays):
+        fn = getattr(orc.lib, "orc_" + name)
+        assert fn(ctypes.byref(orc.g), *[a.ctypes.data_as(dp) for a in arrays]) == 0, name
+
+    for name in ("grad_hor_cov", "grad_vert_cov", "grad_cov", "grad_hor"):
+        a, b = np.full(lay.n_vectors, 7.0), np.full(lay.n_vectors, 7.0)
+        getattr(lib, name).argtypes = [vp] * 3
+        assert getattr(lib, name)(s.ctypes.data, a.ctypes.data, m.grid.ptr) == 0
+        orc_call(name, s, b)
+        assert np.array_equal(a, b), name
+    a, b = wind.copy(), wind.copy()
+    lib.vector_field_hor_cov_to_con.argtypes = [vp] * 2
+    assert lib.vector_field_hor_cov_to_con(a.ctypes.data, m.grid.ptr) == 0
+    orc_call("vector_field_hor_cov_to_con", b)
+    assert np.array_equal(a, b)
+    for name in ("scalar_times_vector_h", "scalar_times_vector_h_upstream", "scalar_times_vector_v"):
+        a, b = np.full(lay.n_vectors, -3.0), np.full(lay.n_vectors, -3.0)
+        getattr(lib, name).argtypes = [vp] * 4
+        assert getattr(lib, name)(rho.ctypes.data, wind.ctypes.data, a.ctypes.data, m.grid.ptr) == 0
+        orc_call(name, rho, wind, b)
+        assert np.array_equal(a, b), name
+    flux = np.zeros(lay.n_vectors)
+    orc_call("scalar_times_vector", dens, wind, flux)
+    a, b = np.zeros(lay.n_scalars), np.zeros(lay.n_scalars)
+    lib.divv_h_tracer.argtypes = [vp] * 5
+    assert lib.divv_h_tracer(flux.ctypes.data, dens.ctypes.data, wind.ctypes.data, a.ctypes.data, m.grid.ptr) == 0
+    orc_call("divv_h_tracer", flux, dens, wind, b)
+    assert np.array_equal(a, b)
+    # calc_rel_vort writes diagnostics->rel_vort and rel_vort_on_triangles
+    lib.calc_rel_vort.argtypes = [vp] * 4
+    assert lib.calc_rel_vort(wind.ctypes.data, m.diagnostics.ptr, m.grid.ptr, m.dualgrid.ptr) == 0
+    rel_ref, tri_ref = m.diagnostics["rel_vort"].copy(), m.diagnostics["rel_vort_on_triangles"].copy()
+    m.diagnostics["rel_vort"][:] = 0.0
+    m.diagnostics["rel_vort_on_triangles"][:] = 0.0
+    od = orc.diag()
+    assert orc.lib.orc_calc_rel_vort(ctypes.byref(orc.g), wind.ctypes.data_as(dp), ctypes.byref(od)) == 0
+    assert np.array_equal(rel_ref, m.diagnostics["rel_vort"])
+    assert np.array_equal(tri_ref, m.diagnostics["rel_vort_on_triangles"])
+    a, b = np.full(rel_ref.size, 5.0), np.full(rel_ref.size, 5.0)
+    lib.add_f_to_rel_vort.argtypes = [vp] * 3
+    assert lib.add_f_to_rel_vort(rel_ref.ctypes.data, a.ctypes.data, m.dualgrid.ptr) == 0
+    orc_call("add_f_to_rel_vort", rel_ref, b)
+    assert np.array_equal(a, b)
