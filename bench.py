@@ -29,6 +29,7 @@ total over ranks.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -102,27 +103,102 @@ def kernel_bytes(res, n_const, r, nl=L):
     out["k_waves_rows"] = (2 * (14 * wi + 8 * s) * d, 2)
     out["k_waves_thomas"] = (2 * 6 * wi * d, 2)
     out["k_waves_apply"] = (2 * ((4 * wi + 12 * s + 2 * wl) * d + (4 * s + wi) * r), 2)
+    # the fused double-float sound-wave solve: state old (rho_gas, rho theta_v,
+    # theta_v', Pi', w), new (rho_gas, rho theta_v, Pi'), tendency (rho_gas,
+    # rho theta_v, w), tables (1/V, V, Pi_bg, theta_v_bg, six row terms, the
+    # damping factor, 1/A of the interfaces) read; the new rho_gas, rho
+    # theta_v, theta_v', Pi' and the inner w written with their FP32 shadow
+    out["k_waves_df"] = (2 * ((17 * s + 3 * wl + 8 * wi) * d + (4 * s + wi) * r), 2)
     if moist:
         out["k_tracers_solve"] = (2 * ((3 * (C - 1) * s + 3 * wl + s) * d + (C - 1) * s * r), 2)
         out["k_tracers_sedheat"] = ((((C - 2) + 5) * s + 2 * wl) * d, 1)
     return out
 
 
-def read_ncu_summary(kernel, key):
-    """a per-kernel figure from the committed ncu summary (lines
-    '<key> <kernel> <value>')"""
-    path = os.path.join(ROOT, "profiles", "ncu_rkhevi_res6_mixed.md")
-    if not os.path.exists(path):
-        return None
-    with open(path) as f:
-        for line in f:
-            parts = line.split()
-            if len(parts) == 3 and parts[0] == key and parts[1] == kernel:
+PROFILE_JSON = os.path.join(ROOT, "profiles", "ncu_rkhevi_res6_mixed.json")
+
+
+# ncu raw-page metrics kept per kernel in the machine-written summary
+NCU_METRICS = {
+    "gpu__time_duration.sum": "duration_ns",
+    "dram__bytes_read.sum": "dram_read_bytes",
+    "dram__bytes_write.sum": "dram_write_bytes",
+    "gpu__dram_throughput.avg.pct_of_peak_sustained_elapsed": "dram_throughput_pct",
+    "sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active": "fp64_pipe_pct",
+    "sm__pipe_fma_cycles_active.avg.pct_of_peak_sustained_active": "fma_pipe_pct",
+    "sm__pipe_alu_cycles_active.avg.pct_of_peak_sustained_active": "alu_pipe_pct",
+    "sm__inst_executed_pipe_xu.avg.pct_of_peak_sustained_active": "xu_pipe_pct",
+    "sm__warps_active.avg.pct_of_peak_sustained_active": "warps_active_pct",
+    "sm__throughput.avg.pct_of_peak_sustained_elapsed": "sm_throughput_pct",
+    "launch__registers_per_thread": "registers_per_thread",
+    "smsp__inst_executed.sum": "warp_instructions",
+}
+
+
+def short_kernel_name(full):
+    """'void game::<anon>::k_waves_df<26>(...)' -> 'k_waves_df'"""
+    import re
+    for name in re.findall(r"([A-Za-z_]\w*)\s*[<(]", full):
+        if name != "void":
+            return name
+    return full.strip()
+
+
+def ncu_json(args):
+    """--ncu-json RAW.csv: summarise `ncu -i REPORT --page raw --csv` output
+    per kernel (launches; means per launch of the metrics in NCU_METRICS) into
+    --out, with the commit of this checkout and the capture command"""
+    import csv
+    with open(args.ncu_json) as f:
+        rows = list(csv.reader(f))
+    head = rows[0]
+    data = [r for r in rows[2:] if len(r) == len(head)]
+    col = {n: i for i, n in enumerate(head)}
+    kernels = {}
+    for r in data:
+        name = short_kernel_name(r[col["Kernel Name"]])
+        k = kernels.setdefault(name, {"launches": 0, "sums": {}})
+        k["launches"] += 1
+        for metric, key in NCU_METRICS.items():
+            if metric in col:
                 try:
-                    return float(parts[2])
+                    v = float(r[col[metric]].replace(",", ""))
                 except ValueError:
-                    return None
-    return None
+                    continue
+                k["sums"][key] = k["sums"].get(key, 0.0) + v
+    out = {}
+    for name, k in kernels.items():
+        e = {"launches": k["launches"]}
+        for key, v in k["sums"].items():
+            e[key] = v / k["launches"]
+        if "dram_read_bytes" in e and "dram_write_bytes" in e:
+            e["dram_bytes_per_launch"] = e["dram_read_bytes"] + e["dram_write_bytes"]
+        out[name] = e
+    try:
+        commit = subprocess.run(["git", "-C", ROOT, "rev-parse", "HEAD"], capture_output=True, text=True,
+                                timeout=30).stdout.strip() or None
+    except (OSError, subprocess.TimeoutExpired):
+        commit = None
+    summary = {"commit": commit, "captured": args.captured, "command": args.command, "kernels": out}
+    with open(args.out, "w") as f:
+        json.dump(summary, f, indent=1, sort_keys=True)
+        f.write("\n")
+
+
+def read_profile(kernel, key):
+    """(value, source) of a per-kernel figure from the machine-written ncu
+    summary (written by --ncu-json from an ncu capture; it records the commit
+    the capture ran at), or (None, None)"""
+    try:
+        with open(PROFILE_JSON) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return None, None
+    k = d.get("kernels", {}).get(kernel)
+    if not k or key not in k:
+        return None, None
+    return k[key], {"file": os.path.relpath(PROFILE_JSON, ROOT), "commit": d.get("commit"),
+                    "captured": d.get("captured")}
 
 
 # ------------------------------------------------------------------ clocks
@@ -185,8 +261,9 @@ MOUNTAIN = (2000.0, 1.5e6, 30.0, 90.0)   # 2 km Gaussian mountain, 1500 km half-
 
 
 def build_model(res, moist, n_lloyd, pinned, mountain=None, n_layers=L):
-    from game_archived_gb300 import abi, cases, structs, tables
-    tab = tables.GridTables(res, n_layers=n_layers, n_lloyd=n_lloyd, mountain=mountain)
+    """grid tables from the input cache (built on first use), host structs"""
+    from game_archived_gb300 import abi, cases, structs, tables, workloads
+    tab = tables.cached(workloads.input_dir(), res, n_layers=n_layers, n_lloyd=n_lloyd, mountain=mountain)
     lay = structs.Layout(res, n_layers, moist)
     m = abi.pinned_model(lay) if pinned else structs.Model(lay)
     tables.fill_grid(tab, m.grid, m.dualgrid)
@@ -219,11 +296,24 @@ def device_used_bytes(device):
     return total - free
 
 
+def repeats_for(ms_per_step, steps, min_seconds):
+    """how many blocks of `steps` steps make a timed region of at least
+    min_seconds"""
+    if min_seconds <= 0 or ms_per_step <= 0:
+        return 1
+    return max(1, math.ceil(min_seconds * 1e3 / (ms_per_step * steps)))
+
+
 def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, profile=False, column_solver=0,
-                  mem_used=None):
+                  mem_used=None, min_seconds=0.0, column_arithmetic=1, world=1, info=None):
+    """ms per step of the device-resident step; the timed region runs
+    `steps` steps, repeated until it covers min_seconds (the estimate comes
+    from a few untimed steps after the warm-up), between two barriers and
+    synchronisations; info receives the number of timed steps"""
     from game_archived_gb300 import abi, driver
     m = copy_model(model0, pinned=False)
-    g = abi.GpuModel(m, precision, resident=True, graphs=True, device=device, column_solver=column_solver)
+    g = abi.GpuModel(m, precision, resident=True, graphs=True, device=device, column_solver=column_solver,
+                     column_arithmetic=column_arithmetic)
     try:
         for s in (m.state_old, m.state_new, m.state_tendency):
             g.sync_to_device(s)
@@ -233,18 +323,32 @@ def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, pr
             driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
             t += dt
         g.synchronize()
-        g.kernel_launches(reset=True)
-        if sampler:
-            sampler.start()
         g.event_record(0)
-        for n in range(steps):
+        for n in range(3):
             driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
             t += dt
         g.event_record(1)
         g.synchronize()
+        est = allreduce_max(g.event_elapsed_ms(0, 1) / 3, world)
+        n_timed = steps * repeats_for(est, steps, min_seconds)
+        g.kernel_launches(reset=True)
+        barrier(world)
+        g.synchronize()
+        if sampler:
+            sampler.start()
+        g.event_record(0)
+        for n in range(n_timed):
+            driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
+            t += dt
+        g.event_record(1)
+        g.synchronize()
+        barrier(world)
         ms = g.event_elapsed_ms(0, 1)
         clocks = sampler.stop() if sampler else None
         launches = g.kernel_launches()
+        if info is not None:
+            info["timed_steps"] = n_timed
+            info["launches_per_step"] = launches / n_timed
         prof = None
         if profile:
             g.profile(True)
@@ -258,12 +362,16 @@ def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, pr
             mem_used.append(device_used_bytes(device))
         import numpy as np
         finite = bool(np.isfinite(m.state_new["rho"]).all() and np.isfinite(m.state_new["wind"]).all())
-        return ms / steps, launches, clocks, prof, finite
+        return ms / n_timed, launches, clocks, prof, finite
     finally:
         g.close()
 
 
-def time_e2e(model0, precision, steps, warmup, dt, device):
+def time_e2e(model0, precision, steps, warmup, dt, device, min_seconds=0.0, world=1, info=None):
+    """seconds per step of the reference's time loop through the C ABI in the
+    default host-in/host-out mode (pinned host structs): every step copies
+    its State arguments in and its results out.  Repeated like
+    time_resident until the timed region covers min_seconds."""
     from game_archived_gb300 import abi, driver
     m = copy_model(model0, pinned=True)
     g = abi.GpuModel(m, precision, resident=False, graphs=True, device=device)
@@ -274,15 +382,26 @@ def time_e2e(model0, precision, steps, warmup, dt, device):
             driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
             t += dt
         g.synchronize()
-        g.transfer_bytes(reset=True)
         t0 = time.perf_counter()
-        for n in range(steps):
+        for n in range(2):
+            driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
+            t += dt
+        g.synchronize()
+        est = allreduce_max((time.perf_counter() - t0) * 1e3 / 2, world)
+        n_timed = steps * repeats_for(est, steps, min_seconds)
+        g.transfer_bytes(reset=True)
+        barrier(world)
+        t0 = time.perf_counter()
+        for n in range(n_timed):
             driver.step(m, g.linear_combine_two_states, g.manage_rkhevi, dt, t)
             t += dt
         g.synchronize()
         sec = time.perf_counter() - t0
+        barrier(world)
         h2d, d2h = g.transfer_bytes()
-        return sec / steps, h2d // steps, d2h // steps
+        if info is not None:
+            info["timed_steps"] = n_timed
+        return sec / n_timed, h2d // n_timed, d2h // n_timed
     finally:
         g.close()
 
@@ -570,31 +689,45 @@ def barrier(world):
 
 
 def run_ours(args):
-    from game_archived_gb300 import abi, cases
+    from game_archived_gb300 import abi, workloads
     from game_archived_gb300.ops import CAbiOps
     rank, world, local = dist_env()
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    res, dt = args.res, args.dt
-    tab, model0 = build_model(res, 1, args.n_lloyd, pinned=False)
+    name = HEADLINE
+    res, moist, case, mountain, dt, _ = workloads.CONFIGS[name]
+    if rank == 0:
+        workloads.prepare(name, args.n_lloyd)
+    barrier(world)
+    tab, model0 = workloads.load(name, args.n_lloyd)
     g = abi.GpuModel(model0, abi.FP64, device=local)
     try:
-        cases.build_initial_state(model0, tab, "jet_moist", CAbiOps(g.lib, model0))
+        workloads.initial_state(name, tab, model0, CAbiOps(g.lib, model0))
     finally:
         g.close()
     n_const = model0.layout.n_const
 
     barrier(world)
-    ms64, _, _, _, ok64 = time_resident(model0, abi.FP64, args.steps, args.warmup, dt, local)
+    i64, i32, i32f, ie = {}, {}, {}, {}
+    ms64, _, _, _, ok64 = time_resident(model0, abi.FP64, args.steps, args.warmup, dt, local,
+                                        min_seconds=args.min_seconds, world=world, info=i64)
+    barrier(world)
+    # the mixed step with its vertical eliminations in FP64 (for comparison)
+    ms32f, _, _, _, ok32f = time_resident(model0, abi.MIXED, args.steps, args.warmup, dt, local,
+                                          min_seconds=args.min_seconds, world=world, column_arithmetic=0,
+                                          info=i32f)
     barrier(world)
     sampler = ClockSampler(local)
     ms32, launches, clocks, prof, ok32 = time_resident(model0, abi.MIXED, args.steps, args.warmup, dt, local,
-                                                       sampler=sampler, profile=True)
+                                                       sampler=sampler, profile=True, min_seconds=args.min_seconds,
+                                                       world=world, info=i32)
     barrier(world)
     ms32_max = allreduce_max(ms32, world)
+    ms32f_max = allreduce_max(ms32f, world)
     ms64_max = allreduce_max(ms64, world)
-    e2e_sec, h2d, d2h = time_e2e(model0, abi.MIXED, max(2, args.steps // 4), min(args.warmup, 3), dt, local)
+    e2e_sec, h2d, d2h = time_e2e(model0, abi.MIXED, args.steps, min(args.warmup, 3), dt, local,
+                                 min_seconds=args.min_seconds, world=world, info=ie)
     e2e_max = allreduce_max(e2e_sec, world)
     if rank != 0:
         barrier(world)
@@ -617,6 +750,8 @@ def run_ours(args):
             bpl = kb[k][0] / kb[k][1]
             v["algorithmic_bytes_per_launch"] = bpl
             v["gbs"] = bpl / (v["ms_per_launch"] * 1e-3) / 1e9
+    g = grid_sizes(res)
+    prof_traffic, prof_src = read_profile(dom_name, "dram_bytes_per_launch")
     line = {
         "metric": METRIC,
         "value": value,
@@ -624,32 +759,38 @@ def run_ours(args):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
+        "timed_steps": i32["timed_steps"],
         "ms_per_step": ms32_max,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32+f64",
         "data": "synthetic",
-        "config": {"workload": f"RKHEVI step RES_ID={res} ({grid_sizes(res)['nc']} cells, {grid_sizes(res)['ne']} edges), "
-                               f"26 layers, moist (6 constituents), barotropic jet + RH 0.7, dt={dt:g} s",
-                   "precision": "mixed: FP32 horizontal operators, FP64 vertical solves and state",
+        "config": {"workload": workload_text(name, res, g, dt),
+                   "precision": "mixed: FP32 horizontal operators; FP64 state, tendencies and mass-flux "
+                                "accumulation; vertical eliminations in double-float (48-bit significands on "
+                                "the FP32 pipe)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
+                   "grid": f"{args.n_lloyd} Lloyd iterations",
+                   "timing": f"{args.steps} steps repeated to cover >= {args.min_seconds:g} s per timed region",
                    "l2": "working set per step > L2 (state+tables+work >> 129 MB)"},
-        "fp64": {"steps_per_s": world * 1000.0 / ms64_max, "ms_per_step": ms64_max},
+        "fp64": {"steps_per_s": world * 1000.0 / ms64_max, "ms_per_step": ms64_max,
+                 "timed_steps": i64["timed_steps"]},
         "mixed_over_fp64": ms64_max / ms32_max,
+        "mixed_fp64_eliminations": {"steps_per_s": world * 1000.0 / ms32f_max, "ms_per_step": ms32f_max,
+                                    "timed_steps": i32f["timed_steps"]},
         "roofline": {"bound": "hbm", "kernel": dom_name,
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
-                     "traffic": read_ncu_summary(dom_name, "traffic_per_launch_bytes"), "peak_source": peak_kind,
-                     "fp64_pipe_pct_ncu": read_ncu_summary(dom_name, "fp64_pipe_pct")},
+                     "traffic": prof_traffic, "traffic_source": prof_src, "peak_source": peak_kind},
         "roofline_step": {"algorithmic_bytes": step_bytes, "achieved": step_bytes / (ms32_max * 1e-3) / 1e9,
                           "peak": peak, "unit": "GB/s", "frac": step_bytes / (ms32_max * 1e-3) / 1e9 / peak},
         "kernels": kernels,
         "e2e": {"value": world / e2e_max, "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h), "timed_steps": ie["timed_steps"]},
         "gpu_launches": int(launches),
         "clocks": clocks,
-        "finite": bool(ok32 and ok64),
+        "finite": bool(ok32 and ok64 and ok32f),
     }
     if not args.no_diffusion:
         line["diffusion"] = time_diffusion(model0, max(20, args.steps // 4), args.warmup, dt, local,
@@ -657,14 +798,15 @@ def run_ours(args):
     if not args.no_output:
         line["output"] = time_output(model0, local)
     if not args.no_adjoint:
-        line["adjoint"] = time_adjoint(args.adjoint_res, args.n_lloyd, 12, 200.0, local)
+        line["adjoint"] = time_adjoint(args.adjoint_res, None, 12, 200.0, local)
     if not args.no_large:
-        line["large_run"] = time_large_run(7, args.n_lloyd, args.large_steps, 50.0, local)
+        line["large_run"] = time_large_run(7, None, args.large_steps, 50.0, local)
     if world == 1 and not args.no_cpu_baseline:
         sec, n = cpu_baseline(model0, dt)
         line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{n} RKHEVI steps of the same RES_ID={res} moist workload, FP64, "
-                                          f"median of steps after the first"}
+                                "sample": f"{n} RKHEVI steps of the same workload, FP64, OpenMP over "
+                                          f"{os.cpu_count()} host threads, median of steps after the first"}
+        line["cpu_1thread"] = one_thread_row(name, args.n_lloyd)
     print(json.dumps(line))
     barrier(world)
 
@@ -714,40 +856,99 @@ def column_study(args):
                     "gpu_launches": int(launches), "finite": bool(ok)}), flush=True)
 
 
+HEADLINE = "config3"
+
+
+def _cpu_steps(name, n_lloyd, warmup, steps):
+    """(median, mean) seconds per step of the oracle on the configuration's
+    prepared inputs, after warmup steps; OpenMP threads as the environment
+    sets them.  Loads only the oracle's library."""
+    from game_archived_gb300 import driver, workloads
+    from oracle.bind import Oracle
+    dt = workloads.CONFIGS[name][4]
+    tab, m = workloads.load(name, n_lloyd)
+    o = Oracle(m)
+    workloads.initial_state(name, tab, m, o)
+    driver.start(m, o.linear_combine_two_states)
+    t = 0.0
+    for _ in range(warmup):
+        driver.step(m, o.linear_combine_two_states, o.manage_rkhevi, dt, t)
+        t += dt
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        driver.step(m, o.linear_combine_two_states, o.manage_rkhevi, dt, t)
+        times.append(time.perf_counter() - t0)
+        t += dt
+    return statistics.median(times), sum(times) / len(times), times
+
+
+def cpu_one_thread(args):
+    """--cpu-one-thread: the oracle on one OpenMP thread (run as a child
+    process with OMP_NUM_THREADS=1); prints one JSON line"""
+    med, mean, _ = _cpu_steps(args.config, args.n_lloyd, 1, args.steps)
+    print(json.dumps({"threads": 1, "steps": args.steps, "median_s": med, "mean_s": mean}))
+
+
+def one_thread_row(name, n_lloyd, steps=2):
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-one-thread", "--config", name,
+                        "--steps", str(steps), "--n-lloyd", str(n_lloyd)], env=env, capture_output=True, text=True,
+                       timeout=900)
+    if r.returncode != 0:
+        return {"error": (r.stderr or r.stdout)[-300:]}
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    return {"value": 1.0 / d["median_s"], "unit": "steps/s", "cores": 1,
+            "sample": f"{steps} steps after 1 warm-up step, one OpenMP thread, median"}
+
+
 def run_reference(args):
+    """The CPU implementation of the same workload: the oracle (the reference's
+    algorithm restated in C with the reference's OpenMP loops, bit-identical to
+    the reference's own build where that compiles) on all host threads, on the
+    prepared inputs.  This process loads no library of the package: the grid
+    and layout come from the files build() prepared (numpy), the initial
+    state from the oracle's own operators."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from game_archived_gb300 import cases, driver
-    from oracle.bind import Oracle
-    res, dt = args.res, args.dt
-    tab, m = build_model(res, 1, args.n_lloyd, pinned=False)
-    o = Oracle(m)
-    cases.build_initial_state(m, tab, "jet_moist", o)
-    driver.start(m, o.linear_combine_two_states)
-    t = 0.0
-    n_warm = min(args.warmup, 1)
-    n_steps = max(1, min(args.steps, 4))
-    for _ in range(n_warm):
-        driver.step(m, o.linear_combine_two_states, o.manage_rkhevi, dt, t)
-        t += dt
-    t0 = time.perf_counter()
-    for _ in range(n_steps):
-        driver.step(m, o.linear_combine_two_states, o.manage_rkhevi, dt, t)
-        t += dt
-    sec = (time.perf_counter() - t0) / n_steps
-    value = 1.0 / sec
-    print(json.dumps({
+    from game_archived_gb300 import workloads
+    name = args.config
+    res, moist, case, mountain, dt, _ = workloads.CONFIGS[name]
+    if not workloads.available(name, args.n_lloyd):
+        print(json.dumps({"impl": "reference", "unavailable": "the benchmark inputs are not prepared: run "
+                                                              "__graft_entry__.build() first"}))
+        return
+    med, mean, times = _cpu_steps(name, args.n_lloyd, args.warmup, args.steps)
+    value = 1.0 / mean
+    g = grid_sizes(res)
+    line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
-        "steps": n_steps, "warmup": n_warm, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"RKHEVI step RES_ID={res}, 26 layers, moist, jet, dt={dt:g} s (CPU)"},
+        "config": {"workload": workload_text(name, res, g, dt), "precision": "FP64 (the reference's arithmetic)",
+                   "parallelism": "OpenMP over all host threads"},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{n_steps} steps after {n_warm} warm-up, OpenMP over all host threads; the "
-                                   "reference's own build cannot run on this host (its sources are not here), so "
-                                   "the oracle port, bit-identical to it, stands in"},
+                         "sample": f"{args.steps} steps after {args.warmup} warm-up steps (mean; median "
+                                   f"{1.0 / med:.4g} steps/s), OpenMP over {os.cpu_count()} host threads; the "
+                                   "oracle port, bit-identical to the reference's own build where that compiles "
+                                   "(the reference's sources do not travel to this host)"},
+        "cpu_1thread": one_thread_row(name, args.n_lloyd),
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }))
+    }
+    print(json.dumps(line))
+
+
+def workload_text(name, res, g, dt):
+    from game_archived_gb300 import workloads
+    _, moist, case, mountain, _, steps = workloads.CONFIGS[name]
+    what = {"baroclinic_moist": "moist (6 constituents), baroclinic jet of Jablonowski-Williamson (2006) in "
+                                "thermal-wind balance + N(0, 0.5 m/s) wind noise, RH 0.7 below 8 km",
+            "std_wind": "dry, ICAO standard atmosphere, u = 20 cos(lat) + N(0, 1 m/s)",
+            "std_wind_tpert": "dry, ICAO standard atmosphere + N(0, 1 K), u = 20 cos(lat) + N(0, 1 m/s)",
+            "tracers": "moist build, five constituents seeded log-normal x exp(-z / 3 km)"}[case]
+    return (f"RKHEVI step, {name}: RES_ID={res} ({g['nc']} cells, {g['ne']} edges), 26 layers, "
+            f"{'2 km Gaussian mountain' if mountain else 'flat'}, {what}, dt={dt:g} s")
 
 
 def main():
@@ -758,7 +959,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--res", type=int, default=6)
     ap.add_argument("--dt", type=float, default=100.0)
-    ap.add_argument("--n-lloyd", type=int, default=300)
+    ap.add_argument("--n-lloyd", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-diffusion", action="store_true")
@@ -766,9 +967,23 @@ def main():
     ap.add_argument("--adjoint-res", type=int, default=5)
     ap.add_argument("--no-large", action="store_true", help="skip the RES_ID=7 run with five constituents")
     ap.add_argument("--large-steps", type=int, default=1728)
+    ap.add_argument("--min-seconds", type=float, default=2.0,
+                    help="repeat the timed steps until each timed region covers this many seconds")
     ap.add_argument("--column-study", action="store_true",
                     help="time the column solvers at 26, 64 and 128 layers instead of the headline line")
+    ap.add_argument("--cpu-one-thread", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--ncu-json", help="summarise an ncu raw-page CSV into --out (see ncu_json)")
+    ap.add_argument("--out")
+    ap.add_argument("--command", default="", help="the capture command, recorded in the summary")
+    ap.add_argument("--captured", default="", help="what was captured (workload, commit state), recorded")
+    ap.add_argument("--config", default=HEADLINE)
     args = ap.parse_args()
+    if args.cpu_one_thread:
+        cpu_one_thread(args)
+        return
+    if args.ncu_json:
+        ncu_json(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.column_study:

@@ -18,6 +18,7 @@ SIGNATURES = {
     "game_gpu_set_resident": ([cint], cint),
     "game_gpu_set_graphs": ([cint], cint),
     "game_gpu_set_column_solver": ([cint], cint),
+    "game_gpu_set_column_arithmetic": ([cint], cint),
     "game_gpu_sync_to_device": ([vp], cint),
     "game_gpu_sync_to_host": ([vp], cint),
     "game_gpu_sync_aux_to_host": ([vp, vp, vp], cint),
@@ -130,7 +131,8 @@ class GpuError(RuntimeError):
 class GpuModel:
     """The CUDA library bound to a Model."""
 
-    def __init__(self, model, precision=FP64, resident=False, graphs=True, device=None, column_solver=0):
+    def __init__(self, model, precision=FP64, resident=False, graphs=True, device=None, column_solver=0,
+                 column_arithmetic=1):
         self.lib = native.gpu()
         self.m = model
         lay = model.layout
@@ -143,6 +145,7 @@ class GpuModel:
             self._check(self.lib.game_gpu_set_resident(1 if resident else 0), "set_resident")
             self._check(self.lib.game_gpu_set_graphs(1 if graphs else 0), "set_graphs")
             self._check(self.lib.game_gpu_set_column_solver(column_solver), "set_column_solver")
+            self._check(self.lib.game_gpu_set_column_arithmetic(column_arithmetic), "set_column_arithmetic")
         except GpuError:
             self.lib.game_gpu_finalize()
             raise

@@ -79,6 +79,7 @@ StepParams params_from_config(Context *c, const void *config, double dt)
     p.rain_velocity = *member<double>(config, GAME_CONFIG, "rain_velocity");
     p.cloud_velocity = *member<double>(config, GAME_CONFIG, "cloud_droplets_velocity");
     p.first_step = *member<int>(config, GAME_CONFIG, "totally_first_step_bool");
+    p.col_df = c->precision == PREC_MIXED && c->column_arith == 1 ? 1 : 0;
     p.inv_dt = 1.0 / dt;
     p.k_rows = 1.0 / (p.impl_thermo_weight * dt * dt * C_D_P);
     p.k_rows2 = 0.5 / (p.impl_thermo_weight * dt * C_D_P);
@@ -321,6 +322,15 @@ int game_gpu_set_column_solver(int mode)
         return fail("column solver mode must be 0 (by layer count and precision), 1 (per-thread Thomas sweeps) or 2 "
                     "(warp cyclic reduction)");
     ctx()->column_solver = mode;
+    return 0;
+}
+
+int game_gpu_set_column_arithmetic(int mode)
+{
+    if (check_ready(nullptr)) return -1;
+    if (mode < 0 || mode > 1)
+        return fail("column arithmetic must be 0 (FP64 eliminations) or 1 (double-float eliminations)");
+    ctx()->column_arith = mode;
     return 0;
 }
 

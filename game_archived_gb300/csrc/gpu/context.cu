@@ -587,6 +587,22 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
         for (size_t k = 0; k < ia.size(); ++k) ia[k] = h_areav[k] != 0.0 ? 1.0 / h_areav[k] : 0.0;
         c->inv_vol = dupload(c, iv);
         c->inv_area_v = dupload(c, ia);
+        /* double-float (hi, lo) pairs of the tracer solver's tables */
+        auto df_pairs = [](const std::vector<double> &x) {
+            std::vector<float> out(2 * x.size());
+            for (size_t k = 0; k < x.size(); ++k) {
+                const float hi = (float)x[k];
+                out[2 * k] = hi;
+                out[2 * k + 1] = (float)(x[k] - (double)hi);
+            }
+            return out;
+        };
+        c->dfg.area_v = (const float2 *)dupload(c, df_pairs(h_areav));
+        c->dfg.inv_area_v = (const float2 *)dupload(c, df_pairs(ia));
+        c->dfg.inv_vol = (const float2 *)dupload(c, df_pairs(iv));
+        c->dfg.volume = (const float2 *)dupload(c, df_pairs(h_vol));
+        c->dfg.exner_bg = (const float2 *)dupload(c, df_pairs(h_ebg));
+        c->dfg.theta_v_bg = (const float2 *)dupload(c, df_pairs(h_tbg));
         /* mixed-path sound-wave rows: dz, H, G1, G2, Cz, Ez per inner interface */
         const size_t ni = (size_t)(L - 1) * NC;
         std::vector<double> geo(6 * ni);
@@ -601,6 +617,9 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
             geo[5 * ni + q] = dz * iv[lo];
         }
         c->wv_geo = dupload(c, geo);
+        c->dfg.geo = (const float2 *)dupload(c, df_pairs(geo));
+        c->damp_inv_df = dalloc<float2>(c, ni);
+        c->dfg.damp_inv = c->damp_inv_df;
     }
     auto work = [&](auto &w, auto tag) {
         using R = decltype(tag);

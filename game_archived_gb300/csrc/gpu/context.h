@@ -147,6 +147,7 @@ struct Context {
      * 1 / (1 + dt * coefficient) for the values in damp_key (start height,
      * maximum coefficient, dt) */
     double *damp_dc = nullptr, *damp_inv = nullptr;
+    float2 *damp_inv_df = nullptr; /* damp_inv as double-float pairs */
     double damp_key[3] = {-1.0, -1.0, -1.0};
     /* grid terms of the mixed-path sound-wave rows [6][L-1][Nc] */
     double *wv_geo = nullptr;
@@ -168,6 +169,10 @@ struct Context {
     void (*obuf_release)(Context *) = nullptr;
     int use_graphs = 1;
     int column_solver = 0; /* 0 by layer count, 1 per-thread sweeps, 2 warp cyclic reduction */
+    /* arithmetic of the mixed path's vertical eliminations: 0 FP64, 1
+     * double-float (default) */
+    int column_arith = 1;
+    DfGrid dfg{};
     int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */
     long long h2d_bytes = 0, d2h_bytes = 0;
 

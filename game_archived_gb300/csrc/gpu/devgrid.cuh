@@ -115,6 +115,23 @@ struct SView {
     const R *rho, *rhotheta_v, *theta_v_pert, *exner_pert, *w, *u;
 };
 
+/* double-float copies (hi, lo) of vertical-solver tables, for the mixed
+ * path's double-float eliminations */
+struct DfGrid {
+    const float2 *area_v;     /* [L+1][Nc] */
+    const float2 *inv_area_v; /* [L+1][Nc] (0 where the area is 0) */
+    const float2 *inv_vol;    /* [L][Nc] */
+    const float2 *volume;     /* [L][Nc] */
+    const float2 *exner_bg;   /* [L][Nc] */
+    const float2 *theta_v_bg; /* [L][Nc] */
+    /* grid terms of the sound-wave rows [6][L-1][Nc] (as the FP64 table
+     * wv_geo: dz, H, G1, G2, Cz, Ez) */
+    const float2 *geo;
+    /* 1 / (1 + dt * Klemp coefficient) of the inner interfaces [L-1][Nc],
+     * for the time step the damping table was last made for */
+    const float2 *damp_inv;
+};
+
 /* FP32 shadow of state_new (mixed path); kernels that write the FP64 state
  * also write the shadow.  All pointers null on the FP64 path. */
 struct Shadow {
@@ -126,8 +143,10 @@ struct StepParams {
     int n_const, n_cond, moist, first_step;
     /* diffusion switches (DIFF_* bits) and whether the step adds the
      * irreversible terms (friction, dissipative and diffusive heating,
-     * radiation, mass diffusion) to its tendencies */
-    int diff, irr, pad_i0, pad_i1;
+     * radiation, mass diffusion) to its tendencies; col_df: the mixed path's
+     * vertical eliminations run in double-float arithmetic (dfloat.cuh)
+     * instead of FP64 */
+    int diff, irr, col_df, pad_i1;
     double dt;
     double impl_thermo_weight, damping_start_height, damping_coeff_max, toa;
     double snow_velocity, rain_velocity, cloud_velocity;

@@ -54,7 +54,7 @@ struct WavesWork {
  * parameters only, so it is tabulated once per parameter pair instead of
  * once per substage. */
 __global__ void k_damping_table(VGrid vg, double start_height, double coeff_max, double dt, double *dc,
-                                double *inv_den)
+                                double *inv_den, float2 *inv_den_df)
 {
     const long long n = (long long)(vg.nl - 1) * vg.nc, q = gtid();
     if (q >= n) return;
@@ -66,7 +66,10 @@ __global__ void k_damping_table(VGrid vg, double start_height, double coeff_max,
         r = coeff_max * (s * s);
     }
     dc[q] = r;
-    inv_den[q] = 1.0 / (1.0 + dt * r);
+    const double inv = 1.0 / (1.0 + dt * r);
+    inv_den[q] = inv;
+    const float hi = (float)inv;
+    inv_den_df[q] = make_float2(hi, (float)(inv - (double)hi));
 }
 
 template <bool EXACT>

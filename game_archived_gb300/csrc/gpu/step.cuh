@@ -10,6 +10,7 @@
 #include "diff.h"
 #include "kernels.cuh"
 #include "solvers.cuh"
+#include "solvers_df.cuh"
 
 namespace game {
 
@@ -143,6 +144,15 @@ void launch_waves(Context *c, const StepParams &p, StateMirror *so, StateMirror 
                   const Shadow &sh)
 {
     const long long ns = c->ns;
+    if constexpr (!EXACT) {
+        if (p.col_df && column_mode(c, EXACT, c->nc) == COLUMN_REGISTERS) {
+            ProfScope ps(c, "k_waves_df");
+            k_waves_df<NL_FIXED><<<nblocks(c->nc, 64), 64, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, c->dfg,
+                                                                           sh, rk);
+            c->kernel_launches++;
+            return;
+        }
+    }
     WavesWork ww = waves_work(c);
     {
         ProfScope ps(c, "k_waves_layer");
@@ -197,6 +207,14 @@ void launch_tracers(Context *c, const StepParams &p, StateMirror *so, StateMirro
         c->kernel_launches++;
     }
     ProfScope ps(c, "k_tracers_solve");
+    if constexpr (!EXACT) {
+        if (p.col_df && mode == COLUMN_REGISTERS) {
+            k_tracers_solve_df<NL_FIXED><<<nblocks(nsys, 64), 64, 0, strm>>>(c->vg, p, so->ds, sn->ds, st->ds, c->dfg,
+                                                                             sh.rho);
+            c->kernel_launches++;
+            return;
+        }
+    }
     if (mode == COLUMN_REGISTERS)
         k_tracers_solve<NL_FIXED, NL_FIXED, EXACT><<<nblocks(nsys, 64), 64, 0, strm>>>(c->vg, p, so->ds, sn->ds,
                                                                                         st->ds, tw, sh.rho);

@@ -18,7 +18,7 @@ int launch_damping_table(Context *c, const StepParams &p)
         return 0;
     const long long n = (long long)(c->nl - 1) * c->nc;
     k_damping_table<<<nblocks(n, 256), 256, 0, c->stream>>>(c->vg, p.damping_start_height, p.damping_coeff_max, p.dt,
-                                                            c->damp_dc, c->damp_inv);
+                                                            c->damp_dc, c->damp_inv, c->damp_inv_df);
     CK(cudaGetLastError());
     c->kernel_launches++;
     c->damp_key[0] = p.damping_start_height;

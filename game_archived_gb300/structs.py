@@ -43,6 +43,28 @@ class Layout:
     def dims_tuple(self):
         return (self.res_id, self.n_layers, self.moisture_on)
 
+    LAYOUT_KEYS = ("res_id", "n_layers", "moisture_on", "nc", "ne", "nt", "nl", "n_scalars", "n_vectors",
+                   "n_dual_vectors", "vpl", "dpl", "n_curl", "n_const", "n_cond", "n_latlon")
+
+    def to_dict(self):
+        """the layout as plain data (sizes, and every member's type, count and
+        offset), for a process that reads it without the native library"""
+        d = {k: getattr(self, k) for k in self.LAYOUT_KEYS}
+        d["members"] = {kind: {n: list(v) for n, v in mem.items()} for kind, mem in self.members.items()}
+        d["sizes"] = dict(self.sizes)
+        return d
+
+    @classmethod
+    def from_dict(cls, d):
+        lay = cls.__new__(cls)
+        for k in cls.LAYOUT_KEYS:
+            setattr(lay, k, d[k])
+        lay.members = {kind: {n: (bool(v[0]), int(v[1]), int(v[2])) for n, v in mem.items()}
+                       for kind, mem in d["members"].items()}
+        lay.sizes = {k: int(v) for k, v in d["sizes"].items()}
+        lay.dims = None
+        return lay
+
 
 class HostStruct:
     """One reference struct in host memory.  ``buffer`` may be supplied (for

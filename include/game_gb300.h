@@ -73,6 +73,11 @@ int game_gpu_set_graphs(int on);
  * 1 per-thread Thomas sweeps; 2 warp cyclic reduction in both precisions (a
  * different elimination order: the FP64 results move by rounding) */
 int game_gpu_set_column_solver(int mode);
+/* arithmetic of the mixed path's vertical eliminations (the tracer solve):
+ * 1 (default) double-float, two FP32 numbers per value carrying 48
+ * significand bits, which runs on the FP32 pipe (GB300 executes FP64 at 1/64
+ * of its FP32 rate); 0 FP64.  The FP64 path always eliminates in FP64. */
+int game_gpu_set_column_arithmetic(int mode);
 int game_gpu_sync_to_device(struct state *state);
 int game_gpu_sync_to_host(struct state *state);
 /* writes the library's copies of the lagged step fields back into the host
