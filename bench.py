@@ -305,7 +305,7 @@ def repeats_for(ms_per_step, steps, min_seconds):
 
 
 def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, profile=False, column_solver=0,
-                  mem_used=None, min_seconds=0.0, column_arithmetic=1, world=1, info=None):
+                  mem_used=None, min_seconds=0.0, double_float=1, world=1, info=None):
     """ms per step of the device-resident step; the timed region runs
     `steps` steps, repeated until it covers min_seconds (the estimate comes
     from a few untimed steps after the warm-up), between two barriers and
@@ -313,7 +313,7 @@ def time_resident(model0, precision, steps, warmup, dt, device, sampler=None, pr
     from game_archived_gb300 import abi, driver
     m = copy_model(model0, pinned=False)
     g = abi.GpuModel(m, precision, resident=True, graphs=True, device=device, column_solver=column_solver,
-                     column_arithmetic=column_arithmetic)
+                     double_float=double_float)
     try:
         for s in (m.state_old, m.state_new, m.state_tendency):
             g.sync_to_device(s)
@@ -715,7 +715,7 @@ def run_ours(args):
     barrier(world)
     # the mixed step with its vertical eliminations in FP64 (for comparison)
     ms32f, _, _, _, ok32f = time_resident(model0, abi.MIXED, args.steps, args.warmup, dt, local,
-                                          min_seconds=args.min_seconds, world=world, column_arithmetic=0,
+                                          min_seconds=args.min_seconds, world=world, double_float=0,
                                           info=i32f)
     barrier(world)
     sampler = ClockSampler(local)

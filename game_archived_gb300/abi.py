@@ -18,7 +18,7 @@ SIGNATURES = {
     "game_gpu_set_resident": ([cint], cint),
     "game_gpu_set_graphs": ([cint], cint),
     "game_gpu_set_column_solver": ([cint], cint),
-    "game_gpu_set_column_arithmetic": ([cint], cint),
+    "game_gpu_set_double_float": ([cint], cint),
     "game_gpu_sync_to_device": ([vp], cint),
     "game_gpu_sync_to_host": ([vp], cint),
     "game_gpu_sync_aux_to_host": ([vp, vp, vp], cint),
@@ -68,6 +68,10 @@ SIGNATURES = {
     "game_gpu_surface_pressure": ([vp, vp, vp], cint),
     "game_gpu_weighted_sums_noalloc": ([vp, cint, ctypes.c_longlong, vp, vp, vp], cint),
     "game_gpu_numerics": ([cint, vp, vp, ctypes.c_longlong], cint),
+    "game_gpu_check_state": ([vp, vp], cint),
+    "game_gpu_set_health_check": ([cint], cint),
+    "game_gpu_write_checkpoint": ([ctypes.c_char_p, vp, vp, vp, vp, vp], cint),
+    "game_gpu_read_checkpoint": ([ctypes.c_char_p, vp, vp, vp, vp, vp], cint),
     "grad_adj": ([vp] * 3, cint),
     "divv_h_adj": ([vp] * 3, cint),
     "divv_h_tracer_adj": ([vp] * 8, cint),
@@ -111,6 +115,13 @@ class OutputFields(ctypes.Structure):
     _fields_ = [(n, ctypes.POINTER(dbl)) for n, _ in OUTPUT_FIELDS]
 
 FP64, MIXED = 0, 1
+UNHEALTHY = 2
+
+
+class Health(ctypes.Structure):
+    """struct game_gpu_health (include/game_gb300.h)"""
+    _fields_ = [(n, ctypes.c_longlong) for n in ("nonfinite", "negative_density", "first_nonfinite",
+                                                 "first_negative_density")]
 
 
 def declare(lib):
@@ -132,7 +143,7 @@ class GpuModel:
     """The CUDA library bound to a Model."""
 
     def __init__(self, model, precision=FP64, resident=False, graphs=True, device=None, column_solver=0,
-                 column_arithmetic=1):
+                 double_float=1):
         self.lib = native.gpu()
         self.m = model
         lay = model.layout
@@ -145,7 +156,7 @@ class GpuModel:
             self._check(self.lib.game_gpu_set_resident(1 if resident else 0), "set_resident")
             self._check(self.lib.game_gpu_set_graphs(1 if graphs else 0), "set_graphs")
             self._check(self.lib.game_gpu_set_column_solver(column_solver), "set_column_solver")
-            self._check(self.lib.game_gpu_set_column_arithmetic(column_arithmetic), "set_column_arithmetic")
+            self._check(self.lib.game_gpu_set_double_float(double_float), "set_double_float")
         except GpuError:
             self.lib.game_gpu_finalize()
             raise
@@ -217,6 +228,28 @@ class GpuModel:
 
     def synchronize(self):
         self._check(self.lib.game_gpu_synchronize(), "synchronize")
+
+    # -- health check and checkpoints
+    def check_state(self, s):
+        """(status, report): status 0 healthy, UNHEALTHY (2) otherwise"""
+        r = Health()
+        rc = self.lib.game_gpu_check_state(s.ptr, ctypes.byref(r))
+        if rc not in (0, UNHEALTHY):
+            raise GpuError(f"check_state: {self.lib.game_gpu_last_error().decode()}")
+        return rc, {k: getattr(r, k) for k, _ in Health._fields_}
+
+    def set_health_check(self, every):
+        self._check(self.lib.game_gpu_set_health_check(every), "set_health_check")
+
+    def write_checkpoint(self, path, state):
+        m = self.m
+        self._check(self.lib.game_gpu_write_checkpoint(str(path).encode(), state.ptr, m.diagnostics.ptr,
+                                                       m.forcings.ptr, m.irrev.ptr, m.config.ptr), "write_checkpoint")
+
+    def read_checkpoint(self, path, state):
+        m = self.m
+        self._check(self.lib.game_gpu_read_checkpoint(str(path).encode(), state.ptr, m.diagnostics.ptr,
+                                                      m.forcings.ptr, m.irrev.ptr, m.config.ptr), "read_checkpoint")
 
     def kernel_launches(self, reset=False):
         return int(self.lib.game_gpu_kernel_launches(1 if reset else 0))

@@ -38,6 +38,20 @@ struct Bound {
 } g_bound;
 
 size_t off(int sid, const char *name) { return game_layout_offset(&ctx()->dims, sid, name); }
+}  // namespace
+
+namespace game {
+/* the lagged fields are imported again from the structs of the next step
+ * (after the caller's structs were overwritten, e.g. by a checkpoint) */
+void forget_imports()
+{
+    g_bound.aux_diag = g_bound.aux_forc = g_bound.aux_irrev = nullptr;
+    g_bound.diff_diag = g_bound.diff_forc = g_bound.diff_irrev = nullptr;
+    g_bound.diff_checked = g_bound.diff_imported = false;
+}
+}  // namespace game
+
+namespace {
 template <typename T>
 T *member(const void *base, int sid, const char *name)
 {
@@ -79,7 +93,7 @@ StepParams params_from_config(Context *c, const void *config, double dt)
     p.rain_velocity = *member<double>(config, GAME_CONFIG, "rain_velocity");
     p.cloud_velocity = *member<double>(config, GAME_CONFIG, "cloud_droplets_velocity");
     p.first_step = *member<int>(config, GAME_CONFIG, "totally_first_step_bool");
-    p.col_df = c->precision == PREC_MIXED && c->column_arith == 1 ? 1 : 0;
+    p.dfloat = c->precision == PREC_MIXED && c->double_float == 1 ? 1 : 0;
     p.inv_dt = 1.0 / dt;
     p.k_rows = 1.0 / (p.impl_thermo_weight * dt * dt * C_D_P);
     p.k_rows2 = 0.5 / (p.impl_thermo_weight * dt * C_D_P);
@@ -325,12 +339,12 @@ int game_gpu_set_column_solver(int mode)
     return 0;
 }
 
-int game_gpu_set_column_arithmetic(int mode)
+int game_gpu_set_double_float(int on)
 {
     if (check_ready(nullptr)) return -1;
-    if (mode < 0 || mode > 1)
-        return fail("column arithmetic must be 0 (FP64 eliminations) or 1 (double-float eliminations)");
-    ctx()->column_arith = mode;
+    if (on < 0 || on > 1)
+        return fail("game_gpu_set_double_float: 0 (FP64) or 1 (double-float) expected");
+    ctx()->double_float = on;
     return 0;
 }
 
@@ -586,7 +600,10 @@ int manage_rkhevi(struct state *state_old, struct state *state_new, struct grid 
         if (tend_async) CK(cudaStreamWaitEvent(c->stream, c->ev_tend_copied, 0));
         else if (download_state(state_tendency, st, 1 | 2 | 16)) return -1;
     }
-    return finish();
+    if (finish()) return -1;
+    if (c->health_every > 0 && ++c->health_count % c->health_every == 0)
+        return check_mirror(c, sn, nullptr, "manage_rkhevi: state_new");
+    return 0;
 }
 
 int linear_combine_two_states(struct state *state_0, struct state *state_1, struct state *state_out, double coeff_0,

@@ -678,6 +678,7 @@ int destroy_context()
     for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
     for (auto &kv : c->states) cudaFree(kv.second.dev);
     for (auto &b : c->owned) cudaFree(b.p);
+    if (c->health) cudaFree(c->health);
     delete c->dbuf;
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->stream2) cudaStreamDestroy(c->stream2);

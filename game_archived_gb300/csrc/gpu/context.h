@@ -15,6 +15,8 @@
 #include "devgrid.cuh"
 #include "layout.h"
 
+struct game_gpu_health; /* include/game_gb300.h */
+
 namespace game {
 
 struct AdjState;
@@ -169,10 +171,15 @@ struct Context {
     void (*obuf_release)(Context *) = nullptr;
     int use_graphs = 1;
     int column_solver = 0; /* 0 by layer count, 1 per-thread sweeps, 2 warp cyclic reduction */
-    /* arithmetic of the mixed path's vertical eliminations: 0 FP64, 1
-     * double-float (default) */
-    int column_arith = 1;
+    /* arithmetic of the mixed path's vertical eliminations and tendency
+     * assembly: 0 FP64, 1 double-float (default) */
+    int double_float = 1;
     DfGrid dfg{};
+    /* health check: device counters, and the step interval of the automatic
+     * check in manage_rkhevi (0 off) */
+    unsigned long long *health = nullptr;
+    int health_every = 0;
+    long long health_count = 0;
     int kernel_launches = 0;  /* launches of this library's kernels since the counter was reset */
     long long h2d_bytes = 0, d2h_bytes = 0;
 
@@ -236,6 +243,10 @@ int download_state_pinned(const void *host_state, StateMirror *m, int which_mask
 int upload_field(const double *host, double *dev, const int *map, long long n, long long host_len);
 int download_field(double *host, const double *dev, const int *map, long long n, long long host_len,
                    long long host_lo, long long host_hi);
+
+/* health check of a State mirror (health.cu): 0 healthy, GAME_GPU_UNHEALTHY
+ * with the message set, -1 on a CUDA error */
+int check_mirror(Context *c, StateMirror *m, struct game_gpu_health *report, const char *what);
 
 /* the step on device mirrors (step.cu templates) */
 int run_step(Context *c, StateMirror *so, StateMirror *sn, StateMirror *st, const void *config, double dt);

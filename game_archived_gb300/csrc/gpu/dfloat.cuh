@@ -34,7 +34,7 @@
  */
 #pragma once
 
-#include "kernels.cuh"
+#include "numeric.cuh"
 
 namespace game {
 namespace {
@@ -63,6 +63,15 @@ __device__ __forceinline__ df two_prod(float a, float b)
 }
 
 __device__ __forceinline__ df df_of(float x) { return {x, 0.0f}; }
+__device__ __forceinline__ df df_one() { return {1.0f, 0.0f}; }
+__device__ __forceinline__ df df_zero() { return {0.0f, 0.0f}; }
+__device__ __forceinline__ df df_half(df x) { return {0.5f * x.hi, 0.5f * x.lo}; } /* exact */
+/* a (hi, lo) table entry */
+__device__ __forceinline__ df ld_df(const float2 *t, long long i)
+{
+    const float2 v = t[i];
+    return {v.x, v.y};
+}
 __device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
 
 /* AccurateDWPlusDW */

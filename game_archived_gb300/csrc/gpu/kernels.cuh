@@ -25,86 +25,13 @@
 #include <cuda_runtime.h>
 
 #include "devgrid.cuh"
+#include "dfloat.cuh"
+#include "numeric.cuh"
 
 namespace game {
 /* internal linkage: the FP64 and the mixed translation unit each compile
  * their own copy with their own contraction flags */
 namespace {
-
-/* ------------------------------------------------------------ utilities */
-__device__ __forceinline__ long long gtid() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
-
-/* FP64 reciprocal for the mixed path (the FP64 path divides exactly as the
- * reference).  The seed is the hardware's approximate reciprocal (PTX
- * rcp.approx.ftz.f64; relative error below 2^-20, measured on GB300 over
- * 2^20 inputs spanning 1e-300..1e300), refined by Newton-Raphson steps
- * r <- r + r (1 - x r), each of which squares the relative error: one step
- * leaves about 2^-40, two steps are within one ulp of the correctly rounded
- * reciprocal and equal to it on all but a few inputs (tested against IEEE
- * 1.0 / x on 2^20 sampled inputs and edge values: only x = 1 - 2^-53, whose
- * reciprocal lies just above the midpoint of two doubles, came out one ulp
- * off).  One multiply-add pair per step
- * instead of the several FP64 operations of an IEEE division, on a GPU whose
- * FP64 rate is 1/64 of FP32.
- * x must be a normal number whose reciprocal is normal (ftz). */
-template <int STEPS>
-__device__ __forceinline__ double rcp_nr(double x)
-{
-    double r;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-#pragma unroll
-    for (int s = 0; s < STEPS; ++s) r = fma(r, fma(-x, r, 1.0), r);
-    return r;
-}
-
-/* x >= 0 for the solvers' branch and clip tests.  The FP64 path compares as
- * the reference does; the mixed path reads the sign bit on the integer pipe
- * instead of issuing an FP64 comparison (FP64 issues at 1/64 of the FP32
- * rate on this GPU).  The two differ only at -0, where every branch they
- * select between yields the same values up to the sign of a zero term. */
-template <bool EXACT>
-__device__ __forceinline__ bool nonneg(double x)
-{
-    return EXACT ? x >= 0.0 : __double2hiint(x) >= 0;
-}
-
-/* double -> float rounded to nearest even, by integer operations for values
- * whose float is a normal number (or overflows to infinity by rounding);
- * zeros, subnormals, infinities and NaNs go through the conversion
- * instruction.  The same bits as float(x); used by the mixed path where it
- * writes its FP32 shadow from FP64 results, to keep the conversion off the
- * FP64 pipe. */
-__device__ __forceinline__ float to_float(double x)
-{
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
-    if (e - 897u <= 253u) { /* float exponent field e - 896 in [1, 254] */
-        const unsigned long long m = b & 0xfffffffffffffULL;
-        unsigned r = ((unsigned)(b >> 63) << 31) | ((e - 896u) << 23) | (unsigned)(m >> 29);
-        const unsigned rem = (unsigned)(m & 0x1fffffffULL), half = 0x10000000u;
-        r += (rem > half || (rem == half && (r & 1u))) ? 1u : 0u;
-        return __uint_as_float(r);
-    }
-    return __double2float_rn(x);
-}
-
-/* float -> double (exact) by integer operations for normal numbers and
- * zeros; subnormals, infinities and NaNs through the conversion instruction.
- * The same bits as double(x); the mixed path widens its FP32 sums and
- * products with it before the FP64 accumulation, keeping the conversion off
- * the FP64 pipe.  wide() is the identity on double. */
-__device__ __forceinline__ double to_double(float x)
-{
-    const unsigned u = __float_as_uint(x);
-    const unsigned fe = (u >> 23) & 0xffu;
-    if (fe - 1u <= 253u) /* normal */
-        return __hiloint2double((int)((u & 0x80000000u) | ((fe + 896u) << 20) | ((u >> 3) & 0xfffffu)),
-                                (int)(u << 29));
-    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    return (double)x;
-}
-__device__ __forceinline__ double wide(float x) { return to_double(x); }
-__device__ __forceinline__ double wide(double x) { return x; }
 
 template <typename R>
 __device__ __forceinline__ R ipw_at(const HGrid<R> &g, int j, int l, int c)
@@ -995,9 +922,15 @@ template <typename R, bool IRR>
 __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, SView<R> sv, DState st,
                                                       const R *theta, const R *cp_ice, const R *cp_water,
                                                       const double *pt_rates, const double *pt_heat,
-                                                      const double *sed_heat, const double *inv_vol_tab, int rk,
-                                                      IrrTerms irr)
+                                                      const double *sed_heat, const double *inv_vol_tab,
+                                                      const float2 *inv_vol_df, int rk, IrrTerms irr)
 {
+    /* mixed path with p.dfloat: the divergences are scaled and the
+     * tendencies assembled in double-float (dfloat.cuh) instead of FP64 --
+     * the same operations in the same order, on the FP32 pipe -- and each
+     * tendency is joined to FP64 once */
+    constexpr bool MIXED = sizeof(R) == sizeof(float);
+    const bool dfl = MIXED && p.dfloat;
     const long long ns = (long long)g.nl * g.nc;
     const long long i = gtid();
     if (i >= ns) return;
@@ -1018,11 +951,17 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
         return R(-0.5) * ipw_at(g, j, ll, c) * g.slope_h[(long long)ll * ne + edge(j)];
     };
     auto uval = [&](int ll, int j) { return sv.u[(long long)ll * ne + edge(j)]; };
-    auto comp_v = [&](R up, R lo) -> double {
-        if (!oro) return 0.0;
-        if (l == nl - n_oro - 1) return wide(-lo * area_lo);
-        if (l == nl - 1) return wide(up * area_up);
-        return wide(up * area_up - lo * area_lo);
+    auto comp_r = [&](R up, R lo) -> R {
+        if (!oro) return R(0);
+        if (l == nl - n_oro - 1) return -lo * area_lo;
+        if (l == nl - 1) return up * area_up;
+        return up * area_up - lo * area_lo;
+    };
+    auto comp_v = [&](R up, R lo) -> double { return oro ? wide(comp_r(up, lo)) : 0.0; };
+    /* the flux sum of a FluxSum<float> and a correction as a double-float */
+    auto dw = [&](const FluxSum<R> &f, R corr) -> df {
+        if constexpr (MIXED) return df_add(two_sum(f.hi, f.lo), df_of(corr));
+        else return df_zero();
     };
     /* terrain correction of the wind at levels l and l+1 (shared by the tracers) */
     R w_up = R(0), w_lo = R(0);
@@ -1073,6 +1012,39 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
         if (up_has_prev) layer_pass(l - 1, false, true, false);
         layer_pass(l, true, up_corr, lo_has_curr);
         if (lo_corr) layer_pass(l + 1, false, false, true);
+        if (dfl) {
+            const df ivd = ld_df(inv_vol_df, i);
+            df y = df_neg(df_mul(ivd, dw(hm, comp_r(um, lm))));
+            if (IRR) y = df_add(y, df_from_double(irr.mass_diff[cond * ns + i]));
+            if (p.moist) y = df_add(y, df_from_double(pt_rates[cond * ns + i]));
+            /* at rk 1 the reference blends 0 x old + 1 x new: the new value */
+            st.rho[cond * ns + i] = df_to_double(y);
+            df yt = df_neg(df_mul(ivd, dw(ht, comp_r(ut, lt))));
+            if (p.moist || IRR) {
+                R cv = R(0);
+                for (int kk = 0; kk < cond; ++kk)
+                    cv += sv.rho[kk * ns + i] * ((kk % 2 == 0) ? cp_ice[i] : cp_water[i]);
+                cv += sv.rho[cond * ns + i] * R(C_D_V);
+                if (p.moist) cv += sv.rho[(cond + 1) * ns + i] * R(C_V_V);
+                df heat, rate = df_from_double(pt_rates[cond * ns + i]);
+                if (IRR) {
+                    heat = df_add(df_add(df_add(df_add(df_from_double(irr.heating_diss[i]),
+                                                       df_from_double(irr.temp_diff_heating[i])),
+                                                df_from_double(irr.radiation[i])),
+                                         df_from_double(pt_heat[i])),
+                                  df_from_double(sed_heat[i]));
+                    rate = df_add(rate, df_from_double(irr.mass_diff[cond * ns + i]));
+                } else {
+                    heat = df_add(df_from_double(pt_heat[i]), df_from_double(sed_heat[i]));
+                }
+                const float fac =
+                    float(R(C_D_V) * sv.rho[cond * ns + i] / cv / (R(C_D_P) * (g.exner_bg[i] + sv.exner_pert[i])));
+                yt = df_add(df_add(yt, df_mul_f(heat, fac)), df_mul_f(rate, float(theta[i])));
+            }
+            st.rhotheta_v[i] = df_to_double(yt);
+            goto tracers;
+        }
+        {
         const double div = inv_vol * (hm.value() + comp_v(um, lm));
         double y = -div;
         if (IRR) y = y + irr.mass_diff[cond * ns + i];
@@ -1101,7 +1073,9 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
             }
         }
         st.rhotheta_v[i] = rk == 0 ? yt : 0.0 * st.rhotheta_v[i] + 1.0 * yt;
+        }
     }
+tracers:
     if (p.n_const == 1) return;
     /* the other constituents: upstream flux.  The cell's edges, neighbours,
      * orientation and layer-l wind and face areas are loaded once for all
@@ -1133,21 +1107,34 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
             const R a = fv * arj[j];
             h.add(sfj[j] ? a : -a);
         }
-        double cv = 0.0;
+        R cvr = R(0);
         if (oro) {
             const R d_here = f[i];
             if (l == nl - n_oro - 1) {
                 const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
-                cv = wide(-d_lo * w_lo * area_lo);
+                cvr = -d_lo * w_lo * area_lo;
             } else if (l == nl - 1) {
                 const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
-                cv = wide(d_up * w_up * area_up);
+                cvr = d_up * w_up * area_up;
             } else {
                 const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
                 const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
-                cv = wide(d_up * w_up * area_up - d_lo * w_lo * area_lo);
+                cvr = d_up * w_up * area_up - d_lo * w_lo * area_lo;
             }
         }
+        if (dfl) {
+            df y = df_neg(df_mul(ld_df(inv_vol_df, i), dw(h, cvr)));
+            if (IRR) y = df_add(y, df_from_double(irr.mass_diff[k * ns + i]));
+            if (p.moist) {
+                long long pt = k * ns;
+                if (k == cond + 1) pt -= ns;
+                y = df_add(y, df_from_double(pt_rates[pt + i]));
+            }
+            if (rk != 0) y = df_add(df_half(df_from_double(st.rho[k * ns + i])), df_half(y));
+            st.rho[k * ns + i] = df_to_double(y);
+            continue;
+        }
+        const double cv = oro ? wide(cvr) : 0.0;
         const double div = inv_vol * (h.value() + cv);
         double y = -div;
         if (IRR) y = y + irr.mass_diff[k * ns + i];

@@ -30,14 +30,6 @@
 namespace game {
 namespace {
 
-__device__ __forceinline__ df ld_df(const float2 *t, long long i)
-{
-    const float2 v = t[i];
-    return {v.x, v.y};
-}
-
-__device__ __forceinline__ df df_one() { return {1.0f, 0.0f}; }
-__device__ __forceinline__ df df_zero() { return {0.0f, 0.0f}; }
 
 template <int NL>
 __global__ void __launch_bounds__(64) k_tracers_solve_df(VGrid vg, StepParams p, DState so, DState sn, DState st,
@@ -137,8 +129,6 @@ __global__ void __launch_bounds__(64) k_tracers_solve_df(VGrid vg, StepParams p,
         rs[(long long)j * nc + i] = v.hi;
     }
 }
-
-__device__ __forceinline__ df df_half(df x) { return {0.5f * x.hi, 0.5f * x.lo}; } /* exact */
 
 /* per-layer quantities of the sound-wave solve (the mixed-path forms of
  * k_waves_layer, solvers.cuh), at layer j of column i */

@@ -145,7 +145,7 @@ void launch_waves(Context *c, const StepParams &p, StateMirror *so, StateMirror 
 {
     const long long ns = c->ns;
     if constexpr (!EXACT) {
-        if (p.col_df && column_mode(c, EXACT, c->nc) == COLUMN_REGISTERS) {
+        if (p.dfloat && column_mode(c, EXACT, c->nc) == COLUMN_REGISTERS) {
             ProfScope ps(c, "k_waves_df");
             k_waves_df<NL_FIXED><<<nblocks(c->nc, 64), 64, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, c->dfg,
                                                                            sh, rk);
@@ -208,7 +208,7 @@ void launch_tracers(Context *c, const StepParams &p, StateMirror *so, StateMirro
     }
     ProfScope ps(c, "k_tracers_solve");
     if constexpr (!EXACT) {
-        if (p.col_df && mode == COLUMN_REGISTERS) {
+        if (p.dfloat && mode == COLUMN_REGISTERS) {
             k_tracers_solve_df<NL_FIXED><<<nblocks(nsys, 64), 64, 0, strm>>>(c->vg, p, so->ds, sn->ds, st->ds, c->dfg,
                                                                              sh.rho);
             c->kernel_launches++;
@@ -318,12 +318,12 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             if (p.irr) {
                 const DiffBufs &b = *c->dbuf;
                 k_scalar_tend2<R, true><<<nblocks(ns, 128), 128, 0, c->stream>>>(
-                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol, rk,
-                    IrrTerms{b.hdiss, b.tdh, b.rad, b.mdt});
+                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol,
+                    c->dfg.inv_vol, rk, IrrTerms{b.hdiss, b.tdh, b.rad, b.mdt});
             } else {
                 k_scalar_tend2<R, false><<<nblocks(ns, 128), 128, 0, c->stream>>>(
-                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol, rk,
-                    IrrTerms{});
+                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol,
+                    c->dfg.inv_vol, rk, IrrTerms{});
             }
         }
         c->kernel_launches += 2;

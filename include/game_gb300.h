@@ -73,11 +73,13 @@ int game_gpu_set_graphs(int on);
  * 1 per-thread Thomas sweeps; 2 warp cyclic reduction in both precisions (a
  * different elimination order: the FP64 results move by rounding) */
 int game_gpu_set_column_solver(int mode);
-/* arithmetic of the mixed path's vertical eliminations (the tracer solve):
- * 1 (default) double-float, two FP32 numbers per value carrying 48
- * significand bits, which runs on the FP32 pipe (GB300 executes FP64 at 1/64
- * of its FP32 rate); 0 FP64.  The FP64 path always eliminates in FP64. */
-int game_gpu_set_column_arithmetic(int mode);
+/* arithmetic of the mixed path's FP64 parts -- the vertical eliminations
+ * (sound waves, tracers) and the assembly of the scalar tendencies from
+ * their accumulated flux divergences: 1 (default) double-float, two FP32
+ * numbers per value carrying 48 significand bits, which runs on the FP32
+ * pipe (GB300 executes FP64 at 1/64 of its FP32 rate); 0 FP64.  The state
+ * stays FP64 either way; the FP64 path never uses double-float. */
+int game_gpu_set_double_float(int on);
 int game_gpu_sync_to_device(struct state *state);
 int game_gpu_sync_to_host(struct state *state);
 /* writes the library's copies of the lagged step fields back into the host
@@ -112,6 +114,44 @@ int game_gpu_profile_get(int i, const char **name, double *ms, long long *launch
  * and in[n + i]; in and out are double arrays except the float side of ops
  * 3 to 6 */
 int game_gpu_numerics(int op, const void *in, void *out, long long n);
+/* ---- health check and checkpoints (no counterpart in the reference's
+ * library interface; see each) ---- */
+enum { GAME_GPU_UNHEALTHY = 2 };
+struct game_gpu_health {
+    long long nonfinite;              /* NaN or +-Inf values anywhere in the State */
+    long long negative_density;       /* negative values among the constituent densities */
+    long long first_nonfinite;        /* position of the first, in doubles from the start of the State, or -1 */
+    long long first_negative_density; /* likewise */
+};
+/* Counts non-finite values and negative densities of a State on the device
+ * (its device copy in resident mode, else the host struct uploaded first).
+ * Returns 0 when there are none, GAME_GPU_UNHEALTHY (message in
+ * game_gpu_last_error) when there are, -1 on a CUDA error.  The reference
+ * aborts on negative densities when it reads a state
+ * (src/io/set_initial_state.c:318-328) and clips its tracer solutions at zero
+ * (src/time_stepping/column_solvers.c:621-627), so either count being nonzero
+ * after a step means the run has broken down. */
+int game_gpu_check_state(struct state *state, struct game_gpu_health *report);
+/* every > 0: manage_rkhevi checks state_new after every every-th call and
+ * returns GAME_GPU_UNHEALTHY if the check fails (the step's results are still
+ * written); 0 (default) switches the check off */
+int game_gpu_set_health_check(int every);
+/* A checkpoint for a bit-identical resume: the State the next step starts
+ * from (state_new after a step) with the whole Diagnostics, Forcings,
+ * Irreversible_quantities and Config structs, after the library's device
+ * copies of the lagged step fields are written back into them.  The
+ * reference's restart reads a State only (src/io/set_initial_state.c:244-336)
+ * and so starts from recomputed lagged fields; a run resumed from this
+ * checkpoint -- read into the host structs by game_gpu_read_checkpoint, in
+ * this process or in a new one with the same grid -- continues the
+ * uninterrupted run bit for bit.  read_checkpoint refuses a file written for
+ * another RES_ID, layer count or moisture build, or whose digest does not
+ * match; in resident mode it also uploads the State. */
+int game_gpu_write_checkpoint(const char *path, struct state *state, struct diagnostics *diagnostics,
+                              struct forcings *forcings, struct irreversible_quantities *irrev, struct config *config);
+int game_gpu_read_checkpoint(const char *path, struct state *state, struct diagnostics *diagnostics,
+                             struct forcings *forcings, struct irreversible_quantities *irrev, struct config *config);
+
 /* bytes copied host->device and device->host by the library */
 int game_gpu_transfer_bytes(long long *h2d, long long *d2h, int reset);
 

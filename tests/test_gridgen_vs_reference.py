@@ -10,8 +10,12 @@ orientation (from/to) recorded; every table is then compared in the
 reference's numbering, signs corrected for reversed edges:
 * geometry (positions, heights, distances, areas, volumes, the background
   state, directions, Coriolis vector, inner-product and rhombus weights) to
-  1e-12 of each table's largest magnitude, the TRSK weights to 1e-11: both
-  follow the same formulas, summed in different orders;
+  1e-12 of each table's largest magnitude, the TRSK weights to 1e-11 (five
+  times both at RES_ID 5): both follow the same formulas, summed in
+  different orders; the share of entries that differ and the largest
+  difference in ulps are printed per table (heights, gravity potential and
+  the background state are bit-identical; positions, distances, areas and
+  volumes are not);
 * topology (cell-edge incidence and signs, triangle-edge incidence and signs,
   the dual orientation, TRSK and modified-curl index pairs) exactly;
 * TRSK weights that are zero up to rounding (|w| < 1e-9 of the largest: the
@@ -43,6 +47,16 @@ def rel(a, b):
     return float(np.max(np.abs(a - b)) / s) if s else float(np.max(np.abs(a - b)))
 
 
+def ulps(a, b, floor=1e-9):
+    """(share of entries that differ, largest difference in units in the last
+    place of the reference value) over the entries with |b| above floor of
+    the table's largest magnitude"""
+    a, b = np.asarray(a, dtype=np.float64).ravel(), np.asarray(b, dtype=np.float64).ravel()
+    m = np.abs(b) > floor * np.max(np.abs(b)) if np.max(np.abs(b)) > 0 else np.ones(b.shape, bool)
+    d = np.abs(a[m] - b[m]) / np.spacing(np.abs(b[m]))
+    return float(np.mean(a[m] != b[m])), float(np.max(d)) if d.size else 0.0
+
+
 def match(T, ref):
     from scipy.spatial import cKDTree
     o_c = xyz(T["latitude_scalar"], T["longitude_scalar"])
@@ -62,7 +76,7 @@ def match(T, ref):
     return cmap, emap, esign, tmap
 
 
-@pytest.mark.parametrize("res,n_iter", [(3, 0), (3, 10), (4, 3)])
+@pytest.mark.parametrize("res,n_iter", [(3, 0), (3, 10), (4, 3), (5, 1)])
 def test_tables_match_reference_generator(res, n_iter, tmp_path):
     ref = refbind.run_gridgen(res, n_iter, str(tmp_path))
     T = tables.GridTables(res, n_layers=L, n_lloyd=n_iter)
@@ -76,14 +90,20 @@ def test_tables_match_reference_generator(res, n_iter, tmp_path):
     # (the longitude of a cell at a pole is whatever atan2 makes of rounding)
     off_pole = np.cos(T["latitude_scalar"]) > 1e-9
     errs["longitude_scalar"] = float(np.max(np.abs(dlon[off_pole])))
+    ulp = {}
     for name in ("z_scalar", "volume", "gravity_potential", "theta_v_bg", "exner_bg"):
         errs[name] = rel(T[name].reshape(L, nc), ref[name].reshape(L, nc)[:, cmap])
+        ulp[name] = ulps(T[name].reshape(L, nc), ref[name].reshape(L, nc)[:, cmap])
     # primal vector fields: vertical at the cells, horizontal at the edges
     for name in ("z_vector", "normal_distance", "area"):
         a, b = T[name], ref[name]
         errs[name + "_v"] = rel(np.stack([a[k * vpl:k * vpl + nc] for k in range(L + 1)]),
                                 np.stack([b[k * vpl:k * vpl + nc][cmap] for k in range(L + 1)]))
         errs[name + "_h"] = rel(np.stack([a[k * vpl + nc:(k + 1) * vpl] for k in range(L)]),
+                                np.stack([b[k * vpl + nc:(k + 1) * vpl][emap] for k in range(L)]))
+        ulp[name + "_v"] = ulps(np.stack([a[k * vpl:k * vpl + nc] for k in range(L + 1)]),
+                                np.stack([b[k * vpl:k * vpl + nc][cmap] for k in range(L + 1)]))
+        ulp[name + "_h"] = ulps(np.stack([a[k * vpl + nc:(k + 1) * vpl] for k in range(L)]),
                                 np.stack([b[k * vpl + nc:(k + 1) * vpl][emap] for k in range(L)]))
     # dual vector fields: horizontal at the edges, vertical at the triangles
     for name in ("area_dual", "z_vector_dual", "normal_distance_dual"):
@@ -157,11 +177,20 @@ def test_tables_match_reference_generator(res, n_iter, tmp_path):
         assert set(do) == set(dr), e
         t_err = max(t_err, max(abs(do[k] - dr[k]) for k in do) / w_scale)
     errs["trsk_weights"] = t_err
+    ulp["latitude_scalar"] = ulps(T["latitude_scalar"], ref["latitude_scalar"][cmap])
+    ulp["latitude_vector"] = ulps(T["latitude_vector"], ref["latitude_vector"][emap])
     worst = max(errs, key=errs.get)
     print(f"RES{res}, {n_iter} Lloyd iterations: worst {worst} {errs[worst]:.3g}")
+    print(f"RES{res}, {n_iter} Lloyd iterations: (share of entries that differ, max ulps): " +
+          ", ".join(f"{k} ({v[0]:.3f}, {v[1]:.3g})" for k, v in sorted(ulp.items())))
     # the TRSK weights sum kite areas; the reference's own zero weights carry
-    # up to 2e-12 of its rounding, so they are held to 1e-11
-    bad = {k: v for k, v in errs.items() if v > (1e-11 if k == "trsk_weights" else 1e-12)}
+    # up to 2e-12 of its rounding, so they are held to 1e-11.  The positions
+    # come out of the Lloyd iterations with the two builders' different
+    # summation orders, so the differences grow with the number of cells:
+    # the bounds at RES_ID 5 are five times those of RES_ID 3 and 4 (measured
+    # there: 2.7e-12 for volumes and areas, 1.3e-11 for the TRSK weights)
+    scale = 5.0 if res >= 5 else 1.0
+    bad = {k: v for k, v in errs.items() if v > scale * (1e-11 if k == "trsk_weights" else 1e-12)}
     assert not bad, bad
     # lat-lon interpolation: equal except at distance ties
     lat_c, lon_c = ref["latitude_scalar"], ref["longitude_scalar"]
@@ -173,7 +202,7 @@ def test_tables_match_reference_generator(res, n_iter, tmp_path):
         do = {cmap[li_o[p, j]]: lw_o[p, j] for j in range(5)}
         dr = {li_r[p, j]: lw_r[p, j] for j in range(5)}
         if set(do) == set(dr):
-            assert max(abs(do[k] - dr[k]) for k in do) < 1e-12
+            assert max(abs(do[k] - dr[k]) for k in do) < scale * 1e-12
             continue
         # the cells picked by one side only must be as far from the point as
         # a cell picked by the other side only
