@@ -103,12 +103,6 @@ def kernel_bytes(res, n_const, r, nl=L):
     out["k_waves_rows"] = (2 * (14 * wi + 8 * s) * d, 2)
     out["k_waves_thomas"] = (2 * 6 * wi * d, 2)
     out["k_waves_apply"] = (2 * ((4 * wi + 12 * s + 2 * wl) * d + (4 * s + wi) * r), 2)
-    # the fused double-float sound-wave solve: state old (rho_gas, rho theta_v,
-    # theta_v', Pi', w), new (rho_gas, rho theta_v, Pi'), tendency (rho_gas,
-    # rho theta_v, w), tables (1/V, V, Pi_bg, theta_v_bg, six row terms, the
-    # damping factor, 1/A of the interfaces) read; the new rho_gas, rho
-    # theta_v, theta_v', Pi' and the inner w written with their FP32 shadow
-    out["k_waves_df"] = (2 * ((17 * s + 3 * wl + 8 * wi) * d + (4 * s + wi) * r), 2)
     if moist:
         out["k_tracers_solve"] = (2 * ((3 * (C - 1) * s + 3 * wl + s) * d + (C - 1) * s * r), 2)
         out["k_tracers_sedheat"] = ((((C - 2) + 5) * s + 2 * wl) * d, 1)
@@ -939,6 +933,47 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def all_configs(args):
+    """--all-configs: one JSON line per benchmark configuration (config1 ..
+    config5): device-resident steps/s of the FP64 and the mixed step, the
+    CPU oracle on all host threads and on one thread (bounded samples), on
+    the configuration's own grid, state and time step"""
+    from game_archived_gb300 import abi, workloads
+    from game_archived_gb300.ops import CAbiOps
+    _, _, local = dist_env()
+    for name in args.configs.split(","):
+        res, moist, case, mountain, dt, steps = workloads.CONFIGS[name]
+        workloads.prepare(name)
+        tab, m = workloads.load(name)
+        g = abi.GpuModel(m, abi.FP64, device=local)
+        try:
+            workloads.initial_state(name, tab, m, CAbiOps(g.lib, m))
+        finally:
+            g.close()
+        k = min(steps, args.steps)
+        line = {"config": name, "workload": workload_text(name, res, grid_sizes(res), dt), "steps_per_block": k}
+        mem = []
+        for prec, key in ((abi.FP64, "gpu_fp64"), (abi.MIXED, "gpu_mixed")):
+            info = {}
+            ms, _, _, _, ok = time_resident(m, prec, k, args.warmup, dt, local, min_seconds=args.min_seconds,
+                                            info=info, mem_used=mem)
+            line[key] = {"steps_per_s": 1000.0 / ms, "ms_per_step": ms, "timed_steps": info["timed_steps"],
+                         "finite": ok}
+        line["mixed_over_fp64"] = line["gpu_fp64"]["ms_per_step"] / line["gpu_mixed"]["ms_per_step"]
+        line["device_bytes_in_use"] = max(mem) if mem else None
+        peak, _ = measured_peak()
+        b = b_step(res, m.layout.n_const, 8, 8, 4)
+        line["roofline_step_mixed"] = {"algorithmic_bytes": b, "frac": b / (line["gpu_mixed"]["ms_per_step"] * 1e-3)
+                                       / 1e9 / peak}
+        if not args.no_cpu_baseline:
+            n_cpu = {4: 6, 5: 4, 6: 3, 7: 2}.get(res, 2)
+            med, mean, _ = _cpu_steps(name, None, 1, n_cpu)
+            line["cpu_all_threads"] = {"steps_per_s": 1.0 / med, "threads": os.cpu_count(),
+                                       "sample": f"{n_cpu} steps after 1, median"}
+            line["cpu_1thread"] = one_thread_row(name, workloads.n_lloyd_default(res), steps=1 if res >= 6 else 2)
+        print(json.dumps(line), flush=True)
+
+
 def workload_text(name, res, g, dt):
     from game_archived_gb300 import workloads
     _, moist, case, mountain, _, steps = workloads.CONFIGS[name]
@@ -972,6 +1007,9 @@ def main():
     ap.add_argument("--column-study", action="store_true",
                     help="time the column solvers at 26, 64 and 128 layers instead of the headline line")
     ap.add_argument("--cpu-one-thread", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--all-configs", action="store_true",
+                    help="one line per benchmark configuration instead of the headline line")
+    ap.add_argument("--configs", default="config1,config2,config3,config4,config5")
     ap.add_argument("--ncu-json", help="summarise an ncu raw-page CSV into --out (see ncu_json)")
     ap.add_argument("--out")
     ap.add_argument("--command", default="", help="the capture command, recorded in the summary")
@@ -986,7 +1024,9 @@ def main():
         return
     if args.warmup < 3:
         args.warmup = 3
-    if args.column_study:
+    if args.all_configs:
+        all_configs(args)
+    elif args.column_study:
         column_study(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -171,8 +171,8 @@ struct Context {
     void (*obuf_release)(Context *) = nullptr;
     int use_graphs = 1;
     int column_solver = 0; /* 0 by layer count, 1 per-thread sweeps, 2 warp cyclic reduction */
-    /* arithmetic of the mixed path's vertical eliminations and tendency
-     * assembly: 0 FP64, 1 double-float (default) */
+    /* arithmetic of the mixed path's vertical eliminations: 0 FP64, 1
+     * double-float (default) */
     int double_float = 1;
     DfGrid dfg{};
     /* health check: device counters, and the step interval of the automatic

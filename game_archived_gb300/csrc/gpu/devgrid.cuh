@@ -144,8 +144,8 @@ struct StepParams {
     /* diffusion switches (DIFF_* bits) and whether the step adds the
      * irreversible terms (friction, dissipative and diffusive heating,
      * radiation, mass diffusion) to its tendencies; dfloat: the mixed path's
-     * vertical eliminations and tendency assembly run in double-float
-     * arithmetic (dfloat.cuh) instead of FP64 */
+     * vertical eliminations run in double-float arithmetic (dfloat.cuh)
+     * instead of FP64 */
     int diff, irr, dfloat, pad_i1;
     double dt;
     double impl_thermo_weight, damping_start_height, damping_coeff_max, toa;

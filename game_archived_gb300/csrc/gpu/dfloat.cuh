@@ -19,9 +19,9 @@
  *                 bounds for basic building blocks of double-word
  *                 arithmetic", ACM TOMS 44(2), 2017: Algorithms 6, 12, 9;
  *                 relative errors at most 3u^2, 4u^2 and 2u^2 with u = 2^-24)
- *   df_rcp        one Newton-Raphson step r + r (1 - y r) from the correctly
- *                 rounded float reciprocal of y.hi, the residual formed with
- *                 TwoProd (relative error about 2^-45)
+ *   df_rcp        one Newton-Raphson step r + r (1 - y r) from the hardware's
+ *                 approximate float reciprocal of y.hi, the residual formed
+ *                 with TwoProd (relative error about 2^-45)
  * Every float operation is an explicit round-to-nearest intrinsic, so that
  * the compiler cannot contract the transformations into FMAs (which would
  * break their exactness) in translation units built with --fmad=true.
@@ -101,12 +101,18 @@ __device__ __forceinline__ df df_mul_f(df x, float y)
     return fast_two_sum(c.hi, __fmaf_rn(x.lo, y, c.lo));
 }
 
-/* 1 / y: r0 = RN(1 / y.hi), then r0 + r0 (1 - y r0) with y r0 = ph + pl
- * formed exactly (TwoProd plus y.lo r0); 1 - ph is exact because ph lies in
- * [1/2, 2] (Sterbenz). */
+/* 1 / y: r0 = the hardware's approximate reciprocal of y.hi (PTX
+ * rcp.approx.ftz.f32, relative error about 2^-23; a correctly rounded seed
+ * gains nothing, since the Newton step squares the seed's error), then one
+ * Newton step
+ * r0 + r0 (1 - y r0) with y r0 = ph + pl formed exactly (TwoProd plus
+ * y.lo r0); 1 - ph is exact because ph lies in [1/2, 2] (Sterbenz).  The
+ * step squares the seed's error: about 2^-45 overall.  y.hi must be a normal
+ * float whose reciprocal is normal. */
 __device__ __forceinline__ df df_rcp(df y)
 {
-    const float r = __frcp_rn(y.hi);
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y.hi));
     const float ph = __fmul_rn(y.hi, r);
     float pl = __fmaf_rn(y.hi, r, -ph);
     pl = __fmaf_rn(y.lo, r, pl);

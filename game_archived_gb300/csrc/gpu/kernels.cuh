@@ -922,15 +922,9 @@ template <typename R, bool IRR>
 __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, SView<R> sv, DState st,
                                                       const R *theta, const R *cp_ice, const R *cp_water,
                                                       const double *pt_rates, const double *pt_heat,
-                                                      const double *sed_heat, const double *inv_vol_tab,
-                                                      const float2 *inv_vol_df, int rk, IrrTerms irr)
+                                                      const double *sed_heat, const double *inv_vol_tab, int rk,
+                                                      IrrTerms irr)
 {
-    /* mixed path with p.dfloat: the divergences are scaled and the
-     * tendencies assembled in double-float (dfloat.cuh) instead of FP64 --
-     * the same operations in the same order, on the FP32 pipe -- and each
-     * tendency is joined to FP64 once */
-    constexpr bool MIXED = sizeof(R) == sizeof(float);
-    const bool dfl = MIXED && p.dfloat;
     const long long ns = (long long)g.nl * g.nc;
     const long long i = gtid();
     if (i >= ns) return;
@@ -951,17 +945,11 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
         return R(-0.5) * ipw_at(g, j, ll, c) * g.slope_h[(long long)ll * ne + edge(j)];
     };
     auto uval = [&](int ll, int j) { return sv.u[(long long)ll * ne + edge(j)]; };
-    auto comp_r = [&](R up, R lo) -> R {
-        if (!oro) return R(0);
-        if (l == nl - n_oro - 1) return -lo * area_lo;
-        if (l == nl - 1) return up * area_up;
-        return up * area_up - lo * area_lo;
-    };
-    auto comp_v = [&](R up, R lo) -> double { return oro ? wide(comp_r(up, lo)) : 0.0; };
-    /* the flux sum of a FluxSum<float> and a correction as a double-float */
-    auto dw = [&](const FluxSum<R> &f, R corr) -> df {
-        if constexpr (MIXED) return df_add(two_sum(f.hi, f.lo), df_of(corr));
-        else return df_zero();
+    auto comp_v = [&](R up, R lo) -> double {
+        if (!oro) return 0.0;
+        if (l == nl - n_oro - 1) return wide(-lo * area_lo);
+        if (l == nl - 1) return wide(up * area_up);
+        return wide(up * area_up - lo * area_lo);
     };
     /* terrain correction of the wind at levels l and l+1 (shared by the tracers) */
     R w_up = R(0), w_lo = R(0);
@@ -1012,39 +1000,6 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
         if (up_has_prev) layer_pass(l - 1, false, true, false);
         layer_pass(l, true, up_corr, lo_has_curr);
         if (lo_corr) layer_pass(l + 1, false, false, true);
-        if (dfl) {
-            const df ivd = ld_df(inv_vol_df, i);
-            df y = df_neg(df_mul(ivd, dw(hm, comp_r(um, lm))));
-            if (IRR) y = df_add(y, df_from_double(irr.mass_diff[cond * ns + i]));
-            if (p.moist) y = df_add(y, df_from_double(pt_rates[cond * ns + i]));
-            /* at rk 1 the reference blends 0 x old + 1 x new: the new value */
-            st.rho[cond * ns + i] = df_to_double(y);
-            df yt = df_neg(df_mul(ivd, dw(ht, comp_r(ut, lt))));
-            if (p.moist || IRR) {
-                R cv = R(0);
-                for (int kk = 0; kk < cond; ++kk)
-                    cv += sv.rho[kk * ns + i] * ((kk % 2 == 0) ? cp_ice[i] : cp_water[i]);
-                cv += sv.rho[cond * ns + i] * R(C_D_V);
-                if (p.moist) cv += sv.rho[(cond + 1) * ns + i] * R(C_V_V);
-                df heat, rate = df_from_double(pt_rates[cond * ns + i]);
-                if (IRR) {
-                    heat = df_add(df_add(df_add(df_add(df_from_double(irr.heating_diss[i]),
-                                                       df_from_double(irr.temp_diff_heating[i])),
-                                                df_from_double(irr.radiation[i])),
-                                         df_from_double(pt_heat[i])),
-                                  df_from_double(sed_heat[i]));
-                    rate = df_add(rate, df_from_double(irr.mass_diff[cond * ns + i]));
-                } else {
-                    heat = df_add(df_from_double(pt_heat[i]), df_from_double(sed_heat[i]));
-                }
-                const float fac =
-                    float(R(C_D_V) * sv.rho[cond * ns + i] / cv / (R(C_D_P) * (g.exner_bg[i] + sv.exner_pert[i])));
-                yt = df_add(df_add(yt, df_mul_f(heat, fac)), df_mul_f(rate, float(theta[i])));
-            }
-            st.rhotheta_v[i] = df_to_double(yt);
-            goto tracers;
-        }
-        {
         const double div = inv_vol * (hm.value() + comp_v(um, lm));
         double y = -div;
         if (IRR) y = y + irr.mass_diff[cond * ns + i];
@@ -1073,9 +1028,7 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
             }
         }
         st.rhotheta_v[i] = rk == 0 ? yt : 0.0 * st.rhotheta_v[i] + 1.0 * yt;
-        }
     }
-tracers:
     if (p.n_const == 1) return;
     /* the other constituents: upstream flux.  The cell's edges, neighbours,
      * orientation and layer-l wind and face areas are loaded once for all
@@ -1107,34 +1060,21 @@ tracers:
             const R a = fv * arj[j];
             h.add(sfj[j] ? a : -a);
         }
-        R cvr = R(0);
+        double cv = 0.0;
         if (oro) {
             const R d_here = f[i];
             if (l == nl - n_oro - 1) {
                 const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
-                cvr = -d_lo * w_lo * area_lo;
+                cv = wide(-d_lo * w_lo * area_lo);
             } else if (l == nl - 1) {
                 const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
-                cvr = d_up * w_up * area_up;
+                cv = wide(d_up * w_up * area_up);
             } else {
                 const R d_up = w_up <= R(0) ? f[i - nc] : d_here;
                 const R d_lo = w_lo <= R(0) ? d_here : f[i + nc];
-                cvr = d_up * w_up * area_up - d_lo * w_lo * area_lo;
+                cv = wide(d_up * w_up * area_up - d_lo * w_lo * area_lo);
             }
         }
-        if (dfl) {
-            df y = df_neg(df_mul(ld_df(inv_vol_df, i), dw(h, cvr)));
-            if (IRR) y = df_add(y, df_from_double(irr.mass_diff[k * ns + i]));
-            if (p.moist) {
-                long long pt = k * ns;
-                if (k == cond + 1) pt -= ns;
-                y = df_add(y, df_from_double(pt_rates[pt + i]));
-            }
-            if (rk != 0) y = df_add(df_half(df_from_double(st.rho[k * ns + i])), df_half(y));
-            st.rho[k * ns + i] = df_to_double(y);
-            continue;
-        }
-        const double cv = oro ? wide(cvr) : 0.0;
         const double div = inv_vol * (h.value() + cv);
         double y = -div;
         if (IRR) y = y + irr.mass_diff[k * ns + i];

@@ -144,16 +144,32 @@ void launch_waves(Context *c, const StepParams &p, StateMirror *so, StateMirror 
                   const Shadow &sh)
 {
     const long long ns = c->ns;
+    WavesWork ww = waves_work(c);
     if constexpr (!EXACT) {
         if (p.dfloat && column_mode(c, EXACT, c->nc) == COLUMN_REGISTERS) {
-            ProfScope ps(c, "k_waves_df");
-            k_waves_df<NL_FIXED><<<nblocks(c->nc, 64), 64, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, c->dfg,
-                                                                           sh, rk);
-            c->kernel_launches++;
+            {
+                ProfScope ps(c, "k_waves_layer");
+                k_waves_layer_df<<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, ww,
+                                                                          c->dfg, rk);
+            }
+            {
+                ProfScope ps(c, "k_waves_rows");
+                k_waves_rows_df<<<nblocks((long long)(c->nl - 1) * c->nc, 256), 256, 0, c->stream>>>(
+                    c->vg, p, so->ds, st->ds, ww, c->dfg);
+            }
+            {
+                ProfScope ps(c, "k_waves_thomas");
+                k_waves_thomas_df<NL_FIXED><<<nblocks(c->nc, WAVES_BLOCK), WAVES_BLOCK, 0, c->stream>>>(c->nc, ww,
+                                                                                                       c->dfg);
+            }
+            {
+                ProfScope ps(c, "k_waves_apply");
+                k_waves_apply_df<<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, ww, c->dfg, sh);
+            }
+            c->kernel_launches += 4;
             return;
         }
     }
-    WavesWork ww = waves_work(c);
     {
         ProfScope ps(c, "k_waves_layer");
         k_waves_layer<EXACT><<<nblocks(ns, 256), 256, 0, c->stream>>>(c->vg, p, so->ds, sn->ds, st->ds, ww, rk);
@@ -209,8 +225,8 @@ void launch_tracers(Context *c, const StepParams &p, StateMirror *so, StateMirro
     ProfScope ps(c, "k_tracers_solve");
     if constexpr (!EXACT) {
         if (p.dfloat && mode == COLUMN_REGISTERS) {
-            k_tracers_solve_df<NL_FIXED><<<nblocks(nsys, 64), 64, 0, strm>>>(c->vg, p, so->ds, sn->ds, st->ds, c->dfg,
-                                                                             sh.rho);
+            k_tracers_solve_df<NL_FIXED><<<nblocks(nsys, TRACER_BLOCK), TRACER_BLOCK, 0, strm>>>(
+                c->vg, p, so->ds, sn->ds, st->ds, c->dfg, sh.rho);
             c->kernel_launches++;
             return;
         }
@@ -318,12 +334,12 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
             if (p.irr) {
                 const DiffBufs &b = *c->dbuf;
                 k_scalar_tend2<R, true><<<nblocks(ns, 128), 128, 0, c->stream>>>(
-                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol,
-                    c->dfg.inv_vol, rk, IrrTerms{b.hdiss, b.tdh, b.rad, b.mdt});
+                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol, rk,
+                    IrrTerms{b.hdiss, b.tdh, b.rad, b.mdt});
             } else {
                 k_scalar_tend2<R, false><<<nblocks(ns, 128), 128, 0, c->stream>>>(
-                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol,
-                    c->dfg.inv_vol, rk, IrrTerms{});
+                    g, p, v.sv, st->ds, theta, cpi, cpw, c->pt_rates, c->pt_heat, c->sed_heat, c->inv_vol, rk,
+                    IrrTerms{});
             }
         }
         c->kernel_launches += 2;

@@ -149,8 +149,7 @@ void sub_scalar_tendencies(Context *c, const StepParams &p, StateMirror *sn, Sta
     const Views<double> v = views<double>(c, sn);
     k_theta<double><<<nblocks(c->ns, 256), 256, 0, c->stream>>>(c->nl, c->nc, c->n_cond, v.sv, theta);
     k_scalar_tend2<double, false><<<nblocks(c->ns, 128), 128, 0, c->stream>>>(
-        c->hg64, p, v.sv, st->ds, theta, cp_ice, cp_water, pt_rates, pt_heat, sed_heat, c->inv_vol, nullptr, rk,
-        IrrTerms{});
+        c->hg64, p, v.sv, st->ds, theta, cp_ice, cp_water, pt_rates, pt_heat, sed_heat, c->inv_vol, rk, IrrTerms{});
     c->kernel_launches += 2;
 }
 

@@ -73,12 +73,12 @@ int game_gpu_set_graphs(int on);
  * 1 per-thread Thomas sweeps; 2 warp cyclic reduction in both precisions (a
  * different elimination order: the FP64 results move by rounding) */
 int game_gpu_set_column_solver(int mode);
-/* arithmetic of the mixed path's FP64 parts -- the vertical eliminations
- * (sound waves, tracers) and the assembly of the scalar tendencies from
- * their accumulated flux divergences: 1 (default) double-float, two FP32
- * numbers per value carrying 48 significand bits, which runs on the FP32
- * pipe (GB300 executes FP64 at 1/64 of its FP32 rate); 0 FP64.  The state
- * stays FP64 either way; the FP64 path never uses double-float. */
+/* arithmetic of the mixed path's vertical eliminations (the sound-wave and
+ * tracer column solves, column_solvers.c): 1 (default) double-float, two
+ * FP32 numbers per value carrying 48 significand bits, which runs on the
+ * FP32 pipe (GB300 executes FP64 at 1/64 of its FP32 rate); 0 FP64.  The
+ * state, the tendencies and the mass-flux accumulation stay FP64 either way;
+ * the FP64 path never uses double-float. */
 int game_gpu_set_double_float(int on);
 int game_gpu_sync_to_device(struct state *state);
 int game_gpu_sync_to_host(struct state *state);

@@ -107,3 +107,32 @@ def test_mixed_precision_close_to_fp64():
     e = state_errors(m32.state_new, m64.state_new, m64.layout)
     assert e["rho[4]"] < 1e-5 and e["rhotheta_v"] < 1e-5 and e["exner_pert"] < 1e-3, e
     assert e["wind_h"] < 1e-3, e
+
+
+@pytest.mark.parametrize("case,mountain", [("tracers", True), ("jet_moist", False)])
+def test_double_float_eliminations_keep_the_mixed_error(case, mountain):
+    """the mixed path with its vertical eliminations in double-float (the
+    default) and in FP64 (game_gpu_set_double_float(0)) stays as close to
+    the FP64 path: per field, the double-float run's error is within 1.5
+    times the FP64-elimination run's, plus 1e-12; and the two mixed runs
+    differ far less than either differs from FP64"""
+    res, moist, dt, steps = 4, 1, 300.0, 4
+    _, m0 = make_model(res, moist, case, mountain)
+    runs = {}
+    for name, prec, dfl in (("fp64", abi.FP64, 1), ("mixed_f64elim", abi.MIXED, 0), ("mixed_df", abi.MIXED, 1)):
+        m = clone(m0)
+        g = abi.GpuModel(m, prec, double_float=dfl)
+        try:
+            driver.run(m, steps, dt, g.linear_combine_two_states, g.manage_rkhevi)
+        finally:
+            g.close()
+        runs[name] = m
+    lay = m0.layout
+    e_ref = state_errors(runs["mixed_f64elim"].state_new, runs["fp64"].state_new, lay)
+    e_df = state_errors(runs["mixed_df"].state_new, runs["fp64"].state_new, lay)
+    e_between = state_errors(runs["mixed_df"].state_new, runs["mixed_f64elim"].state_new, lay)
+    print(f"\n{case}: mixed (FP64 eliminations) vs FP64 {e_ref}\nmixed (double-float) vs FP64 {e_df}\n"
+          f"between the two mixed runs {e_between}")
+    for k in e_ref:
+        assert e_df[k] <= 1.5 * e_ref[k] + 1e-12, (k, e_df[k], e_ref[k])
+    assert max(e_between.values()) <= 0.1 * max(e_ref.values()) + 1e-12
