@@ -1155,14 +1155,16 @@ static int adj_download(struct state *host, StateMirror *m, const double *blk)
 
 /* the window forward on the device: result in the sub-step mirror sn */
 static int window_forward_dev(const char *who, struct state *state_init, struct grid *grid,
-                              struct diagnostics *diagnostics, struct forcings *forcings, struct config *config,
-                              double delta_t, int n_steps)
+                              struct diagnostics *diagnostics, struct forcings *forcings,
+                              struct irreversible_quantities *irrev, struct config *config, double delta_t,
+                              int n_steps)
 {
     if (check_ready(grid)) return -1;
     if (check_config(config)) return -1;
     Context *c = ctx();
-    if (c->n_const != 1)
-        return fail(std::string(who) + ": the adjoint model covers the dry build (MOISTURE_ON = 0)");
+    if (c->n_const != 1 && c->n_const != 6)
+        return fail(std::string(who) + ": the adjoint model covers the dry build and the moist build of six "
+                                       "constituents");
     if (ensure_sub_buffers(c)) return -1;
     Context::SubBuffers &b = c->sub;
     if (upload_state(state_init, &b.so)) return -1;
@@ -1176,7 +1178,10 @@ static int window_forward_dev(const char *who, struct state *state_init, struct 
         if (up_vec(forcings, GAME_FORCINGS, "v_squared_grad", auxG)) return -1;
         adj_add_into(c, auxP, b.vec[4], c->nv); /* the step reads nl + l */
     }
-    return adj_window_forward(c, &b.so, p, n_steps, auxP, auxV, auxG, fl, &b.sn);
+    /* moist: the sedimentation heat the first substage reads */
+    if (c->n_const > 1 && up_scal(irrev, GAME_IRREV, "condensates_sediment_heat", b.sed_heat)) return -1;
+    return adj_window_forward(c, &b.so, p, n_steps, auxP, auxV, auxG, fl, c->n_const > 1 ? b.sed_heat : nullptr,
+                              &b.sn);
 }
 
 int rkhevi_window_forward(struct state *state_init, struct state *state_final, struct grid *grid,
@@ -1184,8 +1189,7 @@ int rkhevi_window_forward(struct state *state_init, struct state *state_final, s
                           struct irreversible_quantities *irrev, struct config *config, double delta_t, int n_steps)
 {
     (void)dualgrid;
-    (void)irrev;
-    if (window_forward_dev("rkhevi_window_forward", state_init, grid, diagnostics, forcings, config, delta_t,
+    if (window_forward_dev("rkhevi_window_forward", state_init, grid, diagnostics, forcings, irrev, config, delta_t,
                            n_steps))
         return -1;
     Context *c = ctx();
@@ -1200,9 +1204,8 @@ int manage_rkhevi_adj(struct state *state_old, struct state *state_new, struct g
     (void)state_new;
     (void)dualgrid;
     (void)state_tendency;
-    (void)irrev;
     (void)time_coordinate;
-    if (window_forward_dev("manage_rkhevi_adj", state_old, grid, diagnostics, forcings, config, delta_t, 1))
+    if (window_forward_dev("manage_rkhevi_adj", state_old, grid, diagnostics, forcings, irrev, config, delta_t, 1))
         return -1;
     Context *c = ctx();
     Context::SubBuffers &b = c->sub;
@@ -1238,7 +1241,8 @@ int game_gpu_sfc_pressure_objective(struct state *state, const double *weights, 
 {
     if (check_ready(nullptr)) return -1;
     Context *c = ctx();
-    if (c->n_const != 1) return fail("game_gpu_sfc_pressure_objective: dry build only (MOISTURE_ON = 0)");
+    if (c->n_const != 1 && c->n_const != 6)
+        return fail("game_gpu_sfc_pressure_objective: dry build or moist build of six constituents");
     if (ensure_sub_buffers(c)) return -1;
     Context::SubBuffers &b = c->sub;
     double *w = adj_obj_weights(c);

@@ -129,19 +129,43 @@ __global__ void ba_theta(long long ns, const double *rho, const double *rt, cons
     rho_b[i] -= tb * (rt[i] / r) / r;
 }
 
-__global__ void ba_pgrad(HGrid<double> g, AState<double> s, const double *P_b, double *tp_b, double *ep_b)
+__global__ void ba_pgrad(HGrid<double> g, AParams ap, AState<double> s, const double *P_b, double *tp_b,
+                         double *ep_b, double *rho_all_b = nullptr)
 {
     const long long nw = (long long)(g.nl + 1) * g.nc, n = nw + (long long)g.nl * g.ne;
+    const long long ns = (long long)g.nl * g.nc;
     const long long i = gtid();
     if (i >= n) return;
-    const double cdp = C_D_P, pb = P_b[i];
+    const double cdp = C_D_P;
+    double pb = P_b[i];
     if (pb == 0.0) return;
+    const bool moist = ap.n_const > 1 && rho_all_b;
+    /* moist: P = dec (nl + l), dec = 0.5 (d_a + d_b), d = rho_gas / rho_total */
+    auto decel = [&](long long a, long long b, double nl_plus_l) {
+        double d = 0.0;
+        for (const long long cell : {a, b}) {
+            double tot = 0.0;
+            for (int q = 0; q < ap.n_const; ++q) tot += s.rho_all[q * ns + cell];
+            const double rg = s.rho[cell];
+            d += 0.5 * (rg / tot);
+            const double hb = 0.5 * nl_plus_l * pb;
+            for (int q = 0; q < ap.n_const; ++q) {
+                const double dq = ((q == ap.n_cond ? tot : 0.0) - rg) / (tot * tot);
+                acc(&rho_all_b[q * ns + cell], dq * hb);
+            }
+        }
+        return d;
+    };
     if (i < nw) {
         const int k = (int)(i / g.nc), c = (int)(i - (long long)k * g.nc);
         if (k == 0 || k == g.nl) return;
         const long long up = (long long)(k - 1) * g.nc + c, lo = (long long)k * g.nc + c;
         const double G = a_gv(g, s.ep, k, c);
         const double S = 0.5 * (cdp * (g.theta_v_bg[up] + s.tp[up]) + cdp * (g.theta_v_bg[lo] + s.tp[lo]));
+        if (moist) {
+            const double lt = (0.5 * (cdp * s.tp[up] + cdp * s.tp[lo])) * g.exner_bg_grad_v[(long long)k * g.nc + c];
+            pb = pb * decel(up, lo, S * G + lt);
+        }
         const double tb = 0.5 * cdp * (G * pb) + 0.5 * cdp * g.exner_bg_grad_v[(long long)k * g.nc + c] * pb;
         acc(&tp_b[up], tb);
         acc(&tp_b[lo], tb);
@@ -153,6 +177,10 @@ __global__ void ba_pgrad(HGrid<double> g, AState<double> s, const double *P_b, d
         const long long cf = (long long)l * g.nc + fr, ct = (long long)l * g.nc + to;
         const double G = a_grad_h(g, s.ep, l, e);
         const double S = 0.5 * (cdp * (g.theta_v_bg[ct] + s.tp[ct]) + cdp * (g.theta_v_bg[cf] + s.tp[cf]));
+        if (moist) {
+            const double lt = (0.5 * (cdp * s.tp[ct] + cdp * s.tp[cf])) * g.exner_bg_grad_h[(long long)l * g.ne + e];
+            pb = pb * decel(ct, cf, S * G + lt);
+        }
         const double tb = 0.5 * cdp * (G * pb) + 0.5 * cdp * g.exner_bg_grad_h[(long long)l * g.ne + e] * pb;
         acc(&tp_b[ct], tb);
         acc(&tp_b[cf], tb);
@@ -344,7 +372,8 @@ __global__ void ba_mom_h(HGrid<double> g, AParams ap, int adv, double new_w, dou
 
 __global__ void ba_mom_v(HGrid<double> g, AParams ap, int adv, double new_w, double old_w, const double *flux_h,
                          const double *zh, const double *t_b, double *tend_in_b, double *P_b, double *pvt_b,
-                         double *v2g_b, double *fh_b, double *zh_b, double *v2_b)
+                         double *v2g_b, double *fh_b, double *zh_b, double *v2_b, const double *rho_all = nullptr,
+                         double *rho_all_b = nullptr)
 {
     const long long n = (long long)(g.nl + 1) * g.nc;
     const long long i = gtid();
@@ -364,6 +393,21 @@ __global__ void ba_mom_v(HGrid<double> g, AParams ap, int adv, double new_w, dou
         const double cur_ver = 1.0 - ap.impl_thermo_weight;
         P_b[i] += -cur_ver * yb;
         pb += yb;
+        if (rho_all && yb != 0.0) {
+            /* condensate term 0.5 (d_up + d_lo) g_m, d = rho_gas / rho_total - 1 */
+            const long long ns = (long long)nl * g.nc, gp = (long long)ap.n_cond * ns;
+            const double hb = 0.5 * g.gravity_m_v[i] * yb;
+            for (const long long cell : {(long long)(k - 1) * g.nc + c, (long long)k * g.nc + c}) {
+                double tot = 0.0;
+                for (int q = 0; q < ap.n_const; ++q) tot += rho_all[q * ns + cell];
+                const double rg = rho_all[gp + cell];
+                /* d(rg / tot) / d rho_q = (delta_q,gas tot - rg) / tot^2 */
+                for (int q = 0; q < ap.n_const; ++q) {
+                    const double dq = ((q == ap.n_cond ? tot : 0.0) - rg) / (tot * tot);
+                    acc(&rho_all_b[q * ns + cell], dq * hb);
+                }
+            }
+        }
         const double gb = v2g_b[i] - 0.5 * yb;
         v2g_b[i] = gb;
         if (adv && gb != 0.0) b_gv(g, v2_b, k, c, gb);

@@ -1,13 +1,17 @@
 /*
- * Adjoint and tangent-linear models of the dry RKHEVI step over multi-step
- * windows (compiled with --fmad=false, like the FP64 step).
+ * Adjoint and tangent-linear models of the RKHEVI step, dry and moist builds,
+ * over multi-step windows (compiled with --fmad=false, like the FP64 step).
  *
  * Window forward: the initial State and, unless the window starts with the
  * model's first step, the lagged fields of the previous step (pressure
  * gradient nl + l, vorticity flux, kinetic-energy gradient) are
  * checkpointed; every step is run with the differentiable kernels of
- * adj_fwd.cuh (the same operations as the fused FP64 step) and its end state
- * and lagged fields are checkpointed.
+ * adj_fwd.cuh and adj_moist.cuh (the same operations as the fused FP64 step)
+ * and its end state and lagged fields are checkpointed.  The moist build
+ * adds the per-step prelude (temperature, phase transitions), the moist
+ * scalar tendencies, the tracer solve and, as a fourth lagged field, the
+ * sedimentation heat (the first substage's scalar tendencies read the
+ * previous step's).
  * Window backward (reverse mode): from the last step to the first, the step
  * is recomputed from its checkpoint with every intermediate field kept (both
  * RK stage states, the momentum, scalar and solver work of both substages),
@@ -24,8 +28,8 @@
 #include <string>
 #include <vector>
 
-#include "adj_bwd.cuh"
 #include "adj.h"
+#include "adj_moist.cuh"
 #include "adj_ops.h"
 #include "diag.h"
 #include "ops.h"
@@ -82,6 +86,8 @@ inline unsigned nbk(long long n, int bs = 256) { return (unsigned)((n + bs - 1) 
 template <class T>
 struct StepBufs {
     T *so = nullptr, *sn1 = nullptr, *sn2 = nullptr;
+    T *pre = nullptr; /* moist: temperature, rates, heating, c_p of ice and water [PRE_OUT][L][Nc] */
+    T *sed = nullptr; /* moist: this step's sedimentation heat [L][Nc] */
     T *P = nullptr, *pgo = nullptr;
     T *tri[2] = {}, *zh[2] = {}, *zv[2] = {}, *fh[2] = {}, *fv[2] = {}, *v2[2] = {};
     T *pvt[2] = {}, *v2g[2] = {}, *tend[2] = {};
@@ -93,7 +99,8 @@ struct StepBufs {
 
 struct AdjState {
     std::vector<void *> owned;
-    long long ns = 0, nw = 0, nu = 0, nv = 0, nblk = 0, ntri = 0, nzh = 0, nwi = 0;
+    long long ns = 0, nw = 0, nu = 0, nv = 0, nblk = 0, ntri = 0, nzh = 0, nwi = 0, nrho = 0;
+    int n_const = 1, n_cond = 0; /* constituents; the main gas's index */
     StepBufs<double> B;          /* forward tape of one step */
     StepBufs<double> Z;          /* bars of one step */
     StepBufs<Dual> D;            /* tangent-linear run */
@@ -102,9 +109,11 @@ struct AdjState {
     double *ck = nullptr;        /* checkpoints: (n_steps + 1) x (state block + 3 Vt) */
     int ck_cap = -1;
     double *obj_w = nullptr, *obj_p = nullptr, *obj_out = nullptr; /* objective work */
-    Dual *tl_aux[3] = {};        /* lagged fields between tangent-linear steps */
+    /* lagged fields between tangent-linear steps: P, pvt, v2g and (moist) the
+     * sedimentation heat */
+    Dual *tl_aux[4] = {};
     double *bar_state = nullptr; /* bar of the current step-end state */
-    double *bar_aux[3] = {}, *bar_aux_prev[3] = {}; /* bars of the lagged fields */
+    double *bar_aux[4] = {}, *bar_aux_prev[4] = {}; /* bars of the lagged fields */
     /* the window of the last forward run */
     int n_steps = 0, first = 0, have = 0;
     AParams ap{};
@@ -134,6 +143,10 @@ bool alloc_step(AdjState *a, StepBufs<T> &S)
     A(S.so, a->nblk);
     A(S.sn1, a->nblk);
     A(S.sn2, a->nblk);
+    if (a->n_const > 1) {
+        A(S.pre, PRE_OUT * a->ns);
+        A(S.sed, a->ns);
+    }
     A(S.P, a->nv);
     A(S.pgo, a->nv);
     for (int r = 0; r < 2; ++r) {
@@ -147,7 +160,7 @@ bool alloc_step(AdjState *a, StepBufs<T> &S)
         A(S.v2g[r], a->nv);
         A(S.tend[r], a->nv);
         A(S.theta[r], a->ns);
-        A(S.str[r], a->ns);
+        A(S.str[r], a->nrho);
         A(S.strt[r], a->ns);
         A(S.wl[r], WL_N * a->ns);
         A(S.wr[r], WR_N * a->nwi);
@@ -166,16 +179,21 @@ void adj_release_fn(Context *c)
 int ensure_adj(Context *c)
 {
     if (c->adj) return 0;
-    if (c->n_const != 1) return fail("adjoint: the adjoint and tangent-linear models cover the dry build (MOISTURE_ON = 0)");
+    if (c->n_const != 1 && c->n_const != 6)
+        return fail("adjoint: the adjoint and tangent-linear models cover the dry build and the moist build of six "
+                    "constituents");
     if (c->nl > MAX_L) return fail("adjoint: more layers than the column solvers support");
     AdjState *a = new AdjState();
     c->adj = a;
     c->adj_release = adj_release_fn;
     a->ns = c->ns;
+    a->n_const = c->n_const;
+    a->n_cond = c->n_cond;
+    a->nrho = (long long)c->n_const * c->ns;
     a->nw = (long long)(c->nl + 1) * c->nc;
     a->nu = (long long)c->nl * c->ne;
     a->nv = a->nw + a->nu;
-    a->nblk = 4 * a->ns + a->nv;
+    a->nblk = a->nrho + 3 * a->ns + a->nv;
     a->ntri = (long long)c->nl * c->nt;
     a->nzh = (long long)(c->nl + 1) * c->ne;
     a->nwi = (long long)(c->nl - 1) * c->nc;
@@ -184,7 +202,7 @@ int ensure_adj(Context *c)
     ok = ok && (a->dden = aalloc<double>(a, a->nwi)) && (a->fv_bounds = aalloc<double>(a, a->nw));
     ok = ok && (a->obj_w = aalloc<double>(a, c->nc)) && (a->obj_p = aalloc<double>(a, c->nc))
          && (a->obj_out = aalloc<double>(a, 1)) && (a->bar_state = aalloc<double>(a, a->nblk));
-    for (int k = 0; k < 3; ++k)
+    for (int k = 0; k < 4; ++k)
         ok = ok && (a->tl_aux[k] = aalloc<Dual>(a, a->nv)) && (a->bar_aux[k] = aalloc<double>(a, a->nv))
              && (a->bar_aux_prev[k] = aalloc<double>(a, a->nv));
     if (!ok) {
@@ -198,79 +216,120 @@ template <class T>
 AState<T> view(const AdjState *a, T *blk)
 {
     AState<T> s;
-    s.rho = blk;
-    s.rt = blk + a->ns;
-    s.tp = blk + 2 * a->ns;
-    s.ep = blk + 3 * a->ns;
-    s.w = blk + 4 * a->ns;
+    s.rho_all = blk;
+    s.rho = blk + (long long)a->n_cond * a->ns;
+    s.rt = blk + a->nrho;
+    s.tp = s.rt + a->ns;
+    s.ep = s.tp + a->ns;
+    s.w = s.ep + a->ns;
     s.u = s.w + a->nw;
     return s;
 }
 
-long long ck_stride(const AdjState *a) { return a->nblk + 3 * a->nv; }
+/* the same block as the DState of the operator adjoints */
+DState dview(const AdjState *a, double *blk)
+{
+    const AState<double> v = view(a, blk);
+    return DState{v.rho_all, v.rt, v.tp, v.ep, v.w, v.u};
+}
+
+bool moist_of(const AdjState *a) { return a->n_const > 1; }
+
+/* checkpoint: the state block and the lagged fields P, pvt, v2g (Vt each)
+ * and, moist, the sedimentation heat (S) */
+long long ck_stride(const AdjState *a) { return a->nblk + 3 * a->nv + (moist_of(a) ? a->ns : 0); }
 
 /* ----------------------------------------------------------- step forward */
+/* the substage rk of a step: sn its input state (so at rk 0), out its
+ * output (sn1, sn2); sed_prev the previous step's sedimentation heat */
 template <class T>
-void step_fwd(Context *c, AdjState *a, StepBufs<T> &B, const T *P_prev, const T *pvt_prev, const T *v2g_prev,
-              bool first)
+void substage_fwd(Context *c, AdjState *a, StepBufs<T> &B, int rk, bool first, const T *sed_prev)
 {
     const HGrid<double> &g = c->hg64;
     const VGrid &vg = c->vg;
     const AParams ap = a->ap;
     cudaStream_t st = c->stream;
     const long long ns = a->ns, nv = a->nv;
-    AState<T> so = view(a, B.so), s1 = view(a, B.sn1), s2 = view(a, B.sn2);
-    /* substage 0 (state_new = state_old) */
-    fa_pgrad<T><<<nbk(nv), 256, 0, st>>>(g, so, B.P);
+    const bool moist = moist_of(a);
+    AState<T> so = view(a, B.so), sn = view(a, rk ? B.sn1 : B.so), out = view(a, rk ? B.sn2 : B.sn1);
+    const bool adv = rk == 1 || first;
+    const double new_w = rk ? 0.5 : 1.0, old_w = 1.0 - new_w;
+    if (adv) {
+        fa_tri<T><<<nbk(a->ntri), 256, 0, st>>>(g, sn.u, B.tri[rk]);
+        fa_edge<T><<<nbk(a->nzh), 256, 0, st>>>(g, sn.u, sn.w, sn.rho, B.tri[rk], B.zh[rk], B.zv[rk], B.fh[rk]);
+        fa_kin<T><<<nbk(ns), 256, 0, st>>>(g, sn.u, sn.w, sn.rho, B.v2[rk], B.fv[rk]);
+    }
+    fa_mom_v<T><<<nbk(a->nw), 256, 0, st>>>(g, ap, adv, new_w, old_w, B.P, B.fh[rk], B.zh[rk], B.v2[rk], B.pvt[rk],
+                                            B.v2g[rk], B.tend[0], B.tend[rk], moist ? sn.rho_all : nullptr);
+    fa_mom_h<T><<<nbk(a->nu), 256, 0, st>>>(g, ap, adv, new_w, old_w, B.P, B.pgo, B.fh[rk], B.fv[rk], B.zh[rk],
+                                            B.zv[rk], B.v2[rk], B.pvt[rk], B.v2g[rk], B.tend[0], B.tend[rk], so.u,
+                                            out.u);
+    fa_theta<T><<<nbk(ns), 256, 0, st>>>(ns, sn.rho, sn.rt, B.theta[rk]);
+    if (moist)
+        fa_scalar_moist<T><<<nbk(ns, 128), 128, 0, st>>>(g, ap, rk, sn.rho_all, B.theta[rk], out.u, sn.ep, B.pre,
+                                                          rk == 0 ? sed_prev : B.sed, B.str[0], B.str[rk],
+                                                          B.strt[rk]);
+    else
+        fa_scalar<T><<<nbk(ns, 128), 128, 0, st>>>(g, sn.rho, B.theta[rk], out.u, B.str[rk], B.strt[rk]);
+    const T *str_gas = B.str[rk] + (long long)a->n_cond * ns;
+    fa_waves_layer<T><<<nbk(ns), 256, 0, st>>>(vg, ap, rk, so, sn, str_gas, B.strt[rk], B.wl[rk]);
+    fa_waves_rows<T><<<nbk(a->nwi), 256, 0, st>>>(vg, ap, so, B.tend[rk], B.wl[rk], B.wr[rk]);
+    fa_waves_thomas<T><<<nbk(c->nc, 64), 64, 0, st>>>(c->nc, c->nl, a->dden, B.wr[rk]);
+    fa_waves_apply<T><<<nbk(ns), 256, 0, st>>>(vg, ap, so, B.wl[rk], B.wr[rk], out);
+    c->kernel_launches += adv ? 11 : 8;
+    if (moist) {
+        if (rk == 0) {
+            fa_sedheat<T><<<nbk(c->nc, 128), 128, 0, st>>>(vg, a->p, so, out.w, B.pre, B.sed);
+            c->kernel_launches++;
+        }
+        fa_tracer_solve<T><<<nbk((long long)(a->n_const - 1) * c->nc, 64), 64, 0, st>>>(vg, a->p, so, out.w,
+                                                                                        B.str[rk], out);
+        c->kernel_launches++;
+    }
+    (void)nv;
+}
+
+template <class T>
+void step_fwd(Context *c, AdjState *a, StepBufs<T> &B, const T *P_prev, const T *pvt_prev, const T *v2g_prev,
+              const T *sed_prev, bool first)
+{
+    const HGrid<double> &g = c->hg64;
+    const AParams ap = a->ap;
+    cudaStream_t st = c->stream;
+    const long long nv = a->nv;
+    AState<T> so = view(a, B.so);
+    if (moist_of(a)) {
+        fa_prelude<T><<<nbk(a->ns), 256, 0, st>>>(c->vg, ap, so, B.pre);
+        c->kernel_launches++;
+    }
+    fa_pgrad<T><<<nbk(nv), 256, 0, st>>>(g, ap, so, B.P);
     ku_neg<T><<<nbk(nv), 256, 0, st>>>(nv, first ? B.P : P_prev, B.pgo);
-    if (first) {
-        fa_tri<T><<<nbk(a->ntri), 256, 0, st>>>(g, so.u, B.tri[0]);
-        fa_edge<T><<<nbk(a->nzh), 256, 0, st>>>(g, so.u, so.w, so.rho, B.tri[0], B.zh[0], B.zv[0], B.fh[0]);
-        fa_kin<T><<<nbk(ns), 256, 0, st>>>(g, so.u, so.w, so.rho, B.v2[0], B.fv[0]);
-    } else {
+    if (!first) {
         ku_copy<T><<<nbk(nv), 256, 0, st>>>(nv, pvt_prev, B.pvt[0]);
         ku_copy<T><<<nbk(nv), 256, 0, st>>>(nv, v2g_prev, B.v2g[0]);
     }
-    fa_mom_v<T><<<nbk(a->nw), 256, 0, st>>>(g, ap, first, 1.0, 0.0, B.P, B.fh[0], B.zh[0], B.v2[0], B.pvt[0],
-                                            B.v2g[0], B.tend[0], B.tend[0]);
-    fa_mom_h<T><<<nbk(a->nu), 256, 0, st>>>(g, ap, first, 1.0, 0.0, B.P, B.pgo, B.fh[0], B.fv[0], B.zh[0], B.zv[0],
-                                            B.v2[0], B.pvt[0], B.v2g[0], B.tend[0], B.tend[0], so.u, s1.u);
-    fa_theta<T><<<nbk(ns), 256, 0, st>>>(ns, so.rho, so.rt, B.theta[0]);
-    fa_scalar<T><<<nbk(ns, 128), 128, 0, st>>>(g, so.rho, B.theta[0], s1.u, B.str[0], B.strt[0]);
-    fa_waves_layer<T><<<nbk(ns), 256, 0, st>>>(vg, ap, 0, so, so, B.str[0], B.strt[0], B.wl[0]);
-    fa_waves_rows<T><<<nbk(a->nwi), 256, 0, st>>>(vg, ap, so, B.tend[0], B.wl[0], B.wr[0]);
-    fa_waves_thomas<T><<<nbk(c->nc, 64), 64, 0, st>>>(c->nc, c->nl, a->dden, B.wr[0]);
-    fa_waves_apply<T><<<nbk(ns), 256, 0, st>>>(vg, ap, so, B.wl[0], B.wr[0], s1);
-    /* substage 1 */
-    fa_tri<T><<<nbk(a->ntri), 256, 0, st>>>(g, s1.u, B.tri[1]);
-    fa_edge<T><<<nbk(a->nzh), 256, 0, st>>>(g, s1.u, s1.w, s1.rho, B.tri[1], B.zh[1], B.zv[1], B.fh[1]);
-    fa_kin<T><<<nbk(ns), 256, 0, st>>>(g, s1.u, s1.w, s1.rho, B.v2[1], B.fv[1]);
-    fa_mom_v<T><<<nbk(a->nw), 256, 0, st>>>(g, ap, 1, 0.5, 0.5, B.P, B.fh[1], B.zh[1], B.v2[1], B.pvt[1], B.v2g[1],
-                                            B.tend[0], B.tend[1]);
-    fa_mom_h<T><<<nbk(a->nu), 256, 0, st>>>(g, ap, 1, 0.5, 0.5, B.P, B.pgo, B.fh[1], B.fv[1], B.zh[1], B.zv[1],
-                                            B.v2[1], B.pvt[1], B.v2g[1], B.tend[0], B.tend[1], so.u, s2.u);
-    fa_theta<T><<<nbk(ns), 256, 0, st>>>(ns, s1.rho, s1.rt, B.theta[1]);
-    fa_scalar<T><<<nbk(ns, 128), 128, 0, st>>>(g, s1.rho, B.theta[1], s2.u, B.str[1], B.strt[1]);
-    fa_waves_layer<T><<<nbk(ns), 256, 0, st>>>(vg, ap, 1, so, s1, B.str[1], B.strt[1], B.wl[1]);
-    fa_waves_rows<T><<<nbk(a->nwi), 256, 0, st>>>(vg, ap, so, B.tend[1], B.wl[1], B.wr[1]);
-    fa_waves_thomas<T><<<nbk(c->nc, 64), 64, 0, st>>>(c->nc, c->nl, a->dden, B.wr[1]);
-    fa_waves_apply<T><<<nbk(ns), 256, 0, st>>>(vg, ap, so, B.wl[1], B.wr[1], s2);
-    c->kernel_launches += first ? 27 : 26;
+    c->kernel_launches += first ? 2 : 4;
+    substage_fwd<T>(c, a, B, 0, first, sed_prev);
+    substage_fwd<T>(c, a, B, 1, first, sed_prev);
 }
 
 /* ---------------------------------------------------------- step backward
  * s2b: bar of the step's end state (modified); P_next_b, pvt_next_b,
- * v2g_next_b: bars of this step's lagged outputs from the next step (may be
- * null); writes sob (bar of the step-start state, theta_v' bar consumed) and,
- * for a step that is not the model's first, the bars of the lagged inputs. */
+ * v2g_next_b, sed_next_b: bars of this step's lagged outputs from the next
+ * step (may be null); writes sob (bar of the step-start state, theta_v' bar
+ * consumed) and, for a step that is not the model's first, the bars of the
+ * lagged inputs; sed_prev_b (moist) receives the bar of the previous step's
+ * sedimentation heat in every case. */
 void step_bwd(Context *c, AdjState *a, bool first, double *s2b, const double *P_next_b, const double *pvt_next_b,
-              const double *v2g_next_b, double *sob, double *P_prev_b, double *pvt_prev_b, double *v2g_prev_b)
+              const double *v2g_next_b, const double *sed_next_b, const double *sed_prev, double *sob,
+              double *P_prev_b, double *pvt_prev_b, double *v2g_prev_b, double *sed_prev_b)
 {
     const HGrid<double> &g = c->hg64;
     const VGrid &vg = c->vg;
     const AParams ap = a->ap;
     cudaStream_t st = c->stream;
     const long long ns = a->ns, nv = a->nv, nw = a->nw;
+    const bool moist = moist_of(a);
     StepBufs<double> &B = a->B, &Z = a->Z;
     /* zero all bars of the step */
     auto zero = [&](double *p, long long n) { cudaMemsetAsync(p, 0, (size_t)n * sizeof(double), st); };
@@ -278,6 +337,11 @@ void step_bwd(Context *c, AdjState *a, bool first, double *s2b, const double *P_
     zero(Z.sn1, a->nblk);
     zero(Z.P, nv);
     zero(Z.pgo, nv);
+    if (moist) {
+        zero(Z.pre, PRE_OUT * ns);
+        zero(Z.sed, ns);
+        zero(sed_prev_b, ns);
+    }
     for (int r = 0; r < 2; ++r) {
         zero(Z.tri[r], a->ntri);
         zero(Z.zh[r], a->nzh);
@@ -289,37 +353,62 @@ void step_bwd(Context *c, AdjState *a, bool first, double *s2b, const double *P_
         zero(Z.v2g[r], nv);
         zero(Z.tend[r], nv);
         zero(Z.theta[r], ns);
-        zero(Z.str[r], ns);
+        zero(Z.str[r], a->nrho);
         zero(Z.strt[r], ns);
         zero(Z.wl[r], WL_N * ns);
         zero(Z.wr[r], WR_N * a->nwi);
     }
     if (pvt_next_b) ku_copy<double><<<nbk(nv), 256, 0, st>>>(nv, pvt_next_b, Z.pvt[1]);
     if (v2g_next_b) ku_copy<double><<<nbk(nv), 256, 0, st>>>(nv, v2g_next_b, Z.v2g[1]);
+    if (moist && sed_next_b) ku_copy<double><<<nbk(ns), 256, 0, st>>>(ns, sed_next_b, Z.sed);
     AState<double> so = view(a, B.so), s1 = view(a, B.sn1), s2 = view(a, B.sn2);
     AState<double> sob_v = view(a, sob), s1b = view(a, Z.sn1), s2b_v = view(a, s2b);
-    /* substage 1: sound waves */
     for (int rk = 1; rk >= 0; --rk) {
         AState<double> out = rk ? s2 : s1, out_b = rk ? s2b_v : s1b;
         AState<double> sn = rk ? s1 : so, sn_b = rk ? s1b : sob_v;
+        double *out_blk = rk ? B.sn2 : B.sn1, *out_b_blk = rk ? s2b : Z.sn1;
+        /* tracer solve (and at rk 0 the sedimentation heat): the operator
+         * adjoint of three_band_solver_gen_densities; the temperature's bar
+         * goes to the prelude's output bar */
+        if (moist) {
+            StateMirror mso, msn, mst, mso_b, msn_b, mst_b;
+            mso.dev = B.so;
+            mso.ds = dview(a, B.so);
+            msn.dev = out_blk;
+            msn.ds = dview(a, out_blk);
+            mst.ds = DState{B.str[rk], nullptr, nullptr, nullptr, nullptr, nullptr};
+            mso_b.ds = dview(a, sob);
+            msn_b.ds = dview(a, out_b_blk);
+            mst_b.ds = DState{Z.str[rk], nullptr, nullptr, nullptr, nullptr, nullptr};
+            if (adj_gen_densities(c, a->p, &mso, &msn, &mst, B.pre, rk, Z.sed, &mso_b, &msn_b, &mst_b, Z.pre))
+                return;
+        }
         ba_apply_layer<<<nbk(ns), 256, 0, st>>>(vg, so, B.wl[rk], out, out_b, a->rn_b, a->rtn_b, sob_v, Z.wl[rk]);
         ba_apply_w<<<nbk(a->nwi), 256, 0, st>>>(vg, so, B.wr[rk], out, out_b, a->rn_b, sob_v, Z.wr[rk]);
         ba_apply_rho<<<nbk(ns), 256, 0, st>>>(vg, ap, B.wr[rk], a->rn_b, a->rtn_b, Z.wl[rk], Z.wr[rk]);
         ba_thomas<<<nbk(c->nc, 64), 64, 0, st>>>(c->nc, c->nl, a->dden, B.wr[rk], Z.wr[rk]);
         ba_waves_rows<<<nbk(a->nwi), 256, 0, st>>>(vg, ap, so, B.wl[rk], B.wr[rk], Z.wr[rk], Z.wl[rk], sob_v,
                                                    Z.tend[rk]);
-        ba_waves_layer<<<nbk(ns), 256, 0, st>>>(vg, ap, rk, so, sn, B.str[rk], B.strt[rk], B.wl[rk], Z.wl[rk], sob_v,
-                                                sn_b, Z.str[rk], Z.strt[rk]);
-        /* scalar tendencies: density and theta_v of sn, the wind of out */
-        ba_scalar<<<nbk(ns, 128), 128, 0, st>>>(g, sn.rho, B.theta[rk], out.u, Z.str[rk], Z.strt[rk], sn_b.rho,
-                                           Z.theta[rk], out_b.u);
+        const long long gas = (long long)a->n_cond * ns;
+        ba_waves_layer<<<nbk(ns), 256, 0, st>>>(vg, ap, rk, so, sn, B.str[rk] + gas, B.strt[rk], B.wl[rk], Z.wl[rk],
+                                                sob_v, sn_b, Z.str[rk] + gas, Z.strt[rk]);
+        /* scalar tendencies: densities and theta_v of sn, the wind of out */
+        if (moist)
+            ba_scalar_moist<<<nbk(ns, 128), 128, 0, st>>>(g, ap, rk, sn.rho_all, B.theta[rk], out.u, sn.ep, B.pre,
+                                                          rk == 0 ? sed_prev : B.sed, Z.str[rk], Z.strt[rk],
+                                                          sn_b.rho_all, Z.theta[rk], out_b.u, sn_b.ep, Z.pre,
+                                                          rk == 0 ? sed_prev_b : Z.sed, Z.str[0]);
+        else
+            ba_scalar<<<nbk(ns, 128), 128, 0, st>>>(g, sn.rho, B.theta[rk], out.u, Z.str[rk], Z.strt[rk], sn_b.rho,
+                                                    Z.theta[rk], out_b.u);
         ba_theta<<<nbk(ns), 256, 0, st>>>(ns, sn.rho, sn.rt, Z.theta[rk], sn_b.rho, sn_b.rt);
         /* momentum */
         const int adv = rk == 1 || first;
         const double new_w = rk ? 0.5 : 1.0, old_w = 1.0 - new_w;
         double *tend_in_b = rk ? Z.tend[0] : nullptr;
         ba_mom_v<<<nbk(nw), 256, 0, st>>>(g, ap, adv, new_w, old_w, B.fh[rk], B.zh[rk], Z.tend[rk], tend_in_b, Z.P,
-                                          Z.pvt[rk], Z.v2g[rk], Z.fh[rk], Z.zh[rk], Z.v2[rk]);
+                                          Z.pvt[rk], Z.v2g[rk], Z.fh[rk], Z.zh[rk], Z.v2[rk],
+                                          moist ? sn.rho_all : nullptr, moist ? sn_b.rho_all : nullptr);
         ba_mom_h<<<nbk(a->nu), 256, 0, st>>>(g, ap, adv, new_w, old_w, B.fh[rk], B.fv[rk], B.zh[rk], B.zv[rk],
                                              Z.tend[rk], out_b.u, sob_v.u, tend_in_b, Z.P, Z.pgo, Z.pvt[rk], Z.v2g[rk],
                                              Z.fh[rk], Z.fv[rk], Z.zh[rk], Z.zv[rk], Z.v2[rk]);
@@ -340,9 +429,10 @@ void step_bwd(Context *c, AdjState *a, bool first, double *s2b, const double *P_
         ku_axpy<<<nbk(nv), 256, 0, st>>>(nv, -1.0, Z.pgo, Z.P);
     else
         ku_neg<double><<<nbk(nv), 256, 0, st>>>(nv, Z.pgo, P_prev_b);
-    ba_pgrad<<<nbk(nv), 256, 0, st>>>(g, so, Z.P, sob_v.tp, sob_v.ep);
+    ba_pgrad<<<nbk(nv), 256, 0, st>>>(g, ap, so, Z.P, sob_v.tp, sob_v.ep, moist ? sob_v.rho_all : nullptr);
+    if (moist) ba_prelude<<<nbk(ns), 256, 0, st>>>(vg, ap, so, Z.pre, sob_v);
     ba_rediag<<<nbk(ns), 256, 0, st>>>(ns, so.rho, so.rt, sob_v.tp, sob_v.rho, sob_v.rt);
-    c->kernel_launches += 40;
+    c->kernel_launches += moist ? 46 : 40;
 }
 
 /* the step-start state of step n from its checkpoint: theta_v' rediagnosed */
@@ -355,7 +445,7 @@ void load_start(Context *c, AdjState *a, int n, T *so_blk)
     fa_rediag<T><<<nbk(a->ns), 256, 0, c->stream>>>(c->vg, view(a, so_blk));
 }
 
-const double *ck_aux(const AdjState *a, int n, int which) /* 0 P, 1 pvt, 2 v2g */
+const double *ck_aux(const AdjState *a, int n, int which) /* 0 P, 1 pvt, 2 v2g, 3 sedimentation heat */
 {
     return a->ck + (long long)n * ck_stride(a) + a->nblk + (long long)which * a->nv;
 }
@@ -388,10 +478,33 @@ __device__ __forceinline__ double sfc_p_dry(const VGrid &vg, const double *gm_v,
     return ps;
 }
 
-__global__ void k_obj(VGrid vg, const double *gm_v, AState<double> s, const double *w, double *p2, AState<double> sb)
+__global__ void k_obj(VGrid vg, const double *gm_v, AState<double> s, const double *w, double *p2, AState<double> sb,
+                      int n_cond, int moist)
 {
     const int i = (int)gtid();
     if (i >= vg.nc) return;
+    if (moist) {
+        /* moist air: the gas constant and temperature of the lowest layer
+         * carry the vapour; derivatives by forward mode */
+        const long long ns = (long long)vg.nl * vg.nc, si = (long long)(vg.nl - 1) * vg.nc + i;
+        const double xv[SFC_IN] = {s.rho_all[n_cond * ns + si], s.rho_all[(n_cond + 1) * ns + si], s.tp[si], s.ep[si]};
+        const double ps = sfc_pressure_moist<double>(vg, gm_v, i, xv);
+        p2[i] = ps * ps;
+        if (sb.rho) {
+            const double pb = 2.0 * w[i] * ps;
+            double g[SFC_IN];
+            for (int m = 0; m < SFC_IN; ++m) {
+                Dual x[SFC_IN];
+                for (int k = 0; k < SFC_IN; ++k) x[k] = {xv[k], k == m ? 1.0 : 0.0};
+                g[m] = sfc_pressure_moist<Dual>(vg, gm_v, i, x).d * pb;
+            }
+            sb.rho_all[n_cond * ns + si] += g[0];
+            sb.rho_all[(n_cond + 1) * ns + si] += g[1];
+            sb.tp[si] += g[2];
+            sb.ep[si] += g[3];
+        }
+        return;
+    }
     double dr, dt_, de;
     const double ps = sfc_p_dry(vg, gm_v, s.rho, s.tp, s.ep, i, sb.rho ? &dr : nullptr, &dt_, &de);
     p2[i] = ps * ps;
@@ -410,6 +523,8 @@ int set_params(Context *c, AdjState *a, const StepParams &p)
     a->p = p;
     a->ap.dt = p.dt;
     a->ap.impl_thermo_weight = p.impl_thermo_weight;
+    a->ap.n_const = a->n_const;
+    a->ap.n_cond = a->n_cond;
     if (launch_damping_table(c, p)) return -1;
     ku_dden<<<nbk(a->nwi), 256, 0, c->stream>>>(a->nwi, p.dt, c->damp_dc, a->dden);
     return 0;
@@ -419,7 +534,8 @@ int set_params(Context *c, AdjState *a, const StepParams &p)
 
 /* ---------------------------------------------------------------- API */
 int adj_window_forward(Context *c, StateMirror *init, const StepParams &p, int n_steps, const double *aux_P,
-                       const double *aux_pvt, const double *aux_v2g, const double *fv_bounds, StateMirror *final_out)
+                       const double *aux_pvt, const double *aux_v2g, const double *fv_bounds, const double *aux_sed,
+                       StateMirror *final_out)
 {
     if (ensure_adj(c)) return -1;
     AdjState *a = c->adj;
@@ -445,15 +561,24 @@ int adj_window_forward(Context *c, StateMirror *init, const StepParams &p, int n
         ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, aux_pvt, ck0 + a->nblk + a->nv);
         ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, aux_v2g, ck0 + a->nblk + 2 * a->nv);
     }
+    const bool moist = moist_of(a);
+    if (moist) {
+        /* the sedimentation heat the first substage of the window's first
+         * step reads (the caller's, whatever the first-step flag) */
+        if (!aux_sed) return fail("adjoint window: the moist build needs the sedimentation heat");
+        ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, aux_sed, ck0 + a->nblk + 3 * a->nv);
+    }
     for (int n = 0; n < n_steps; ++n) {
         load_start<double>(c, a, n, a->B.so);
         const bool first = a->first && n == 0;
-        step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2), first);
+        step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2),
+                         moist ? ck_aux(a, n, 3) : nullptr, first);
         double *ckn = a->ck + (long long)(n + 1) * ck_stride(a);
         ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->B.sn2, ckn);
         ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.P, ckn + a->nblk);
         ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.pvt[1], ckn + a->nblk + a->nv);
         ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.v2g[1], ckn + a->nblk + 2 * a->nv);
+        if (moist) ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, a->B.sed, ckn + a->nblk + 3 * a->nv);
     }
     a->have = 1;
     if (final_out)
@@ -472,16 +597,20 @@ int adj_window_tl(Context *c, const double *init_dot, double *final_dot)
     for (int r = 0; r < 2; ++r) ku_fv_bounds<Dual><<<nbk(c->nc), 256, 0, st>>>(c->nc, c->nl, a->fv_bounds, D.fv[r]);
     /* lagged inputs of the window's first step: values from checkpoint 0,
      * derivative 0 (they are not part of the control) */
+    const bool moist = moist_of(a);
     for (int k = 0; k < 3; ++k)
         ku_to_dual<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, 0, k), nullptr, a->tl_aux[k]);
+    if (moist) ku_to_dual<<<nbk(a->ns), 256, 0, st>>>(a->ns, ck_aux(a, 0, 3), nullptr, a->tl_aux[3]);
     ku_to_dual<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->ck, init_dot, D.so);
     for (int n = 0; n < a->n_steps; ++n) {
         if (n > 0) ku_copy<Dual><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, D.sn2, D.so);
         fa_rediag<Dual><<<nbk(a->ns), 256, 0, st>>>(c->vg, view(a, D.so));
-        step_fwd<Dual>(c, a, D, a->tl_aux[0], a->tl_aux[1], a->tl_aux[2], a->first && n == 0);
+        step_fwd<Dual>(c, a, D, a->tl_aux[0], a->tl_aux[1], a->tl_aux[2], moist ? a->tl_aux[3] : nullptr,
+                       a->first && n == 0);
         ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.P, a->tl_aux[0]);
         ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.pvt[1], a->tl_aux[1]);
         ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.v2g[1], a->tl_aux[2]);
+        if (moist) ku_copy<Dual><<<nbk(a->ns), 256, 0, st>>>(a->ns, D.sed, a->tl_aux[3]);
     }
     ku_dual_part<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, D.sn2, final_dot);
     CK(cudaGetLastError());
@@ -495,19 +624,23 @@ int adj_window_backward(Context *c, const double *final_bar, double *init_bar)
     cudaStream_t st = c->stream;
     const long long nv = a->nv;
     ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, final_bar, a->bar_state);
-    bool have_next = false;
+    const bool moist = moist_of(a);
+    bool have_next = false, have_next_sed = false;
     for (int n = a->n_steps - 1; n >= 0; --n) {
         const bool first = a->first && n == 0;
         /* recompute the step from its checkpoint, keeping the tape */
         load_start<double>(c, a, n, a->B.so);
-        step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2), first);
+        const double *sed_prev = moist ? ck_aux(a, n, 3) : nullptr;
+        step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2), sed_prev, first);
         step_bwd(c, a, first, a->bar_state, have_next ? a->bar_aux[0] : nullptr,
-                 have_next ? a->bar_aux[1] : nullptr, have_next ? a->bar_aux[2] : nullptr, init_bar,
-                 a->bar_aux_prev[0], a->bar_aux_prev[1], a->bar_aux_prev[2]);
+                 have_next ? a->bar_aux[1] : nullptr, have_next ? a->bar_aux[2] : nullptr,
+                 have_next_sed ? a->bar_aux[3] : nullptr, sed_prev, init_bar, a->bar_aux_prev[0],
+                 a->bar_aux_prev[1], a->bar_aux_prev[2], a->bar_aux_prev[3]);
         /* the step-start bar is the previous step's end-state bar */
         ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, init_bar, a->bar_state);
-        for (int k = 0; k < 3; ++k) std::swap(a->bar_aux[k], a->bar_aux_prev[k]);
+        for (int k = 0; k < 4; ++k) std::swap(a->bar_aux[k], a->bar_aux_prev[k]);
         have_next = !first;
+        have_next_sed = moist;
     }
     (void)nv;
     CK(cudaGetLastError());
@@ -524,7 +657,8 @@ int adj_objective(Context *c, StateMirror *s, const double *w_dev, double *J, do
         cudaMemsetAsync(bar_blk, 0, (size_t)a->nblk * sizeof(double), c->stream);
         sb = view(a, bar_blk);
     }
-    k_obj<<<nbk(c->nc, 128), 128, 0, c->stream>>>(c->vg, c->hg64.gravity_m_v, sv, w_dev, a->obj_p, sb);
+    k_obj<<<nbk(c->nc, 128), 128, 0, c->stream>>>(c->vg, c->hg64.gravity_m_v, sv, w_dev, a->obj_p, sb, a->n_cond,
+                                                  moist_of(a) ? 1 : 0);
     if (launch_integral(a->obj_p, 0, 1, c->nc, nullptr, w_dev, c->red_partials, c->red_counters, a->obj_out,
                         c->stream))
         return -1;
@@ -607,6 +741,9 @@ int adj_waves_backward(Context *c, StateMirror *so_m, StateMirror *sn_m, StateMi
     return 0;
 }
 
-long long adj_block_len(Context *c) { return 4 * c->ns + (long long)(c->nl + 1) * c->nc + (long long)c->nl * c->ne; }
+long long adj_block_len(Context *c)
+{
+    return (long long)(c->n_const + 3) * c->ns + (long long)(c->nl + 1) * c->nc + (long long)c->nl * c->ne;
+}
 
 }  // namespace game

@@ -12,9 +12,11 @@
  * every value -- the tangent-linear model of exactly this arithmetic.  Grid
  * tables are double in both cases.
  *
- * Scope: the dry build (one constituent), where the condensate deceleration
+ * Both builds: in the dry one (one constituent) the condensate deceleration
  * factor of the pressure gradient is rho/rho = 1 and the condensate term of
- * the vertical momentum equation is 0; both are left out.
+ * the vertical momentum equation is 0, and both are left out; the moist
+ * build's own terms (phase transitions, the moist scalar tendencies, the
+ * tracer solve) are in adj_moist.cuh.
  */
 #pragma once
 
@@ -65,16 +67,28 @@ __device__ __forceinline__ double tconst<double>(double v) { return v; }
 template <>
 __device__ __forceinline__ Dual tconst<Dual>(double v) { return {v, 0.0}; }
 
-/* one dry state in device layout, value type T */
+/* one state in device layout, value type T: rho is the main gas's density
+ * (the only constituent of the dry build), rho_all all constituents
+ * [C][L][Nc] (rho_all == rho when C = 1) */
 template <class T>
 struct AState {
     T *rho, *rt, *tp, *ep, *w, *u; /* [L][Nc] x4, [L+1][Nc], [L][Ne] */
+    T *rho_all;
 };
 
 /* run constants of the differentiable step */
 struct AParams {
     double dt, impl_thermo_weight;
+    int n_const, n_cond; /* constituents; condensates (the main gas's index) */
 };
+
+template <class T>
+__device__ __forceinline__ T a_density_total(const T *rho_all, int n_const, long long ns, long long i)
+{
+    T r = tzero<T>();
+    for (int k = 0; k < n_const; ++k) r += rho_all[k * ns + i];
+    return r;
+}
 
 __device__ __forceinline__ double ipw_d(const HGrid<double> &g, int j, int l, int c)
 {
@@ -130,12 +144,21 @@ __device__ __forceinline__ T a_hor_cov(const HGrid<double> &g, const T *u, const
 /* pressure gradient nl + l (manage_pressure_gradient.c:32-60) at every edge
  * and inner interface; device vector layout [w (L+1) Nc][u L Ne] */
 template <class T>
-__global__ void fa_pgrad(HGrid<double> g, AState<T> s, T *P)
+__global__ void fa_pgrad(HGrid<double> g, AParams ap, AState<T> s, T *P)
 {
     const long long nw = (long long)(g.nl + 1) * g.nc, n = nw + (long long)g.nl * g.ne;
+    const long long ns = (long long)g.nl * g.nc;
     const long long i = gtid();
     if (i >= n) return;
     const double cdp = C_D_P;
+    /* deceleration by the condensates (manage_pressure_gradient.c:63-69):
+     * the gas share of the total density, averaged to the edge or interface
+     * (1 exactly in the dry build, where it is left out) */
+    auto decel = [&](long long a, long long b) {
+        const T d_a = s.rho[a] / a_density_total(s.rho_all, ap.n_const, ns, a);
+        const T d_b = s.rho[b] / a_density_total(s.rho_all, ap.n_const, ns, b);
+        return 0.5 * (d_a + d_b);
+    };
     if (i < nw) {
         const int k = (int)(i / g.nc), c = (int)(i - (long long)k * g.nc);
         if (k == 0 || k == g.nl) return;
@@ -144,6 +167,11 @@ __global__ void fa_pgrad(HGrid<double> g, AState<T> s, T *P)
         T s_up = cdp * (g.theta_v_bg[up] + s.tp[up]), s_lo = cdp * (g.theta_v_bg[lo] + s.tp[lo]);
         nl = (0.5 * (s_up + s_lo)) * nl;
         T lt = (0.5 * (cdp * s.tp[up] + cdp * s.tp[lo])) * g.exner_bg_grad_v[(long long)k * g.nc + c];
+        if (ap.n_const > 1) {
+            const T dec = decel(up, lo);
+            nl = dec * nl;
+            lt = dec * lt;
+        }
         P[i] = nl + lt;
     } else {
         const long long j = i - nw;
@@ -154,6 +182,11 @@ __global__ void fa_pgrad(HGrid<double> g, AState<T> s, T *P)
         T s_to = cdp * (g.theta_v_bg[ct] + s.tp[ct]), s_fr = cdp * (g.theta_v_bg[cf] + s.tp[cf]);
         nl = (0.5 * (s_to + s_fr)) * nl;
         T lt = (0.5 * (cdp * s.tp[ct] + cdp * s.tp[cf])) * g.exner_bg_grad_h[(long long)l * g.ne + e];
+        if (ap.n_const > 1) {
+            const T dec = decel(ct, cf);
+            nl = dec * nl;
+            lt = dec * lt;
+        }
         P[i] = nl + lt;
     }
 }
@@ -344,7 +377,8 @@ __global__ void fa_mom_h(HGrid<double> g, AParams ap, int adv, double new_w, dou
  * gradient, tendency; w itself is advanced by the sound-wave solver */
 template <class T>
 __global__ void fa_mom_v(HGrid<double> g, AParams ap, int adv, double new_w, double old_w, const T *P,
-                         const T *flux_h, const T *zh, const T *v2, T *pvt, T *v2g, const T *tend_in, T *tend_out)
+                         const T *flux_h, const T *zh, const T *v2, T *pvt, T *v2g, const T *tend_in, T *tend_out,
+                         const T *rho_all = nullptr)
 {
     const long long n = (long long)(g.nl + 1) * g.nc;
     const long long i = gtid();
@@ -375,6 +409,17 @@ __global__ void fa_mom_v(HGrid<double> g, AParams ap, int adv, double new_w, dou
     if (adv) v2g[i] = a_gv(g, v2, k, c);
     const double cur_ver = 1.0 - ap.impl_thermo_weight;
     T y = -cur_ver * P[i] + pvt[i] - 0.5 * v2g[i];
+    if (rho_all) {
+        /* condensate term (manage_pressure_gradient.c:74-87): the gas
+         * deficit of the total density times gravity, averaged to the
+         * interface, from the substage's state */
+        const long long ns = (long long)nl * g.nc;
+        const long long up = (long long)(k - 1) * g.nc + c, lo = (long long)k * g.nc + c;
+        const long long gp = (long long)ap.n_cond * ns;
+        const T d_up = rho_all[gp + up] / a_density_total(rho_all, ap.n_const, ns, up) - 1.0;
+        const T d_lo = rho_all[gp + lo] / a_density_total(rho_all, ap.n_const, ns, lo) - 1.0;
+        y = y + (0.5 * (d_up + d_lo)) * g.gravity_m_v[i];
+    }
     T t = (new_w == 1.0) ? y : old_w * tend_in[i] + new_w * y;
     tend_out[i] = t;
 }

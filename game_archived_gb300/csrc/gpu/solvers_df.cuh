@@ -140,6 +140,55 @@ __global__ void __launch_bounds__(TRACER_BLOCK) k_tracers_solve_df(VGrid vg, Ste
     }
 }
 
+/* sedimentation heating (rk 0, column_solvers.c:455-462, 551-623): the
+ * divergence of the condensates' enthalpy fluxes c_p T rho w_sink A at the
+ * interfaces, summed over the condensates in the reference's order.  One
+ * thread per (layer, column), each forming the fluxes of its two
+ * interfaces (the per-column FP64 kernel of solvers.cuh forms each once but
+ * has 26 times fewer threads). */
+__global__ void k_tracers_sedheat_df(VGrid vg, StepParams p, DState so, DState sn, const double *temperature,
+                                     TracerWork tw, DfGrid dg, double *sed_heat)
+{
+    const int nc = vg.nc, nl = vg.nl;
+    const long long ns = (long long)nl * nc, b = gtid();
+    if (b >= ns) return;
+    const int j = (int)(b / nc), i = (int)(b - (long long)j * nc);
+    const int n_cond = p.n_cond < SEDHEAT_MAX_COND ? p.n_cond : SEDHEAT_MAX_COND;
+    /* enthalpy flux of constituent k at interface jj (below layer jj) */
+    auto fe = [&](int k, int jj, df vs, bool has) {
+        const long long bb = i + (long long)jj * nc, wi = bb + nc;
+        df b_ = df_from_double(sn.w[wi]);
+        if (has) b_ = df_sub(b_, vs);
+        b_ = df_mul(ld_df(dg.area_v, wi), b_);
+        const long long up = df_nonneg(b_) ? bb + nc : bb;
+        const df fr = df_mul(df_from_double(so.rho[k * ns + up]), b_);
+        const df cp = df_from_double((k % 2 == 0) ? tw.cp_ice[up] : tw.cp_water[up]);
+        return df_mul(df_mul(cp, df_from_double(temperature[up])), fr);
+    };
+    const df ivol = ld_df(dg.inv_vol, b);
+    df sh = df_zero();
+#pragma unroll 1
+    for (int k = 0; k < n_cond; ++k) {
+        bool has;
+        const double vsd = sink_velocity(p, k, has);
+        const df vs = df_from_double(vsd);
+        if (j == 0) {
+            sh = df_add(sh, df_mul(fe(k, 0, vs, has), ivol));
+        } else if (j == nl - 1) {
+            sh = df_add(sh, df_mul(df_neg(fe(k, j - 1, vs, has)), ivol));
+            const long long bot = b;
+            const df cp = df_from_double((k % 2 == 0) ? tw.cp_ice[bot] : tw.cp_water[bot]);
+            const df e = df_mul(df_mul(df_mul(df_mul(df_neg(vs), df_from_double(temperature[bot])), cp),
+                                       df_from_double(so.rho[k * ns + bot])),
+                                ld_df(dg.area_v, (long long)nl * nc + i));
+            sh = df_add(sh, df_mul(e, ivol));
+        } else {
+            sh = df_add(sh, df_mul(df_add(df_neg(fe(k, j - 1, vs, has)), fe(k, j, vs, has)), ivol));
+        }
+    }
+    sed_heat[b] = df_to_double(sh);
+}
+
 /* ---------------------------------------------------------- sound waves
  * The four kernels of solvers.cuh's mixed path (k_waves_layer,
  * k_waves_rows_mixed, k_waves_thomas, k_waves_apply) with their FP64

@@ -218,8 +218,12 @@ void launch_tracers(Context *c, const StepParams &p, StateMirror *so, StateMirro
     const int mode = column_mode(c, EXACT, nsys);
     if (rk == 0) {
         ProfScope ps(c, "k_tracers_sedheat");
-        k_tracers_sedheat<EXACT><<<nblocks(c->nc, 128), 128, 0, strm>>>(c->vg, p, so->ds, sn->ds, temperature, tw,
-                                                                            sed_heat);
+        if (!EXACT && p.dfloat)
+            k_tracers_sedheat_df<<<nblocks(ns, 128), 128, 0, strm>>>(c->vg, p, so->ds, sn->ds, temperature, tw,
+                                                                     c->dfg, sed_heat);
+        else
+            k_tracers_sedheat<EXACT><<<nblocks(c->nc, 128), 128, 0, strm>>>(c->vg, p, so->ds, sn->ds, temperature,
+                                                                                tw, sed_heat);
         c->kernel_launches++;
     }
     ProfScope ps(c, "k_tracers_solve");
