@@ -3,14 +3,18 @@
  * (dfloat.cuh), so that they issue on the FP32 pipe instead of GB300's FP64
  * pipe (1/64 of the FP32 rate), at close to FP64 precision (about 2^-45 per
  * operation against 2^-53).  Same rows, same branch structure and the same
- * elimination order as the mixed-path kernels of solvers.cuh; the prognostic
- * results are joined back to FP64 (one FP64 addition each) and clipped as
- * there.
+ * elimination order as the mixed-path kernels of solvers.cuh.  A double
+ * carried in double-float keeps 48 of its 53 significand bits, so the
+ * kernels compute only increments in double-float and add them to the FP64
+ * state with one FP64 addition each: the densities, rho theta_v and Pi' keep
+ * their full precision, and the mass-flux form of the density update stays
+ * conservative to FP64 rounding.
  *
  * k_tracers_solve_df  vertical advection and sedimentation of the non-main
  *                     constituents (column_solvers.c:385-639), one thread
  *                     per (constituent, column), the elimination
- *                     coefficients in shared memory
+ *                     coefficients in shared memory, solved for the
+ *                     increment of the density
  * k_waves_*_df        the implicit sound-wave solve (column_solvers.c:19-383):
  *                     per (layer, column) the explicit predictors and
  *                     partial derivatives (:102-139), per (interface,
@@ -32,6 +36,12 @@ namespace {
  * coefficients live in shared memory, NL x TRACER_BLOCK (hi, lo) pairs each */
 constexpr int TRACER_BLOCK = 64;
 
+/* The column system A x = r of the tracer (rows as k_tracers_solve's mixed
+ * path) is solved for the increment delta = x - rho_old: A delta = r - A
+ * rho_old, whose right-hand side holds only the tendency and flux terms
+ * (dt tr + g (fr_j - fr_{j-1}) - (A - I) rho_old), so that the new density
+ * is the FP64 old value plus a double-float increment: the state keeps its
+ * 53 bits (a double carried in double-float keeps 48). */
 template <int NL>
 __global__ void __launch_bounds__(TRACER_BLOCK) k_tracers_solve_df(VGrid vg, StepParams p, DState so, DState sn,
                                                                    DState st, DfGrid dg, float *sh_rho)
@@ -57,7 +67,7 @@ __global__ void __launch_bounds__(TRACER_BLOCK) k_tracers_solve_df(VGrid vg, Ste
     const double *tr = st.rho + k * ns;
     const df a_sfc = ld_df(dg.area_v, (long long)nl * nc + i);
     df fi_prev = df_zero(), fr_prev = df_zero(), ep_prev = df_zero(), rp_prev = df_zero();
-    df ro_j = df_from_double(ro[i]);
+    df ro_j = df_from_double(ro[i]), ro_prev = df_zero();
     /* inputs of row j, loaded one row ahead (indices clamped to the column) */
     auto wi_of = [&](int j) { return (long long)(j < nl - 1 ? j + 1 : nl - 1) * nc + i; };
     float2 iv_c = dg.inv_vol[i];
@@ -93,32 +103,38 @@ __global__ void __launch_bounds__(TRACER_BLOCK) k_tracers_solve_df(VGrid vg, Ste
         /* sub-diagonal of row j (coupling to layer j - 1), formed with row
          * j's factor */
         const df c_j = df_nonneg(fi_prev) ? df_zero() : df_mul(g, fi_prev);
-        df dj, rj = df_add(ro_j, df_mul(dtd, df_from_double(tr_c)));
+        /* dm1 = d_j - 1 and the explicit right-hand side minus rho_old */
+        df dm1, rx = df_mul(dtd, df_from_double(tr_c));
         if (j == 0) {
-            dj = df_nonneg(fi) ? df_one() : df_sub(df_one(), df_mul(g, fi));
-            rj = df_add(rj, df_mul(g, fr));
+            dm1 = df_nonneg(fi) ? df_zero() : df_neg(df_mul(g, fi));
+            rx = df_add(rx, df_mul(g, fr));
         } else if (j == nl - 1) {
-            dj = df_nonneg(fi_prev) ? df_add(df_one(), df_mul(g, fi_prev)) : df_one();
-            rj = df_sub(rj, df_mul(g, fr_prev));
+            dm1 = df_nonneg(fi_prev) ? df_mul(g, fi_prev) : df_zero();
+            rx = df_sub(rx, df_mul(g, fr_prev));
             if (has_sink) {
                 const df gs = df_mul(df_mul(g, vs), a_sfc);
-                dj = df_add(dj, gs);
-                rj = df_sub(rj, df_mul(gs, ro_j));
+                dm1 = df_add(dm1, gs);
+                rx = df_sub(rx, df_mul(gs, ro_j));
             }
         } else {
-            dj = df_one();
-            if (df_nonneg(fi_prev)) dj = df_add(dj, df_mul(g, fi_prev));
-            if (!df_nonneg(fi)) dj = df_sub(dj, df_mul(g, fi));
-            rj = df_add(rj, df_mul(g, df_sub(fr, fr_prev)));
+            dm1 = df_zero();
+            if (df_nonneg(fi_prev)) dm1 = df_add(dm1, df_mul(g, fi_prev));
+            if (!df_nonneg(fi)) dm1 = df_sub(dm1, df_mul(g, fi));
+            rx = df_add(rx, df_mul(g, df_sub(fr, fr_prev)));
         }
+        /* the increment's right-hand side r - A rho_old */
+        df r_inc = df_sub(rx, df_mul(dm1, ro_j));
+        if (j > 0) r_inc = df_sub_mul(r_inc, c_j, ro_prev);
+        if (j < nl - 1) r_inc = df_sub_mul(r_inc, ej, ro_next);
         /* forward elimination (row 0: ep_prev = rp_prev = c_0 = 0) */
-        const df inv = df_rcp(df_sub_mul(dj, ep_prev, c_j));
+        const df inv = df_rcp(df_sub_mul(df_add(df_one(), dm1), ep_prev, c_j));
         ep_prev = df_mul(ej, inv);
-        rp_prev = df_mul(df_sub_mul(rj, rp_prev, c_j), inv);
+        rp_prev = df_mul(df_sub_mul(r_inc, rp_prev, c_j), inv);
         s_ep[j][t] = make_float2(ep_prev.hi, ep_prev.lo);
         s_rp[j][t] = make_float2(rp_prev.hi, rp_prev.lo);
         fi_prev = fi;
         fr_prev = fr;
+        ro_prev = ro_j;
         ro_j = ro_next;
         iv_c = iv_n;
         tr_c = tr_n;
@@ -134,9 +150,11 @@ __global__ void __launch_bounds__(TRACER_BLOCK) k_tracers_solve_df(VGrid vg, Ste
     for (int j = nl - 1; j >= 0; --j) {
         const float2 e2 = s_ep[j][t], r2 = s_rp[j][t];
         x = df_sub_mul(df{r2.x, r2.y}, df{e2.x, e2.y}, x); /* e_{nl-1} = 0 */
-        const df v = df_nonneg(x) ? x : df_zero();
-        rn[(long long)j * nc + i] = df_to_double(v);
-        rs[(long long)j * nc + i] = v.hi;
+        const long long b = (long long)j * nc + i;
+        const double xn = ro[b] + df_to_double(x);
+        const double v = nonneg<false>(xn) ? xn : 0.0;
+        rn[b] = v;
+        rs[b] = to_float(v);
     }
 }
 
@@ -229,8 +247,11 @@ __global__ void k_waves_layer_df(VGrid vg, StepParams p, DState so, DState sn, D
     stw(ww.alpha, b, alpha);
     stw(ww.beta, b, beta);
     stw(ww.gam, b, gam);
-    stw(ww.rho_expl, b, df_add(ro, df_mul(dt, str)));
-    stw(ww.rt_expl, b, df_add(rto, df_mul(dt, strt)));
+    /* the explicit increments dt * tendency (not the predictors themselves):
+     * the new densities are formed as the FP64 old value plus an increment,
+     * so the double-float arithmetic never rounds the state itself */
+    stw(ww.rho_expl, b, df_mul(dt, str));
+    stw(ww.rt_expl, b, df_mul(dt, strt));
     stw(ww.tp_expl, b, df_add(df_from_double(so.theta_v_pert[b]),
                               df_mul(dtv, df_add(df_mul(alpha, str), df_mul(beta, strt)))));
     stw(ww.ep_expl, b, df_add(df_from_double(so.exner_pert[b]), df_mul(df_mul(dtv, gam), strt)));
@@ -250,8 +271,9 @@ __global__ void k_waves_rows_df(VGrid vg, StepParams p, DState so, DState st, Wa
     const df dt = df_from_double(p.dt), inv_dt = df_from_double(p.inv_dt);
     const df dz = ld_df(dg.geo, q), H = ld_df(dg.geo, n + q), G1 = ld_df(dg.geo, 2 * n + q),
              G2 = ld_df(dg.geo, 3 * n + q);
-    const df irio = df_rcp(df_half(df_add(df_from_double(so.rho[gp + b]), df_from_double(so.rho[gp + lo]))));
-    const df rho_ie = df_half(df_add(ldw(ww.rho_expl, b), ldw(ww.rho_expl, lo)));
+    const df ro_b = df_from_double(so.rho[gp + b]), ro_lo = df_from_double(so.rho[gp + lo]);
+    const df irio = df_rcp(df_half(df_add(ro_b, ro_lo)));
+    const df rho_ie = df_half(df_add(df_add(ro_b, ldw(ww.rho_expl, b)), df_add(ro_lo, ldw(ww.rho_expl, lo))));
     const df tl_b = ldw(ww.thl, b), tl_lo = ldw(ww.thl, lo);
     const df th = df_half(df_add(tl_b, tl_lo));
     const df wo = df_from_double(so.w[wi]);
@@ -324,36 +346,40 @@ __global__ void k_waves_apply_df(VGrid vg, StepParams p, DState so, DState sn, W
     const int j = (int)(b / nc);
     const long long gp = p.n_cond * ns;
     const df dt = df_from_double(p.dt);
+    /* the new density as the FP64 old value plus the increment
+     * dt (tendency + flux divergence / V), joined in FP64 */
     auto rho_new = [&](int jj, long long bb) {
         df num;
         if (jj == 0) num = ldw(ww.r, bb);
         else if (jj == nl - 1) num = df_neg(ldw(ww.r, bb - nc));
         else num = df_sub(ldw(ww.r, bb), ldw(ww.r, bb - nc));
-        return df_add(ldw(ww.rho_expl, bb), df_mul(df_mul(dt, num), ld_df(dg.inv_vol, bb)));
+        const df inc = df_add(ldw(ww.rho_expl, bb), df_mul(df_mul(dt, num), ld_df(dg.inv_vol, bb)));
+        return so.rho[gp + bb] + df_to_double(inc);
     };
-    const df r_new = rho_new(j, b);
+    const double r_new = rho_new(j, b);
     df num;
     if (j == 0) num = df_mul(ldw(ww.th_int, b), ldw(ww.r, b));
     else if (j == nl - 1) num = df_neg(df_mul(ldw(ww.th_int, b - nc), ldw(ww.r, b - nc)));
     else num = df_sub(df_mul(ldw(ww.th_int, b), ldw(ww.r, b)), df_mul(ldw(ww.th_int, b - nc), ldw(ww.r, b - nc)));
-    const df rt_new = df_add(ldw(ww.rt_expl, b), df_mul(df_mul(dt, num), ld_df(dg.inv_vol, b)));
-    const df tp_new = df_sub(df_mul(rt_new, df_rcp(r_new)), ld_df(dg.theta_v_bg, b));
-    const df ep_new = df_add(df_from_double(so.exner_pert[b]),
-                             df_mul(df_mul(ld_df(dg.volume, b), ldw(ww.gam, b)),
-                                    df_sub(rt_new, df_from_double(so.rhotheta_v[b]))));
-    sn.rho[gp + b] = df_to_double(r_new);
-    sn.rhotheta_v[b] = df_to_double(rt_new);
+    const df rt_inc = df_add(ldw(ww.rt_expl, b), df_mul(df_mul(dt, num), ld_df(dg.inv_vol, b)));
+    const double rt_new = so.rhotheta_v[b] + df_to_double(rt_inc);
+    const df rn = df_from_double(r_new), rtn = df_from_double(rt_new);
+    const df tp_new = df_sub(df_mul(rtn, df_rcp(rn)), ld_df(dg.theta_v_bg, b));
+    /* Pi' = Pi'_old + V gamma (rho theta_v new - old): the increment */
+    const double ep_new = so.exner_pert[b] + df_to_double(df_mul(df_mul(ld_df(dg.volume, b), ldw(ww.gam, b)), rt_inc));
+    sn.rho[gp + b] = r_new;
+    sn.rhotheta_v[b] = rt_new;
     sn.theta_v_pert[b] = df_to_double(tp_new);
-    sn.exner_pert[b] = df_to_double(ep_new);
+    sn.exner_pert[b] = ep_new;
     if (sh.rho) {
-        sh.rho[gp + b] = r_new.hi;
-        sh.rhotheta_v[b] = rt_new.hi;
+        sh.rho[gp + b] = to_float(r_new);
+        sh.rhotheta_v[b] = to_float(rt_new);
         sh.theta_v_pert[b] = tp_new.hi;
-        sh.exner_pert[b] = ep_new.hi;
+        sh.exner_pert[b] = to_float(ep_new);
     }
     if (j < nl - 1) {
         const long long wi = b + nc;
-        const df dint = df_half(df_add(r_new, rho_new(j + 1, b + nc)));
+        const df dint = df_half(df_add(rn, df_from_double(rho_new(j + 1, b + nc))));
         /* rho_io holds 1 / rho at the interface */
         const df wn = df_mul(df_sub(df_mul(df_mul({2.0f, 0.0f}, ldw(ww.r, b)), ld_df(dg.inv_area_v, wi)),
                                     df_mul(dint, df_from_double(so.w[wi]))),
