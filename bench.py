@@ -128,7 +128,21 @@ NCU_METRICS = {
     "sm__throughput.avg.pct_of_peak_sustained_elapsed": "sm_throughput_pct",
     "launch__registers_per_thread": "registers_per_thread",
     "smsp__inst_executed.sum": "warp_instructions",
+    "lts__t_sector_hit_rate.pct": "l2_hit_pct",
+    "l1tex__t_sector_hit_rate.pct": "l1_hit_pct",
+    "smsp__warp_issue_stalled_long_scoreboard_per_warp_active.pct": "stall_long_scoreboard_pct",
+    "smsp__warp_issue_stalled_no_instruction_per_warp_active.pct": "stall_no_instruction_pct",
+    "smsp__warp_issue_stalled_lg_throttle_per_warp_active.pct": "stall_lg_throttle_pct",
+    "smsp__warp_issue_stalled_math_pipe_throttle_per_warp_active.pct": "stall_math_pipe_throttle_pct",
+    "smsp__warp_issue_stalled_wait_per_warp_active.pct": "stall_wait_pct",
+    "smsp__warp_issue_stalled_short_scoreboard_per_warp_active.pct": "stall_short_scoreboard_pct",
 }
+
+
+# ncu's units (second row of a raw-page CSV) -> the summary's: nanoseconds
+# and bytes
+NCU_UNIT_SCALE = {"nsecond": 1.0, "ns": 1.0, "usecond": 1e3, "us": 1e3, "msecond": 1e6, "ms": 1e6, "second": 1e9,
+                  "byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3, "MB": 1e6, "GB": 1e9}
 
 
 # the step's timing scopes (game_gpu_profile names) -> the kernels ncu sees
@@ -155,27 +169,31 @@ def short_kernel_name(full):
 
 
 def ncu_json(args):
-    """--ncu-json RAW.csv: summarise `ncu -i REPORT --page raw --csv` output
-    per kernel (launches; means per launch of the metrics in NCU_METRICS) into
-    --out, with the commit of this checkout and the capture command"""
+    """--ncu-json RAW.csv [RAW.csv ...]: summarise `ncu -i REPORT --page raw
+    --csv` outputs per kernel (launches; means per launch of the metrics in
+    NCU_METRICS) into --out, with the commit of this checkout and the capture
+    command"""
     import csv
-    with open(args.ncu_json) as f:
-        rows = list(csv.reader(f))
-    head = rows[0]
-    data = [r for r in rows[2:] if len(r) == len(head)]
-    col = {n: i for i, n in enumerate(head)}
     kernels = {}
-    for r in data:
-        name = short_kernel_name(r[col["Kernel Name"]])
-        k = kernels.setdefault(name, {"launches": 0, "sums": {}})
-        k["launches"] += 1
-        for metric, key in NCU_METRICS.items():
-            if metric in col:
-                try:
-                    v = float(r[col[metric]].replace(",", ""))
-                except ValueError:
-                    continue
-                k["sums"][key] = k["sums"].get(key, 0.0) + v
+    for path in args.ncu_json:
+        with open(path) as f:
+            rows = list(csv.reader(f))
+        if not rows:
+            continue
+        head, units = rows[0], rows[1]
+        data = [r for r in rows[2:] if len(r) == len(head)]
+        col = {n: i for i, n in enumerate(head)}
+        for r in data:
+            name = short_kernel_name(r[col["Kernel Name"]])
+            k = kernels.setdefault(name, {"launches": 0, "sums": {}})
+            k["launches"] += 1
+            for metric, key in NCU_METRICS.items():
+                if metric in col:
+                    try:
+                        v = float(r[col[metric]].replace(",", ""))
+                    except ValueError:
+                        continue
+                    k["sums"][key] = k["sums"].get(key, 0.0) + v * NCU_UNIT_SCALE.get(units[col[metric]].strip(), 1.0)
     out = {}
     for name, k in kernels.items():
         e = {"launches": k["launches"]}
@@ -1051,7 +1069,9 @@ def main():
     ap.add_argument("--all-configs", action="store_true",
                     help="one line per benchmark configuration instead of the headline line")
     ap.add_argument("--configs", default="config1,config2,config3,config4,config5")
-    ap.add_argument("--ncu-json", help="summarise an ncu raw-page CSV into --out (see ncu_json)")
+    ap.add_argument("--ncu-json", nargs="+", help="summarise ncu raw-page CSVs into --out (see ncu_json)")
+    ap.add_argument("--ncu-metric-list", action="store_true",
+                    help="print the metrics the summary keeps, comma-separated (for ncu --metrics)")
     ap.add_argument("--out")
     ap.add_argument("--command", default="", help="the capture command, recorded in the summary")
     ap.add_argument("--captured", default="", help="what was captured (workload, commit state), recorded")
@@ -1065,6 +1085,9 @@ def main():
         return
     if args.ncu_json:
         ncu_json(args)
+        return
+    if args.ncu_metric_list:
+        print(",".join(NCU_METRICS))
         return
     if args.warmup < 3:
         args.warmup = 3

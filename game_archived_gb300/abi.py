@@ -358,7 +358,7 @@ class GpuModel:
                                                m.config.ptr, dt, t, s_new_bar.ptr, s_old_bar.ptr),
                     "manage_rkhevi_adj")
 
-    # -- adjoint / tangent-linear windows (dry build)
+    # -- adjoint / tangent-linear windows (dry and moist builds; forward in the library's precision)
     def window_forward(self, s_init, s_final, dt, n_steps):
         m = self.m
         self._check(self.lib.rkhevi_window_forward(s_init.ptr, s_final.ptr, m.grid.ptr, m.dualgrid.ptr,

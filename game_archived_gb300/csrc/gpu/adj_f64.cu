@@ -18,7 +18,20 @@
  * then the hand-written adjoint kernels of adj_bwd.cuh run in reverse order.
  * The bars of the lagged fields carry over to the earlier step.
  * Window tangent-linear: the same forward kernels instantiated with dual
- * numbers.
+ * numbers, each step linearised about its checkpoint (values from the
+ * checkpoint, derivatives carried from the previous step), so that it is the
+ * transpose of the backward sweep whatever computed the checkpoints.
+ *
+ * Mixed precision: when the library's precision is the mixed one, the
+ * forward of record is the fused mixed step itself (FP32 horizontal
+ * operators, double-float eliminations, FP64 state), run on private state
+ * blocks; its step-start states and lagged fields (widened to FP64) are the
+ * checkpoints, so the window's end state is the mixed run's.  The
+ * tangent-linear and adjoint models are the FP64 ones, linearised about
+ * that trajectory: the backward sweep recomputes each step in FP64 from its
+ * mixed checkpoint.  The library's own lagged step fields (those a
+ * device-resident run carries from one manage_rkhevi call to the next) are
+ * saved before the mixed window and restored after it.
  *
  * The control is the State at the window start: rho, rho theta_v, Pi', w and
  * u.  theta_v' is rediagnosed from rho theta_v / rho at every step start
@@ -26,6 +39,7 @@
  */
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "adj.h"
@@ -59,6 +73,13 @@ __global__ void ku_to_dual(long long n, const double *v, const double *d, Dual *
 {
     const long long i = gtid();
     if (i < n) out[i] = Dual{v[i], d ? d[i] : 0.0};
+}
+/* out = (v, derivative of dsrc): a tangent-linear value re-seeded from a
+ * checkpoint */
+__global__ void ku_reseed(long long n, const double *v, const Dual *dsrc, Dual *out)
+{
+    const long long i = gtid();
+    if (i < n) out[i] = Dual{v[i], dsrc[i].d};
 }
 __global__ void ku_dual_part(long long n, const Dual *in, double *d)
 {
@@ -114,6 +135,14 @@ struct AdjState {
     Dual *tl_aux[4] = {};
     double *bar_state = nullptr; /* bar of the current step-end state */
     double *bar_aux[4] = {}, *bar_aux_prev[4] = {}; /* bars of the lagged fields */
+    /* mixed forward of record: the fused step's three state blocks, and the
+     * library's lagged step fields saved around the window (FP32: P, the
+     * old pressure gradient, vorticity flux, KE gradient, mass flux;
+     * FP64: temperature, phase-transition rates and heating, sedimentation
+     * heat) */
+    StateMirror mso{}, msn{}, mst{};
+    float *save32 = nullptr;
+    double *save64 = nullptr;
     /* the window of the last forward run */
     int n_steps = 0, first = 0, have = 0;
     AParams ap{};
@@ -530,6 +559,87 @@ int set_params(Context *c, AdjState *a, const StepParams &p)
     return 0;
 }
 
+/* ------------------------------------------------ mixed forward of record */
+int ensure_mixed_fwd(Context *c, AdjState *a)
+{
+    if (a->mso.dev) return 0;
+    for (StateMirror *m : {&a->mso, &a->msn, &a->mst}) {
+        m->dev = aalloc<double>(a, c->state_len);
+        if (!m->dev) return fail("adjoint window: device allocation of the mixed step's states failed");
+        set_mirror_views(c, *m);
+    }
+    a->save32 = aalloc<float>(a, 5 * a->nu + 4 * a->nw);
+    a->save64 = aalloc<double>(a, 8 * a->ns);
+    if (!a->save32 || !a->save64) return fail("adjoint window: device allocation failed");
+    return 0;
+}
+
+/* copies the library's lagged step fields into the save area (save) or back */
+int swap_step_fields(Context *c, AdjState *a, bool save)
+{
+    const Work<float> &w = c->w32;
+    const size_t nu = (size_t)a->nu * sizeof(float), nw = (size_t)a->nw * sizeof(float),
+                 ns = (size_t)a->ns * sizeof(double);
+    const std::pair<void *, size_t> f32[] = {{w.P_h, nu},  {w.pg_old_h, nu}, {w.pvt_h, nu},
+                                             {w.v2g_h, nu}, {w.flux_h, nu},   {w.P_v, nw},
+                                             {w.pvt_v, nw}, {w.v2g_v, nw},    {w.flux_v, nw}};
+    const std::pair<void *, size_t> f64[] = {
+        {c->temperature, ns}, {c->pt_rates, 5 * ns}, {c->pt_heat, ns}, {c->sed_heat, ns}};
+    char *q = (char *)a->save32;
+    for (const auto &f : f32) {
+        CK(cudaMemcpyAsync(save ? (void *)q : f.first, save ? f.first : (void *)q, f.second,
+                           cudaMemcpyDeviceToDevice, c->stream));
+        q += f.second;
+    }
+    q = (char *)a->save64;
+    for (const auto &f : f64) {
+        CK(cudaMemcpyAsync(save ? (void *)q : f.first, save ? f.first : (void *)q, f.second,
+                           cudaMemcpyDeviceToDevice, c->stream));
+        q += f.second;
+    }
+    return 0;
+}
+
+/* the window's steps by the fused mixed step (checkpoint 0 written): as the
+ * reference's time loop runs them, state_new = state_old at every step start;
+ * each step's end state and its lagged fields become the next checkpoint */
+int window_forward_mixed(Context *c, AdjState *a, const StepParams &p, int n_steps, const double *aux_P,
+                         const double *aux_pvt, const double *aux_v2g, const double *flux, const double *aux_sed)
+{
+    if (ensure_mixed_fwd(c, a)) return -1;
+    cudaStream_t st = c->stream;
+    const bool moist = moist_of(a);
+    if (swap_step_fields(c, a, true)) return -1;
+    if (a->first)
+        aux_load_mixed(c, nullptr, nullptr, nullptr, flux);
+    else
+        aux_load_mixed(c, aux_P, aux_pvt, aux_v2g, flux);
+    if (moist) ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, aux_sed, c->sed_heat);
+    int rc = 0;
+    for (int n = 0; n < n_steps && !rc; ++n) {
+        const double *ck_in = a->ck + (long long)n * ck_stride(a);
+        /* the step start as the reference's time loop leaves it:
+         * linear_combine_two_states(state_new -> state_old) rediagnoses
+         * theta_v' in state_old only, state_new keeps the previous step's
+         * solution (the window's state_init for its first step); at the
+         * model's first step state_new is state_old, rediagnosed as well
+         * (src/coordinator.c:291-305) */
+        load_start<double>(c, a, n, a->mso.dev);
+        ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, n == 0 && a->first ? a->mso.dev : ck_in,
+                                                      a->msn.dev);
+        StepParams pn = p;
+        pn.first_step = a->first && n == 0 ? 1 : 0;
+        rc = launch_step_mixed(c, pn, &a->mso, &a->msn, &a->mst);
+        if (rc) break;
+        double *ckn = a->ck + (long long)(n + 1) * ck_stride(a);
+        ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->msn.dev, ckn);
+        aux_store_mixed(c, ckn + a->nblk, ckn + a->nblk + a->nv, ckn + a->nblk + 2 * a->nv);
+        if (moist) ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, c->sed_heat, ckn + a->nblk + 3 * a->nv);
+    }
+    if (swap_step_fields(c, a, false)) return -1;
+    return rc;
+}
+
 }  // namespace
 
 /* ---------------------------------------------------------------- API */
@@ -568,17 +678,22 @@ int adj_window_forward(Context *c, StateMirror *init, const StepParams &p, int n
         if (!aux_sed) return fail("adjoint window: the moist build needs the sedimentation heat");
         ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, aux_sed, ck0 + a->nblk + 3 * a->nv);
     }
-    for (int n = 0; n < n_steps; ++n) {
-        load_start<double>(c, a, n, a->B.so);
-        const bool first = a->first && n == 0;
-        step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2),
-                         moist ? ck_aux(a, n, 3) : nullptr, first);
-        double *ckn = a->ck + (long long)(n + 1) * ck_stride(a);
-        ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->B.sn2, ckn);
-        ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.P, ckn + a->nblk);
-        ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.pvt[1], ckn + a->nblk + a->nv);
-        ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.v2g[1], ckn + a->nblk + 2 * a->nv);
-        if (moist) ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, a->B.sed, ckn + a->nblk + 3 * a->nv);
+    a->have = 0;
+    if (c->precision == PREC_MIXED) {
+        if (window_forward_mixed(c, a, p, n_steps, aux_P, aux_pvt, aux_v2g, fv_bounds, aux_sed)) return -1;
+    } else {
+        for (int n = 0; n < n_steps; ++n) {
+            load_start<double>(c, a, n, a->B.so);
+            const bool first = a->first && n == 0;
+            step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2),
+                             moist ? ck_aux(a, n, 3) : nullptr, first);
+            double *ckn = a->ck + (long long)(n + 1) * ck_stride(a);
+            ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->B.sn2, ckn);
+            ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.P, ckn + a->nblk);
+            ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.pvt[1], ckn + a->nblk + a->nv);
+            ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.v2g[1], ckn + a->nblk + 2 * a->nv);
+            if (moist) ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, a->B.sed, ckn + a->nblk + 3 * a->nv);
+        }
     }
     a->have = 1;
     if (final_out)
@@ -602,15 +717,17 @@ int adj_window_tl(Context *c, const double *init_dot, double *final_dot)
         ku_to_dual<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, 0, k), nullptr, a->tl_aux[k]);
     if (moist) ku_to_dual<<<nbk(a->ns), 256, 0, st>>>(a->ns, ck_aux(a, 0, 3), nullptr, a->tl_aux[3]);
     ku_to_dual<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->ck, init_dot, D.so);
+    /* every step is linearised about its checkpoint: values from checkpoint
+     * n, derivatives carried from step n - 1 */
     for (int n = 0; n < a->n_steps; ++n) {
-        if (n > 0) ku_copy<Dual><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, D.sn2, D.so);
+        if (n > 0) ku_reseed<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->ck + (long long)n * ck_stride(a), D.sn2, D.so);
         fa_rediag<Dual><<<nbk(a->ns), 256, 0, st>>>(c->vg, view(a, D.so));
         step_fwd<Dual>(c, a, D, a->tl_aux[0], a->tl_aux[1], a->tl_aux[2], moist ? a->tl_aux[3] : nullptr,
                        a->first && n == 0);
-        ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.P, a->tl_aux[0]);
-        ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.pvt[1], a->tl_aux[1]);
-        ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.v2g[1], a->tl_aux[2]);
-        if (moist) ku_copy<Dual><<<nbk(a->ns), 256, 0, st>>>(a->ns, D.sed, a->tl_aux[3]);
+        ku_reseed<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, n + 1, 0), D.P, a->tl_aux[0]);
+        ku_reseed<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, n + 1, 1), D.pvt[1], a->tl_aux[1]);
+        ku_reseed<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, n + 1, 2), D.v2g[1], a->tl_aux[2]);
+        if (moist) ku_reseed<<<nbk(a->ns), 256, 0, st>>>(a->ns, ck_aux(a, n + 1, 3), D.sed, a->tl_aux[3]);
     }
     ku_dual_part<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, D.sn2, final_dot);
     CK(cudaGetLastError());

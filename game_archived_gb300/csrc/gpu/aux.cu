@@ -10,22 +10,28 @@
 namespace game {
 namespace {
 
+/* l_f may be null (nl_f then holds the sum); nl_f, pvt and v2g may all be
+ * null, which imports zeros (a window that starts with the model's first
+ * step reads none of them) */
 template <typename R>
 __global__ void k_import(int nc, int ne, int nl, const double *nl_f, const double *l_f, const double *pvt,
                          const double *v2g, const double *flux, Work<R> w)
 {
     const long long nw = (long long)(nl + 1) * nc, nu = (long long)nl * ne;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nw + nu) return;
+    const R P = nl_f ? R(l_f ? nl_f[i] + l_f[i] : nl_f[i]) : R(0);
+    const R pv = pvt ? R(pvt[i]) : R(0), kg = v2g ? R(v2g[i]) : R(0);
     if (i < nw) {
-        w.P_v[i] = R(nl_f[i] + l_f[i]);
-        w.pvt_v[i] = R(pvt[i]);
-        w.v2g_v[i] = R(v2g[i]);
+        w.P_v[i] = P;
+        w.pvt_v[i] = pv;
+        w.v2g_v[i] = kg;
         w.flux_v[i] = R(flux[i]);
-    } else if (i < nw + nu) {
+    } else {
         const long long j = i - nw;
-        w.P_h[j] = R(nl_f[i] + l_f[i]);
-        w.pvt_h[j] = R(pvt[i]);
-        w.v2g_h[j] = R(v2g[i]);
+        w.P_h[j] = P;
+        w.pvt_h[j] = pv;
+        w.v2g_h[j] = kg;
         w.flux_h[j] = R(flux[i]);
     }
 }
@@ -57,6 +63,21 @@ void aux_sum_to_work(Context *c, const double *nl, const double *l, const double
     k_import<double><<<nb, 256, 0, c->stream>>>(c->nc, c->ne, c->nl, nl, l, pvt, v2g, flux, c->w64);
     k_import<float><<<nb, 256, 0, c->stream>>>(c->nc, c->ne, c->nl, nl, l, pvt, v2g, flux, c->w32);
     c->kernel_launches += 2;
+}
+
+void aux_load_mixed(Context *c, const double *P, const double *pvt, const double *v2g, const double *flux)
+{
+    const long long n = c->nv;
+    k_import<float><<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->nc, c->ne, c->nl, P, nullptr, pvt, v2g,
+                                                                        flux, c->w32);
+    c->kernel_launches++;
+}
+
+void aux_store_mixed(Context *c, double *P, double *pvt, double *v2g)
+{
+    const long long n = c->nv;
+    k_export<float><<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->nc, c->ne, c->nl, c->w32, P, pvt, v2g);
+    c->kernel_launches++;
 }
 
 int aux_export(Context *c, double *P, double *pvt, double *v2g)

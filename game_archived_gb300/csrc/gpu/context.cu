@@ -369,6 +369,21 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     }
     std::vector<double> h_ndh = edge_field(nd), h_areah = edge_field(area), h_zh = edge_field(zv),
                         h_slope = edge_field(slope), h_ebggh = edge_field(ebgg);
+    /* cells none of whose edges slopes in any layer: there every
+     * terrain-following correction of the scalar tendencies vanishes, and the
+     * mixed path skips it (the FP64 path keeps the reference's operations) */
+    std::vector<int> h_tilt(NC, 0);
+    for (int i = 0; i < NC; ++i) {
+        const int n_edges = i < N_PENT ? 5 : 6;
+        for (int j = 0; j < n_edges && !h_tilt[i]; ++j) {
+            const int e = h_adj[(size_t)j * NC + i];
+            for (int l = 0; l < L; ++l)
+                if (h_slope[(size_t)l * NE + e] != 0.0) {
+                    h_tilt[i] = 1;
+                    break;
+                }
+        }
+    }
     std::vector<double> h_tw((size_t)10 * NE), h_rw((size_t)4 * NE), h_fvec((size_t)2 * NE);
     std::vector<int> h_ti((size_t)10 * NE), h_tm((size_t)10 * NE), h_ri((size_t)4 * NE);
     for (int e = 0; e < NE; ++e) {
@@ -497,7 +512,7 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     int *d_adj = dupload(c, h_adj), *d_sign = dupload(c, h_sign), *d_nbr = dupload(c, h_nbr);
     int *d_from = dupload(c, h_from), *d_to = dupload(c, h_to), *d_ti = dupload(c, h_ti), *d_tm = dupload(c, h_tm);
     int *d_ri = dupload(c, h_ri), *d_dfrom = dupload(c, h_dfrom), *d_dto = dupload(c, h_dto);
-    int *d_vi = dupload(c, h_vi), *d_vs = dupload(c, h_vs);
+    int *d_vi = dupload(c, h_vi), *d_vs = dupload(c, h_vs), *d_tilt = dupload(c, h_tilt);
     double *d_zs = dupload(c, h_zs), *d_tbg = t_tbg.d, *d_ebg = t_ebg.d, *d_zv = dupload(c, h_zv);
 
     auto fill = [&](auto &hg, auto pick) {
@@ -509,6 +524,7 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
         hg.trsk_m = d_tm; hg.rhombi_w = pick(t_rw); hg.rhombi_i = d_ri; hg.f_vec = pick(t_fvec);
         hg.dual_from = d_dfrom; hg.dual_to = d_dto; hg.dual_area_h = pick(t_dah); hg.pvz = pick(t_pvz);
         hg.vort_i = d_vi; hg.vort_s = d_vs; hg.dual_area_t = pick(t_dat); hg.dual_z_t = pick(t_dzt);
+        hg.tilt = d_tilt;
     };
     fill(c->hg64, [](const Dual &x) { return (const double *)x.d; });
     c->hg64.radius = c->radius;
@@ -568,8 +584,13 @@ int init_context(int res_id, int n_layers, int moisture_on, const void *grid_p, 
     c->sed_heat = dalloc<double>(c, NS);
     c->cp_ice = dalloc<double>(c, NS);
     c->cp_water = dalloc<double>(c, NS);
+    /* k_make_shadow moves element pairs: every field must start on an even
+     * element (true of every icosahedral grid: 10 * 4^RES_ID + 2 cells,
+     * 30 * 4^RES_ID edges) */
+    if (NC % 2 != 0 || NE % 2 != 0) return fail("grid with an odd number of cells or edges");
     c->shadow = dalloc<float>(c, (size_t)(c->n_const + 3) * NS + (size_t)(L + 1) * NC + (size_t)L * NE);
     c->theta32 = dalloc<float>(c, NS);
+    c->pg_cell = dalloc<float4>(c, NS);
     c->cp32_ice = dalloc<float>(c, NS);
     c->cp32_water = dalloc<float>(c, NS);
     c->gravity_potential = dupload(c, cell_field(gpot));
@@ -693,7 +714,7 @@ int destroy_context()
 
 /* --------------------------------------------------------- state mirrors */
 /* device layout pointers of a state block */
-static void set_mirror_views(Context *c, StateMirror &m)
+void set_mirror_views(Context *c, StateMirror &m)
 {
     const long long ns = c->ns;
     m.ds.rho = m.dev;

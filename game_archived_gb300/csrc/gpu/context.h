@@ -96,6 +96,9 @@ struct Context {
     /* mixed path: FP32 shadow of state_new and FP32 copies of per-step fields */
     float *shadow = nullptr;          /* [rho C*S][rhotheta S][theta' S][Pi' S][w (L+1)Nc][u L*Ne] */
     float *theta32 = nullptr, *cp32_ice = nullptr, *cp32_water = nullptr;
+    /* mixed path: pressure-gradient factors of the step start per (layer,
+     * cell): Pi', c_p theta_v, c_p theta_v', rho_gas / rho_total (k_pg_cells) */
+    float4 *pg_cell = nullptr;
     double *gravity_potential = nullptr; /* [L][Nc] */
     /* global integrals: per-block (hi, lo) partial sums, one counter and one
      * result per field, and three energy-density fields [3][L][Nc] */
@@ -228,6 +231,8 @@ int fail(const std::string &msg);
 int init_context(int res_id, int n_layers, int moisture_on, const void *grid, const void *dualgrid);
 int destroy_context();
 StateMirror *mirror(const void *host_state, int create);
+/* sets m.ds from m.dev (a state block of the context's layout) */
+void set_mirror_views(Context *c, StateMirror &m);
 int ensure_sub_buffers(Context *c);
 int ensure_diff_buffers(Context *c);
 /* the library's own pinned host allocations (game_gpu_host_alloc) and
@@ -243,6 +248,14 @@ int download_state_pinned(const void *host_state, StateMirror *m, int which_mask
 int upload_field(const double *host, double *dev, const int *map, long long n, long long host_len);
 int download_field(double *host, const double *dev, const int *map, long long n, long long host_len,
                    long long host_lo, long long host_hi);
+
+/* the mixed step's lagged fields in its FP32 work arrays (aux.cu), from and to
+ * device vector fields [w (L+1) Nc][u L Ne] of doubles: P the pressure
+ * gradient nl + l, pvt the vorticity flux, v2g the kinetic-energy gradient,
+ * flux the mass flux density (its levels 0 and L are read by the step);
+ * P, pvt and v2g may be null on load (zeros) */
+void aux_load_mixed(Context *c, const double *P, const double *pvt, const double *v2g, const double *flux);
+void aux_store_mixed(Context *c, double *P, double *pvt, double *v2g);
 
 /* health check of a State mirror (health.cu): 0 healthy, GAME_GPU_UNHEALTHY
  * with the message set, -1 on a CUDA error */

@@ -48,6 +48,7 @@ struct HGrid {
     const int *adj;         /* [6][Nc] edges of the cell, reference order */
     const int *adj_sign;    /* [6][Nc] +1 cell is the edge's from cell, -1 to cell, 0 none */
     const int *adj_nbr;     /* [6][Nc] cell on the other side of edge j */
+    const int *tilt;        /* [Nc] 1 where an edge of the cell has a nonzero slope in some layer */
     /* interfaces */
     const R *nd_v;          /* [L+1][Nc] vertical normal distance */
     const R *area_v;        /* [L+1][Nc] */

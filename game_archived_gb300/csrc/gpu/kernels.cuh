@@ -57,6 +57,8 @@ __device__ __forceinline__ R grad_h(const HGrid<R> &g, const F *f, int l, int e)
     const long long le = (long long)l * g.ne + e;
     R out = (R(f[(long long)l * g.nc + to]) - R(f[(long long)l * g.nc + fr])) / g.nd_h[le];
     if (l >= g.nl - g.n_oro) {
+        /* a zero slope adds -0: the mixed path skips it */
+        if (sizeof(R) == sizeof(float) && g.slope_h[le] == R(0)) return out;
         R c = ipw_at(g, 6, l, fr) * grad_v(g, f, l, fr);
         c += ipw_at(g, 6, l, to) * grad_v(g, f, l, to);
         if (l < g.nl - 1) {
@@ -76,6 +78,9 @@ __device__ __forceinline__ R hor_covariant(const HGrid<R> &g, const F *u, const 
     const long long le = (long long)l * g.ne + e;
     R r = R(u[le]);
     if (l >= g.nl - g.n_oro) {
+        const R slope = g.slope_h[le];
+        /* a zero slope adds 0: the mixed path skips it */
+        if (sizeof(R) == sizeof(float) && slope == R(0)) return r;
         const int fr = g.from[e], to = g.to[e];
         R c = ipw_at(g, 6, l, fr) * R(w[(long long)l * g.nc + fr]);
         c += ipw_at(g, 6, l, to) * R(w[(long long)l * g.nc + to]);
@@ -84,7 +89,7 @@ __device__ __forceinline__ R hor_covariant(const HGrid<R> &g, const F *u, const 
             c += ipw_at(g, 7, l, to) * R(w[(long long)(l + 1) * g.nc + to]);
         }
         c = R(0.5) * c;
-        r += g.slope_h[le] * c;
+        r += slope * c;
     }
     return r;
 }
@@ -376,19 +381,19 @@ __global__ void k_cell_prepare_f32(VGrid vg, StepParams p, DState so, double *te
     if (i >= ns) return;
     const int cond = p.n_cond;
     const double *rho = so.rho;
-    const float th = float(vg.theta_v_bg[i] + so.theta_v_pert[i]), pi = float(vg.exner_bg[i] + so.exner_pert[i]);
+    const float th = to_float(vg.theta_v_bg[i] + so.theta_v_pert[i]), pi = to_float(vg.exner_bg[i] + so.exner_pert[i]);
     if (!p.moist) {
-        temperature[i] = double(th) * double(pi);
+        temperature[i] = to_double(th) * to_double(pi);
         return;
     }
     float r[6];
-    for (int k = 0; k < 6; ++k) r[k] = float(rho[k * ns + i]);
+    for (int k = 0; k < 6; ++k) r[k] = to_float(rho[k * ns + i]);
     const float rv = r[cond + 1], rg = r[cond];
     const float T = th * pi / (1.f + rv / rg * float(M_D / M_V - 1.0));
-    temperature[i] = double(T);
+    temperature[i] = to_double(T);
     const float cpi = c_p_ice_f(T), cpw = c_p_water_f(T);
-    cp_ice_out[i] = double(cpi);
-    cp_water_out[i] = double(cpw);
+    cp_ice_out[i] = to_double(cpi);
+    cp_water_out[i] = to_double(cpw);
     cp32_ice[i] = cpi;
     cp32_water[i] = cpw;
     const float dt = float(p.dt), T0 = float(T_0);
@@ -476,26 +481,38 @@ __global__ void k_cell_prepare_f32(VGrid vg, StepParams p, DState so, double *te
         r0 -= r1;
         heat += -r1 * h_melt;
     }
-    pt_rates[i] = r0;
-    pt_rates[ns + i] = r1;
-    pt_rates[2 * ns + i] = r2;
-    pt_rates[3 * ns + i] = r3;
-    pt_rates[4 * ns + i] = r4;
-    pt_heat[i] = heat;
+    /* widened by integer operations (to_double): the FP64 pipe was this
+     * kernel's bound */
+    pt_rates[i] = to_double(r0);
+    pt_rates[ns + i] = to_double(r1);
+    pt_rates[2 * ns + i] = to_double(r2);
+    pt_rates[3 * ns + i] = to_double(r3);
+    pt_rates[4 * ns + i] = to_double(r4);
+    pt_heat[i] = to_double(heat);
 }
 
-/* FP32 shadow of the state at the start of a mixed step */
+/* FP32 shadow of the state at the start of a mixed step.  Each thread
+ * converts the pairs 2i, 2i + 1 of every field with one 16-byte load and one
+ * 8-byte store (every field length is even: 10 * 4^RES_ID + 2 cells, 30 *
+ * 4^RES_ID edges, so every field of the mirror and of the shadow starts on
+ * an even element), rounding with to_float (the conversion instruction's
+ * bits, on the integer pipe instead of the FP64 pipe). */
+__device__ __forceinline__ void shadow_pair(const double *src, float *dst, long long j)
+{
+    const double2 v = reinterpret_cast<const double2 *>(src)[j];
+    reinterpret_cast<float2 *>(dst)[j] = make_float2(to_float(v.x), to_float(v.y));
+}
 __global__ void k_make_shadow(long long n_rho, long long ns, long long nw, long long nu, DState s, Shadow sh)
 {
-    const long long i = gtid();
-    if (i < n_rho) sh.rho[i] = float(s.rho[i]);
-    if (i < ns) {
-        sh.rhotheta_v[i] = float(s.rhotheta_v[i]);
-        sh.theta_v_pert[i] = float(s.theta_v_pert[i]);
-        sh.exner_pert[i] = float(s.exner_pert[i]);
+    const long long j = gtid();
+    if (2 * j < n_rho) shadow_pair(s.rho, sh.rho, j);
+    if (2 * j < ns) {
+        shadow_pair(s.rhotheta_v, sh.rhotheta_v, j);
+        shadow_pair(s.theta_v_pert, sh.theta_v_pert, j);
+        shadow_pair(s.exner_pert, sh.exner_pert, j);
     }
-    if (i < nw) sh.w[i] = float(s.w[i]);
-    if (i < nu) sh.u[i] = float(s.u[i]);
+    if (2 * j < nw) shadow_pair(s.w, sh.w, j);
+    if (2 * j < nu) shadow_pair(s.u, sh.u, j);
 }
 
 /* ------------------------------------------------------- k_tri_vort
@@ -734,16 +751,74 @@ __device__ __forceinline__ R pgrad_v(const HGrid<R> &g, const StepParams &p, con
     return nl + l_term;
 }
 
+/* Mixed path: the cell factors of the pressure gradient at the step start,
+ * one float4 per (layer, cell): x = Pi', y = c_p (theta_v_bg + theta_v'),
+ * z = c_p theta_v', w = rho_gas / (sum of all densities) -- the float
+ * expressions of pgrad_h_parts / pgrad_v_parts, so that the first
+ * substage's gradients gather two float4 per edge (or interface) instead of
+ * some twenty scalars.  Read from the FP32 shadow of state_new, which the
+ * first substage's pressure gradient reads. */
+__global__ void k_pg_cells(HGrid<float> g, StepParams p, SView<float> s, float4 *pc)
+{
+    const long long ns = (long long)g.nl * g.nc;
+    const long long i = gtid();
+    if (i >= ns) return;
+    const float cdp = float(C_D_P);
+    const float tp = s.theta_v_pert[i];
+    pc[i] = make_float4(s.exner_pert[i], cdp * (g.theta_v_bg[i] + tp), cdp * tp,
+                        s.rho[p.n_cond * ns + i] / density_total_r(s.rho, p.n_const, ns, i));
+}
+
+/* pgrad_h from the cell factors (mixed path, first substage) */
+__device__ __forceinline__ float pgrad_h_packed(const HGrid<float> &g, const float4 *pc, const SView<float> &s, int l,
+                                                int e)
+{
+    const int fr = g.from[e], to = g.to[e];
+    const long long le = (long long)l * g.ne + e;
+    const float4 a = pc[(long long)l * g.nc + fr], b = pc[(long long)l * g.nc + to];
+    float nl = (b.x - a.x) / g.nd_h[le];
+    const float slope = l >= g.nl - g.n_oro ? g.slope_h[le] : 0.0f;
+    if (slope != 0.0f) { /* a zero slope adds -0 */
+        float c = ipw_at(g, 6, l, fr) * grad_v(g, s.exner_pert, l, fr);
+        c += ipw_at(g, 6, l, to) * grad_v(g, s.exner_pert, l, to);
+        if (l < g.nl - 1) {
+            c += ipw_at(g, 7, l, fr) * grad_v(g, s.exner_pert, l + 1, fr);
+            c += ipw_at(g, 7, l, to) * grad_v(g, s.exner_pert, l + 1, to);
+        }
+        c = 0.5f * c;
+        nl += -slope * c;
+    }
+    nl = (0.5f * (b.y + a.y)) * nl;
+    float l_term = (0.5f * (b.z + a.z)) * g.exner_bg_grad_h[le];
+    const float dec = 0.5f * (b.w + a.w);
+    nl = dec * nl;
+    l_term = dec * l_term;
+    return nl + l_term;
+}
+
+/* pgrad_v from the cell factors of the interface's two cells */
+__device__ __forceinline__ float pgrad_v_packed(const HGrid<float> &g, float4 u, float4 d, int k, int c)
+{
+    float nl = (u.x - d.x) / g.nd_v[(long long)k * g.nc + c];
+    nl = (0.5f * (u.y + d.y)) * nl;
+    float l_term = (0.5f * (u.z + d.z)) * g.exner_bg_grad_v[(long long)k * g.nc + c];
+    const float dec = 0.5f * (u.w + d.w);
+    nl = dec * nl;
+    l_term = dec * l_term;
+    return nl + l_term;
+}
+
 /* ------------------------------------------------------- k_momentum_h
  * horizontal momentum: explicit tendency (vector_tendencies_expl.c:74-131) and
  * the wind update (manage_rkhevi.c:67-75).  ADV: the advection terms are
- * recomputed in this substage; PG: the pressure gradient is recomputed.
- * The wind update is FP64; u_shadow (mixed path) receives its FP32 copy. */
+ * recomputed in this substage; PG: the pressure gradient is recomputed (on
+ * the mixed path from the cell factors pc of k_pg_cells).  The wind update
+ * is FP64; u_shadow (mixed path) receives its FP32 copy. */
 template <typename R, bool ADV, bool PG>
 __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_momentum_h(HGrid<R> g, StepParams p, SView<R> sv, double *u_new, float *u_shadow, const double *u_old,
                              double *tend_u, R *P_h, R *pg_old_h, R *pvt_h, R *v2g_h, const R *flux_h,
                              const R *flux_v, const R *zh, const R *zv, const R *v2, double new_w, double old_w,
-                             const double *fric_u)
+                             const double *fric_u, const float4 *pc)
 {
     const long long n = (long long)g.nl * g.ne;
     const long long i = gtid();
@@ -751,7 +826,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_mom
     const int l = (int)(i / g.ne), e = (int)(i - (long long)l * g.ne);
     R P, pgo;
     if (PG) {
-        P = pgrad_h(g, p, sv, l, e);
+        if constexpr (sizeof(R) == sizeof(float))
+            P = pgrad_h_packed(g, pc, sv, l, e);
+        else
+            P = pgrad_h(g, p, sv, l, e);
         pgo = p.first_step ? -P : -P_h[i];
         P_h[i] = P;
         pg_old_h[i] = pgo;
@@ -789,7 +867,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_mom
 template <typename R, bool ADV, bool PG>
 __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_momentum_v(HGrid<R> g, StepParams p, SView<R> sv, double *tend_w, R *P_v, R *pvt_v, R *v2g_v,
                              const R *flux_h, const R *zh, const R *v2, double new_w, double old_w,
-                             const double *fric_w)
+                             const double *fric_w, const float4 *pc)
 {
     const long long n = (long long)(g.nl + 1) * g.nc;
     const long long i = gtid();
@@ -818,9 +896,19 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_mom
         tend_w[i] = 0.0;
         return;
     }
-    R P, v2g;
+    /* the mixed path's first substage takes the pressure gradient and the
+     * condensate factors from the cell factors pc of k_pg_cells */
+    constexpr bool PACKED = PG && sizeof(R) == sizeof(float);
+    R P, v2g, d_up, d_lo;
     if (PG) {
-        P = pgrad_v(g, p, sv, k, c);
+        if constexpr (PACKED) {
+            const float4 fu = pc[(long long)(k - 1) * g.nc + c], fd = pc[(long long)k * g.nc + c];
+            P = pgrad_v_packed(g, fu, fd, k, c);
+            d_up = fu.w - 1.0f;
+            d_lo = fd.w - 1.0f;
+        } else {
+            P = pgrad_v(g, p, sv, k, c);
+        }
         P_v[i] = P;
     } else {
         P = P_v[i];
@@ -832,10 +920,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 8 : 1) k_mom
         pvt = pvt_v[i];
         v2g = v2g_v[i];
     }
-    const long long ns = (long long)nl * g.nc;
-    const long long up = (long long)(k - 1) * g.nc + c, lo = (long long)k * g.nc + c;
-    R d_up = sv.rho[p.n_cond * ns + up] / density_total_r(sv.rho, p.n_const, ns, up) - R(1);
-    R d_lo = sv.rho[p.n_cond * ns + lo] / density_total_r(sv.rho, p.n_const, ns, lo) - R(1);
+    if constexpr (!PACKED) {
+        const long long ns = (long long)nl * g.nc;
+        const long long up = (long long)(k - 1) * g.nc + c, lo = (long long)k * g.nc + c;
+        d_up = sv.rho[p.n_cond * ns + up] / density_total_r(sv.rho, p.n_const, ns, up) - R(1);
+        d_lo = sv.rho[p.n_cond * ns + lo] / density_total_r(sv.rho, p.n_const, ns, lo) - R(1);
+    }
     R pgc = (R(0.5) * (d_up + d_lo)) * g.gravity_m_v[i];
     const R cur_ver = sizeof(R) == sizeof(float) ? R(p.cur_ver_f) : R(p.cur_ver);
     R y = -cur_ver * P + pvt - R(0.5) * v2g;
@@ -933,7 +1023,9 @@ __global__ void __launch_bounds__(128) k_scalar_tend2(HGrid<R> g, StepParams p, 
     const long long nc = g.nc, ne = g.ne;
     const int n_edges = c < N_PENT ? 5 : 6;
     const int cond = p.n_cond;
-    const bool oro = l >= nl - n_oro - 1;
+    /* terrain-following corrections: in the orography layers (on the mixed
+     * path only where the cell's edges slope; elsewhere they are zero) */
+    const bool oro = l >= nl - n_oro - 1 && (sizeof(R) == sizeof(double) || g.tilt[c]);
     const bool up_corr = oro && l >= nl - n_oro;            /* contra_corr at level l needed   */
     const bool lo_corr = oro && l < nl - 1;                 /* contra_corr at level l+1 needed */
     const bool up_has_prev = up_corr && l > nl - n_oro;     /* level l sums layer l-1, then l  */

@@ -85,6 +85,13 @@ __device__ __forceinline__ double to_double(float x)
     if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
     return (double)x;
 }
+/* x == +-0 by an integer test (an FP64 comparison would issue on the FP64
+ * pipe) */
+__device__ __forceinline__ bool is_zero(double x) { return ((unsigned long long)__double_as_longlong(x) << 1) == 0ULL; }
+
+/* a double passed to either conversion would be narrowed silently */
+double to_double(double) = delete;
+float to_float(float) = delete;
 __device__ __forceinline__ double wide(float x) { return to_double(x); }
 __device__ __forceinline__ double wide(double x) { return x; }
 

@@ -173,13 +173,18 @@ __global__ void k_tracers_sedheat_df(VGrid vg, StepParams p, DState so, DState s
     const int j = (int)(b / nc), i = (int)(b - (long long)j * nc);
     const int n_cond = p.n_cond < SEDHEAT_MAX_COND ? p.n_cond : SEDHEAT_MAX_COND;
     /* enthalpy flux of constituent k at interface jj (below layer jj) */
+    /* a condensate's flux is c_p T rho w A with rho its upstream density:
+     * exactly zero where that density is (no cloud), so the double-float
+     * products are skipped there */
     auto fe = [&](int k, int jj, df vs, bool has) {
         const long long bb = i + (long long)jj * nc, wi = bb + nc;
         df b_ = df_from_double(sn.w[wi]);
         if (has) b_ = df_sub(b_, vs);
         b_ = df_mul(ld_df(dg.area_v, wi), b_);
         const long long up = df_nonneg(b_) ? bb + nc : bb;
-        const df fr = df_mul(df_from_double(so.rho[k * ns + up]), b_);
+        const double r_up = so.rho[k * ns + up];
+        if (is_zero(r_up)) return df_zero();
+        const df fr = df_mul(df_from_double(r_up), b_);
         const df cp = df_from_double((k % 2 == 0) ? tw.cp_ice[up] : tw.cp_water[up]);
         return df_mul(df_mul(cp, df_from_double(temperature[up])), fr);
     };
@@ -195,11 +200,14 @@ __global__ void k_tracers_sedheat_df(VGrid vg, StepParams p, DState so, DState s
         } else if (j == nl - 1) {
             sh = df_add(sh, df_mul(df_neg(fe(k, j - 1, vs, has)), ivol));
             const long long bot = b;
-            const df cp = df_from_double((k % 2 == 0) ? tw.cp_ice[bot] : tw.cp_water[bot]);
-            const df e = df_mul(df_mul(df_mul(df_mul(df_neg(vs), df_from_double(temperature[bot])), cp),
-                                       df_from_double(so.rho[k * ns + bot])),
-                                ld_df(dg.area_v, (long long)nl * nc + i));
-            sh = df_add(sh, df_mul(e, ivol));
+            const double r_bot = so.rho[k * ns + bot];
+            if (!is_zero(r_bot)) {
+                const df cp = df_from_double((k % 2 == 0) ? tw.cp_ice[bot] : tw.cp_water[bot]);
+                const df e = df_mul(df_mul(df_mul(df_mul(df_neg(vs), df_from_double(temperature[bot])), cp),
+                                           df_from_double(r_bot)),
+                                    ld_df(dg.area_v, (long long)nl * nc + i));
+                sh = df_add(sh, df_mul(e, ivol));
+            }
         } else {
             sh = df_add(sh, df_mul(df_add(df_neg(fe(k, j - 1, vs, has)), fe(k, j, vs, has)), ivol));
         }

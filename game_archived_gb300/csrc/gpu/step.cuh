@@ -111,8 +111,9 @@ static void launch_momentum_v(Context *c, const StepParams &p, const Views<R> &v
     Work<R> &w = work<R>(c);
     ProfScope ps(c, "k_momentum_v");
     const double *fric_w = p.irr ? c->dbuf->fric : nullptr;
+    const float4 *pc = sizeof(R) == sizeof(float) && PG ? c->pg_cell : nullptr;
     k_momentum_v<R, ADV, PG><<<nblocks((long long)(c->nl + 1) * c->nc, 256), 256, 0, c->stream>>>(
-        g, p, v.sv, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w, fric_w);
+        g, p, v.sv, st->ds.w, w.P_v, w.pvt_v, w.v2g_v, w.flux_h, w.zh, w.v2, new_w, old_w, fric_w, pc);
     c->kernel_launches++;
 }
 
@@ -124,9 +125,10 @@ static void launch_momentum_h(Context *c, const StepParams &p, const Views<R> &v
     Work<R> &w = work<R>(c);
     ProfScope ps(c, "k_momentum_h");
     const double *fric_u = p.irr ? c->dbuf->fric + (long long)(c->nl + 1) * c->nc : nullptr;
+    const float4 *pc = sizeof(R) == sizeof(float) && PG ? c->pg_cell : nullptr;
     k_momentum_h<R, ADV, PG><<<nblocks((long long)c->nl * c->ne, 256), 256, 0, c->stream>>>(
         g, p, v.sv, sn->ds.u, v.sh.u, so->ds.u, st->ds.u, w.P_h, w.pg_old_h, w.pvt_h, w.v2g_h, w.flux_h, w.flux_v,
-        w.zh, w.zv, w.v2, new_w, old_w, fric_u);
+        w.zh, w.zv, w.v2, new_w, old_w, fric_u, pc);
     c->kernel_launches++;
 }
 
@@ -268,8 +270,15 @@ void launch_step(Context *c, const StepParams &p, StateMirror *so, StateMirror *
         ProfScope ps(c, "k_make_shadow");
         const long long n_rho = (long long)c->n_const * ns, nw = (long long)(c->nl + 1) * c->nc,
                         nu = (long long)c->nl * c->ne;
-        k_make_shadow<<<nblocks(std::max(std::max(n_rho, nw), nu), bs), bs, 0, c->stream>>>(n_rho, ns, nw, nu, sn->ds,
-                                                                                            v.sh);
+        const long long pairs = (std::max(std::max(n_rho, nw), nu) + 1) / 2;
+        k_make_shadow<<<nblocks(pairs, bs), bs, 0, c->stream>>>(n_rho, ns, nw, nu, sn->ds, v.sh);
+        c->kernel_launches++;
+    }
+    if constexpr (!EXACT) {
+        /* the first substage's pressure-gradient factors per cell (the
+         * diffusion branch, which runs before it, changes none of its inputs) */
+        ProfScope ps(c, "k_pg_cells");
+        k_pg_cells<<<nblocks(ns, bs), bs, 0, c->stream>>>(c->hg32, p, v.sv, c->pg_cell);
         c->kernel_launches++;
     }
     {

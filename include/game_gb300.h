@@ -267,13 +267,23 @@ int game_gpu_write_out_integral(struct state *state, int integral_id, double *re
  * No counterpart function in the reference (the loop is inside write_out). */
 int game_gpu_surface_pressure(struct state *state, double *surface_p, double *mslp);
 
-/* ---- 4. adjoint and tangent-linear models of the step (dry build) ----
+/* ---- 4. adjoint and tangent-linear models of the step ----
  *
- * A window of n_steps RKHEVI steps of the FP64 dry step, with hand-written
- * adjoint kernels for every operator of the step (pressure gradient,
- * vorticities, vorticity flux, kinetic energy and its gradient, momentum
- * tendencies, flux divergences, the sound-wave rows, the tridiagonal solve and
- * its back-substitution).  No counterpart in the reference.
+ * A window of n_steps RKHEVI steps, with hand-written adjoint kernels for
+ * every operator of the step (pressure gradient, vorticities, vorticity
+ * flux, kinetic energy and its gradient, momentum tendencies, flux
+ * divergences, the sound-wave rows, the tridiagonal solve and its
+ * back-substitution; on the moist build also the temperature and phase
+ * transitions of every step, the moist scalar tendencies, the tracer column
+ * solve with its sedimentation heat and the condensate terms of the
+ * momentum).  No counterpart in the reference.
+ *
+ * The forward of record runs in the library's precision
+ * (game_gpu_set_precision): GAME_GPU_FP64, the FP64 step; GAME_GPU_MIXED,
+ * the fused mixed step itself, so that state_final is what a mixed run
+ * produces.  The tangent-linear and adjoint models are FP64 in both cases,
+ * linearised about the forward's checkpointed trajectory.  A mixed window
+ * leaves the lagged step fields of a device-resident run as it found them.
  *
  * rkhevi_window_forward runs the window from state_init as the reference's
  * time loop would (src/coordinator.c:302-324: each step starts with
@@ -296,9 +306,12 @@ int game_gpu_surface_pressure(struct state *state, double *surface_p, double *ms
  * game_gpu_sfc_pressure_objective: J = sum_i weights[i] p_sfc,i^2 over the
  * columns (surface pressure of src/io/write_output.c:105-121, reference
  * column order) and, when state_bar is not NULL, dJ/dstate written to
- * state_bar (nonzero on the lowest layer's rho, theta_v_pert, exner_pert).
+ * state_bar (nonzero on the lowest layer's rho, theta_v_pert, exner_pert;
+ * moist build: the gas constant of the moist air and the temperature of
+ * temperature_diagnostics, so also the vapour density).
  *
- * Dry build only (MOISTURE_ON = 0): other builds return an error. */
+ * The dry build and the moist build of six constituents; the diffusion
+ * switches and the Held-Suarez forcing must be off (an error otherwise). */
 /* Adjoints of the single operators, the reverse half of each forward/backward
  * pair.  Host arrays in the reference layouts of the forward call.  Bars of
  * the forward's inputs are accumulated (in_bar += (d out / d in)^T out_bar),

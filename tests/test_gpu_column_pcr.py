@@ -81,8 +81,8 @@ def test_column_solver_matches_oracle(cfg):
         assert max(v for f, v in e.items() if f != "exner_pert") <= TOL, f"step {n}: {e}"
 
 
-def _run(m, precision, solver, steps, dt):
-    g = abi.GpuModel(m, precision, column_solver=solver)
+def _run(m, precision, solver, steps, dt, double_float=1):
+    g = abi.GpuModel(m, precision, column_solver=solver, double_float=double_float)
     try:
         driver.run(m, steps, dt, g.linear_combine_two_states, g.manage_rkhevi)
     finally:
@@ -106,15 +106,35 @@ def test_mixed_pcr_close_to_fp64(n_layers, solver):
 
 @pytest.mark.parametrize("n_layers", [26, 80])
 def test_mixed_pcr_equals_thomas_to_rounding(n_layers):
-    """mixed path: the cyclic reduction and the Thomas sweeps solve the same
-    systems, so two steps agree far below the mixed path's own error"""
+    """mixed path with FP64 eliminations: the cyclic reduction and the Thomas
+    sweeps solve the same systems, so two steps agree far below the mixed
+    path's own error"""
     _, m_a = make_model(3, 1, "jet_moist", False, n_layers=n_layers)
     m_b = clone(m_a)
-    _run(m_a, abi.MIXED, 1, 2, 300.0)
+    _run(m_a, abi.MIXED, 1, 2, 300.0, double_float=0)
+    _run(m_b, abi.MIXED, 2, 2, 300.0, double_float=0)
+    e = state_errors(m_b.state_new, m_a.state_new, m_a.layout)
+    print(f"mixed, {n_layers} layers, cyclic reduction vs FP64 Thomas sweeps after 2 steps: {e}")
+    assert max(e.values()) < 1e-9, e
+
+
+def test_mixed_pcr_close_to_double_float_thomas():
+    """the default mixed path at 26 layers sweeps in double-float (48
+    significand bits): its inputs' rounding, 2^-48, is amplified by the
+    acoustic system's condition number (of order (c dt / dz)^2, about 1e4 at
+    dt = 300 s on this grid), so two steps agree with the FP64 cyclic
+    reduction to about 1e-10 in the state and 1e-7 in the (small) vertical
+    wind -- still far below the mixed path's own error against FP64 (1e-6
+    in w after one step)"""
+    _, m_a = make_model(3, 1, "jet_moist", False, n_layers=26)
+    m_b = clone(m_a)
+    _run(m_a, abi.MIXED, 1, 2, 300.0, double_float=1)
     _run(m_b, abi.MIXED, 2, 2, 300.0)
     e = state_errors(m_b.state_new, m_a.state_new, m_a.layout)
-    print(f"mixed, {n_layers} layers, cyclic reduction vs Thomas sweeps after 2 steps: {e}")
-    assert max(e.values()) < 1e-9, e
+    print(f"mixed, 26 layers, cyclic reduction vs double-float Thomas sweeps after 2 steps: {e}")
+    w = e.pop("wind_v")
+    assert w < 1e-6, w
+    assert max(e.values()) < 1e-8, e
 
 
 def test_solver_switch_and_layer_limit():
