@@ -89,11 +89,14 @@ def kernel_bytes(res, n_const, r, nl=L):
     out["k_edge_vort"] = ((ul + wl + s) * r + tl * r + 4 * ne * i + zl * r + ul * r + wl * r + 6 * ne * r
                           + 4 * ne * (r + i) + tl * r + zl * r + 2 * ul * r, 1)
     out["k_cell_kinetic"] = ((ul + wl + s) * r + 8 * s * r + 6 * nc * i + s * r + wl * r, 1)
-    rk0_h = (3 + C) * s * r + 3 * ul * r + 2 * ne * i + 3 * ul * r + 2 * ul * r + 3 * ul * d + ul * r
+    # first substage: the pressure gradient gathers one float4 of cell
+    # factors per cell (k_pg_cells)
+    out["k_pg_cells"] = ((C + 3) * s * r + 4 * s * r, 1)
+    rk0_h = 4 * s * r + 3 * ul * r + 2 * ne * i + 3 * ul * r + 2 * ul * r + 3 * ul * d + ul * r
     rk1_h = (2 * ul + zl) * r + 10 * ne * (r + 2 * i) + 2 * ne * i + 2 * s * r + wl * r + s * r + ul * r \
         + 4 * ul * r + 2 * ul * d + ul * d + ul * d + ul * r
     out["k_momentum_h"] = (rk0_h + rk1_h, 2)
-    rk0_v = (3 + C) * s * r + 2 * wl * r + wl * r + 2 * wl * r + wl * r + wl * d
+    rk0_v = 4 * s * r + 2 * wl * r + wl * r + 2 * wl * r + wl * r + wl * d
     rk1_v = 6 * nc * i + 6 * s * r + ul * r + zl * r + 4 * wl * r + s * r + C * s * r + wl * r + 2 * wl * d
     out["k_momentum_v"] = (rk0_v + rk1_v, 2)
     out["k_theta"] = (2 * 3 * s * r, 2)

@@ -161,8 +161,9 @@ void launch_waves(Context *c, const StepParams &p, StateMirror *so, StateMirror 
             }
             {
                 ProfScope ps(c, "k_waves_thomas");
-                k_waves_thomas_df<NL_FIXED><<<nblocks(c->nc, WAVES_BLOCK), WAVES_BLOCK, 0, c->stream>>>(c->nc, ww,
-                                                                                                       c->dfg);
+                /* two lanes per column (twisted elimination) */
+                k_waves_thomas_df<NL_FIXED><<<nblocks(2 * (long long)c->nc, WAVES_BLOCK), WAVES_BLOCK, 0,
+                                              c->stream>>>(c->nc, ww, c->dfg);
             }
             {
                 ProfScope ps(c, "k_waves_apply");
