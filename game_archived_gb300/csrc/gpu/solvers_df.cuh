@@ -65,6 +65,27 @@ __global__ void __launch_bounds__(TRACER_BLOCK) k_tracers_solve_df(VGrid vg, Ste
     const df half_dt = df_half(dtd);
     const double *ro = so.rho + k * ns;
     const double *tr = st.rho + k * ns;
+    {
+        /* a constituent absent from the column, old density and tendency 0 in
+         * every layer (a cloud-free column's condensates): the system's
+         * right-hand side is 0 and so is the new density, exactly */
+        bool empty = true;
+#pragma unroll 1
+        for (int j = 0; j < nl && empty; ++j) {
+            const long long b = (long long)j * nc + i;
+            empty = is_zero(ro[b]) && is_zero(tr[b]);
+        }
+        if (empty) {
+            double *rn = sn.rho + k * ns;
+            float *rs = sh_rho + k * ns;
+#pragma unroll 1
+            for (int j = 0; j < nl; ++j) {
+                rn[(long long)j * nc + i] = 0.0;
+                rs[(long long)j * nc + i] = 0.0f;
+            }
+            return;
+        }
+    }
     const df a_sfc = ld_df(dg.area_v, (long long)nl * nc + i);
     df fi_prev = df_zero(), fr_prev = df_zero(), ep_prev = df_zero(), rp_prev = df_zero();
     df ro_j = df_from_double(ro[i]), ro_prev = df_zero();
@@ -175,9 +196,12 @@ __global__ void k_tracers_sedheat_df(VGrid vg, StepParams p, DState so, DState s
     /* enthalpy flux of constituent k at interface jj (below layer jj) */
     /* a condensate's flux is c_p T rho w A with rho its upstream density:
      * exactly zero where that density is (no cloud), so the double-float
-     * products are skipped there */
+     * products are skipped there, and the upwind choice too where both
+     * candidate densities are zero */
     auto fe = [&](int k, int jj, df vs, bool has) {
         const long long bb = i + (long long)jj * nc, wi = bb + nc;
+        /* no density on either side: zero whichever way the wind blows */
+        if (is_zero(so.rho[k * ns + bb]) && is_zero(so.rho[k * ns + bb + nc])) return df_zero();
         df b_ = df_from_double(sn.w[wi]);
         if (has) b_ = df_sub(b_, vs);
         b_ = df_mul(ld_df(dg.area_v, wi), b_);
