@@ -600,9 +600,9 @@ int swap_step_fields(Context *c, AdjState *a, bool save)
     return 0;
 }
 
-/* the window's steps by the fused mixed step (checkpoint 0 written): as the
- * reference's time loop runs them, state_new = state_old at every step start;
- * each step's end state and its lagged fields become the next checkpoint */
+/* the window's steps by the fused mixed step (checkpoint 0 written), started
+ * as the reference's time loop starts them (below); each step's end state
+ * and its lagged fields become the next checkpoint */
 int window_forward_mixed(Context *c, AdjState *a, const StepParams &p, int n_steps, const double *aux_P,
                          const double *aux_pvt, const double *aux_v2g, const double *flux, const double *aux_sed)
 {
