@@ -19,6 +19,7 @@ SIGNATURES = {
     "game_gpu_set_graphs": ([cint], cint),
     "game_gpu_set_column_solver": ([cint], cint),
     "game_gpu_set_double_float": ([cint], cint),
+    "game_gpu_set_checkpoint_stride": ([cint], cint),
     "game_gpu_sync_to_device": ([vp], cint),
     "game_gpu_sync_to_host": ([vp], cint),
     "game_gpu_sync_aux_to_host": ([vp, vp, vp], cint),
@@ -364,6 +365,9 @@ class GpuModel:
         self._check(self.lib.rkhevi_window_forward(s_init.ptr, s_final.ptr, m.grid.ptr, m.dualgrid.ptr,
                                                    m.diagnostics.ptr, m.forcings.ptr, m.irrev.ptr, m.config.ptr,
                                                    dt, n_steps), "rkhevi_window_forward")
+
+    def set_checkpoint_stride(self, every):
+        self._check(self.lib.game_gpu_set_checkpoint_stride(every), "set_checkpoint_stride")
 
     def window_tl(self, s_dot, s_final_dot):
         self._check(self.lib.rkhevi_window_tl(s_dot.ptr, s_final_dot.ptr), "rkhevi_window_tl")

@@ -1214,6 +1214,14 @@ int manage_rkhevi_adj(struct state *state_old, struct state *state_new, struct g
     return adj_download(state_old_bar, &b.sn, b.sn.dev);
 }
 
+int game_gpu_set_checkpoint_stride(int every)
+{
+    if (check_ready(nullptr)) return -1;
+    if (every < 1) return fail("game_gpu_set_checkpoint_stride: a stride of at least 1 expected");
+    ctx()->adj_ck_every = every;
+    return 0;
+}
+
 int rkhevi_window_tl(struct state *state_init_dot, struct state *state_final_dot)
 {
     if (check_ready(nullptr)) return -1;

@@ -127,8 +127,12 @@ struct AdjState {
     StepBufs<Dual> D;            /* tangent-linear run */
     double *rn_b = nullptr, *rtn_b = nullptr;
     double *dden = nullptr, *fv_bounds = nullptr; /* (L+1) Nc */
-    double *ck = nullptr;        /* checkpoints: (n_steps + 1) x (state block + 3 Vt) */
-    int ck_cap = -1;
+    /* checkpoints of every ck_every-th step start and of the window's end,
+     * (state block + 3 Vt [+ S]) each, and one scratch slot for the start
+     * of a step recomputed from the nearest checkpoint before it */
+    double *ck = nullptr, *ck_tmp = nullptr;
+    long long ck_cap = -1;       /* slots allocated */
+    int ck_every = 1;
     double *obj_w = nullptr, *obj_p = nullptr, *obj_out = nullptr; /* objective work */
     /* lagged fields between tangent-linear steps: P, pvt, v2g and (moist) the
      * sedimentation heat */
@@ -464,11 +468,23 @@ void step_bwd(Context *c, AdjState *a, bool first, double *s2b, const double *P_
     c->kernel_launches += moist ? 46 : 40;
 }
 
+/* checkpoint slot of step start n: every ck_every-th step and the window's
+ * end are stored; any other start lives in the scratch slot, valid after the
+ * previous step was run (forward) or recomputed (backward) into it */
+bool ck_stored(const AdjState *a, int n) { return n % a->ck_every == 0 || n == a->n_steps; }
+double *ck_ptr(const AdjState *a, int n)
+{
+    const int K = a->ck_every;
+    if (n % K == 0) return a->ck + (long long)(n / K) * ck_stride(a);
+    if (n == a->n_steps) return a->ck + (long long)(a->n_steps / K + 1) * ck_stride(a);
+    return a->ck_tmp;
+}
+
 /* the step-start state of step n from its checkpoint: theta_v' rediagnosed */
 template <class T>
 void load_start(Context *c, AdjState *a, int n, T *so_blk)
 {
-    const double *ck = a->ck + (long long)n * ck_stride(a);
+    const double *ck = ck_ptr(a, n);
     if constexpr (sizeof(T) == sizeof(double))
         ku_copy<double><<<nbk(a->nblk), 256, 0, c->stream>>>(a->nblk, ck, (double *)so_blk);
     fa_rediag<T><<<nbk(a->ns), 256, 0, c->stream>>>(c->vg, view(a, so_blk));
@@ -476,7 +492,24 @@ void load_start(Context *c, AdjState *a, int n, T *so_blk)
 
 const double *ck_aux(const AdjState *a, int n, int which) /* 0 P, 1 pvt, 2 v2g, 3 sedimentation heat */
 {
-    return a->ck + (long long)n * ck_stride(a) + a->nblk + (long long)which * a->nv;
+    return ck_ptr(a, n) + a->nblk + (long long)which * a->nv;
+}
+
+/* the FP64 step n of the window from its start's checkpoint, its end state
+ * and lagged fields written to the checkpoint of start n + 1 */
+void step_to_checkpoint(Context *c, AdjState *a, int n)
+{
+    cudaStream_t st = c->stream;
+    const bool moist = moist_of(a);
+    load_start<double>(c, a, n, a->B.so);
+    step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2), moist ? ck_aux(a, n, 3) : nullptr,
+                     a->first && n == 0);
+    double *ckn = ck_ptr(a, n + 1);
+    ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->B.sn2, ckn);
+    ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.P, ckn + a->nblk);
+    ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.pvt[1], ckn + a->nblk + a->nv);
+    ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.v2g[1], ckn + a->nblk + 2 * a->nv);
+    if (moist) ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, a->B.sed, ckn + a->nblk + 3 * a->nv);
 }
 
 /* --------------------------------------------------------------- objective */
@@ -617,7 +650,7 @@ int window_forward_mixed(Context *c, AdjState *a, const StepParams &p, int n_ste
     if (moist) ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, aux_sed, c->sed_heat);
     int rc = 0;
     for (int n = 0; n < n_steps && !rc; ++n) {
-        const double *ck_in = a->ck + (long long)n * ck_stride(a);
+        const double *ck_in = ck_ptr(a, n);
         /* the step start as the reference's time loop leaves it:
          * linear_combine_two_states(state_new -> state_old) rediagnoses
          * theta_v' in state_old only, state_new keeps the previous step's
@@ -631,7 +664,7 @@ int window_forward_mixed(Context *c, AdjState *a, const StepParams &p, int n_ste
         pn.first_step = a->first && n == 0 ? 1 : 0;
         rc = launch_step_mixed(c, pn, &a->mso, &a->msn, &a->mst);
         if (rc) break;
-        double *ckn = a->ck + (long long)(n + 1) * ck_stride(a);
+        double *ckn = ck_ptr(a, n + 1);
         ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->msn.dev, ckn);
         aux_store_mixed(c, ckn + a->nblk, ckn + a->nblk + a->nv, ckn + a->nblk + 2 * a->nv);
         if (moist) ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, c->sed_heat, ckn + a->nblk + 3 * a->nv);
@@ -650,12 +683,19 @@ int adj_window_forward(Context *c, StateMirror *init, const StepParams &p, int n
     if (ensure_adj(c)) return -1;
     AdjState *a = c->adj;
     if (n_steps < 1) return fail("adjoint window: n_steps must be at least 1");
-    if (a->ck_cap < n_steps) {
-        double *ck = aalloc<double>(a, (long long)(n_steps + 1) * ck_stride(a));
+    a->ck_every = c->adj_ck_every;
+    /* the multiples of ck_every, the end when it is not one, and (stride
+     * above 1) the scratch slot after them */
+    const int K = a->ck_every;
+    const long long stored = n_steps / K + 1 + (n_steps % K != 0 ? 1 : 0);
+    const long long slots = stored + (K > 1 ? 1 : 0);
+    if (a->ck_cap < slots) {
+        double *ck = aalloc<double>(a, slots * ck_stride(a));
         if (!ck) return fail("adjoint window: device allocation of the checkpoints failed");
         a->ck = ck;
-        a->ck_cap = n_steps;
+        a->ck_cap = slots;
     }
+    a->ck_tmp = K > 1 ? a->ck + stored * ck_stride(a) : nullptr;
     if (set_params(c, a, p)) return -1;
     a->n_steps = n_steps;
     a->first = p.first_step ? 1 : 0;
@@ -682,23 +722,10 @@ int adj_window_forward(Context *c, StateMirror *init, const StepParams &p, int n
     if (c->precision == PREC_MIXED) {
         if (window_forward_mixed(c, a, p, n_steps, aux_P, aux_pvt, aux_v2g, fv_bounds, aux_sed)) return -1;
     } else {
-        for (int n = 0; n < n_steps; ++n) {
-            load_start<double>(c, a, n, a->B.so);
-            const bool first = a->first && n == 0;
-            step_fwd<double>(c, a, a->B, ck_aux(a, n, 0), ck_aux(a, n, 1), ck_aux(a, n, 2),
-                             moist ? ck_aux(a, n, 3) : nullptr, first);
-            double *ckn = a->ck + (long long)(n + 1) * ck_stride(a);
-            ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->B.sn2, ckn);
-            ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.P, ckn + a->nblk);
-            ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.pvt[1], ckn + a->nblk + a->nv);
-            ku_copy<double><<<nbk(a->nv), 256, 0, st>>>(a->nv, a->B.v2g[1], ckn + a->nblk + 2 * a->nv);
-            if (moist) ku_copy<double><<<nbk(a->ns), 256, 0, st>>>(a->ns, a->B.sed, ckn + a->nblk + 3 * a->nv);
-        }
+        for (int n = 0; n < n_steps; ++n) step_to_checkpoint(c, a, n);
     }
     a->have = 1;
-    if (final_out)
-        ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->ck + (long long)n_steps * ck_stride(a),
-                                                      final_out->dev);
+    if (final_out) ku_copy<double><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, ck_ptr(a, n_steps), final_out->dev);
     CK(cudaGetLastError());
     return 0;
 }
@@ -720,14 +747,26 @@ int adj_window_tl(Context *c, const double *init_dot, double *final_dot)
     /* every step is linearised about its checkpoint: values from checkpoint
      * n, derivatives carried from step n - 1 */
     for (int n = 0; n < a->n_steps; ++n) {
-        if (n > 0) ku_reseed<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, a->ck + (long long)n * ck_stride(a), D.sn2, D.so);
+        /* a step whose start is not stored carries the values of the step
+         * before it, as the backward sweep recomputes them */
+        if (n > 0 && ck_stored(a, n))
+            ku_reseed<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, ck_ptr(a, n), D.sn2, D.so);
+        else if (n > 0)
+            ku_copy<Dual><<<nbk(a->nblk), 256, 0, st>>>(a->nblk, D.sn2, D.so);
         fa_rediag<Dual><<<nbk(a->ns), 256, 0, st>>>(c->vg, view(a, D.so));
         step_fwd<Dual>(c, a, D, a->tl_aux[0], a->tl_aux[1], a->tl_aux[2], moist ? a->tl_aux[3] : nullptr,
                        a->first && n == 0);
-        ku_reseed<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, n + 1, 0), D.P, a->tl_aux[0]);
-        ku_reseed<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, n + 1, 1), D.pvt[1], a->tl_aux[1]);
-        ku_reseed<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, n + 1, 2), D.v2g[1], a->tl_aux[2]);
-        if (moist) ku_reseed<<<nbk(a->ns), 256, 0, st>>>(a->ns, ck_aux(a, n + 1, 3), D.sed, a->tl_aux[3]);
+        if (ck_stored(a, n + 1)) {
+            ku_reseed<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, n + 1, 0), D.P, a->tl_aux[0]);
+            ku_reseed<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, n + 1, 1), D.pvt[1], a->tl_aux[1]);
+            ku_reseed<<<nbk(a->nv), 256, 0, st>>>(a->nv, ck_aux(a, n + 1, 2), D.v2g[1], a->tl_aux[2]);
+            if (moist) ku_reseed<<<nbk(a->ns), 256, 0, st>>>(a->ns, ck_aux(a, n + 1, 3), D.sed, a->tl_aux[3]);
+        } else {
+            ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.P, a->tl_aux[0]);
+            ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.pvt[1], a->tl_aux[1]);
+            ku_copy<Dual><<<nbk(a->nv), 256, 0, st>>>(a->nv, D.v2g[1], a->tl_aux[2]);
+            if (moist) ku_copy<Dual><<<nbk(a->ns), 256, 0, st>>>(a->ns, D.sed, a->tl_aux[3]);
+        }
     }
     ku_dual_part<<<nbk(a->nblk), 256, 0, st>>>(a->nblk, D.sn2, final_dot);
     CK(cudaGetLastError());
@@ -745,6 +784,10 @@ int adj_window_backward(Context *c, const double *final_bar, double *init_bar)
     bool have_next = false, have_next_sed = false;
     for (int n = a->n_steps - 1; n >= 0; --n) {
         const bool first = a->first && n == 0;
+        /* a start that is not stored: recomputed in FP64 from the checkpoint
+         * before it into the scratch slot */
+        if (!ck_stored(a, n))
+            for (int m = (n / a->ck_every) * a->ck_every; m < n; ++m) step_to_checkpoint(c, a, m);
         /* recompute the step from its checkpoint, keeping the tape */
         load_start<double>(c, a, n, a->B.so);
         const double *sed_prev = moist ? ck_aux(a, n, 3) : nullptr;

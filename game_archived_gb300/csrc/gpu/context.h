@@ -117,8 +117,10 @@ struct Context {
 
     std::map<const void *, StateMirror> states;
 
-    /* adjoint / tangent-linear window state (adj_f64.cu), created on first use */
+    /* adjoint / tangent-linear window state (adj_f64.cu), created on first use;
+     * the windows store every adj_ck_every-th step start */
     struct AdjState *adj = nullptr;
+    int adj_ck_every = 1;
     void (*adj_release)(Context *) = nullptr;
 
     /* private buffers of the sub-step entry points (three_band_solver_*,

@@ -390,6 +390,13 @@ int rkhevi_window_forward(struct state *state_init, struct state *state_final, s
                           struct dualgrid *dualgrid, struct diagnostics *diagnostics, struct forcings *forcings,
                           struct irreversible_quantities *irrev, struct config *config, double delta_t, int n_steps);
 int rkhevi_window_tl(struct state *state_init_dot, struct state *state_final_dot);
+/* checkpoints of the windows that follow: every-th step start (default 1:
+ * all) and the window's end are stored; the backward sweep recomputes any
+ * other step start in FP64 from the checkpoint before it (every - 1 extra
+ * steps at most per backward step), and the tangent-linear model
+ * re-linearises only at stored starts, so the two stay exact transposes.
+ * Device memory of the checkpoints falls by about that factor. */
+int game_gpu_set_checkpoint_stride(int every);
 int rkhevi_window_backward(struct state *state_final_bar, struct state *state_init_bar);
 int game_gpu_sfc_pressure_objective(struct state *state, const double *weights, double *objective,
                                     struct state *state_bar);
