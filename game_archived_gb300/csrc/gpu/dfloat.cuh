@@ -62,7 +62,6 @@ __device__ __forceinline__ df two_prod(float a, float b)
     return {p, __fmaf_rn(a, b, -p)};
 }
 
-__device__ __forceinline__ df df_of(float x) { return {x, 0.0f}; }
 __device__ __forceinline__ df df_one() { return {1.0f, 0.0f}; }
 __device__ __forceinline__ df df_zero() { return {0.0f, 0.0f}; }
 __device__ __forceinline__ df df_half(df x) { return {0.5f * x.hi, 0.5f * x.lo}; } /* exact */
@@ -155,9 +154,6 @@ __device__ __forceinline__ df df_from_double(double x)
 /* double-float -> double: hi + lo is exact in a double for a normalised pair
  * (at most 49 significant bits); the widenings are integer operations */
 __device__ __forceinline__ double df_to_double(df x) { return to_double(x.hi) + to_double(x.lo); }
-
-/* the nearest float of a double-float (for the FP32 shadow) */
-__device__ __forceinline__ float df_to_float(df x) { return __fadd_rn(x.hi, x.lo); }
 
 }  // namespace
 }  // namespace game

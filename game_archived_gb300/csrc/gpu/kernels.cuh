@@ -152,15 +152,6 @@ __device__ __forceinline__ double enthalpy_sublimation(double t)
     return r / M_V;
 }
 
-__device__ __forceinline__ double phase_trans_heat(int dir, double t)
-{
-    double r = 0.0;
-    if (dir == 0) r = enthalpy_evaporation(t);
-    if (dir == 1) r = enthalpy_sublimation(t);
-    if (dir == 2) r = enthalpy_sublimation(t) - enthalpy_evaporation(t);
-    return r;
-}
-
 __device__ __forceinline__ double sat_pressure_water(double t)
 {
     double tc = t - T_0, r;
