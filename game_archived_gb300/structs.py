@@ -40,9 +40,6 @@ class Layout:
             self.members[name] = mem
             self.sizes[name] = int(lib.game_layout_sizeof(ctypes.byref(self.dims), sid))
 
-    def dims_tuple(self):
-        return (self.res_id, self.n_layers, self.moisture_on)
-
     LAYOUT_KEYS = ("res_id", "n_layers", "moisture_on", "nc", "ne", "nt", "nl", "n_scalars", "n_vectors",
                    "n_dual_vectors", "vpl", "dpl", "n_curl", "n_const", "n_cond", "n_latlon")
 
@@ -123,9 +120,6 @@ class Model:
         for k in self.KINDS:
             kind = "state" if k.startswith("state") else k
             setattr(self, k, HostStruct(layout, kind, buffers.get(k)))
-
-    def pointers(self):
-        return {k: getattr(self, k).ptr for k in self.KINDS}
 
 
 class ConfigIo(ctypes.Structure):
