@@ -51,11 +51,12 @@ __device__ __forceinline__ bool nonneg(double x)
 }
 
 /* double -> float rounded to nearest even, by integer operations for values
- * whose float is a normal number (or overflows to infinity by rounding);
- * zeros, subnormals, infinities and NaNs go through the conversion
+ * whose float is a normal number (or overflows to infinity by rounding) and
+ * for zeros; subnormal results, infinities and NaNs go through the conversion
  * instruction.  The same bits as float(x); used by the mixed path where it
  * writes its FP32 shadow from FP64 results, to keep the conversion off the
- * FP64 pipe. */
+ * FP64 pipe (zeros included: constituents absent from a run are zero
+ * everywhere, and each conversion instruction costs an FP64-pipe issue). */
 __device__ __forceinline__ float to_float(double x)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -67,6 +68,7 @@ __device__ __forceinline__ float to_float(double x)
         r += (rem > half || (rem == half && (r & 1u))) ? 1u : 0u;
         return __uint_as_float(r);
     }
+    if ((b << 1) == 0ULL) return __uint_as_float((unsigned)(b >> 63) << 31); /* +-0 */
     return __double2float_rn(x);
 }
 
